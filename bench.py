@@ -1,0 +1,351 @@
+"""Benchmark of the FP64 2D DG shallow-water stage on GB300.
+
+Workload (one "step" = one full SSP-RK3 step: the positivity-bounded dt,
+three fused stages of RHS + combination + damping + wet/dry correction):
+the synthetic coastal box of ≈ 1.0 M quads at N = 3 (16 M nodes), a seeded
+Gaussian random bed of 2–300 m with 30 islands, a 4-constituent tide at the
+open western side, Manning n = 0.02, Coriolis at 63° N.
+
+Metric: DOF-updates/s = 3 · K · (N+1)² · steps / s (one DOF advanced by one
+full step). ``value`` is device time (CUDA events on the library's stream)
+with the state resident in HBM; ``e2e`` is the same metric through the C
+ABI with host buffers (pinned upload, dt, step, download every step).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) every rank runs its own replica of the workload on
+its GPU (the path has no exchange between independent runs: replicas only,
+weak scaling); rank 0 prints the line. ``--impl reference`` times the
+reference's CPU path — the oracle port (oracle/, a C++ restatement of the
+reference CPU path; the Rust reference cannot be built here) — on the host
+cores."""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+METRIC = "FP64 DG SWE DOF-updates/s"
+UNIT = "DOF-updates/s"
+BYTES_PER_NODE_STAGE = {2: 81.8, 3: 77.5}  # algorithmic bytes (state, bed, mesh), N=2 / N=3
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier and max over ranks (torch.distributed), a no-op alone."""
+
+    def __init__(self, world: int, backend: str):
+        self.world = world
+        self.dist = None
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.init_process_group(backend=backend)
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.dist:
+            return x
+        import torch
+
+        dev = "cuda" if self.dist.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if not self.dist:
+            return x
+        import torch
+
+        dev = "cuda" if self.dist.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.dist:
+            self.dist.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons of one GPU every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.gpu)], stdout=self.file, stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def stop(self) -> dict | None:
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.file.flush()
+        rows = []
+        for line in Path(self.file.name).read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.file.name)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, flags in rows for i, f in enumerate(flags)
+                          if f.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def build_workload(n_elements: int, order: int):
+    from dgcom_gb300 import cases
+
+    return cases.coastal_box(n_elements=n_elements, order=order)
+
+
+def oracle_baseline(case, steps: int, threads: int) -> dict:
+    """The oracle (C++ restatement of the reference CPU path, OpenMP) timed
+    on the host cores over ``steps`` SSP-RK3 steps of ``case``."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    from oracle_lib import oracle
+
+    ref = oracle(case.form, threads=threads)
+    try:
+        ref.upload(*case.state)
+        t0 = time.perf_counter()
+        t = 0.0
+        for _ in range(steps):
+            dt = ref.compute_dt_ssp(case.cfl)
+            ref.step(t, dt)
+            t += dt
+        seconds = time.perf_counter() - t0
+    finally:
+        ref.close()
+    nodes = case.form.n_values
+    return {"value": 3.0 * nodes * steps / seconds, "seconds": seconds, "steps": steps}
+
+
+def run_reference(args, rank: int, world: int):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    # each bench step is one oracle SSP-RK3 step; the mesh shrinks when many
+    # steps are asked for, so the whole run stays within a few minutes
+    total = args.steps + args.warmup
+    n_el = args.elements if total <= 12 else max(50_000, int(args.elements * 12 / total))
+    case = build_workload(n_el, args.order)
+    sys.path.insert(0, str(ROOT / "tests"))
+    from oracle_lib import oracle
+
+    ref = oracle(case.form, threads=threads)
+    ref.upload(*case.state)
+    t = 0.0
+    for _ in range(args.warmup):
+        dt = ref.compute_dt_ssp(case.cfl)
+        ref.step(t, dt)
+        t += dt
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        dt = ref.compute_dt_ssp(case.cfl)
+        ref.step(t, dt)
+        t += dt
+    seconds = time.perf_counter() - t0
+    ref.close()
+    nodes = case.form.n_values
+    value = 3.0 * nodes * args.steps / seconds
+    sample = (f"{args.steps} SSP-RK3 steps of the coastal box at {case.form.mesh.n_elements} "
+              f"elements, N={args.order}, oracle port on {threads} host threads")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * seconds / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": f"coastal box {case.form.mesh.n_elements} quads N={args.order} "
+                               "SSP-RK3 (wet/dry, Manning, Coriolis, 4-constituent tide)",
+                   "elements": case.form.mesh.n_elements, "order": args.order,
+                   "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank: int, world: int, local: int):
+    import ctypes as C
+
+    from dgcom_gb300 import abi
+    from dgcom_gb300.device import SWEPhysics2D
+
+    dist = Dist(world, "nccl")
+    case = build_workload(args.elements, args.order)
+    form = case.form
+    nodes = form.n_values
+    dev = SWEPhysics2D(form, local)
+    dev.upload(*case.state)
+    lib = dev.lib
+
+    def profile(steps: int, t_start: float) -> abi.Profile:
+        cfg = abi.RunConfig()
+        cfg.scheme = abi.SSP_RK3
+        cfg.cfl = case.cfl
+        cfg.t_start = t_start
+        cfg.t_end = 1e300
+        out = abi.Profile()
+        st = lib.profile_steps(dev.handle, C.byref(cfg), steps, C.byref(out))
+        if st != abi.OK:
+            raise RuntimeError(lib.error_text(dev.handle, st))
+        return out
+
+    warm = profile(args.warmup, 0.0)
+    sampler = ClockSampler(local)
+    dist.barrier()
+    sampler.start()
+    timed = profile(args.steps, warm.t_final)
+    clocks = sampler.stop()
+    dist.barrier()
+    seconds = dist.max(timed.total_ms * 1e-3)
+    total_nodes = dist.sum(float(nodes))
+    value = 3.0 * total_nodes * args.steps / seconds
+
+    # e2e: through the C ABI with pinned host buffers, every step: upload
+    # the state, the positivity-bounded dt, one step, download the state
+    e2e_steps = max(1, min(args.steps, 5))
+    try:
+        import torch
+
+        pinned = [torch.empty(nodes, dtype=torch.float64, pin_memory=True).numpy() for _ in range(3)]
+    except Exception:  # noqa: BLE001 - pinned memory is an optimisation of the copy
+        pinned = [np.empty(nodes) for _ in range(3)]
+    h, hu, hv = dev.download()
+    for dst, src in zip(pinned, (h, hu, hv)):
+        dst[:] = src
+    dist.barrier()
+    t0 = time.perf_counter()
+    t = timed.t_final
+    for _ in range(e2e_steps):
+        dev.upload(*pinned)
+        dt = dev.compute_dt_ssp(case.cfl)
+        dev.step(t, dt)
+        t += dt
+        ptrs = [p.ctypes.data_as(C.POINTER(C.c_double)) for p in pinned]
+        st = lib.download(dev.handle, 0, *ptrs, nodes)
+        if st != abi.OK:
+            raise RuntimeError(lib.error_text(dev.handle, st))
+    e2e_seconds = dist.max(time.perf_counter() - t0)
+    e2e_value = 3.0 * total_nodes * e2e_steps / e2e_seconds
+
+    peak, peak_kind = peaks()
+    stage_avg_ms = timed.stage_ms / max(1, timed.stage_launches)
+    bytes_per_launch = BYTES_PER_NODE_STAGE.get(args.order, 77.5) * nodes
+    achieved = bytes_per_launch / (stage_avg_ms * 1e-3) / 1e9
+    baseline = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        dev_state = dev.download()
+        probe = oracle_baseline(case, 1, threads)
+        steps = int(max(1, min(10, 15.0 / max(probe["seconds"], 1e-3))))
+        b = oracle_baseline(case, steps, threads)
+        baseline = {"value": b["value"], "unit": UNIT, "cores": threads, "kind": "port",
+                    "sample": f"{steps} SSP-RK3 steps of the same {form.mesh.n_elements}-element "
+                              f"mesh from rest ({b['seconds']:.1f} s on {threads} host threads)"}
+        del dev_state
+    dev.close()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * seconds / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": f"coastal box {form.mesh.n_elements} quads N={args.order} "
+                                   "SSP-RK3 (wet/dry, Manning, Coriolis, 4-constituent tide)",
+                       "elements": form.mesh.n_elements, "order": args.order,
+                       "nodes": nodes, "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2 (state and tables ≫ 129 MB)"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                         "kernel": "stage_kernel<4>",
+                         "note": "FP64-pipe bound: see profiles/ for the FP64 fraction"},
+            "kernel_ms": {"stage": timed.stage_ms / args.steps, "face": timed.face_ms / args.steps,
+                          "dt": timed.dt_ms / args.steps, "control": timed.control_ms / args.steps},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 3 * 8 * nodes,
+                    "d2h_bytes_per_step": 3 * 8 * nodes + 8},
+            "gpu_launches": int(timed.face_launches + timed.stage_launches + timed.dt_launches
+                                + timed.control_launches),
+            "clocks": clocks,
+            "cpu_baseline": baseline,
+        }
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--elements", type=int, default=1_000_000)
+    ap.add_argument("--order", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,235 @@
+"""ctypes mirror of the C ABI in ``include/dgswe.h`` and the loader of the
+in-tree CUDA library ``libdgswe.so``.
+
+The structs below are the header's, field for field; ``Library`` binds the
+entry points of any shared library that exports this ABI under a symbol
+prefix (``dgswe_`` for the CUDA library)."""
+
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+LIBRARY_PATH = HERE / "libdgswe.so"
+
+ABI_VERSION = 1
+
+# dgswe_status
+OK, ERR_INVALID, ERR_CUDA, ERR_NONFINITE, ERR_DT_MIN, ERR_MAX_STEPS, ERR_STOPPED, \
+    ERR_UNSUPPORTED, ERR_NO_DEVICE = range(9)
+# dgswe_formulation
+WET_DRY, ENTROPY_STABLE, ENTROPY_CONSERVATIVE = range(3)
+# dgswe_boundary_kind
+BC_WALL, BC_CHARACTERISTIC = range(2)
+# dgswe_elevation_only
+AT_REST, INCOMING_WAVE = range(2)
+# dgswe_friction
+FRICTION_NONE, FRICTION_MANNING, FRICTION_MANNING_NODES = range(3)
+# dgswe_scheme
+SSP_RK3, SSP_RK43 = range(2)
+# dgswe_numerics
+NUMERICS_FAST, NUMERICS_EXACT = range(2)
+
+STATE = 0
+N_BUFFERS = 6
+
+_dp = C.POINTER(C.c_double)
+
+
+class TideConstituent(C.Structure):
+    _fields_ = [
+        ("amplitude", C.c_double),
+        ("period", C.c_double),
+        ("phase", C.c_double),
+        ("f", C.c_double),
+        ("f_rate", C.c_double),
+        ("u_deg", C.c_double),
+        ("u_rate_deg", C.c_double),
+        ("v0_deg", C.c_double),
+    ]
+
+
+class Boundary(C.Structure):
+    _fields_ = [
+        ("tag", C.c_int32),
+        ("kind", C.c_int32),
+        ("wall_h_min", C.c_double),
+        ("elevation_only", C.c_int32),
+        ("n_constituents", C.c_int32),
+        ("constituents", C.POINTER(TideConstituent)),
+        ("mean_elevation", C.c_double),
+        ("ramp_duration", C.c_double),
+    ]
+
+
+class Form(C.Structure):
+    _fields_ = [
+        ("abi_version", C.c_uint32),
+        ("order", C.c_int32),
+        ("n_vertices", C.c_int64),
+        ("vertices", _dp),
+        ("n_elements", C.c_int64),
+        ("elements", C.POINTER(C.c_int64)),
+        ("n_periodic", C.c_int64),
+        ("periodic", C.POINTER(C.c_int64)),
+        ("face_tags", C.POINTER(C.c_int32)),
+        ("bathymetry", _dp),
+        ("g", C.c_double),
+        ("h_min", C.c_double),
+        ("formulation", C.c_int32),
+        ("subcell_depth", C.c_double),
+        ("subcell_h_dry", C.c_double),
+        ("has_wet_dry", C.c_int32),
+        ("wet_dry_h_dry", C.c_double),
+        ("wet_dry_relaxation_time", C.c_double),
+        ("wet_dry_max_velocity", C.c_double),
+        ("positivity_h_dry", C.c_double),
+        ("friction", C.c_int32),
+        ("friction_g", C.c_double),
+        ("manning_n", C.c_double),
+        ("manning_h_min", C.c_double),
+        ("manning_n_nodes", _dp),
+        ("has_coriolis", C.c_int32),
+        ("coriolis_f0", C.c_double),
+        ("coriolis_beta", C.c_double),
+        ("coriolis_y0", C.c_double),
+        ("n_boundaries", C.c_int32),
+        ("boundaries", C.POINTER(Boundary)),
+        ("numerics", C.c_int32),
+    ]
+
+
+class StagePlan(C.Structure):
+    _fields_ = [
+        ("base", C.c_int32),
+        ("input", C.c_int32),
+        ("out", C.c_int32),
+        ("acc", C.c_int32),
+        ("time", C.c_double),
+        ("a", C.c_double),
+        ("b", C.c_double),
+        ("c", C.c_double),
+        ("accumulate", C.c_int32),
+        ("w", C.c_double),
+        ("keep", C.c_double),
+    ]
+
+
+class RunConfig(C.Structure):
+    _fields_ = [
+        ("scheme", C.c_int32),
+        ("cfl", C.c_double),
+        ("t_start", C.c_double),
+        ("t_end", C.c_double),
+        ("interval", C.c_double),
+        ("dt_max", C.c_double),
+        ("dt_min", C.c_double),
+        ("max_steps", C.c_int64),
+        ("stop", C.POINTER(C.c_int32)),
+    ]
+
+
+class Report(C.Structure):
+    _fields_ = [
+        ("success", C.c_int32),
+        ("final_time", C.c_double),
+        ("n_steps", C.c_int64),
+        ("dt_min_used", C.c_double),
+        ("dt_max_used", C.c_double),
+        ("wall_time", C.c_double),
+        ("negative_depth_clips", C.c_int64),
+        ("message", C.c_char * 256),
+        ("device", C.c_char * 128),
+    ]
+
+
+class Profile(C.Structure):
+    _fields_ = [
+        ("steps", C.c_int64),
+        ("total_ms", C.c_double),
+        ("face_ms", C.c_double),
+        ("stage_ms", C.c_double),
+        ("dt_ms", C.c_double),
+        ("control_ms", C.c_double),
+        ("face_launches", C.c_int64),
+        ("stage_launches", C.c_int64),
+        ("dt_launches", C.c_int64),
+        ("control_launches", C.c_int64),
+        ("t_final", C.c_double),
+    ]
+
+
+CALLBACK = C.CFUNCTYPE(None, C.c_void_p, C.c_double, _dp, _dp, _dp, C.c_int64)
+
+# entry points shared by every library with this ABI: name → (restype, argtypes)
+ENTRY_POINTS = {
+    "create": (C.c_int, [C.POINTER(Form), C.c_int, C.POINTER(C.c_void_p)]),
+    "destroy": (None, [C.c_void_p]),
+    "n_values": (C.c_int64, [C.c_void_p]),
+    "upload": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp, _dp, C.c_int64]),
+    "download": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp, _dp, C.c_int64]),
+    "compute_rhs": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, _dp, _dp, _dp, C.c_int64]),
+    "stage": (C.c_int, [C.c_void_p, C.POINTER(StagePlan)]),
+    "finish": (C.c_int, [C.c_void_p, C.c_int32]),
+    "element_dt": (C.c_int, [C.c_void_p, C.c_double, C.c_int32, _dp, _dp]),
+    "step": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double]),
+    "run": (C.c_int, [C.c_void_p, C.POINTER(RunConfig), CALLBACK, C.c_void_p, C.POINTER(Report)]),
+    "negative_depth_clips": (C.c_int64, [C.c_void_p]),
+}
+# the CUDA library's own
+CUDA_ONLY = {
+    "abi_version": (C.c_uint32, []),
+    "status_string": (C.c_char_p, [C.c_int]),
+    "last_error": (C.c_char_p, [C.c_void_p]),
+    "profile_steps": (C.c_int, [C.c_void_p, C.POINTER(RunConfig), C.c_int64, C.POINTER(Profile)]),
+}
+
+
+class Library:
+    """The entry points of a shared library exporting this ABI under
+    ``prefix`` (``prefix_create``, ``prefix_stage``, …)."""
+
+    def __init__(self, cdll: C.CDLL, prefix: str, extra: dict | None = None):
+        self.cdll = cdll
+        self.prefix = prefix
+        table = dict(ENTRY_POINTS)
+        table.update(extra or {})
+        for name, (res, args) in table.items():
+            fn = getattr(cdll, f"{prefix}_{name}")
+            fn.restype = res
+            fn.argtypes = args
+            setattr(self, name, fn)
+        self.has_last_error = hasattr(self, "last_error")
+
+    def error_text(self, handle, status: int) -> str:
+        text = ""
+        if self.has_last_error and handle:
+            raw = self.last_error(handle)
+            text = raw.decode() if raw else ""
+        return text or f"status {status}"
+
+
+_cuda_library: Library | None = None
+
+
+def cuda_library() -> Library:
+    """The in-tree CUDA library. Fails loudly if it has not been built: there
+    is no CPU fallback."""
+    global _cuda_library
+    if _cuda_library is None:
+        if not LIBRARY_PATH.exists():
+            raise RuntimeError(
+                f"{LIBRARY_PATH} is missing: build it with "
+                "`python -c 'import __graft_entry__ as g; g.build()'`")
+        cdll = C.CDLL(str(LIBRARY_PATH))
+        lib = Library(cdll, "dgswe", CUDA_ONLY)
+        if lib.abi_version() != ABI_VERSION:
+            raise RuntimeError("libdgswe ABI version mismatch: rebuild it")
+        _cuda_library = lib
+    return _cuda_library
+
+
+def exported_symbols() -> list[str]:
+    """Every entry point the C header declares, as ``dgswe_<name>``."""
+    return sorted(f"dgswe_{n}" for n in list(ENTRY_POINTS) + list(CUDA_ONLY))

@@ -1,0 +1,255 @@
+"""The workloads of the device path, built on the host with fixed seeds:
+
+- :func:`tidal_channel`: the idealised tidal channel (50 km × 5 km,
+  200 × 20 quads, N = 2) whose bed ramps from 20 m deep at the open western
+  end to 1 m above datum at the head, so a tidal flat floods and drains,
+  under an M2 tide of 1 m, Manning n = 0.025 and f = 1.26e-4 s⁻¹;
+- :func:`coastal_box`: a synthetic coastal quad mesh of ≈ 1.0 M elements
+  (200 km × 150 km, element sizes 100–250 m, jittered, in Hilbert order),
+  N = 3, over a seeded Gaussian random bed of 2–300 m with 30 Gaussian
+  islands above the datum, under a 4-constituent tide (M2, S2, N2, K1) with
+  seeded phases, Manning n = 0.02 and Coriolis at 63° N;
+- :func:`split_form_setup`: the meshes, beds and states of the reference's
+  split-form unit tests (src/solver/rhs/swe_2d_split_form.rs:1144-1232).
+
+No public dataset is involved: every input is generated here."""
+
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import abi, tides
+from .mesh import (TAG_OPEN, TAG_WALL, QuadMesh, graded_jittered_box, in_hilbert_order,
+                   node_positions, uniform_periodic, uniform_rectangle, move_vertices)
+from .physics import SWEDeviceForm2D, TidalBoundary, WallBoundary, at_rest
+
+EARTH_ROTATION_RATE = 7.292_115e-5  # rad/s (src/source/swe_2d/coriolis.rs:24-25)
+
+
+def coriolis_parameter(latitude_deg: float) -> float:
+    """f = 2Ω sin φ (src/source/swe_2d/coriolis.rs:28-31)."""
+    return 2.0 * EARTH_ROTATION_RATE * math.sin(math.radians(latitude_deg))
+
+
+def ramp_depth(x, y, from_m, to_m, depth_m):
+    """[bathymetry.ramp]: depth linear along from → to, constant across
+    (src/case/schema.rs:658-663)."""
+    x0, y0 = from_m
+    dx, dy = to_m[0] - x0, to_m[1] - y0
+    s = np.clip(((x - x0) * dx + (y - y0) * dy) / (dx * dx + dy * dy), 0.0, 1.0)
+    return depth_m[0] + s * (depth_m[1] - depth_m[0])
+
+
+@dataclass
+class Case:
+    form: SWEDeviceForm2D
+    state: tuple  # (h, hu, hv)
+    cfl: float
+    scheme: int
+    t_end: float
+    stations: np.ndarray | None = None  # (n, 2) positions
+
+
+def tidal_channel(nx: int = 200, ny: int = 20, order: int = 2,
+                  numerics: int = abi.NUMERICS_FAST) -> Case:
+    lx, ly = 50_000.0, 5_000.0
+    mesh = uniform_rectangle(0.0, lx, 0.0, ly, nx, ny,
+                             sides=(TAG_WALL, TAG_WALL, TAG_WALL, TAG_OPEN))
+    form = SWEDeviceForm2D(mesh=mesh, order=order, numerics=numerics)
+    x, y = node_positions(mesh, order)
+    depth = ramp_depth(x, y, (0.0, 0.5 * ly), (lx, 0.5 * ly), (20.0, -1.0))
+    form.bathymetry = -depth
+    form.manning_n = 0.025
+    form.coriolis_f0 = 1.26e-4
+    form.boundaries = {
+        TAG_WALL: WallBoundary(),
+        TAG_OPEN: TidalBoundary([tides.constituent("M2", 1.0, 0.0)], ramp_duration=3600.0),
+    }
+    stations = np.stack([np.arange(0.0, lx + 1.0, 5_000.0), np.full(11, 0.5 * ly)], axis=1)
+    return Case(form, at_rest(form), 0.5, abi.SSP_RK3, 25.0 * 3600.0, stations)
+
+
+def gaussian_random_field(nx: int, ny: int, spacing: float, corr: float,
+                          rng: np.random.Generator) -> np.ndarray:
+    """Unit-variance Gaussian random field on an (ny, nx) grid of the given
+    spacing with a Gaussian correlation of length ``corr``, by spectral
+    synthesis (white noise filtered in Fourier space)."""
+    noise = rng.standard_normal((ny, nx))
+    kx = np.fft.fftfreq(nx, d=spacing) * 2.0 * np.pi
+    ky = np.fft.fftfreq(ny, d=spacing) * 2.0 * np.pi
+    k2 = kx[None, :] ** 2 + ky[:, None] ** 2
+    field = np.real(np.fft.ifft2(np.fft.fft2(noise) * np.exp(-0.25 * k2 * corr * corr)))
+    field -= field.mean()
+    return field / field.std()
+
+
+def _bilinear_grid(field: np.ndarray, spacing: float, x: np.ndarray, y: np.ndarray) -> np.ndarray:
+    ny, nx = field.shape
+    fx = np.clip(x / spacing, 0.0, nx - 1.000001)
+    fy = np.clip(y / spacing, 0.0, ny - 1.000001)
+    i = fx.astype(np.int64)
+    j = fy.astype(np.int64)
+    tx, ty = fx - i, fy - j
+    return ((1 - tx) * (1 - ty) * field[j, i] + tx * (1 - ty) * field[j, i + 1]
+            + (1 - tx) * ty * field[j + 1, i] + tx * ty * field[j + 1, i + 1])
+
+
+def coastal_bed(x: np.ndarray, y: np.ndarray, lx: float, ly: float, seed: int,
+                n_islands: int = 30) -> np.ndarray:
+    """Bed elevation B at (x, y): a seeded Gaussian random field (5 km
+    correlation, on a 1 km grid, bilinear to the points) mapped to depths of
+    2–300 m, with ``n_islands`` Gaussian islands (radius 1–5 km) whose crests
+    reach 2–20 m above the datum, away from the open western side."""
+    from scipy.special import ndtr
+
+    rng = np.random.default_rng(seed)
+    spacing = 1000.0
+    gx, gy = int(lx / spacing) + 2, int(ly / spacing) + 2
+    z = gaussian_random_field(gx, gy, spacing, 5000.0, rng)
+    depth_grid = 2.0 + 298.0 * ndtr(z)
+    depth = _bilinear_grid(depth_grid, spacing, x, y)
+    bed = -depth
+    cx = rng.uniform(0.15 * lx, 0.95 * lx, n_islands)
+    cy = rng.uniform(0.05 * ly, 0.95 * ly, n_islands)
+    radius = rng.uniform(1000.0, 5000.0, n_islands)
+    crest = rng.uniform(2.0, 20.0, n_islands)
+    centre_depth = _bilinear_grid(depth_grid, spacing, cx, cy)
+    for i in range(n_islands):
+        r2 = (x - cx[i]) ** 2 + (y - cy[i]) ** 2
+        bed = bed + (centre_depth[i] + crest[i]) * np.exp(-r2 / radius[i] ** 2)
+    return bed
+
+
+def coastal_box(n_elements: int = 1_000_000, order: int = 3, seed: int = 2026,
+                numerics: int = abi.NUMERICS_FAST, lx: float = 200_000.0,
+                ly: float = 150_000.0) -> Case:
+    nx = max(2, int(round(math.sqrt(n_elements * lx / ly))))
+    ny = max(2, int(round(n_elements / nx)))
+    mean = lx / nx
+    mesh = graded_jittered_box(lx, ly, nx, ny, size_range=(100.0 * mean / 173.0,
+                                                           250.0 * mean / 173.0),
+                               jitter=0.15, seed=seed,
+                               sides=(TAG_WALL, TAG_WALL, TAG_WALL, TAG_OPEN))
+    mesh, _ = in_hilbert_order(mesh)
+    form = SWEDeviceForm2D(mesh=mesh, order=order, numerics=numerics)
+    x, y = node_positions(mesh, order)
+    form.bathymetry = coastal_bed(x, y, lx, ly, seed)
+    form.manning_n = 0.02
+    form.coriolis_f0 = coriolis_parameter(63.0)
+    rng = np.random.default_rng(seed + 1)
+    phases = rng.uniform(0.0, 360.0, 4)
+    cons = [tides.constituent(name, amp, ph) for (name, amp), ph in
+            zip([("M2", 1.0), ("S2", 0.35), ("N2", 0.2), ("K1", 0.1)], phases)]
+    form.boundaries = {TAG_WALL: WallBoundary(), TAG_OPEN: TidalBoundary(cons, ramp_duration=3600.0)}
+    return Case(form, at_rest(form), 0.5, abi.SSP_RK3, 2000.0)
+
+
+# -- the reference's split-form test setups ------------------------------------
+
+L_TEST = 20_000.0
+
+
+def smooth_bed(x, y):
+    tau = 2.0 * math.pi / L_TEST
+    return -200.0 + 150.0 * np.sin(tau * x) * np.cos(tau * y)
+
+
+def xorshift_noise(n: int, seed: int = 0x9E37_79B9_7F4A_7C15) -> np.ndarray:
+    """The reference tests' xorshift64 sequence, (seed >> 11)/2⁵³ per draw."""
+    mask = (1 << 64) - 1
+    out = np.empty(n)
+    for i in range(n):
+        seed ^= (seed << 13) & mask
+        seed ^= seed >> 7
+        seed ^= (seed << 17) & mask
+        out[i] = (seed >> 11) / float(1 << 53)
+    return out
+
+
+def split_form_setup(order: int, periodic: bool, bed: str = "smooth", curved: bool = False,
+                     numerics: int = abi.NUMERICS_FAST, formulation: int = abi.WET_DRY,
+                     wet_dry: bool = False) -> SWEDeviceForm2D:
+    """A 12 × 12 periodic mesh of [0, L]² or an 8 × 5 walled mesh of
+    [0, L] × [0, L/2] (L = 20 km), with the smooth, cell-average or rough
+    bed of the reference's tests; ``curved`` moves the vertices so every
+    element is a general quadrilateral."""
+    if periodic:
+        mesh = uniform_periodic(0.0, L_TEST, 0.0, L_TEST, 12, 12)
+    else:
+        mesh = uniform_rectangle(0.0, L_TEST, 0.0, 0.5 * L_TEST, 8, 5)
+    if curved:
+        h_el = L_TEST / 12.0
+        tau = 2.0 * math.pi / L_TEST
+
+        def move(x, y):
+            interior = (x > 0) & (x < L_TEST) & (y > 0) & (y < (L_TEST if periodic else 0.5 * L_TEST))
+            a = 0.15 * h_el
+            sx, sy = np.sin(3.0 * tau * x), np.sin(2.0 * tau * y)
+            return (np.where(interior, x + a * sx * sy, x),
+                    np.where(interior, y - 0.7 * a * sx * sy, y))
+        mesh = move_vertices(mesh, move)
+    form = SWEDeviceForm2D(mesh=mesh, order=order, numerics=numerics, formulation=formulation,
+                           wet_dry=wet_dry, positivity_h_dry=1e-3 if wet_dry else None)
+    x, y = node_positions(mesh, order)
+    b = smooth_bed(x, y)
+    if bed == "cell_average":
+        b = np.repeat((b.sum(axis=1) / b.shape[1])[:, None], b.shape[1], axis=1)
+    elif bed == "rough":
+        b = b + 30.0 * (xorshift_noise(b.size).reshape(b.shape) - 0.5)
+    form.bathymetry = b
+    form.boundaries = {TAG_WALL: WallBoundary()}
+    return form
+
+
+def split_form_state(form: SWEDeviceForm2D, speed: float, eta: float = 0.3):
+    """η = 0.3 m over the bed with the velocity speed·(cos·cos, ½ sin·cos)
+    (src/solver/rhs/swe_2d_split_form.rs:1197-1214)."""
+    tau = 2.0 * math.pi / L_TEST
+    x, y = form.positions()
+    h = eta - form.bathymetry
+    u = speed * np.cos(tau * x) * np.cos(tau * y)
+    v = 0.5 * speed * np.sin(tau * x) * np.cos(tau * y)
+    return h.reshape(-1), (h * u).reshape(-1), (h * v).reshape(-1)
+
+
+def shoreline_setup(order: int, periodic: bool, rough: bool, curved: bool = False,
+                    numerics: int = abi.NUMERICS_FAST, formulation: int = abi.WET_DRY,
+                    wet_dry: bool = False, h_min: float = 1e-6) -> SWEDeviceForm2D:
+    """The reference's shoreline setup (src/solver/rhs/swe_2d_split_form.rs:1394-1417):
+    B = −1 + 1.5 cos(τx) cos(τy), plus ±0.2 m of xorshift noise if ``rough``,
+    so η = 0.3 leaves dry land and shorelines."""
+    form = split_form_setup(order, periodic, "smooth", curved=curved, numerics=numerics,
+                            formulation=formulation, wet_dry=wet_dry)
+    form.h_min = h_min
+    tau = 2.0 * math.pi / L_TEST
+    x, y = form.positions()
+    b = -1.0 + 1.5 * np.cos(tau * x) * np.cos(tau * y)
+    if rough:
+        b = b + 0.4 * (xorshift_noise(b.size, 0x2545_F491_4F6C_DD1D).reshape(b.shape) - 0.5)
+    form.bathymetry = b
+    return form
+
+
+def shoreline_state(form: SWEDeviceForm2D, speed: float, eta: float = 0.3):
+    """Lake at rest η = 0.3 (h = max(0, η − B)) with the test velocity field
+    times ``speed`` at wet nodes (swe_2d_split_form.rs:1421-1437)."""
+    h0, hu0, hv0 = split_form_state(form, speed, eta)
+    h = np.maximum(eta - form.bathymetry.reshape(-1), 0.0)
+    scale = np.where(h0 > 0.0, h / np.where(h0 > 0.0, h0, 1.0), 0.0)
+    return h, hu0 * scale, hv0 * scale
+
+
+def with_flow(case: Case, eta_amp: float = 0.5, u: float = 0.3, v: float = -0.1) -> tuple:
+    """A flowing state on ``case``'s mesh: η = η_amp·cos(2πx/L_x) and a
+    uniform velocity at the wet nodes, so that every field is O(1) (a state
+    at rest has roundoff-level momentum, which no relative comparison can
+    judge)."""
+    x, _ = case.form.positions()
+    lx = float(case.form.mesh.vertices[:, 0].max() - case.form.mesh.vertices[:, 0].min())
+    b = case.form.bathymetry.reshape(x.shape)
+    h = np.maximum(eta_amp * np.cos(2.0 * math.pi * x / lx) - b, 0.0)
+    wet = h > 0.0
+    return h.reshape(-1), np.where(wet, u * h, 0.0).reshape(-1), np.where(wet, v * h, 0.0).reshape(-1)

@@ -1,0 +1,827 @@
+// The C ABI (include/dgswe.h): a handle owns the device copy of a
+// dgswe_form's physics, the solution buffers, the face-flux buffer and the
+// step control block, and runs host-driven calls (one stage, one step, the
+// RHS, the element steps) or a device-driven run whose steps are one CUDA
+// graph each, the clock kept on the device.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/dgswe.h"
+#include "device.hpp"
+#include "kernel_set.hpp"
+#include "setup.hpp"
+
+using namespace dgswe;
+
+namespace {
+
+constexpr int kRhsBuffer = DGSWE_N_BUFFERS;  // scratch buffer of dgswe_compute_rhs
+
+struct DeviceBuffer {
+    double* base = nullptr;  // one allocation of 5 fields
+    DevBuf view{};
+};
+
+}  // namespace
+
+struct dgswe_handle {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string error;
+    dgswe_form form{};
+    std::vector<dgswe_tide_constituent> constituents;
+    Operators* ops = nullptr;
+    int n1 = 0, nn = 0;
+    int64_t K = 0, n_values = 0;
+    const KernelSet* ks = nullptr;
+    DevTables T{};
+    Physics P{};
+    StageExtra X{};
+    std::vector<void*> allocations;
+    DeviceBuffer buf[DGSWE_N_BUFFERS + 1];
+    double *fb_h = nullptr, *fb_hu = nullptr, *fb_hv = nullptr;
+    double* dt_el = nullptr;
+    StepCtl* ctl = nullptr;    // device
+    StepCtl* h_ctl = nullptr;  // pinned host mirror
+    std::string device_name;
+    // graph of one device-driven step
+    cudaGraphExec_t step_graph = nullptr;
+    int graph_scheme = -1;
+    double graph_cfl = -1.0;
+
+    ~dgswe_handle() {
+        if (step_graph) cudaGraphExecDestroy(step_graph);
+        for (void* p : allocations) cudaFree(p);
+        if (h_ctl) cudaFreeHost(h_ctl);
+        if (stream) cudaStreamDestroy(stream);
+        delete ops;
+    }
+};
+
+namespace {
+
+int fail(dgswe_handle* h, int status, const char* fmt, ...) {
+    char msg[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(msg, sizeof msg, fmt, ap);
+    va_end(ap);
+    if (h) h->error = msg;
+    return status;
+}
+
+#define CK(call)                                                                             \
+    do {                                                                                     \
+        cudaError_t err_ = (call);                                                           \
+        if (err_ != cudaSuccess)                                                             \
+            return fail(h, DGSWE_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(err_)); \
+    } while (0)
+
+template <class T>
+int upload_vec(dgswe_handle* h, const std::vector<T>& v, const T** out) {
+    *out = nullptr;
+    if (v.empty()) return DGSWE_OK;
+    void* p = nullptr;
+    CK(cudaMalloc(&p, v.size() * sizeof(T)));
+    h->allocations.push_back(p);
+    CK(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    *out = (const T*)p;
+    return DGSWE_OK;
+}
+
+int ensure_buffer(dgswe_handle* h, int id) {
+    DeviceBuffer& b = h->buf[id];
+    if (b.base) return DGSWE_OK;
+    void* p = nullptr;
+    size_t n = (size_t)h->n_values;
+    CK(cudaMalloc(&p, 5 * n * sizeof(double)));
+    h->allocations.push_back(p);
+    CK(cudaMemset(p, 0, 5 * n * sizeof(double)));
+    b.base = (double*)p;
+    b.view = {b.base, b.base + n, b.base + 2 * n, b.base + 3 * n, b.base + 4 * n};
+    return DGSWE_OK;
+}
+
+bool valid_buffer(int id) { return id >= 0 && id < DGSWE_N_BUFFERS; }
+
+// SspScheme::stages (src/time/integrator.rs:239-263): (start, input, beta, c)
+int scheme_table(int scheme, double st[4][4]) {
+    if (scheme == DGSWE_SSP_RK43) {
+        const double t[4][4] = {{1.0, 0.0, 0.5, 0.0},
+                                {0.0, 1.0, 0.5, 0.5},
+                                {2.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0, 1.0},
+                                {0.0, 1.0, 0.5, 0.5}};
+        std::memcpy(st, t, sizeof t);
+        return 4;
+    }
+    const double t[3][4] = {{1.0, 0.0, 1.0, 0.0}, {0.75, 0.25, 0.25, 1.0},
+                            {1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0, 0.5}};
+    std::memcpy(st, t, sizeof t);
+    return 3;
+}
+
+// PositivityBound::new (src/solver/rhs/swe_2d.rs:2194-2212) with the linear
+// limits of linear_cfl_swe_2d / linear_cfl_subcells_swe_2d (swe_2d.rs:1263-1300)
+DtParams dt_params(const dgswe_handle* h, double cfl, int scheme) {
+    DtParams d{};
+    d.cfl = cfl;
+    d.positivity = h->form.positivity_h_dry > 0.0 ? 1 : 0;
+    const int order = h->form.order;
+    const double n = (double)order;
+    const double ssp = scheme == DGSWE_SSP_RK43 ? 2.0 : 1.0;
+    const double bound = ssp * ((2.0 * n + 1.0) / (2.0 * n * (n + 1.0)));
+    static const double lin3[4] = {1.6, 1.04, 0.73, 0.56}, lin43[4] = {2.2, 1.51, 1.15, 0.93};
+    static const double sub3[4] = {0.94, 0.65, 0.47, 0.36}, sub43[4] = {1.5, 1.1, 0.97, 0.75};
+    const double lin = scheme == DGSWE_SSP_RK43 ? lin43[order - 1] : lin3[order - 1];
+    const double sub = scheme == DGSWE_SSP_RK43 ? sub43[order - 1] : sub3[order - 1];
+    d.bound_cfl = bound;
+    d.max_cfl = std::fmax(bound, 0.9 * lin);
+    d.max_cfl_subcells = std::fmax(bound, 0.9 * sub);
+    d.shallow = 100.0 * h->form.positivity_h_dry;
+    return d;
+}
+
+int sync(dgswe_handle* h) {
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaGetLastError());
+    return DGSWE_OK;
+}
+
+// Launch one stage: the face pass then the element stage
+void launch_stage(dgswe_handle* h, int in, int base, int out, int acc, int slot, int mode,
+                  int check_finite, const int* active) {
+    h->ks->face(h->n1, h->T, h->P, h->buf[in].view, h->fb_h, h->fb_hu, h->fb_hv, h->ctl, slot,
+                active, h->stream);
+    h->ks->stage(h->n1, h->T, h->P, h->X, h->buf[in].view, h->buf[base].view, h->buf[out].view,
+                 h->buf[acc].view, h->fb_h, h->fb_hu, h->fb_hv, h->ctl, slot, mode, check_finite,
+                 active, h->stream);
+}
+
+int write_host_args(dgswe_handle* h, const StageArgs& a) {
+    h->h_ctl->stage[kHostSlot] = a;
+    CK(cudaMemcpyAsync(&h->ctl->stage[kHostSlot], &h->h_ctl->stage[kHostSlot], sizeof(StageArgs),
+                       cudaMemcpyHostToDevice, h->stream));
+    return DGSWE_OK;
+}
+
+const int* always(dgswe_handle* h) { return &h->ctl->always; }
+
+int check_form(const dgswe_form* f, std::string& why) {
+    if (!f) return why = "form is NULL", DGSWE_ERR_INVALID;
+    if (f->abi_version != DGSWE_ABI_VERSION) return why = "ABI version mismatch", DGSWE_ERR_INVALID;
+    if (f->order < 1 || f->order > 4) return why = "order must be 1..4", DGSWE_ERR_UNSUPPORTED;
+    if (f->n_elements <= 0 || f->n_vertices <= 0 || !f->vertices || !f->elements)
+        return why = "the mesh is empty", DGSWE_ERR_INVALID;
+    if (f->n_elements >= (1ll << 40)) return why = "too many elements", DGSWE_ERR_INVALID;
+    if (f->n_periodic < 0 || (f->n_periodic > 0 && !f->periodic))
+        return why = "periodic pairs without data", DGSWE_ERR_INVALID;
+    if (f->formulation < DGSWE_WET_DRY || f->formulation > DGSWE_ENTROPY_CONSERVATIVE)
+        return why = "unknown formulation", DGSWE_ERR_UNSUPPORTED;
+    if (!(f->g > 0.0) || !(f->h_min >= 0.0)) return why = "g and h_min", DGSWE_ERR_INVALID;
+    if (f->friction < DGSWE_FRICTION_NONE || f->friction > DGSWE_FRICTION_MANNING_NODES)
+        return why = "unknown friction law", DGSWE_ERR_UNSUPPORTED;
+    if (f->friction == DGSWE_FRICTION_MANNING_NODES && !f->manning_n_nodes)
+        return why = "per-node Manning without data", DGSWE_ERR_INVALID;
+    if (f->has_wet_dry && !(f->wet_dry_h_dry > 0.0 && f->wet_dry_relaxation_time > 0.0))
+        return why = "the wet/dry depth and relaxation time must be positive", DGSWE_ERR_INVALID;
+    if (f->n_boundaries < 0 || f->n_boundaries > kMaxConditions ||
+        (f->n_boundaries > 0 && !f->boundaries))
+        return why = "boundary conditions", DGSWE_ERR_INVALID;
+    for (int b = 0; b < f->n_boundaries; ++b) {
+        const dgswe_boundary& c = f->boundaries[b];
+        if (c.kind != DGSWE_BC_WALL && c.kind != DGSWE_BC_CHARACTERISTIC)
+            return why = "a boundary condition without a device form", DGSWE_ERR_UNSUPPORTED;
+        if (c.n_constituents < 0 || c.n_constituents > kMaxConstituents ||
+            (c.n_constituents > 0 && !c.constituents))
+            return why = "tide constituents", DGSWE_ERR_INVALID;
+        for (int i = 0; i < c.n_constituents; ++i)
+            if (!(c.constituents[i].period > 0.0)) return why = "a tide period", DGSWE_ERR_INVALID;
+    }
+    if (f->numerics != DGSWE_NUMERICS_FAST && f->numerics != DGSWE_NUMERICS_EXACT)
+        return why = "unknown numerics", DGSWE_ERR_INVALID;
+    return DGSWE_OK;
+}
+
+// The device clock of a run from run->t_start towards `target`
+int begin_run(dgswe_handle* h, const dgswe_run_config* run, double target) {
+    double st[4][4];
+    const int n_stages = scheme_table(run->scheme, st);
+    StepCtl& c = *h->h_ctl;
+    long long clips0 = 0;
+    CK(cudaMemcpy(&clips0, &h->ctl->clips, sizeof clips0, cudaMemcpyDeviceToHost));
+    std::memset(&c, 0, sizeof c);
+    c.t = run->t_start;
+    c.t_end = run->t_end;
+    c.target = target;
+    c.dt_max = run->dt_max;
+    c.dt_min = run->dt_min;
+    c.cfl = run->cfl;
+    c.dt_min_used = INFINITY;
+    c.dt_max_used = 0.0;
+    c.dt_bits = 0x7FF0000000000000ull;
+    c.max_steps = run->max_steps > 0 ? run->max_steps : 0;
+    c.clips = clips0;
+    c.always = 1;
+    c.scheme_stages = n_stages;
+    for (int s = 0; s < n_stages; ++s) {
+        c.st_start[s] = st[s][0];
+        c.st_input[s] = st[s][1];
+        c.st_beta[s] = st[s][2];
+        c.st_c[s] = st[s][3];
+    }
+    CK(cudaMemcpyAsync(h->ctl, &c, sizeof c, cudaMemcpyHostToDevice, h->stream));
+    h->ks->velocity(h->buf[DGSWE_STATE].view, h->n_values, h->P.h_min, h->stream);
+    return sync(h);
+}
+
+int run_device_step_graph(dgswe_handle* h, int scheme, double cfl) {
+    if (h->step_graph && h->graph_scheme == scheme && h->graph_cfl == cfl) return DGSWE_OK;
+    if (h->step_graph) {
+        cudaGraphExecDestroy(h->step_graph);
+        h->step_graph = nullptr;
+    }
+    double st[4][4];
+    const int n = scheme_table(scheme, st);
+    for (int b = 1; b < n; ++b)
+        if (int s = ensure_buffer(h, b)) return s;
+    const DtParams D = dt_params(h, cfl, scheme);
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    const int* active = &h->ctl->active;
+    h->ks->step_begin(h->ctl, h->stream);
+    h->ks->dt(h->n1, h->T, h->P, h->buf[DGSWE_STATE].view, D, nullptr, h->ctl, active, h->stream);
+    h->ks->step_dt(h->ctl, h->stream);
+    for (int s = 0; s < n; ++s) {
+        const int in = s == 0 ? DGSWE_STATE : s;
+        const int out = s + 1 < n ? s + 1 : DGSWE_STATE;
+        launch_stage(h, in, DGSWE_STATE, out, DGSWE_STATE, s, kModePost, s + 1 == n, active);
+    }
+    h->ks->step_end(h->ctl, h->stream);
+    cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+    if (e != cudaSuccess) return fail(h, DGSWE_ERR_CUDA, "stream capture: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&h->step_graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(h, DGSWE_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    h->graph_scheme = scheme;
+    h->graph_cfl = cfl;
+    return DGSWE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+uint32_t dgswe_abi_version(void) { return DGSWE_ABI_VERSION; }
+
+const char* dgswe_status_string(int status) {
+    switch (status) {
+        case DGSWE_OK: return "ok";
+        case DGSWE_ERR_INVALID: return "invalid input";
+        case DGSWE_ERR_CUDA: return "CUDA error";
+        case DGSWE_ERR_NONFINITE: return "the state is not finite";
+        case DGSWE_ERR_DT_MIN: return "time step below the minimum";
+        case DGSWE_ERR_MAX_STEPS: return "step limit reached";
+        case DGSWE_ERR_STOPPED: return "stopped";
+        case DGSWE_ERR_UNSUPPORTED: return "unsupported physics";
+        case DGSWE_ERR_NO_DEVICE: return "no CUDA device";
+        default: return "unknown status";
+    }
+}
+
+const char* dgswe_last_error(const dgswe_handle* h) { return h ? h->error.c_str() : ""; }
+
+int64_t dgswe_n_values(const dgswe_handle* h) { return h ? h->n_values : 0; }
+
+int64_t dgswe_negative_depth_clips(const dgswe_handle* h) {
+    if (!h) return 0;
+    long long clips = 0;
+    if (cudaMemcpy(&clips, &h->ctl->clips, sizeof clips, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return -1;
+    return clips;
+}
+
+}  // extern "C"
+
+namespace {
+
+int create_impl(dgswe_handle* h, const dgswe_form* f, int device) {
+    auto bail = [](int s) { return s; };
+    h->device = device;
+    h->form = *f;
+    CK(cudaSetDevice(device));
+    cudaDeviceProp prop{};
+    CK(cudaGetDeviceProperties(&prop, device));
+    h->device_name = prop.name;
+    CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    h->ks = f->numerics == DGSWE_NUMERICS_EXACT ? kernels_exact() : kernels_fast();
+    h->ops = new Operators(f->order);
+    const Operators& ops = *h->ops;
+    h->n1 = ops.n1;
+    h->nn = ops.nn;
+    h->K = f->n_elements;
+    h->n_values = h->K * ops.nn;
+
+    Topology topo;
+    std::string err = build_topology(*f, topo);
+    if (!err.empty()) return bail(fail(h, DGSWE_ERR_INVALID, "%s", err.c_str()));
+    std::vector<int32_t> tags, cond_index;
+    for (int b = 0; b < f->n_boundaries; ++b) {
+        tags.push_back(f->boundaries[b].tag);
+        cond_index.push_back(b);
+    }
+    Tables t;
+    err = build_tables(*f, ops, topo, tags, cond_index, t);
+    if (!err.empty()) return bail(fail(h, DGSWE_ERR_INVALID, "%s", err.c_str()));
+    PairSchedule sched(ops);
+    std::vector<int8_t> owned;
+    for (const PairSlot& p : sched.owned) {
+        owned.push_back(p.a);
+        owned.push_back(p.c);
+        owned.push_back(p.dir);
+        owned.push_back(p.pa);
+        owned.push_back(p.pc);
+    }
+
+    DevTables& T = h->T;
+    T.K = h->K;
+    T.n_edges = (int64_t)t.edge_left.size();
+    T.n_bfaces = (int64_t)t.bface.size();
+    int s = DGSWE_OK;
+#define UP(field, vec)                          \
+    if ((s = upload_vec(h, vec, &T.field)) != 0) \
+        return bail(s);
+    UP(bed, t.bed);
+    UP(jinv, t.jinv);
+    UP(pair_hm, t.pair_hm);
+    UP(gdb, t.gdb);
+    UP(contra, t.contra);
+    UP(lift_scale, t.lift_scale);
+    UP(outer_dist, t.outer_dist);
+    UP(fcor, t.fcor);
+    UP(g_n2, t.g_n2);
+    UP(mass, t.mass);
+    UP(inv_area, t.inv_area);
+    UP(weight_ratio, t.weight_ratio);
+    UP(dtm_own, t.dtm_own);
+    UP(dtm_face, t.dtm_face);
+    UP(edge_geo, t.edge_geo);
+    UP(bface_geo, t.bface_geo);
+    UP(outer_idx, t.outer_idx);
+    UP(nb_face_node, t.nb_face_node);
+    UP(edge_left, t.edge_left);
+    UP(edge_right, t.edge_right);
+    UP(bface, t.bface);
+    UP(bface_cond, t.bface_cond);
+    UP(affine, t.affine);
+    UP(sched_owned, owned);
+    UP(sched_slot, sched.accum_slot);
+    UP(sched_coef, sched.accum_coef);
+#undef UP
+
+    Physics& P = h->P;
+    P.order = f->order;
+    P.n1 = ops.n1;
+    P.nn = ops.nn;
+    P.formulation = f->formulation;
+    P.g = f->g;
+    P.h_min = f->h_min;
+    P.subcell_depth = f->subcell_depth;
+    P.subcell_h_dry = f->subcell_h_dry;
+    P.has_bed = f->bathymetry ? 1 : 0;
+    P.has_wet_dry = f->has_wet_dry ? 1 : 0;
+    P.h_dry = f->wet_dry_h_dry;
+    P.relaxation_time = f->wet_dry_relaxation_time;
+    P.max_velocity = f->wet_dry_max_velocity;
+    P.friction = f->friction;
+    P.g_n2 = f->friction_g * f->manning_n * f->manning_n;
+    P.manning_h_min = f->manning_h_min;
+    P.has_coriolis = f->has_coriolis ? 1 : 0;
+    P.coriolis_field = t.fcor.empty() ? 0 : 1;
+    P.f0 = f->coriolis_f0;
+    P.n_conditions = f->n_boundaries;
+    for (int b = 0; b < f->n_boundaries; ++b) {
+        const dgswe_boundary& in = f->boundaries[b];
+        Condition& c = P.cond[b];
+        c.kind = in.kind;
+        c.elevation_only = in.elevation_only;
+        c.n_constituents = in.n_constituents;
+        c.wall_h_min = in.wall_h_min;
+        c.mean = in.mean_elevation;
+        c.ramp = in.ramp_duration;
+        for (int i = 0; i < in.n_constituents; ++i) {
+            const dgswe_tide_constituent& k = in.constituents[i];
+            // TidalConstituent::angular_frequency (src/boundary/tidal.rs:40-43)
+            c.c[i] = {k.amplitude, 2.0 * M_PI / k.period, k.phase, k.f,
+                      k.f_rate,    k.u_deg,                k.u_rate_deg, k.v0_deg};
+        }
+    }
+    for (int i = 0; i < ops.n1; ++i) {
+        P.x[i] = ops.x[i];
+        P.w[i] = ops.w[i];
+    }
+    for (int i = 0; i < ops.n1 * ops.n1; ++i) P.d[i] = ops.d[i];
+    for (int face = 0; face < 4; ++face)
+        for (int fi = 0; fi < ops.n1; ++fi) P.face_node[face][fi] = ops.face_node[face][fi];
+    // subcell bounds as the reference sums them (swe_2d_split_form.rs:968-990)
+    double x_left = -1.0;
+    for (int a = 0; a < ops.n1; ++a) {
+        const double x_right = x_left + ops.w[a];
+        h->X.xl[a] = x_left;
+        h->X.xr[a] = x_right;
+        h->X.inv_w[a] = 1.0 / ops.w[a];
+        x_left = x_right;
+    }
+
+    // buffers, faces, control
+    if ((s = ensure_buffer(h, DGSWE_STATE))) return bail(s);
+    const size_t nf = (size_t)h->K * 4 * ops.n1;
+    void* p = nullptr;
+    CK(cudaMalloc(&p, 3 * nf * sizeof(double)));
+    h->allocations.push_back(p);
+    CK(cudaMemset(p, 0, 3 * nf * sizeof(double)));
+    h->fb_h = (double*)p;
+    h->fb_hu = h->fb_h + nf;
+    h->fb_hv = h->fb_hu + nf;
+    CK(cudaMalloc(&p, (size_t)h->K * sizeof(double)));
+    h->allocations.push_back(p);
+    h->dt_el = (double*)p;
+    CK(cudaMalloc(&p, sizeof(StepCtl)));
+    h->allocations.push_back(p);
+    h->ctl = (StepCtl*)p;
+    CK(cudaMallocHost(&p, sizeof(StepCtl)));
+    h->h_ctl = (StepCtl*)p;
+    std::memset(h->h_ctl, 0, sizeof(StepCtl));
+    h->h_ctl->always = 1;
+    h->h_ctl->active = 1;
+    CK(cudaMemcpy(h->ctl, h->h_ctl, sizeof(StepCtl), cudaMemcpyHostToDevice));
+    h->form.vertices = nullptr;
+    h->form.elements = nullptr;
+    h->form.periodic = nullptr;
+    h->form.face_tags = nullptr;
+    h->form.bathymetry = nullptr;
+    h->form.manning_n_nodes = nullptr;
+    h->form.boundaries = nullptr;
+    return DGSWE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dgswe_create(const dgswe_form* f, int device, dgswe_handle** out) {
+    if (!out) return DGSWE_ERR_INVALID;
+    *out = nullptr;
+    std::string why;
+    dgswe_handle* h = new dgswe_handle();
+    int s = check_form(f, why);
+    if (s == DGSWE_OK) {
+        int count = 0;
+        if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0 || device < 0 ||
+            device >= count) {
+            s = DGSWE_ERR_NO_DEVICE;
+            why = "no CUDA device " + std::to_string(device);
+        }
+    }
+    if (s == DGSWE_OK) {
+        s = create_impl(h, f, device);
+    } else {
+        h->error = why;
+    }
+    // On failure the handle is still returned, so that dgswe_last_error can
+    // tell why; the caller destroys it
+    *out = h;
+    return s;
+}
+
+void dgswe_destroy(dgswe_handle* h) {
+    if (!h) return;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    delete h;
+}
+
+int dgswe_upload(dgswe_handle* h, int32_t buffer, const double* hh, const double* hu,
+                 const double* hv, int64_t n) {
+    if (!h) return DGSWE_ERR_INVALID;
+    if (!valid_buffer(buffer) || n != h->n_values || !hh || !hu || !hv)
+        return fail(h, DGSWE_ERR_INVALID, "upload: buffer %d, %lld values (expected %lld)", buffer,
+                    (long long)n, (long long)h->n_values);
+    CK(cudaSetDevice(h->device));
+    if (int s = ensure_buffer(h, buffer)) return s;
+    const DevBuf& b = h->buf[buffer].view;
+    const size_t bytes = (size_t)n * sizeof(double);
+    CK(cudaMemcpyAsync(b.h, hh, bytes, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(b.hu, hu, bytes, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(b.hv, hv, bytes, cudaMemcpyHostToDevice, h->stream));
+    h->ks->velocity(b, n, h->P.h_min, h->stream);
+    return sync(h);
+}
+
+int dgswe_download(dgswe_handle* h, int32_t buffer, double* hh, double* hu, double* hv,
+                   int64_t n) {
+    if (!h) return DGSWE_ERR_INVALID;
+    if (!valid_buffer(buffer) || n != h->n_values || !hh || !hu || !hv)
+        return fail(h, DGSWE_ERR_INVALID, "download: buffer %d, %lld values (expected %lld)",
+                    buffer, (long long)n, (long long)h->n_values);
+    CK(cudaSetDevice(h->device));
+    if (int s = ensure_buffer(h, buffer)) return s;
+    const DevBuf& b = h->buf[buffer].view;
+    const size_t bytes = (size_t)n * sizeof(double);
+    CK(cudaMemcpyAsync(hh, b.h, bytes, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(hu, b.hu, bytes, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(hv, b.hv, bytes, cudaMemcpyDeviceToHost, h->stream));
+    return sync(h);
+}
+
+int dgswe_compute_rhs(dgswe_handle* h, int32_t input, double time, double* out_h, double* out_hu,
+                      double* out_hv, int64_t n) {
+    if (!h) return DGSWE_ERR_INVALID;
+    if (!valid_buffer(input) || n != h->n_values || !out_h || !out_hu || !out_hv)
+        return fail(h, DGSWE_ERR_INVALID, "compute_rhs: buffer %d, %lld values", input,
+                    (long long)n);
+    CK(cudaSetDevice(h->device));
+    if (int s = ensure_buffer(h, input)) return s;
+    if (int s = ensure_buffer(h, kRhsBuffer)) return s;
+    if (int s = write_host_args(h, StageArgs{time, 0.0, 0.0, 1.0, 1.0, 0.0})) return s;
+    launch_stage(h, input, input, kRhsBuffer, kRhsBuffer, kHostSlot, kModeRhsOnly, 0, always(h));
+    CK(cudaGetLastError());
+    const DevBuf& b = h->buf[kRhsBuffer].view;
+    const size_t bytes = (size_t)n * sizeof(double);
+    CK(cudaMemcpyAsync(out_h, b.h, bytes, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(out_hu, b.hu, bytes, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(out_hv, b.hv, bytes, cudaMemcpyDeviceToHost, h->stream));
+    return sync(h);
+}
+
+int dgswe_stage(dgswe_handle* h, const dgswe_stage_plan* plan) {
+    if (!h) return DGSWE_ERR_INVALID;
+    if (!plan || !valid_buffer(plan->base) || !valid_buffer(plan->input) ||
+        !valid_buffer(plan->out) || (plan->accumulate && !valid_buffer(plan->acc)))
+        return fail(h, DGSWE_ERR_INVALID, "stage: invalid plan or buffer ids");
+    if (plan->out == plan->input)
+        return fail(h, DGSWE_ERR_INVALID, "stage: out must differ from input");
+    CK(cudaSetDevice(h->device));
+    for (int id : {plan->base, plan->input, plan->out})
+        if (int s = ensure_buffer(h, id)) return s;
+    const int acc = plan->accumulate ? plan->acc : plan->out;
+    if (int s = ensure_buffer(h, acc)) return s;
+    if (int s = write_host_args(h, StageArgs{plan->time, plan->a, plan->b, plan->c, plan->w,
+                                             plan->keep}))
+        return s;
+    launch_stage(h, plan->input, plan->base, plan->out, acc, kHostSlot,
+                 plan->accumulate ? kModeAccumulate : kModePost, 0, always(h));
+    if (plan->accumulate) {
+        h->ks->velocity(h->buf[plan->out].view, h->n_values, h->P.h_min, h->stream);
+        h->ks->velocity(h->buf[acc].view, h->n_values, h->P.h_min, h->stream);
+    }
+    CK(cudaGetLastError());
+    return sync(h);
+}
+
+int dgswe_finish(dgswe_handle* h, int32_t acc) {
+    if (!h) return DGSWE_ERR_INVALID;
+    if (!valid_buffer(acc) || acc == DGSWE_STATE)
+        return fail(h, DGSWE_ERR_INVALID, "finish: invalid accumulation buffer %d", acc);
+    CK(cudaSetDevice(h->device));
+    if (int s = ensure_buffer(h, acc)) return s;
+    h->ks->finish(h->n1, h->T, h->P, h->buf[acc].view, h->buf[DGSWE_STATE].view, h->ctl,
+                  h->stream);
+    CK(cudaGetLastError());
+    return sync(h);
+}
+
+int dgswe_element_dt(dgswe_handle* h, double cfl, int32_t scheme, double* dt_elements,
+                     double* dt_min) {
+    if (!h) return DGSWE_ERR_INVALID;
+    if (!(cfl > 0.0) || (scheme != DGSWE_SSP_RK3 && scheme != DGSWE_SSP_RK43))
+        return fail(h, DGSWE_ERR_INVALID, "element_dt: cfl %g, scheme %d", cfl, scheme);
+    CK(cudaSetDevice(h->device));
+    const unsigned long long inf_bits = 0x7FF0000000000000ull;
+    CK(cudaMemcpyAsync(&h->ctl->dt_bits, &inf_bits, sizeof inf_bits, cudaMemcpyHostToDevice,
+                       h->stream));
+    const DtParams D = dt_params(h, cfl, scheme);
+    h->ks->dt(h->n1, h->T, h->P, h->buf[DGSWE_STATE].view, D, h->dt_el, h->ctl, always(h),
+              h->stream);
+    CK(cudaGetLastError());
+    unsigned long long bits = 0;
+    CK(cudaMemcpyAsync(&bits, &h->ctl->dt_bits, sizeof bits, cudaMemcpyDeviceToHost, h->stream));
+    if (dt_elements)
+        CK(cudaMemcpyAsync(dt_elements, h->dt_el, (size_t)h->K * sizeof(double),
+                           cudaMemcpyDeviceToHost, h->stream));
+    if (int s = sync(h)) return s;
+    if (dt_min) std::memcpy(dt_min, &bits, sizeof(double));
+    return DGSWE_OK;
+}
+
+int dgswe_step(dgswe_handle* h, int32_t scheme, double t, double dt) {
+    if (!h) return DGSWE_ERR_INVALID;
+    if (scheme != DGSWE_SSP_RK3 && scheme != DGSWE_SSP_RK43)
+        return fail(h, DGSWE_ERR_INVALID, "step: scheme %d", scheme);
+    CK(cudaSetDevice(h->device));
+    double st[4][4];
+    const int n = scheme_table(scheme, st);
+    for (int b = 1; b < n; ++b)
+        if (int s = ensure_buffer(h, b)) return s;
+    // element_stage with one level (src/time/multirate.rs:169-200)
+    for (int s = 0; s < n; ++s)
+        h->h_ctl->stage[s] = StageArgs{t + st[s][3] * dt, st[s][0], st[s][1], st[s][2] * dt, 1.0, 0.0};
+    CK(cudaMemcpyAsync(&h->ctl->stage[0], &h->h_ctl->stage[0], n * sizeof(StageArgs),
+                       cudaMemcpyHostToDevice, h->stream));
+    for (int s = 0; s < n; ++s) {
+        const int in = s == 0 ? DGSWE_STATE : s;
+        const int out = s + 1 < n ? s + 1 : DGSWE_STATE;
+        launch_stage(h, in, DGSWE_STATE, out, DGSWE_STATE, s, kModePost, 0, always(h));
+    }
+    CK(cudaGetLastError());
+    return sync(h);
+}
+
+int dgswe_run(dgswe_handle* h, const dgswe_run_config* run, dgswe_callback callback, void* user,
+              dgswe_report* report) {
+    if (!h) return DGSWE_ERR_INVALID;
+    if (!run || !report) return fail(h, DGSWE_ERR_INVALID, "run: NULL config or report");
+    if (!(run->cfl > 0.0) || (run->scheme != DGSWE_SSP_RK3 && run->scheme != DGSWE_SSP_RK43) ||
+        !(run->t_end >= run->t_start))
+        return fail(h, DGSWE_ERR_INVALID, "run: cfl %g, scheme %d, span (%g, %g)", run->cfl,
+                    run->scheme, run->t_start, run->t_end);
+    std::memset(report, 0, sizeof(*report));
+    std::snprintf(report->device, sizeof report->device, "%s", h->device_name.c_str());
+    CK(cudaSetDevice(h->device));
+    const auto wall0 = std::chrono::steady_clock::now();
+    if (int s = run_device_step_graph(h, run->scheme, run->cfl)) return s;
+    // host copies for the callbacks
+    std::vector<double> hh, hu, hv;
+    const bool has_interval = run->interval > 0.0;
+    auto next_callback = [&](unsigned long long k) {
+        return run->t_start + (double)(k + 1) * run->interval;
+    };
+    unsigned long long callbacks_done = 0;
+    auto call = [&](double t) -> int {
+        if (!callback) return DGSWE_OK;
+        hh.resize(h->n_values);
+        hu.resize(h->n_values);
+        hv.resize(h->n_values);
+        if (int s = dgswe_download(h, DGSWE_STATE, hh.data(), hu.data(), hv.data(), h->n_values))
+            return s;
+        callback(user, t, hh.data(), hu.data(), hv.data(), h->n_values);
+        return DGSWE_OK;
+    };
+
+    StepCtl& c = *h->h_ctl;
+    const double first_target = has_interval ? std::fmin(next_callback(0), run->t_end) : run->t_end;
+    if (int s = begin_run(h, run, first_target)) return s;
+
+    auto finish = [&](int status, const char* msg) {
+        report->success = status == DGSWE_OK;
+        report->final_time = c.t;
+        report->n_steps = c.steps;
+        report->dt_min_used = c.dt_min_used;
+        report->dt_max_used = c.dt_max_used;
+        report->negative_depth_clips = c.clips;
+        report->wall_time =
+            std::chrono::duration<double>(std::chrono::steady_clock::now() - wall0).count();
+        std::snprintf(report->message, sizeof report->message, "%s", msg);
+        if (status != DGSWE_OK) h->error = msg;
+        return status;
+    };
+    if (int s = call(c.t)) return s;
+    // steps launched between host checks: one when the host acts after
+    // every step (callbacks every step, a stop flag)
+    const int chunk = (!has_interval || run->stop) ? 1 : 4;
+    char msg[256];
+    while (c.t < run->t_end) {
+        if (run->stop && *run->stop) {
+            std::snprintf(msg, sizeof msg, "Stopped at t = %.1f s", c.t);
+            return finish(DGSWE_ERR_STOPPED, msg);
+        }
+        for (int i = 0; i < chunk; ++i) CK(cudaGraphLaunch(h->step_graph, h->stream));
+        CK(cudaMemcpyAsync(&c, h->ctl, sizeof c, cudaMemcpyDeviceToHost, h->stream));
+        if (int s = sync(h)) return s;
+        if (c.failure == 3) {
+            std::snprintf(msg, sizeof msg, "The state is not finite at t = %.1f s: it has blown up",
+                          c.t);
+            return finish(DGSWE_ERR_NONFINITE, msg);
+        }
+        if (c.failure == 4) {
+            std::snprintf(msg, sizeof msg, "Time step (%.2e) below minimum (%.2e)", c.dt,
+                          run->dt_min);
+            return finish(DGSWE_ERR_DT_MIN, msg);
+        }
+        if (c.failure == 5) {
+            std::snprintf(msg, sizeof msg, "Maximum step limit (%lld) reached",
+                          (long long)run->max_steps);
+            return finish(DGSWE_ERR_MAX_STEPS, msg);
+        }
+        if (has_interval) {
+            if (c.t >= next_callback(callbacks_done)) {
+                if (int s = call(c.t)) return s;
+                callbacks_done += 1;
+                c.target = std::fmin(next_callback(callbacks_done), run->t_end);
+                CK(cudaMemcpyAsync(&h->ctl->target, &c.target, sizeof c.target,
+                                   cudaMemcpyHostToDevice, h->stream));
+                if (int s = sync(h)) return s;
+            }
+        } else {
+            if (int s = call(c.t)) return s;
+        }
+    }
+    return finish(DGSWE_OK, "");
+}
+
+int dgswe_profile_steps(dgswe_handle* h, const dgswe_run_config* run, int64_t n_steps,
+                        dgswe_profile* out) {
+    if (!h) return DGSWE_ERR_INVALID;
+    if (!run || !out || n_steps <= 0 || !(run->cfl > 0.0) ||
+        (run->scheme != DGSWE_SSP_RK3 && run->scheme != DGSWE_SSP_RK43))
+        return fail(h, DGSWE_ERR_INVALID, "profile_steps: invalid arguments");
+    CK(cudaSetDevice(h->device));
+    std::memset(out, 0, sizeof(*out));
+    double st[4][4];
+    const int n = scheme_table(run->scheme, st);
+    for (int b = 1; b < n; ++b)
+        if (int s = ensure_buffer(h, b)) return s;
+    if (int s = begin_run(h, run, INFINITY)) return s;
+    const DtParams D = dt_params(h, run->cfl, run->scheme);
+    const int* active = &h->ctl->active;
+    // per step: begin, dt, fit, n × (face, stage), end → 4 + 2n kernels
+    const int per_step = 4 + 2 * n;
+    std::vector<cudaEvent_t> ev((size_t)n_steps * (per_step + 1));
+    for (auto& e : ev) CK(cudaEventCreate(&e));
+    auto cleanup = [&]() {
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
+    };
+    size_t q = 0;
+    for (int64_t step = 0; step < n_steps; ++step) {
+        CK(cudaEventRecord(ev[q++], h->stream));
+        h->ks->step_begin(h->ctl, h->stream);
+        CK(cudaEventRecord(ev[q++], h->stream));
+        h->ks->dt(h->n1, h->T, h->P, h->buf[DGSWE_STATE].view, D, nullptr, h->ctl, active,
+                  h->stream);
+        CK(cudaEventRecord(ev[q++], h->stream));
+        h->ks->step_dt(h->ctl, h->stream);
+        CK(cudaEventRecord(ev[q++], h->stream));
+        for (int s = 0; s < n; ++s) {
+            const int in = s == 0 ? DGSWE_STATE : s;
+            const int o = s + 1 < n ? s + 1 : DGSWE_STATE;
+            h->ks->face(h->n1, h->T, h->P, h->buf[in].view, h->fb_h, h->fb_hu, h->fb_hv, h->ctl, s,
+                        active, h->stream);
+            CK(cudaEventRecord(ev[q++], h->stream));
+            h->ks->stage(h->n1, h->T, h->P, h->X, h->buf[in].view, h->buf[DGSWE_STATE].view,
+                         h->buf[o].view, h->buf[DGSWE_STATE].view, h->fb_h, h->fb_hu, h->fb_hv,
+                         h->ctl, s, kModePost, s + 1 == n, active, h->stream);
+            CK(cudaEventRecord(ev[q++], h->stream));
+        }
+        h->ks->step_end(h->ctl, h->stream);
+    }
+    const size_t last = q;
+    CK(cudaEventRecord(ev[q++], h->stream));
+    CK(cudaGetLastError());
+    if (int s = sync(h)) {
+        cleanup();
+        return s;
+    }
+    auto ms = [&](size_t a, size_t b) {
+        float v = 0.0f;
+        cudaEventElapsedTime(&v, ev[a], ev[b]);
+        return (double)v;
+    };
+    q = 0;
+    for (int64_t step = 0; step < n_steps; ++step) {
+        const size_t s0 = q;
+        out->control_ms += ms(s0, s0 + 1);  // begin
+        out->dt_ms += ms(s0 + 1, s0 + 2);
+        out->control_ms += ms(s0 + 2, s0 + 3);  // fit
+        size_t e = s0 + 3;
+        for (int s = 0; s < n; ++s) {
+            out->face_ms += ms(e, e + 1);
+            out->stage_ms += ms(e + 1, e + 2);
+            e += 2;
+        }
+        out->control_ms += ms(e, e + 1);  // end (to the next step's first event)
+        q = e + 1;
+    }
+    out->total_ms = ms(0, last);
+    out->steps = n_steps;
+    out->face_launches = n_steps * n;
+    out->stage_launches = n_steps * n;
+    out->dt_launches = n_steps;
+    out->control_launches = n_steps * 3;
+    StepCtl c{};
+    CK(cudaMemcpy(&c, h->ctl, sizeof c, cudaMemcpyDeviceToHost));
+    out->t_final = c.t;
+    cleanup();
+    if (c.failure) return fail(h, DGSWE_ERR_NONFINITE, "profile_steps: the run failed (%d)", c.failure);
+    return DGSWE_OK;
+}
+
+}  // extern "C"

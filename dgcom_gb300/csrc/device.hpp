@@ -1,0 +1,107 @@
+// Device-side data of a dgswe handle shared by the host runtime and the
+// kernel translation units: table pointers, physics constants, stage
+// arguments and the step control block. Plain structs, passed to kernels by
+// value.
+#pragma once
+
+#include <cstdint>
+
+namespace dgswe {
+
+constexpr int kMaxConstituents = 8;
+constexpr int kMaxConditions = 8;
+constexpr int kMaxStages = 4;
+// stage argument slots: 0..3 the device-driven step's stages, 4 host calls
+constexpr int kHostSlot = 4;
+constexpr int kArgSlots = 5;
+
+struct DevBuf {
+    double *h, *hu, *hv;  // conserved
+    double *u, *v;        // node velocity (hu, hv)/h, 0 at h ≤ h_min
+};
+
+struct DevTables {
+    int64_t K = 0;
+    int64_t n_edges = 0, n_bfaces = 0;
+    const double *bed, *jinv, *pair_hm, *gdb, *contra, *lift_scale, *outer_dist;
+    const double *fcor, *g_n2, *mass, *inv_area, *weight_ratio, *dtm_own, *dtm_face;
+    const double *edge_geo, *bface_geo;
+    const int64_t *outer_idx, *nb_face_node, *edge_left, *edge_right, *bface;
+    const int32_t* bface_cond;
+    const uint8_t* affine;
+    // order-N schedule: owned pairs (a, c, dir, pa, pc as int8 x5) and the
+    // accumulation (slot, coefficient) of every node
+    const int8_t* sched_owned;  // [nn][n1-1][5]
+    const int32_t* sched_slot;  // [nn][2(n1-1)]
+    const double* sched_coef;   // [nn][2(n1-1)]
+};
+
+struct Constituent {
+    double amplitude, omega, phase, f, f_rate, u_deg, u_rate_deg, v0_deg;
+};
+
+struct Condition {
+    int kind;
+    int elevation_only;
+    int n_constituents;
+    double wall_h_min;
+    double mean, ramp;
+    Constituent c[kMaxConstituents];
+};
+
+struct Physics {
+    int order, n1, nn;
+    int formulation;
+    double g, h_min;
+    double subcell_depth, subcell_h_dry;
+    int has_bed;
+    int has_wet_dry;
+    double h_dry, relaxation_time, max_velocity;
+    int friction;  // 0 none, 1 uniform, 2 per node
+    double g_n2, manning_h_min;
+    int has_coriolis, coriolis_field;
+    double f0;
+    int n_conditions;
+    Condition cond[kMaxConditions];
+    double x[5], w[5], d[25];  // GLL nodes, weights, D
+    int face_node[4][5];
+};
+
+// Subcell bounds x_l, x_r of each GLL subcell (sums of the weights from
+// −1, in order) and the reciprocal weights
+struct StageExtra {
+    double xl[5], xr[5], inv_w[5];
+};
+
+// The element step's parameters: the CFL and the positivity bound of a
+// wet/dry run (PositivityBound, src/solver/rhs/swe_2d.rs:2165-2212)
+struct DtParams {
+    double cfl;
+    double bound_cfl, max_cfl, max_cfl_subcells, shallow;
+    int positivity;
+};
+
+struct StageArgs {
+    double time, a, b, c, w, keep;
+};
+
+// Step control (device memory): the run's clock, the step's dt and stage
+// arguments, and the failure flags. Written by the step kernels of a
+// device-driven run or by the host between host-driven calls.
+struct StepCtl {
+    StageArgs stage[kArgSlots];
+    double t, dt, target, t_end;
+    double dt_max, dt_min, cfl;
+    double dt_min_used, dt_max_used;
+    unsigned long long dt_bits;  // atomicMin of the element steps
+    long long steps, max_steps, clips;
+    int active;     // the current step runs
+    int landed;
+    int nonfinite;  // the state stopped being finite
+    int failure;    // 0, or the dgswe_status that stopped the run
+    int always;     // 1: a flag host-driven calls point kernels at
+    int scheme_stages;
+    double st_start[kMaxStages], st_input[kMaxStages], st_beta[kMaxStages], st_c[kMaxStages];
+};
+
+}  // namespace dgswe

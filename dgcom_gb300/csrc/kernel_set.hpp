@@ -1,0 +1,37 @@
+// The launchers of one numerics variant of the kernels, as a table the
+// host runtime picks from at dgswe_create.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "device.hpp"
+
+namespace dgswe {
+
+struct KernelSet {
+    void (*face)(int n1, const DevTables&, const Physics&, const DevBuf& in, double* fh,
+                 double* fhu, double* fhv, const StepCtl* ctl, int slot, const int* active,
+                 cudaStream_t);
+    void (*stage)(int n1, const DevTables&, const Physics&, const StageExtra&, const DevBuf& in,
+                  const DevBuf& base, const DevBuf& out, const DevBuf& acc, const double* fh,
+                  const double* fhu, const double* fhv, StepCtl* ctl, int slot, int mode,
+                  int check_finite, const int* active, cudaStream_t);
+    void (*finish)(int n1, const DevTables&, const Physics&, const DevBuf& acc,
+                   const DevBuf& state, StepCtl* ctl, cudaStream_t);
+    void (*dt)(int n1, const DevTables&, const Physics&, const DevBuf& q, const DtParams&,
+               double* dt_el, StepCtl* ctl, const int* active, cudaStream_t);
+    void (*velocity)(const DevBuf&, int64_t n, double h_min, cudaStream_t);
+    void (*step_begin)(StepCtl*, cudaStream_t);
+    void (*step_dt)(StepCtl*, cudaStream_t);
+    void (*step_end)(StepCtl*, cudaStream_t);
+};
+
+// kernels_fast.cu: FMA contraction, division-free Manning rate
+const KernelSet* kernels_fast();
+// kernels_exact.cu: every operation separately rounded, the reference's cube root
+const KernelSet* kernels_exact();
+
+// stage modes of the stage kernel
+enum { kModeRhsOnly = 0, kModePost = 1, kModeAccumulate = 2 };
+
+}  // namespace dgswe

@@ -1,0 +1,1169 @@
+// The sm_103a kernels of the FP64 2D shallow-water split-form stage.
+//
+// This file is compiled twice (kernels_fast.cu, kernels_exact.cu) into two
+// namespaces: DGSWE_FAST = 1 lets the compiler contract multiply-adds into
+// FMA (-fmad=true) and evaluates the Manning rate without divisions; 0 keeps
+// every multiply and add separately rounded (-fmad=false) and follows the
+// reference's arithmetic, its cube root included. Both are FP64 throughout.
+//
+// Kernels of one stage (one RK stage of every element):
+//  - face_kernel: the numerical flux F* of every interior edge node once,
+//    from the edge's left side with that side's normal (the reference's
+//    edge_fluxes, src/solver/rhs/swe_2d_split_form.rs:580-616), and of every
+//    boundary face node (wall or characteristic open boundary), scaled by
+//    each side's sJ·LIFT and stored per element face node;
+//  - stage_kernel<N1>: per element, the split-form volume term (flux
+//    differencing on wet elements, subcell finite volumes on elements with a
+//    node shallower than the subcell depth), the lifted face fluxes, 1/J,
+//    Coriolis, the Shu–Osher combination, the point-implicit damping and the
+//    wet/dry correction or the accumulation (the reference's fused
+//    stage_where, src/physics/builder.rs:652-737), and the node velocities
+//    the next stage reads.
+// Per step: dt_kernel<N1> (element steps, atomic minimum) and three
+// one-thread kernels that run the step's clock on the device, so that a
+// whole step is one CUDA graph.
+//
+// The volume and surface terms use the summation-by-parts identity of the
+// GLL operators: at a line end the volume term's 2·D₀₀·F(q)·Ja and the
+// surface term's LIFT·sJ·F(q)·n are equal and opposite (2D₀₀ = −1/w₀,
+// LIFT = 1/w₀ on the face node, sJ·n = −Ja), so neither is evaluated: the
+// interior diagonal of D is zero, and what remains is the pair fluxes and
+// −LIFT·sJ·F*. The same holds for the subcells' end fluxes. The result
+// differs from the reference's by rounding only.
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "device.hpp"
+
+namespace dgswe {
+namespace DGSWE_NS {
+
+constexpr int kWetDry = 0, kEntropyStable = 1, kEntropyConservative = 2;
+constexpr int kBcWall = 0;
+constexpr int kIncomingWave = 1;
+enum StageMode { kRhsOnly = 0, kPost = 1, kAccumulate = 2 };
+
+// ---------------------------------------------------------------------------
+// arithmetic
+
+__device__ __forceinline__ double lmax(double a, double b) { return a > b ? a : b; }
+__device__ __forceinline__ double lmin(double a, double b) { return a < b ? a : b; }
+
+struct Q {
+    double h, hu, hv, u, v, b;
+};
+struct Sd {
+    double h, u, v, b;
+};
+struct F3 {
+    double h, hu, hv;
+};
+
+__device__ __forceinline__ Sd side(const Q& q) { return {q.h, q.u, q.v, q.b}; }
+
+// node velocity (src/flux/swe_2d_entropy.rs:106-116)
+__device__ __forceinline__ void node_velocity(double h, double hu, double hv, double h_min,
+                                              double& u, double& v) {
+    const bool wet = h > h_min;
+    const double inv_h = 1.0 / h;
+    u = wet ? hu * inv_h : 0.0;
+    v = wet ? hv * inv_h : 0.0;
+}
+
+// Two-point flux F#(q_l, q_r)·m (src/flux/swe_2d_entropy.rs:140-160)
+__device__ __forceinline__ F3 wflux(const Q& l, const Q& r, double m0, double m1, double g) {
+    const double mass = 0.5 * ((l.hu + r.hu) * m0 + (l.hv + r.hv) * m1);
+    const double pressure = (0.5 * g) * (l.h * r.h);
+    const double u_avg = 0.5 * (l.u + r.u), v_avg = 0.5 * (l.v + r.v);
+    return {mass, mass * u_avg + pressure * m0, mass * v_avg + pressure * m1};
+}
+
+// HLL in face-aligned components with Einfeldt speeds
+// (src/flux/swe_2d.rs:277-375); l/r: depth, normal and tangential momentum,
+// and the velocities (zero on a dry side)
+__device__ __forceinline__ F3 hll_aligned(double h_l, double hun_l, double hut_l, double un_l,
+                                          double ut_l, double h_r, double hun_r, double hut_r,
+                                          double un_r, double ut_r, double g, double sqrt_g,
+                                          double h_min) {
+    const bool dry = (h_l <= h_min) && (h_r <= h_min);
+    const double sh_l = sqrt(lmax(h_l, 0.0)), sh_r = sqrt(lmax(h_r, 0.0));
+    const double c_l = sqrt_g * sh_l, c_r = sqrt_g * sh_r;
+    const bool roe = (sh_l + sh_r) > 1e-10;
+    const double h_roe = 0.5 * (h_l + h_r);
+    const double un_roe = roe ? (sh_l * un_l + sh_r * un_r) / (sh_l + sh_r) : 0.0;
+    const double c_roe = roe ? sqrt(g * h_roe) : 0.0;
+    const double s_l = h_l > h_min ? lmin(un_l - c_l, un_roe - c_roe) : un_r - 2.0 * c_r;
+    const double s_r = h_r > h_min ? lmax(un_r + c_r, un_roe + c_roe) : un_l + 2.0 * c_l;
+    const double half_g = 0.5 * g;
+    const double fl_h = h_l * un_l, fl_hu = h_l * un_l * un_l + half_g * h_l * h_l,
+                 fl_hv = h_l * un_l * ut_l;
+    const double fr_h = h_r * un_r, fr_hu = h_r * un_r * un_r + half_g * h_r * h_r,
+                 fr_hv = h_r * un_r * ut_r;
+    const double inv_ds = 1.0 / (s_r - s_l);
+    const double s_lr = s_l * s_r;
+    const double st_h = inv_ds * (s_r * fl_h - s_l * fr_h + s_lr * (h_r - h_l));
+    const double st_hu = inv_ds * (s_r * fl_hu - s_l * fr_hu + s_lr * (hun_r - hun_l));
+    const double st_hv = inv_ds * (s_r * fl_hv - s_l * fr_hv + s_lr * (hut_r - hut_l));
+    const bool from_l = s_l >= 0.0, from_r = s_r <= 0.0;
+    F3 f;
+    f.h = dry ? 0.0 : (from_l ? fl_h : (from_r ? fr_h : st_h));
+    f.hu = dry ? 0.0 : (from_l ? fl_hu : (from_r ? fr_hu : st_hu));
+    f.hv = dry ? 0.0 : (from_l ? fl_hv : (from_r ? fr_hv : st_hv));
+    return f;
+}
+
+// wall_ram_pressure (src/solver/rhs/swe_2d_split_form.rs:147-156)
+__device__ __forceinline__ double wall_ram(double h, double un, double sill, double g) {
+    un = lmax(un, 0.0);
+    const double head = un * un * (0.5 / g);
+    const double ram = (1.0 - head / sill) * h * un * (2.0 * un + sqrt(g * h));
+    return sill > head ? ram : 0.0;
+}
+
+// hydrostatic_hll (src/solver/rhs/swe_2d_split_form.rs:336-402) along m with
+// |m| = norm and m/|m| = (nx, ny): the flux seen from side a and from side b
+__device__ __forceinline__ void hydro_hll(const Sd& qa, const Sd& qb, double m0, double m1,
+                                          double norm, double nx, double ny, double g,
+                                          double sqrt_g, double h_min, F3& fa, F3& fb) {
+    const double b_face = lmax(qa.b, qb.b);
+    const double hs_a = lmax(qa.h + qa.b - b_face, 0.0);
+    const double hs_b = lmax(qb.h + qb.b - b_face, 0.0);
+    const bool wet_a = qa.h > h_min, wet_b = qb.h > h_min;
+    const double ua = wet_a ? qa.u : 0.0, va = wet_a ? qa.v : 0.0;
+    const double ub = wet_b ? qb.u : 0.0, vb = wet_b ? qb.v : 0.0;
+    const double un_a = ua * nx + va * ny, ut_a = -ua * ny + va * nx;
+    const double un_b = ub * nx + vb * ny, ut_b = -ub * ny + vb * nx;
+    const bool sw_a = hs_a > h_min, sw_b = hs_b > h_min;
+    const F3 r = hll_aligned(hs_a, hs_a * un_a, hs_a * ut_a, sw_a ? un_a : 0.0, sw_a ? ut_a : 0.0,
+                             hs_b, hs_b * un_b, hs_b * ut_b, sw_b ? un_b : 0.0, sw_b ? ut_b : 0.0,
+                             g, sqrt_g, h_min);
+    // rotate back (src/flux/swe_2d.rs:38-44), times |m|
+    const double f_h = norm * r.h;
+    const double f_hu = norm * (r.hu * nx - r.hv * ny);
+    const double f_hv = norm * (r.hu * ny + r.hv * nx);
+    const bool hll_dry = (hs_a <= h_min) && (hs_b <= h_min);
+    const double hsa = hll_dry ? 0.0 : hs_a, hsb = hll_dry ? 0.0 : hs_b;
+    double wall_a = 0.0, wall_b = 0.0;
+    if (hll_dry) {
+        if (qa.h > h_min) wall_a = wall_ram(qa.h, qa.u * nx + qa.v * ny, b_face - (qa.h + qa.b), g);
+        if (qb.h > h_min)
+            wall_b = wall_ram(qb.h, -1.0 * (qb.u * nx + qb.v * ny), b_face - (qb.h + qb.b), g);
+    }
+    const double half_g = 0.5 * g;
+    const double dp_a = half_g * (qa.h * qa.h - hsa * hsa) + wall_a;
+    const double dp_b = half_g * (qb.h * qb.h - hsb * hsb) + wall_b;
+    fa = {f_h, f_hu + dp_a * m0, f_hv + dp_a * m1};
+    fb = {f_h, f_hu + dp_b * m0, f_hv + dp_b * m1};
+}
+
+// ---------------------------------------------------------------------------
+// face kernel
+
+// HarmonicTide::elevation (src/boundary/harmonic_tide.rs:124-136)
+__device__ double tide_elevation(const Condition& c, double t) {
+    double tide = 0.0;
+    for (int i = 0; i < c.n_constituents; ++i) {
+        const Constituent& k = c.c[i];
+        const double f = k.f + k.f_rate * t;
+        const double u_deg = k.u_deg + k.u_rate_deg * t;
+        const double offset = (k.v0_deg + u_deg) * (M_PI / 180.0);
+        tide += f * k.amplitude * cos(k.omega * t + k.phase + offset);
+    }
+    double ramp = 1.0;
+    if (c.ramp > 0.0) {
+        double tau = t / c.ramp;
+        tau = tau < 0.0 ? 0.0 : (tau > 1.0 ? 1.0 : tau);
+        ramp = tau * tau * (3.0 - 2.0 * tau);
+    }
+    return c.mean + ramp * tide;
+}
+
+__device__ __forceinline__ Q load_q(const DevBuf& in, const DevTables& T, const Physics& P,
+                                    int64_t g) {
+    Q q;
+    q.h = in.h[g];
+    q.hu = in.hu[g];
+    q.hv = in.hv[g];
+    q.u = in.u[g];
+    q.v = in.v[g];
+    q.b = P.has_bed ? T.bed[g] : 0.0;
+    return q;
+}
+
+// The interface flux of the other split forms (EntropyStable / EntropyConservative):
+// F#·n (+ dissipation) with the bed interface term per side
+// (src/solver/rhs/swe_2d_split_form.rs:639-650, src/flux/swe_2d_entropy.rs:166-205)
+__device__ void entropy_surface(const Q& qa, const Q& qb, double nx, double ny, const Physics& P,
+                                F3& fa, F3& fb) {
+    const double g = P.g;
+    F3 s = wflux(qa, qb, nx, ny, g);
+    if (P.formulation == kEntropyStable) {
+        const double sp_i = fabs(qa.u * nx + qa.v * ny) + sqrt(g * fmax(qa.h, 0.0));
+        const double sp_e = fabs(qb.u * nx + qb.v * ny) + sqrt(g * fmax(qb.h, 0.0));
+        const double scale = -0.5 * fmax(sp_i, sp_e);
+        const double jump = (qb.h + qb.b) - (qa.h + qa.b);
+        const double h_avg = 0.5 * (qa.h + qb.h), u_avg = 0.5 * (qa.u + qb.u),
+                     v_avg = 0.5 * (qa.v + qb.v);
+        s.h = s.h + scale * jump;
+        s.hu = s.hu + scale * (u_avg * jump + h_avg * (qb.u - qa.u));
+        s.hv = s.hv + scale * (v_avg * jump + h_avg * (qb.v - qa.v));
+    }
+    const double fa_b = 0.5 * g * qa.h * (qb.b - qa.b);
+    const double fb_b = 0.5 * g * qb.h * (qa.b - qb.b);
+    fa = {s.h + 0.0, s.hu + fa_b * nx, s.hv + fa_b * ny};
+    fb = {-s.h + 0.0, -s.hu + fb_b * (-nx), -s.hv + fb_b * (-ny)};
+}
+
+template <int N1>
+__global__ void __launch_bounds__(256) face_kernel(DevTables T, Physics P, DevBuf in, double* fb_h,
+                                                   double* fb_hu, double* fb_hv,
+                                                   const StepCtl* ctl, int slot,
+                                                   const int* active) {
+    if (!*active) return;
+    const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t n_int = T.n_edges * N1;
+    if (item >= n_int + T.n_bfaces * N1) return;
+    constexpr int NN = N1 * N1;
+    const double g = P.g, h_min = P.h_min, sqrt_g = sqrt(P.g);
+    if (item < n_int) {
+        const int64_t e = item / N1;
+        const int fi = (int)(item % N1);
+        const int64_t L = T.edge_left[e], R = T.edge_right[e];
+        const int64_t kl = L >> 2, kr = R >> 2;
+        const int fl = (int)(L & 3), fr = (int)(R & 3);
+        const int rfi = N1 - 1 - fi;
+        const int nl = P.face_node[fl][fi], nr = P.face_node[fr][rfi];
+        const Q ql = load_q(in, T, P, kl * NN + nl), qr = load_q(in, T, P, kr * NN + nr);
+        const double* geo = &T.edge_geo[e * 5];
+        F3 fa, fbb;
+        if (P.formulation == kWetDry) {
+            hydro_hll(side(ql), side(qr), geo[0], geo[1], geo[2], geo[3], geo[4], g, sqrt_g, h_min,
+                      fa, fbb);
+            fbb = {-fbb.h, -fbb.hu, -fbb.hv};
+        } else {
+            entropy_surface(ql, qr, geo[0], geo[1], P, fa, fbb);
+        }
+        const int64_t sl = (L * N1) + fi, sr = (R * N1) + rfi;
+        const double cl = T.lift_scale[sl], cr = T.lift_scale[sr];
+        fb_h[sl] = cl * fa.h;
+        fb_hu[sl] = cl * fa.hu;
+        fb_hv[sl] = cl * fa.hv;
+        fb_h[sr] = cr * fbb.h;
+        fb_hu[sr] = cr * fbb.hu;
+        fb_hv[sr] = cr * fbb.hv;
+        return;
+    }
+    // boundary face node (src/solver/rhs/swe_2d_split_form.rs:1090-1123)
+    const int64_t bfi = (item - n_int) / N1;
+    const int fi = (int)((item - n_int) % N1);
+    const int64_t B = T.bface[bfi];
+    const int64_t k = B >> 2;
+    const int face = (int)(B & 3);
+    const int node = P.face_node[face][fi];
+    const Q qi = load_q(in, T, P, k * NN + node);
+    const double* geo = &T.bface_geo[bfi * 5];
+    const double nx = geo[0], ny = geo[1];
+    const Condition& c = P.cond[T.bface_cond[bfi]];
+    F3 fs;
+    // the interior velocity of BCContext2D (velocity_simple)
+    double u = 0.0, v = 0.0;
+    if (qi.h > h_min) {
+        const double inv = 1.0 / qi.h;
+        u = qi.hu * inv;
+        v = qi.hv * inv;
+    }
+    if (c.kind == kBcWall) {
+        // Reflective2D mirror ghost (src/boundary/boundary_2d.rs:271-283)
+        double gh = qi.h, ghu = 0.0, ghv = 0.0;
+        if (!(qi.h <= c.wall_h_min)) {
+            const double un = u * nx + v * ny;
+            ghu = qi.h * (u - 2.0 * un * nx);
+            ghv = qi.h * (v - 2.0 * un * ny);
+        }
+        Q qe;
+        qe.h = gh;
+        qe.hu = ghu;
+        qe.hv = ghv;
+        qe.b = qi.b;
+        node_velocity(gh, ghu, ghv, h_min, qe.u, qe.v);
+        F3 fdummy;
+        if (P.formulation == kWetDry)
+            hydro_hll(side(qi), side(qe), nx, ny, geo[2], geo[3], geo[4], g, sqrt_g, h_min, fs,
+                      fdummy);
+        else
+            entropy_surface(qi, qe, nx, ny, P, fs, fdummy);
+    } else {
+        // CharacteristicOBC with a uniform harmonic tide
+        // (src/boundary/characteristic.rs:411-437, 481-520)
+        const double eta = tide_elevation(c, ctl->stage[slot].time);
+        const double bathy = qi.b;
+        const double h_e = fmax(eta - bathy, 0.0);
+        double un_e = 0.0;
+        if (c.elevation_only == kIncomingWave)
+            un_e = 2.0 * (sqrt(g * fmax(-bathy, 0.0)) - sqrt(g * h_e));
+        const double ut_e = -u * ny + v * nx;
+        const double h_i = fmax(qi.h, 0.0);
+        double un_i = 0.0, ut_i = 0.0;
+        if (h_i > h_min) {
+            const double ui = qi.hu / h_i, vi = qi.hv / h_i;
+            un_i = ui * nx + vi * ny;
+            ut_i = -ui * ny + vi * nx;
+        }
+        const double c_i = sqrt(g * h_i), c_e = sqrt(g * h_e);
+        const double w_out = un_i + 2.0 * c_i, w_in = un_e - 2.0 * c_e;
+        const bool wi = h_i > h_min, we = h_e > h_min;
+        double h_b, un_b;
+        if (!wi && !we) {
+            h_b = 0.0;
+            un_b = 0.0;
+        } else if (wi && un_i >= c_i) {
+            h_b = h_i;
+            un_b = un_i;
+        } else if (we && un_e <= -c_e) {
+            h_b = h_e;
+            un_b = un_e;
+        } else if (wi && !we) {
+            const double cc = fmax(w_out / 3.0, 0.0);
+            h_b = cc * cc / g;
+            un_b = cc;
+        } else if (!wi && we) {
+            const double cc = fmax(-w_in / 3.0, 0.0);
+            h_b = cc * cc / g;
+            un_b = -cc;
+        } else {
+            const double cc = fmax(0.25 * (w_out - w_in), 0.0);
+            h_b = cc * cc / g;
+            un_b = 0.5 * (w_out + w_in);
+        }
+        const double ut_b = un_b > 0.0 ? ut_i : ut_e;
+        const double ub = un_b * nx - ut_b * ny, vb = un_b * ny + ut_b * nx;
+        Q qb;
+        qb.h = h_b;
+        qb.hu = h_b * ub;
+        qb.hv = h_b * vb;
+        qb.b = qi.b;
+        node_velocity(qb.h, qb.hu, qb.hv, h_min, qb.u, qb.v);
+        fs = wflux(qb, qb, nx, ny, g);  // F(q_b)·n
+    }
+    const int64_t sl = B * N1 + fi;
+    const double cl = T.lift_scale[sl];
+    fb_h[sl] = cl * fs.h;
+    fb_hu[sl] = cl * fs.hu;
+    fb_hv[sl] = cl * fs.hv;
+}
+
+// ---------------------------------------------------------------------------
+// damping and the wet/dry correction
+
+// The reference's cube root (src/source/swe_2d/friction.rs:39-70)
+__device__ __forceinline__ double ref_cbrt(double x) {
+    if (!(x >= 2.2250738585072014e-308 && x <= 1.7976931348623157e308)) return cbrt(x);
+    unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    double y = __longlong_as_double((long long)(bits / 3ull + 0x2A9F7893782DA1CEull));
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const double y3 = y * y * y;
+        y += y * ((x - y3) / (2.0 * y3 + x));
+    }
+    return y;
+}
+
+// Manning's rate g n² |u| / h^{4/3} at a floored depth h
+__device__ __forceinline__ double manning_rate(double g_n2, double h, double speed) {
+#if DGSWE_FAST
+    // h^{-1/3} by Newton steps z ← z + z(1 − h z³)/3 from a single-precision
+    // seed; then the rate is g n² |u| z⁴, no division
+    double z = (double)rcbrtf((float)h);
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        const double e = 1.0 - h * (z * z * z);
+        z = z + z * e * (1.0 / 3.0);
+    }
+    const double z2 = z * z;
+    return g_n2 * speed * (z2 * z2);
+#else
+    return g_n2 * speed / (ref_cbrt(h) * h);
+#endif
+}
+
+struct DampIn {
+    double h, hu, hv, u, v;  // the RHS input (u, v: node velocity)
+};
+
+// damp_node (src/solver/algorithms/wetting_drying.rs:324-357)
+__device__ __forceinline__ void damp(const Physics& P, double g_n2, double h, double& hu,
+                                     double& hv, const DampIn& from, double dt) {
+    if (h <= 0.0) {
+        hu = 0.0;
+        hv = 0.0;
+        return;
+    }
+    double rate = 0.0;
+    if (P.friction) {
+        double u, v;
+        if (P.has_wet_dry) {
+            // desingularized_velocity (wetting_drying.rs:115-130): the node
+            // velocity where h ≥ h_dry (> h_min)
+            if (from.h <= 0.0) {
+                u = v = 0.0;
+            } else if (from.h >= P.h_dry) {
+                if (P.h_dry > P.h_min) {
+                    u = from.u;
+                    v = from.v;
+                } else {
+                    const double inv = 1.0 / from.h;
+                    u = from.hu * inv;
+                    v = from.hv * inv;
+                }
+            } else {
+                const double r = from.h / P.h_dry;
+                const double factor =
+                    1.4142135623730951 * r / (P.h_dry * sqrt(1.0 + r * r * r * r));
+                u = factor * from.hu;
+                v = factor * from.hv;
+            }
+        } else {
+            // SWEState2D::velocity (src/solver/state/swe_2d.rs:54-61)
+            const double h_reg = fmax(from.h, P.h_min);
+            const double inv_d = 1.0 / (from.h * from.h + h_reg * h_reg);
+            const double factor = 2.0 * from.h * inv_d;
+            u = from.hu * factor;
+            v = from.hv * factor;
+        }
+        const double speed = sqrt(u * u + v * v);
+        if (speed > 0.0) rate += manning_rate(g_n2, fmax(h, P.manning_h_min), speed);
+    }
+    if (P.has_wet_dry && h < P.h_dry) {
+        // thin_layer_rate (wetting_drying.rs:135-146); h > 0 here
+        const double excess = P.h_dry / h - 1.0;
+        rate += excess * excess / P.relaxation_time;
+    }
+    const double factor = 1.0 / (1.0 + dt * rate);
+    hu *= factor;
+    hv *= factor;
+}
+
+// correct_node (src/solver/algorithms/wetting_drying.rs:148-165)
+__device__ __forceinline__ void correct_node(const Physics& P, double h, double& hu, double& hv) {
+    if (h <= 0.0) {
+        hu = 0.0;
+        hv = 0.0;
+        return;
+    }
+    if (h < P.h_dry) {
+        const double r = h / P.h_dry;
+        const double factor = 1.4142135623730951 * r / (P.h_dry * sqrt(1.0 + r * r * r * r));
+        hu = h * (factor * hu);
+        hv = h * (factor * hv);
+    }
+    // |hu| > h·u_max; the square root only near the cap
+    const double m2 = hu * hu + hv * hv;
+    const double cap = P.max_velocity * h;
+    if (m2 > 0.99 * (cap * cap)) {
+        const double momentum = sqrt(m2);
+        if (momentum > cap) {
+            const double scale = cap / momentum;
+            hu *= scale;
+            hv *= scale;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// the stage kernel
+
+template <int N1>
+struct Cfg {
+    static constexpr int NN = N1 * N1;
+    static constexpr int NP = N1 - 1;      // pairs a node owns
+    static constexpr int NA = 2 * (N1 - 1);  // pairs a node is in
+    static constexpr int EPB = (128 / NN) > 0 ? (128 / NN) : 1;
+    static constexpr int THREADS = EPB * NN;
+    static constexpr int PAIR_DOUBLES = NN * NP * 3;
+    static constexpr int FACE_DOUBLES = 2 * NN * 8;           // reconstructed faces
+    static constexpr int IFL_DOUBLES = 2 * N1 * (N1 - 1) * 6;  // subcell interface fluxes
+    static constexpr int X = PAIR_DOUBLES > FACE_DOUBLES + IFL_DOUBLES ? PAIR_DOUBLES
+                                                                       : FACE_DOUBLES + IFL_DOUBLES;
+};
+
+__device__ __forceinline__ int line_node(int n1, int dir, int line, int pos) {
+    return dir == 0 ? line * n1 + pos : pos * n1 + line;
+}
+
+// The subcell interface directions of one line (src/solver/rhs/subcells.rs:63-92)
+template <int N1>
+__device__ void telescoped(const Physics& P, const double (&m0)[N1], const double (&m1)[N1],
+                           bool affine, double (&i0)[N1 + 1], double (&i1)[N1 + 1]) {
+    if (affine) {
+#pragma unroll
+        for (int a = 0; a <= N1; ++a) {
+            i0[a] = m0[0];
+            i1[a] = m1[0];
+        }
+        return;
+    }
+    i0[0] = m0[0];
+    i1[0] = m1[0];
+    double s0 = 0.0, s1 = 0.0;
+#pragma unroll
+    for (int a = 0; a < N1 - 1; ++a) {
+#pragma unroll
+        for (int c = 0; c < N1; ++c) {
+            if (c == a) continue;
+            const double q2 = 2.0 * P.w[a] * P.d[a * N1 + c];
+            s0 += q2 * 0.5 * (m0[a] + m0[c]);
+            s1 += q2 * 0.5 * (m1[a] + m1[c]);
+        }
+        i0[a + 1] = s0;
+        i1[a + 1] = s1;
+    }
+    i0[N1] = m0[N1 - 1];
+    i1[N1] = m1[N1 - 1];
+}
+
+template <int N1>
+__device__ __forceinline__ void line_metric(const DevTables& T, int64_t k, int dir, int line,
+                                            double (&m0)[N1], double (&m1)[N1]) {
+    constexpr int NN = N1 * N1;
+#pragma unroll
+    for (int p = 0; p < N1; ++p) {
+        const int64_t g = k * NN + line_node(N1, dir, line, p);
+        m0[p] = T.contra[g * 4 + 2 * dir];
+        m1[p] = T.contra[g * 4 + 2 * dir + 1];
+    }
+}
+
+// limited_slope with SlopeDistances (src/solver/rhs/swe_2d_split_form.rs:168-203)
+__device__ __forceinline__ double limited_slope(double q0, double q1, double q2, double ic,
+                                                double im, double ip) {
+    const double dm = q1 - q0, dp = q2 - q1;
+    const bool extremum = (dm * dp) <= 0.0;
+    const double central = (q2 - q0) * ic;
+    const double bound = lmin(fabs(dm * im), fabs(dp * ip));
+    const double sign = central < 0.0 ? -1.0 : 1.0;
+    return extremum ? 0.0 : sign * lmin(fabs(central), bound);
+}
+
+// reconstruct_subcell (src/solver/rhs/swe_2d_split_form.rs:279-317)
+__device__ __forceinline__ void reconstruct(const Sd& m, const Sd& c, const Sd& p, double x0,
+                                            double x1, double x2, double xl, double xr,
+                                            double h_dry, Sd& left, Sd& right) {
+    const double e0 = m.h + m.b, e1 = c.h + c.b, e2 = p.h + p.b;
+    double ws = -INFINITY;
+    ws = (m.h >= h_dry && e0 > ws) ? e0 : ws;
+    ws = (c.h >= h_dry && e1 > ws) ? e1 : ws;
+    ws = (p.h >= h_dry && e2 > ws) ? e2 : ws;
+    const bool flooding =
+        (m.h < h_dry && e0 < ws) || (c.h < h_dry && e1 < ws) || (p.h < h_dry && e2 < ws);
+    const double fm = x1 - xl, fp = xr - x1;
+    const double ic = 1.0 / (x2 - x0);
+    const double im = 1.0 / (fm > 0.0 ? fm : 0.5 * (x1 - x0));
+    const double ip = 1.0 / (fp > 0.0 ? fp : 0.5 * (x2 - x1));
+    const double s_h = limited_slope(m.h, c.h, p.h, ic, im, ip);
+    const double s_eta = flooding ? 0.0 : limited_slope(e0, e1, e2, ic, im, ip);
+    const double s_u = limited_slope(m.u, c.u, p.u, ic, im, ip);
+    const double s_v = limited_slope(m.v, c.v, p.v, ic, im, ip);
+    double d = xl - x1;
+    double hh = lmax(c.h + s_h * d, 0.0);
+    left = {hh, c.u + s_u * d, c.v + s_v * d, e1 + s_eta * d - hh};
+    d = xr - x1;
+    hh = lmax(c.h + s_h * d, 0.0);
+    right = {hh, c.u + s_u * d, c.v + s_v * d, e1 + s_eta * d - hh};
+}
+
+template <int N1>
+__global__ void __launch_bounds__(Cfg<N1>::THREADS)
+    stage_kernel(DevTables T, Physics P, StageExtra X, DevBuf in, DevBuf base, DevBuf out,
+                 DevBuf acc, const double* __restrict__ fb_h, const double* __restrict__ fb_hu,
+                 const double* __restrict__ fb_hv, StepCtl* ctl, int slot, int mode,
+                 int check_finite, const int* active) {
+    using C = Cfg<N1>;
+    constexpr int NN = C::NN, NP = C::NP, NA = C::NA, EPB = C::EPB;
+    __shared__ double s_q[EPB][6][NN];
+    __shared__ double s_x[EPB][C::X];
+    __shared__ int s_flag[EPB][2];
+    __shared__ double s_red[EPB][5];
+
+    if (!*active) return;
+    const int tid = threadIdx.x;
+    const int e = tid / NN, i = tid % NN;
+    const int64_t k = (int64_t)blockIdx.x * EPB + e;
+    const bool valid = k < T.K;
+    const int64_t gi = k * NN + i;
+    const int a = i % N1, j = i / N1;
+    const double g = P.g, h_min = P.h_min, sqrt_g = sqrt(P.g);
+
+    if (i == 0) {
+        s_flag[e][0] = 0;
+        s_flag[e][1] = 0;
+    }
+    double h = 0, hu = 0, hv = 0, u = 0, v = 0, b = 0;
+    if (valid) {
+        h = in.h[gi];
+        hu = in.hu[gi];
+        hv = in.hv[gi];
+        u = in.u[gi];
+        v = in.v[gi];
+        b = P.has_bed ? T.bed[gi] : 0.0;
+    }
+    s_q[e][0][i] = h;
+    s_q[e][1][i] = hu;
+    s_q[e][2][i] = hv;
+    s_q[e][3][i] = u;
+    s_q[e][4][i] = v;
+    s_q[e][5][i] = b;
+    __syncthreads();
+    if (valid && P.formulation == kWetDry && h < P.subcell_depth) atomicOr(&s_flag[e][0], 1);
+    __syncthreads();
+    const bool sub = s_flag[e][0] != 0;
+    double rh = 0.0, rhu = 0.0, rhv = 0.0;
+    const bool affine = valid ? T.affine[k] != 0 : true;
+
+    auto node_side = [&](int n) {
+        return Sd{s_q[e][0][n], s_q[e][3][n], s_q[e][4][n], s_q[e][5][n]};
+    };
+    double* faces = &s_x[e][0];                      // [dir][line][pos][8]
+    double* ifl = &s_x[e][C::FACE_DOUBLES];          // [dir][line][pos][6]
+
+    // ---- phase A: pair fluxes, or the subcells' reconstructed faces ----
+    if (valid && !sub) {
+        const double two_g = 2.0 * g;
+#pragma unroll
+        for (int q = 0; q < NP; ++q) {
+            const int8_t* own = &T.sched_owned[(i * NP + q) * 5];
+            const int na = own[0], nc = own[1];
+            const double hm0 = T.pair_hm[(gi * NP + q) * 2];
+            const double hm1 = T.pair_hm[(gi * NP + q) * 2 + 1];
+            const double ha = s_q[e][0][na], hc = s_q[e][0][nc];
+            // ½·F#(q_a, q_c)·{{Ja}} scaled: mass, 2·F_hu, 2·F_hv
+            const double mass = (s_q[e][1][na] + s_q[e][1][nc]) * hm0 +
+                                (s_q[e][2][na] + s_q[e][2][nc]) * hm1;
+            const double gp2 = two_g * (ha * hc);
+            const double g_hu = mass * (s_q[e][3][na] + s_q[e][3][nc]) + gp2 * hm0;
+            const double g_hv = mass * (s_q[e][4][na] + s_q[e][4][nc]) + gp2 * hm1;
+            double* slot_f = &s_x[e][(i * NP + q) * 3];
+            slot_f[0] = mass;
+            slot_f[1] = g_hu;
+            slot_f[2] = g_hv;
+        }
+    } else if (valid && sub) {
+        // subcell faces of this node's subcell on its r-line and s-line
+#pragma unroll
+        for (int dir = 0; dir < 2; ++dir) {
+            const int line = dir == 0 ? j : a;
+            const int pos = dir == 0 ? a : j;
+            const Sd q = node_side(i);
+            Sd l{}, r{};
+            double x_l = 0.0, x_r = 0.0;
+            bool have_l = true, have_r = true;
+            if (pos > 0) {
+                l = node_side(line_node(N1, dir, line, pos - 1));
+                x_l = P.x[pos - 1];
+            } else {
+                // r-lines end on faces 3 (reversed) and 1; s-lines on 0 and 2 (reversed)
+                const int face = dir == 0 ? 3 : 0;
+                const int fi = dir == 0 ? N1 - 1 - line : line;
+                const int64_t o = (k * 4 + face) * N1 + fi;
+                const int64_t og = T.outer_idx[o];
+                have_l = og >= 0;
+                if (have_l) {
+                    l = Sd{in.h[og], in.u[og], in.v[og], P.has_bed ? T.bed[og] : 0.0};
+                    x_l = -1.0 - T.outer_dist[o];
+                }
+            }
+            if (pos + 1 < N1) {
+                r = node_side(line_node(N1, dir, line, pos + 1));
+                x_r = P.x[pos + 1];
+            } else {
+                const int face = dir == 0 ? 1 : 2;
+                const int fi = dir == 0 ? line : N1 - 1 - line;
+                const int64_t o = (k * 4 + face) * N1 + fi;
+                const int64_t og = T.outer_idx[o];
+                have_r = og >= 0;
+                if (have_r) {
+                    r = Sd{in.h[og], in.u[og], in.v[og], P.has_bed ? T.bed[og] : 0.0};
+                    x_r = 1.0 + T.outer_dist[o];
+                }
+            }
+            Sd fl = q, fr = q;
+            if (have_l && have_r)
+                reconstruct(l, q, r, x_l, P.x[pos], x_r, X.xl[pos], X.xr[pos], P.subcell_h_dry,
+                            fl, fr);
+            double* f = &faces[((dir * N1 + line) * N1 + pos) * 8];
+            f[0] = fl.h;
+            f[1] = fl.u;
+            f[2] = fl.v;
+            f[3] = fl.b;
+            f[4] = fr.h;
+            f[5] = fr.u;
+            f[6] = fr.v;
+            f[7] = fr.b;
+        }
+    }
+    __syncthreads();
+
+    // ---- phase B: sum the pairs; or the subcell interface fluxes ----
+    if (valid && !sub) {
+#pragma unroll
+        for (int q = 0; q < NA; ++q) {
+            const int slot_id = T.sched_slot[i * NA + q];
+            const double coef = T.sched_coef[i * NA + q];
+            const double hcoef = 0.5 * coef;
+            const double* f = &s_x[e][slot_id * 3];
+            rh -= coef * f[0];
+            rhu -= hcoef * f[1];
+            rhv -= hcoef * f[2];
+        }
+        if (P.has_bed) {
+            rhu -= h * T.gdb[gi * 2];
+            rhv -= h * T.gdb[gi * 2 + 1];
+        }
+    } else if (valid && sub) {
+#pragma unroll
+        for (int dir = 0; dir < 2; ++dir) {
+            const int line = dir == 0 ? j : a;
+            const int pos = dir == 0 ? a : j;
+            if (pos + 1 >= N1) continue;
+            double m0[N1], m1[N1], i0[N1 + 1], i1[N1 + 1];
+            line_metric<N1>(T, k, dir, line, m0, m1);
+            telescoped<N1>(P, m0, m1, affine, i0, i1);
+            const double mx = i0[pos + 1], my = i1[pos + 1];
+            const double norm = sqrt(mx * mx + my * my);
+            const double inv = 1.0 / norm;
+            const double* fa_ = &faces[((dir * N1 + line) * N1 + pos) * 8 + 4];   // right face of pos
+            const double* fb_ = &faces[((dir * N1 + line) * N1 + pos + 1) * 8];   // left face of pos+1
+            F3 fa, fb;
+            hydro_hll(Sd{fa_[0], fa_[1], fa_[2], fa_[3]}, Sd{fb_[0], fb_[1], fb_[2], fb_[3]}, mx, my,
+                      norm, mx * inv, my * inv, g, sqrt_g, h_min, fa, fb);
+            double* o = &ifl[((dir * N1 + line) * (N1 - 1) + pos) * 6];
+            o[0] = fa.h;
+            o[1] = fa.hu;
+            o[2] = fa.hv;
+            o[3] = fb.h;
+            o[4] = fb.hu;
+            o[5] = fb.hv;
+        }
+    }
+    __syncthreads();
+
+    // ---- phase C: the subcells' fluxes and bed terms at this node ----
+    if (valid && sub) {
+#pragma unroll
+        for (int dir = 0; dir < 2; ++dir) {
+            const int line = dir == 0 ? j : a;
+            const int pos = dir == 0 ? a : j;
+            const double iw = X.inv_w[pos];
+            if (pos + 1 < N1) {
+                const double* o = &ifl[((dir * N1 + line) * (N1 - 1) + pos) * 6];
+                rh -= iw * o[0];
+                rhu -= iw * o[1];
+                rhv -= iw * o[2];
+            }
+            if (pos > 0) {
+                const double* o = &ifl[((dir * N1 + line) * (N1 - 1) + pos - 1) * 6];
+                rh += iw * o[3];
+                rhu += iw * o[4];
+                rhv += iw * o[5];
+            }
+            const double* f = &faces[((dir * N1 + line) * N1 + pos) * 8];
+            const double lh = f[0], lb = f[3], rhh = f[4], rb = f[7];
+            const double w_a = P.w[pos];
+            const double bed = -0.5 * g * (lh + rhh) * (rb - lb) / w_a;
+            double m0[N1], m1[N1];
+            line_metric<N1>(T, k, dir, line, m0, m1);
+            double fx, fy;
+            if (affine) {
+                fx = bed * m0[0];
+                fy = bed * m1[0];
+            } else {
+                double i0[N1 + 1], i1[N1 + 1];
+                telescoped<N1>(P, m0, m1, false, i0, i1);
+                const double ml0 = i0[pos], ml1 = i1[pos], mr0 = i0[pos + 1], mr1 = i1[pos + 1];
+                const double metric =
+                    0.25 * g * ((rhh + h) * (b - rb) + (lh + h) * (b - lb)) / w_a;
+                fx = bed * 0.5 * (ml0 + mr0) + metric * (mr0 - ml0);
+                fy = bed * 0.5 * (ml1 + mr1) + metric * (mr1 - ml1);
+            }
+            rhu += fx;
+            rhv += fy;
+        }
+    }
+
+    // ---- surface: −LIFT·sJ·F* of the node's faces ----
+    if (valid) {
+        const int64_t fbase = k * 4 * N1;
+        if (j == 0) {
+            const int64_t s = fbase + 0 * N1 + a;
+            rh -= fb_h[s];
+            rhu -= fb_hu[s];
+            rhv -= fb_hv[s];
+        }
+        if (a == N1 - 1) {
+            const int64_t s = fbase + 1 * N1 + j;
+            rh -= fb_h[s];
+            rhu -= fb_hu[s];
+            rhv -= fb_hv[s];
+        }
+        if (j == N1 - 1) {
+            const int64_t s = fbase + 2 * N1 + (N1 - 1 - a);
+            rh -= fb_h[s];
+            rhu -= fb_hu[s];
+            rhv -= fb_hv[s];
+        }
+        if (a == 0) {
+            const int64_t s = fbase + 3 * N1 + (N1 - 1 - j);
+            rh -= fb_h[s];
+            rhu -= fb_hu[s];
+            rhv -= fb_hv[s];
+        }
+    }
+
+    // ---- 1/J and the sources ----
+    double Fh = 0.0, Fhu = 0.0, Fhv = 0.0;
+    if (valid) {
+        const double jinv = T.jinv[gi];
+        Fh = jinv * rh;
+        Fhu = jinv * rhu;
+        Fhv = jinv * rhv;
+        if (P.has_coriolis) {
+            const double f = P.coriolis_field ? T.fcor[gi] : P.f0;
+            Fhu += f * hv;
+            Fhv += -f * hu;
+        }
+        if (mode == kRhsOnly) {
+            out.h[gi] = Fh;
+            out.hu[gi] = Fhu;
+            out.hv[gi] = Fhv;
+        }
+    }
+    if (mode == kRhsOnly) return;  // uniform: no barrier follows for this mode
+
+    // ---- stage combination and damping ----
+    const StageArgs sa = ctl->stage[slot];
+    double vh = 0.0, vhu = 0.0, vhv = 0.0;
+    if (valid) {
+        if (sa.a != 0.0) {
+            vh = sa.a * base.h[gi];
+            vhu = sa.a * base.hu[gi];
+            vhv = sa.a * base.hv[gi];
+        }
+        if (sa.b != 0.0) {
+            vh += sa.b * h;
+            vhu += sa.b * hu;
+            vhv += sa.b * hv;
+        }
+        if (sa.c != 0.0) {
+            vh += sa.c * Fh;
+            vhu += sa.c * Fhu;
+            vhv += sa.c * Fhv;
+        }
+        if (P.friction || P.has_wet_dry) {
+            const double g_n2 = P.friction == 2 ? T.g_n2[gi] : P.g_n2;
+            damp(P, g_n2, vh, vhu, vhv, DampIn{h, hu, hv, u, v}, sa.c);
+        }
+    }
+
+    if (mode == kAccumulate) {
+        if (valid) {
+            out.h[gi] = vh;
+            out.hu[gi] = vhu;
+            out.hv[gi] = vhv;
+            const double w = sa.w, keep = sa.keep;
+            if (keep != 0.0) {
+                acc.h[gi] = w * vh + keep * acc.h[gi];
+                acc.hu[gi] = w * vhu + keep * acc.hu[gi];
+                acc.hv[gi] = w * vhv + keep * acc.hv[gi];
+            } else {
+                acc.h[gi] = w * vh;
+                acc.hu[gi] = w * vhu;
+                acc.hv[gi] = w * vhv;
+            }
+        }
+        return;
+    }
+
+    // ---- wet/dry correction (wetting_drying.rs:194-215) ----
+    if (P.has_wet_dry) {
+        __syncthreads();  // s_q is free again
+        if (valid && vh < P.h_dry) atomicOr(&s_flag[e][1], 1);
+        s_q[e][0][i] = vh;
+        s_q[e][1][i] = vhu;
+        s_q[e][2][i] = vhv;
+        __syncthreads();
+        const bool needs = s_flag[e][1] != 0;
+        if (valid && needs && i == 0) {
+            // element_mean and positivity_limit_element
+            // (src/solver/limiters/swe_2d.rs:135-203), in node order
+            const double* mass = &T.mass[k * NN];
+            double sh = 0.0, shu = 0.0, shv = 0.0, hmin = INFINITY;
+            for (int p = 0; p < NN; ++p) {
+                sh += mass[p] * s_q[e][0][p];
+                shu += mass[p] * s_q[e][1][p];
+                shv += mass[p] * s_q[e][2][p];
+                hmin = fmin(hmin, s_q[e][0][p]);
+            }
+            const double inv_area = T.inv_area[k];
+            const double h_avg = sh * inv_area;
+            s_red[e][0] = h_avg;
+            s_red[e][1] = shu * inv_area;
+            s_red[e][2] = shv * inv_area;
+            double theta = 1.0;
+            if (h_avg > 0.0 && hmin < 0.0) {
+                theta = h_avg / (h_avg - hmin);
+                theta = theta < 0.0 ? 0.0 : (theta > 1.0 ? 1.0 : theta);
+            }
+            s_red[e][3] = theta;
+            s_red[e][4] = hmin;
+            if (h_avg < 0.0) atomicAdd((unsigned long long*)&ctl->clips, 1ull);
+        }
+        __syncthreads();
+        if (valid && needs) {
+            const double h_avg = s_red[e][0];
+            if (h_avg <= 0.0) {
+                vh = vhu = vhv = 0.0;
+            } else {
+                if (s_red[e][4] < 0.0) {
+                    const double th = s_red[e][3];
+                    vh = th * (vh - h_avg) + h_avg;
+                    vhu = th * (vhu - s_red[e][1]) + s_red[e][1];
+                    vhv = th * (vhv - s_red[e][2]) + s_red[e][2];
+                    vh = fmax(vh, 0.0);
+                }
+                if (h_avg < P.h_dry) vhu = vhv = 0.0;
+            }
+        }
+        if (valid) correct_node(P, vh, vhu, vhv);
+    }
+    if (valid) {
+        out.h[gi] = vh;
+        out.hu[gi] = vhu;
+        out.hv[gi] = vhv;
+        double uo, vo;
+        node_velocity(vh, vhu, vhv, h_min, uo, vo);
+        out.u[gi] = uo;
+        out.v[gi] = vo;
+        if (check_finite && !(isfinite(vh) && isfinite(vhu) && isfinite(vhv))) ctl->nonfinite = 1;
+    }
+}
+
+// finish_where over every element: state ← acc, then the wet/dry correction
+template <int N1>
+__global__ void __launch_bounds__(Cfg<N1>::THREADS)
+    finish_kernel(DevTables T, Physics P, DevBuf acc, DevBuf state, StepCtl* ctl) {
+    using C = Cfg<N1>;
+    constexpr int NN = C::NN, EPB = C::EPB;
+    __shared__ double s_v[EPB][3][NN];
+    __shared__ int s_flag[EPB];
+    __shared__ double s_red[EPB][5];
+    const int tid = threadIdx.x;
+    const int e = tid / NN, i = tid % NN;
+    const int64_t k = (int64_t)blockIdx.x * EPB + e;
+    const bool valid = k < T.K;
+    const int64_t gi = k * NN + i;
+    if (i == 0) s_flag[e] = 0;
+    double vh = 0, vhu = 0, vhv = 0;
+    if (valid) {
+        vh = acc.h[gi];
+        vhu = acc.hu[gi];
+        vhv = acc.hv[gi];
+    }
+    s_v[e][0][i] = vh;
+    s_v[e][1][i] = vhu;
+    s_v[e][2][i] = vhv;
+    __syncthreads();
+    if (P.has_wet_dry) {
+        if (valid && vh < P.h_dry) atomicOr(&s_flag[e], 1);
+        __syncthreads();
+        const bool needs = s_flag[e] != 0;
+        if (valid && needs && i == 0) {
+            const double* mass = &T.mass[k * NN];
+            double sh = 0.0, shu = 0.0, shv = 0.0, hmin = INFINITY;
+            for (int p = 0; p < NN; ++p) {
+                sh += mass[p] * s_v[e][0][p];
+                shu += mass[p] * s_v[e][1][p];
+                shv += mass[p] * s_v[e][2][p];
+                hmin = fmin(hmin, s_v[e][0][p]);
+            }
+            const double inv_area = T.inv_area[k];
+            const double h_avg = sh * inv_area;
+            s_red[e][0] = h_avg;
+            s_red[e][1] = shu * inv_area;
+            s_red[e][2] = shv * inv_area;
+            double theta = 1.0;
+            if (h_avg > 0.0 && hmin < 0.0) {
+                theta = h_avg / (h_avg - hmin);
+                theta = theta < 0.0 ? 0.0 : (theta > 1.0 ? 1.0 : theta);
+            }
+            s_red[e][3] = theta;
+            s_red[e][4] = hmin;
+            if (h_avg < 0.0) atomicAdd((unsigned long long*)&ctl->clips, 1ull);
+        }
+        __syncthreads();
+        if (valid && needs) {
+            const double h_avg = s_red[e][0];
+            if (h_avg <= 0.0) {
+                vh = vhu = vhv = 0.0;
+            } else {
+                if (s_red[e][4] < 0.0) {
+                    const double th = s_red[e][3];
+                    vh = th * (vh - h_avg) + h_avg;
+                    vhu = th * (vhu - s_red[e][1]) + s_red[e][1];
+                    vhv = th * (vhv - s_red[e][2]) + s_red[e][2];
+                    vh = fmax(vh, 0.0);
+                }
+                if (h_avg < P.h_dry) vhu = vhv = 0.0;
+            }
+        }
+        if (valid) correct_node(P, vh, vhu, vhv);
+    }
+    if (valid) {
+        state.h[gi] = vh;
+        state.hu[gi] = vhu;
+        state.hv[gi] = vhv;
+        double uo, vo;
+        node_velocity(vh, vhu, vhv, P.h_min, uo, vo);
+        state.u[gi] = uo;
+        state.v[gi] = vo;
+    }
+}
+
+// node velocities of a buffer (after an upload)
+__global__ void velocity_kernel(DevBuf b, int64_t n, double h_min) {
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    double u, v;
+    node_velocity(b.h[g], b.hu[g], b.hv[g], h_min, u, v);
+    b.u[g] = u;
+    b.v[g] = v;
+}
+
+// ---------------------------------------------------------------------------
+// the time step (src/solver/rhs/swe_2d.rs:2072-2115, 1346-1367, 2165-2258)
+
+__device__ __forceinline__ double node_rate(double h, double u, double v, const double* m,
+                                            double g) {
+    const double c = sqrt(g * fmax(h, 0.0));
+    const double lr = fabs(u * m[0] + v * m[1]) + c * m[4];
+    const double ls = fabs(u * m[2] + v * m[3]) + c * m[5];
+    return 0.25 * (lr + ls);
+}
+
+template <int N1>
+__global__ void __launch_bounds__(Cfg<N1>::THREADS)
+    dt_kernel(DevTables T, Physics P, DevBuf q, DtParams D, double* dt_el, StepCtl* ctl,
+              const int* active) {
+    using C = Cfg<N1>;
+    constexpr int NN = C::NN, EPB = C::EPB;
+    __shared__ unsigned long long s_rate[EPB];
+    __shared__ double s_h[EPB][NN];
+    if (!*active) return;
+    const int tid = threadIdx.x;
+    const int e = tid / NN, i = tid % NN;
+    const int64_t k = (int64_t)blockIdx.x * EPB + e;
+    const bool valid = k < T.K;
+    const int64_t gi = k * NN + i;
+    const double g = P.g, h_min = P.h_min;
+    if (i == 0) s_rate[e] = 0ull;
+    __syncthreads();
+    double rate = 0.0;
+    if (valid) {
+        const double h = q.h[gi];
+        s_h[e][i] = h;
+        if (h > h_min) rate = node_rate(h, q.u[gi], q.v[gi], &T.dtm_own[gi * 6], g);
+        for (int it = i; it < 4 * N1; it += NN) {
+            const int64_t o = k * 4 * N1 + it;
+            const int64_t nb = T.nb_face_node[o];
+            if (nb < 0) continue;
+            const double hn = q.h[nb];
+            if (hn <= h_min) continue;
+            rate = fmax(rate, node_rate(hn, q.u[nb], q.v[nb], &T.dtm_face[o * 6], g));
+        }
+        atomicMax(&s_rate[e], (unsigned long long)__double_as_longlong(rate));
+    }
+    __syncthreads();
+    if (!valid || i != 0) return;
+    const double rmax = __longlong_as_double((long long)s_rate[e]);
+    double cfl = D.cfl;
+    if (D.positivity) {
+        // PositivityBound::element_cfl / positivity_relaxation, in node order
+        const double* mass = &T.mass[k * NN];
+        double water = 0.0, water_b = 0.0;
+        bool shallow = false;
+        for (int p = 0; p < NN; ++p) {
+            const double hp = s_h[e][p];
+            shallow = shallow || (hp <= D.shallow);
+            const double wi = mass[p] * fmax(hp, 0.0);
+            water += wi;
+            const int pa = p % N1, pj = p / N1;
+            if (pa == 0 || pa == N1 - 1 || pj == 0 || pj == N1 - 1) water_b += wi;
+        }
+        const double ratio = fmin(water / water_b, T.weight_ratio[k]);
+        const double rho = fmax(0.9 * ratio, 1.0);
+        const double cap = shallow ? D.max_cfl_subcells : D.max_cfl;
+        cfl = fmin(cfl, fmin(D.bound_cfl * rho, cap));
+    }
+    const double dt = rmax < 1e-14 ? INFINITY : cfl / ((2.0 * (double)P.order + 1.0) * rmax);
+    if (dt_el) dt_el[k] = dt;
+    atomicMin(&ctl->dt_bits, (unsigned long long)__double_as_longlong(dt));
+}
+
+// ---------------------------------------------------------------------------
+// the run's clock on the device (Simulation::run_with_callback's loop body,
+// src/simulation/runner.rs:355-450)
+
+constexpr int kFailDtMin = 4, kFailMaxSteps = 5, kFailNonFinite = 3;
+
+// Whether the step runs: no failure, time left before the target, steps left
+__global__ void step_begin(StepCtl* c) {
+    c->dt_bits = 0x7FF0000000000000ull;  // +∞
+    bool run = c->failure == 0 && c->t < c->target;
+    if (run && c->max_steps > 0 && c->steps >= c->max_steps) {
+        c->failure = kFailMaxSteps;
+        run = false;
+    }
+    c->active = run ? 1 : 0;
+}
+
+// dt from the element steps, capped, checked, fitted to land on the target;
+// the stages' times and weights (element_stage, src/time/multirate.rs:169-200)
+__global__ void step_dt(StepCtl* c) {
+    if (!c->active) return;
+    double dt = __longlong_as_double((long long)c->dt_bits);
+    if (c->dt_max > 0.0) dt = fmin(dt, c->dt_max);
+    if (c->dt_min > 0.0 && dt < c->dt_min) {
+        c->failure = kFailDtMin;
+        c->active = 0;
+        c->dt = dt;
+        return;
+    }
+    c->dt_min_used = fmin(c->dt_min_used, dt);
+    c->dt_max_used = fmax(c->dt_max_used, dt);
+    const bool landed = c->t + dt * (1.0 + 1e-9) >= c->target;
+    if (landed) dt = c->target - c->t;
+    c->landed = landed ? 1 : 0;
+    c->dt = dt;
+    for (int s = 0; s < c->scheme_stages; ++s) {
+        StageArgs& a = c->stage[s];
+        a.time = c->t + c->st_c[s] * dt;
+        a.a = c->st_start[s];
+        a.b = c->st_input[s];
+        a.c = c->st_beta[s] * dt;
+        a.w = 1.0;
+        a.keep = 0.0;
+    }
+}
+
+__global__ void step_end(StepCtl* c) {
+    if (!c->active) return;
+    c->t = c->landed ? c->target : c->t + c->dt;
+    c->steps += 1;
+    if (c->nonfinite) {
+        c->failure = kFailNonFinite;
+        c->active = 0;
+    }
+}
+
+}  // namespace DGSWE_NS
+}  // namespace dgswe

@@ -1,0 +1,94 @@
+// Launchers of one numerics variant (included after kernels.cuh by
+// kernels_fast.cu and kernels_exact.cu): the order N is a template
+// parameter of the kernels and a run-time value of the handle.
+#pragma once
+
+#include "kernel_set.hpp"
+
+namespace dgswe {
+namespace DGSWE_NS {
+
+template <int N1>
+static void face_n(const DevTables& T, const Physics& P, const DevBuf& in, double* fh, double* fhu,
+                   double* fhv, const StepCtl* ctl, int slot, const int* active, cudaStream_t s) {
+    const int64_t items = (T.n_edges + T.n_bfaces) * N1;
+    if (items == 0) return;
+    const int threads = 256;
+    const unsigned blocks = (unsigned)((items + threads - 1) / threads);
+    face_kernel<N1><<<blocks, threads, 0, s>>>(T, P, in, fh, fhu, fhv, ctl, slot, active);
+}
+
+template <int N1>
+static void stage_n(const DevTables& T, const Physics& P, const StageExtra& X, const DevBuf& in,
+                    const DevBuf& base, const DevBuf& out, const DevBuf& acc, const double* fh,
+                    const double* fhu, const double* fhv, StepCtl* ctl, int slot, int mode,
+                    int check_finite, const int* active, cudaStream_t s) {
+    using C = Cfg<N1>;
+    const unsigned blocks = (unsigned)((T.K + C::EPB - 1) / C::EPB);
+    stage_kernel<N1><<<blocks, C::THREADS, 0, s>>>(T, P, X, in, base, out, acc, fh, fhu, fhv, ctl,
+                                                   slot, mode, check_finite, active);
+}
+
+template <int N1>
+static void finish_n(const DevTables& T, const Physics& P, const DevBuf& acc, const DevBuf& state,
+                     StepCtl* ctl, cudaStream_t s) {
+    using C = Cfg<N1>;
+    const unsigned blocks = (unsigned)((T.K + C::EPB - 1) / C::EPB);
+    finish_kernel<N1><<<blocks, C::THREADS, 0, s>>>(T, P, acc, state, ctl);
+}
+
+template <int N1>
+static void dt_n(const DevTables& T, const Physics& P, const DevBuf& q, const DtParams& D,
+                 double* dt_el, StepCtl* ctl, const int* active, cudaStream_t s) {
+    using C = Cfg<N1>;
+    const unsigned blocks = (unsigned)((T.K + C::EPB - 1) / C::EPB);
+    dt_kernel<N1><<<blocks, C::THREADS, 0, s>>>(T, P, q, D, dt_el, ctl, active);
+}
+
+#define DGSWE_BY_ORDER(fn, ...)            \
+    switch (n1) {                          \
+        case 2: fn<2>(__VA_ARGS__); break; \
+        case 3: fn<3>(__VA_ARGS__); break; \
+        case 4: fn<4>(__VA_ARGS__); break; \
+        default: fn<5>(__VA_ARGS__); break; \
+    }
+
+static void face(int n1, const DevTables& T, const Physics& P, const DevBuf& in, double* fh,
+                 double* fhu, double* fhv, const StepCtl* ctl, int slot, const int* active,
+                 cudaStream_t s) {
+    DGSWE_BY_ORDER(face_n, T, P, in, fh, fhu, fhv, ctl, slot, active, s);
+}
+
+static void stage(int n1, const DevTables& T, const Physics& P, const StageExtra& X,
+                  const DevBuf& in, const DevBuf& base, const DevBuf& out, const DevBuf& acc,
+                  const double* fh, const double* fhu, const double* fhv, StepCtl* ctl, int slot,
+                  int mode, int check_finite, const int* active, cudaStream_t s) {
+    DGSWE_BY_ORDER(stage_n, T, P, X, in, base, out, acc, fh, fhu, fhv, ctl, slot, mode,
+                   check_finite, active, s);
+}
+
+static void finish(int n1, const DevTables& T, const Physics& P, const DevBuf& acc,
+                   const DevBuf& state, StepCtl* ctl, cudaStream_t s) {
+    DGSWE_BY_ORDER(finish_n, T, P, acc, state, ctl, s);
+}
+
+static void dt(int n1, const DevTables& T, const Physics& P, const DevBuf& q, const DtParams& D,
+               double* dt_el, StepCtl* ctl, const int* active, cudaStream_t s) {
+    DGSWE_BY_ORDER(dt_n, T, P, q, D, dt_el, ctl, active, s);
+}
+
+#undef DGSWE_BY_ORDER
+
+static void velocity(const DevBuf& b, int64_t n, double h_min, cudaStream_t s) {
+    if (n == 0) return;
+    velocity_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b, n, h_min);
+}
+
+static void begin(StepCtl* c, cudaStream_t s) { step_begin<<<1, 1, 0, s>>>(c); }
+static void dt_fit(StepCtl* c, cudaStream_t s) { step_dt<<<1, 1, 0, s>>>(c); }
+static void end(StepCtl* c, cudaStream_t s) { step_end<<<1, 1, 0, s>>>(c); }
+
+static const KernelSet kSet = {face, stage, finish, dt, velocity, begin, dt_fit, end};
+
+}  // namespace DGSWE_NS
+}  // namespace dgswe

@@ -1,0 +1,212 @@
+"""The device path behind the reference's solver API: a handle on the CUDA
+library with the methods of ``PhysicsModule`` / ``LocalTimeStepping``
+(src/physics/traits.rs:61-165, src/physics/builder.rs:420-783) and the
+``CaseDevice::run_2d`` entry of a case run (src/case/run.rs:179-212).
+
+Every call goes through the C ABI (include/dgswe.h); a failure raises
+:class:`DeviceError` with the library's message, as the reference's device
+returns ``Err(String)``. There is no CPU fallback: without the built CUDA
+library, or without a GPU, construction fails."""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import abi
+from .physics import SWEDeviceForm2D
+
+_dp = C.POINTER(C.c_double)
+
+
+class DeviceError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(message)
+        self.status = status
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(_dp)
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+
+
+@dataclass
+class DeviceRun:
+    """DeviceRun (src/case/run.rs:273-289)."""
+
+    span: tuple[float, float]
+    cfl: float = 0.5
+    interval: float | None = None
+    dt_max: float | None = None
+    dt_min: float | None = None
+    max_steps: int | None = None
+    scheme: int = abi.SSP_RK3
+    stop: C.c_int32 | None = None  # set .value = 1 to stop at the next step
+
+
+@dataclass
+class DeviceRunReport:
+    """DeviceRunReport (src/case/run.rs:292-300) with its SimulationResult."""
+
+    success: bool
+    final_time: float
+    n_steps: int
+    dt_min: float
+    dt_max: float
+    wall_time: float
+    negative_depth_clips: int
+    message: str
+    device: str
+
+
+class SWEPhysics2D:
+    """The device's SWE physics on one mesh: a dgswe handle.
+
+    ``library`` is any :class:`abi.Library` exporting the ABI (default: the
+    in-tree CUDA library)."""
+
+    def __init__(self, form: SWEDeviceForm2D, device: int = 0, library: abi.Library | None = None):
+        self.lib = library or abi.cuda_library()
+        self.form = form
+        c_form, self._keep = form.to_c()
+        handle = C.c_void_p()
+        status = self.lib.create(C.byref(c_form), device, C.byref(handle))
+        if status != abi.OK:
+            message = self.lib.error_text(handle, status)
+            if handle:
+                self.lib.destroy(handle)
+            raise DeviceError(status, f"create: {message}")
+        self.handle = handle
+        self.n_values = int(self.lib.n_values(handle))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, status: int, what: str):
+        if status != abi.OK:
+            raise DeviceError(status, f"{what}: {self.lib.error_text(self.handle, status)}")
+
+    # -- state ---------------------------------------------------------------
+    def upload(self, h, hu, hv, buffer: int = abi.STATE):
+        h, hu, hv = _f64(h), _f64(hu), _f64(hv)
+        self._check(self.lib.upload(self.handle, buffer, _ptr(h), _ptr(hu), _ptr(hv),
+                                    self.n_values), "upload")
+
+    def download(self, buffer: int = abi.STATE):
+        out = [np.empty(self.n_values) for _ in range(3)]
+        self._check(self.lib.download(self.handle, buffer, *map(_ptr, out), self.n_values),
+                    "download")
+        return tuple(out)
+
+    # -- PhysicsModule ---------------------------------------------------------
+    def compute_rhs_into(self, time: float, input: int = abi.STATE):
+        """The RHS of buffer ``input`` at ``time`` (compute_rhs_into)."""
+        out = [np.empty(self.n_values) for _ in range(3)]
+        self._check(self.lib.compute_rhs(self.handle, input, time, *map(_ptr, out),
+                                         self.n_values), "compute_rhs")
+        return tuple(out)
+
+    def element_dt(self, cfl: float, scheme: int = abi.SSP_RK3) -> np.ndarray:
+        """LocalTimeStepping::element_dt: every element's stable step."""
+        out = np.empty(self.form.mesh.n_elements)
+        dt_min = C.c_double()
+        self._check(self.lib.element_dt(self.handle, cfl, scheme, _ptr(out), C.byref(dt_min)),
+                    "element_dt")
+        return out
+
+    def compute_dt_ssp(self, cfl: float, scheme: int = abi.SSP_RK3) -> float:
+        """PhysicsModule::compute_dt_ssp of a wet/dry run: the smallest
+        positivity-bounded element step."""
+        dt_min = C.c_double()
+        self._check(self.lib.element_dt(self.handle, cfl, scheme, None, C.byref(dt_min)),
+                    "element_dt")
+        return dt_min.value
+
+    # -- LocalTimeStepping -------------------------------------------------------
+    def stage_where(self, *, base: int, input: int, out: int, time: float, a: float, b: float,
+                    c: float, acc: int | None = None, w: float = 1.0, keep: float = 0.0):
+        """One stage pass over every element: out = a·base + b·input +
+        c·F(input), damped, then summed into ``acc`` (w·out + keep·acc) or
+        post-processed."""
+        plan = abi.StagePlan(base, input, out, acc if acc is not None else 0, time, a, b, c,
+                             1 if acc is not None else 0, w, keep)
+        self._check(self.lib.stage(self.handle, C.byref(plan)), "stage")
+
+    def finish_where(self, acc: int):
+        """state ← acc, post-processed."""
+        self._check(self.lib.finish(self.handle, acc), "finish")
+
+    def step(self, t: float, dt: float, scheme: int = abi.SSP_RK3):
+        """One fused one-level SSP step of the state."""
+        self._check(self.lib.step(self.handle, scheme, t, dt), "step")
+
+    def negative_depth_clips(self) -> int:
+        return int(self.lib.negative_depth_clips(self.handle))
+
+    # -- Simulation --------------------------------------------------------------
+    def run_with_callback(self, run: DeviceRun, callback=None) -> DeviceRunReport:
+        """Simulation::run_with_callback on the state; ``callback(t, h, hu,
+        hv)`` gets copies of the state on the host."""
+        cfg = abi.RunConfig()
+        cfg.scheme = run.scheme
+        cfg.cfl = run.cfl
+        cfg.t_start, cfg.t_end = run.span
+        cfg.interval = run.interval or 0.0
+        cfg.dt_max = run.dt_max or 0.0
+        cfg.dt_min = run.dt_min or 0.0
+        cfg.max_steps = run.max_steps or 0
+        cfg.stop = C.pointer(run.stop) if run.stop is not None else None
+
+        def trampoline(_user, t, h, hu, hv, count):
+            if callback is not None:
+                callback(t, *(np.ctypeslib.as_array(p, shape=(count,)).copy() for p in (h, hu, hv)))
+
+        cb = abi.CALLBACK(trampoline)
+        report = abi.Report()
+        status = self.lib.run(self.handle, C.byref(cfg), cb, None, C.byref(report))
+        result = DeviceRunReport(
+            success=bool(report.success), final_time=report.final_time,
+            n_steps=int(report.n_steps), dt_min=report.dt_min_used, dt_max=report.dt_max_used,
+            wall_time=report.wall_time, negative_depth_clips=int(report.negative_depth_clips),
+            message=report.message.decode(), device=report.device.decode())
+        if status not in (abi.OK, abi.ERR_NONFINITE, abi.ERR_DT_MIN, abi.ERR_MAX_STEPS,
+                          abi.ERR_STOPPED):
+            self._check(status, "run")
+        result.status = status
+        return result
+
+
+class Cuda:
+    """CaseDevice for CUDA (src/case/run.rs:179-212; the reference's
+    gpu/src/case.rs:36-70): step ``form`` on device ``ordinal`` from ``q``
+    over the run's span, calling ``callback(q, t)`` with the state on the
+    host at the start, every interval and the end; ``q`` is left with the
+    state at the end. A run that stops early (a non-finite state, a step
+    below dt_min, the step limit, the stop flag) returns its report with
+    ``success`` false and the reason, as the reference's SimulationResult
+    does; a device failure raises :class:`DeviceError`, the reference's
+    ``Err(String)``."""
+
+    def run_2d(self, ordinal: int, form: SWEDeviceForm2D, q, run: DeviceRun,
+               callback=None) -> DeviceRunReport:
+        dev = SWEPhysics2D(form, ordinal)
+        try:
+            dev.upload(*q)
+            report = dev.run_with_callback(
+                run, (lambda t, h, hu, hv: callback((h, hu, hv), t)) if callback else None)
+            h, hu, hv = dev.download()
+            for dst, src in zip(q, (h, hu, hv)):
+                dst[...] = src.reshape(dst.shape)
+            return report
+        finally:
+            dev.close()

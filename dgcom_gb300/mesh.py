@@ -1,0 +1,236 @@
+"""Host-side meshes for the device path: quadrilateral meshes as
+``Mesh2D::from_quads`` takes them (vertices, counter-clockwise element
+corners, periodic face pairs, one tag per boundary face), their node
+positions, and the seeded generators of the workloads.
+
+The generators follow the reference's (src/mesh/core/mesh2d.rs:309-420):
+``uniform_rectangle`` numbers vertices row by row from the bottom left and
+tags a boundary face with the side its face number names (face 0 south,
+1 east, 2 north, 3 west); ``uniform_periodic`` pairs the right face of each
+row's last element with the left face of its first, and the top faces of
+the top row with the bottom faces of the bottom row."""
+
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+# BoundaryTag (src/mesh/data/boundary_tags.rs:8-34) as the ABI's face tags
+TAG_WALL, TAG_OPEN, TAG_TIDAL, TAG_RIVER = 0, 1, 2, 4
+
+
+@dataclass
+class QuadMesh:
+    vertices: np.ndarray  # (n_vertices, 2) float64
+    elements: np.ndarray  # (n_elements, 4) int64, counter-clockwise
+    periodic: np.ndarray = field(default_factory=lambda: np.zeros((0, 4), np.int64))
+    face_tags: np.ndarray | None = None  # (n_elements, 4) int32
+
+    @property
+    def n_elements(self) -> int:
+        return int(self.elements.shape[0])
+
+    def corners(self) -> np.ndarray:
+        """(n_elements, 4, 2) corner coordinates."""
+        return self.vertices[self.elements]
+
+
+def _legendre_pd(n: int, x: float) -> tuple[float, float]:
+    # P_n and P_n' by the three-term recurrence (src/polynomial/legendre.rs:62-94)
+    if n == 0:
+        return 1.0, 0.0
+    if n == 1:
+        return x, 1.0
+    pm, pc = 1.0, x
+    for k in range(1, n):
+        pn = (float(2 * k + 1) * x * pc - float(k) * pm) / float(k + 1)
+        pm, pc = pc, pn
+    if abs(x - 1.0) < 1e-14:
+        dp = float(n * (n + 1)) / 2.0
+    elif abs(x + 1.0) < 1e-14:
+        dp = (1.0 if n % 2 else -1.0) * float(n * (n + 1)) / 2.0
+    else:
+        dp = float(n) * (x * pc - pm) / (x * x - 1.0)
+    return pc, dp
+
+
+def gll_nodes(order: int) -> np.ndarray:
+    """GLL nodes by Newton from the Chebyshev–Lobatto points
+    (src/polynomial/nodes.rs:17-77); the same values as the library's."""
+    n = order
+    x = [-math.cos(math.pi * j / n) for j in range(n + 1)]
+    x[0], x[n] = -1.0, 1.0
+    for j in range(1, n):
+        xj = x[j]
+        for _ in range(100):
+            p, dp = _legendre_pd(n, xj)
+            step = (1.0 - xj * xj) * dp / (float(n) * float(n + 1) * p)
+            if abs(step) < 1e-15:
+                break
+            xj += step
+        x[j] = xj
+    return np.array(x)
+
+
+def gll_weights(order: int) -> np.ndarray:
+    n = order
+    return np.array([2.0 / (float(n * (n + 1)) * _legendre_pd(n, xj)[0] ** 2)
+                     for xj in gll_nodes(order)])
+
+
+def reference_nodes(order: int) -> tuple[np.ndarray, np.ndarray]:
+    """(r, s) of the element nodes, node i = j·(N+1) + a, r fastest."""
+    x = gll_nodes(order)
+    n1 = order + 1
+    r = np.tile(x, n1)
+    s = np.repeat(x, n1)
+    return r, s
+
+
+def node_positions(mesh: QuadMesh, order: int) -> tuple[np.ndarray, np.ndarray]:
+    """Physical (x, y) of every node, (n_elements, (N+1)²) each, by the
+    bilinear map of Mesh2D::bilinear (src/mesh/core/mesh2d.rs:644-660)."""
+    r, s = reference_nodes(order)
+    c = mesh.corners()
+    n0 = (1.0 - r) * (1.0 - s) / 4.0
+    n1 = (1.0 + r) * (1.0 - s) / 4.0
+    n2 = (1.0 + r) * (1.0 + s) / 4.0
+    n3 = (1.0 - r) * (1.0 + s) / 4.0
+    x = (n0 * c[:, 0:1, 0] + n1 * c[:, 1:2, 0]) + n2 * c[:, 2:3, 0] + n3 * c[:, 3:4, 0]
+    y = (n0 * c[:, 0:1, 1] + n1 * c[:, 1:2, 1]) + n2 * c[:, 2:3, 1] + n3 * c[:, 3:4, 1]
+    return x, y
+
+
+def _structured(x0, x1, y0, y1, nx, ny):
+    # structured_quads (src/mesh/core/mesh2d.rs:226-254)
+    dx = (x1 - x0) / nx
+    dy = (y1 - y0) / ny
+    i = np.arange(nx + 1, dtype=np.float64)
+    j = np.arange(ny + 1, dtype=np.float64)
+    vx = np.tile(x0 + i * dx, ny + 1)
+    vy = np.repeat(y0 + j * dy, nx + 1)
+    verts = np.stack([vx, vy], axis=1)
+    jj, ii = np.meshgrid(np.arange(ny), np.arange(nx), indexing="ij")
+    v0 = (jj * (nx + 1) + ii).ravel().astype(np.int64)
+    elems = np.stack([v0, v0 + 1, v0 + nx + 2, v0 + nx + 1], axis=1)
+    return verts, elems
+
+
+def uniform_rectangle(x0, x1, y0, y1, nx, ny, sides=(TAG_WALL,) * 4) -> QuadMesh:
+    """Mesh2D::uniform_rectangle_with_sides: ``sides`` are the tags of the
+    [south, east, north, west] sides."""
+    verts, elems = _structured(x0, x1, y0, y1, nx, ny)
+    tags = np.tile(np.array(sides, dtype=np.int32), (nx * ny, 1))
+    return QuadMesh(verts, elems, np.zeros((0, 4), np.int64), tags)
+
+
+def uniform_periodic(x0, x1, y0, y1, nx, ny) -> QuadMesh:
+    """Mesh2D::uniform_periodic (src/mesh/core/mesh2d.rs:398-414)."""
+    verts, elems = _structured(x0, x1, y0, y1, nx, ny)
+    pairs = [(j * nx + nx - 1, 1, j * nx, 3) for j in range(ny)]
+    pairs += [((ny - 1) * nx + i, 2, i, 0) for i in range(nx)]
+    return QuadMesh(verts, elems, np.array(pairs, np.int64).reshape(-1, 4),
+                    np.zeros((nx * ny, 4), np.int32))
+
+
+def channel_periodic_x(x0, x1, y0, y1, nx, ny, south=TAG_WALL, north=TAG_WALL) -> QuadMesh:
+    """Mesh2D::channel_periodic_x_with_sides (src/mesh/core/mesh2d.rs:365-393)."""
+    verts, elems = _structured(x0, x1, y0, y1, nx, ny)
+    pairs = [(j * nx + nx - 1, 1, j * nx, 3) for j in range(ny)]
+    tags = np.zeros((nx * ny, 4), np.int32)
+    tags[:, 0] = south
+    tags[:, 2] = north
+    return QuadMesh(verts, elems, np.array(pairs, np.int64).reshape(-1, 4), tags)
+
+
+def move_vertices(mesh: QuadMesh, fn) -> QuadMesh:
+    """The mesh with every vertex moved to fn(x, y) (vectorised)."""
+    x, y = fn(mesh.vertices[:, 0], mesh.vertices[:, 1])
+    return QuadMesh(np.stack([x, y], axis=1), mesh.elements, mesh.periodic, mesh.face_tags)
+
+
+def hilbert_index(x: np.ndarray, y: np.ndarray, bits: int) -> np.ndarray:
+    """Position of the cells (x, y) of a 2^bits grid along the Hilbert curve
+    (src/mesh/core/mesh2d.rs:112-132), vectorised."""
+    x = x.astype(np.uint64).copy()
+    y = y.astype(np.uint64).copy()
+    d = np.zeros_like(x)
+    s = np.uint64(1 << (bits - 1))
+    while s > 0:
+        rx = (x & s) != 0
+        ry = (y & s) != 0
+        d += s * s * ((np.uint64(3) * rx.astype(np.uint64)) ^ ry.astype(np.uint64))
+        x &= s - np.uint64(1)
+        y &= s - np.uint64(1)
+        flip = (~ry) & rx
+        x = np.where(flip, s - np.uint64(1) - x, x)
+        y = np.where(flip, s - np.uint64(1) - y, y)
+        swap = ~ry
+        x, y = np.where(swap, y, x), np.where(swap, x, y)
+        s = np.uint64(int(s) >> 1)
+    return d
+
+
+def in_hilbert_order(mesh: QuadMesh) -> tuple[QuadMesh, np.ndarray]:
+    """The mesh with its elements along a Hilbert curve through their
+    centroids (Mesh2D::in_hilbert_order, src/mesh/core/mesh2d.rs:711-760),
+    and for each new element its old index. Periodic pairs are renumbered."""
+    c = mesh.corners().mean(axis=1)
+    lo, hi = c.min(axis=0), c.max(axis=0)
+    span = np.where(hi > lo, hi - lo, 1.0)
+    cells = np.minimum(((c - lo) / span * 65535.0).astype(np.int64), 65535)
+    order = np.argsort(hilbert_index(cells[:, 0], cells[:, 1], 16), kind="stable")
+    new_of_old = np.empty_like(order)
+    new_of_old[order] = np.arange(order.size)
+    periodic = mesh.periodic.copy()
+    if periodic.size:
+        periodic[:, 0] = new_of_old[periodic[:, 0]]
+        periodic[:, 2] = new_of_old[periodic[:, 2]]
+    tags = None if mesh.face_tags is None else mesh.face_tags[order]
+    return QuadMesh(mesh.vertices, mesh.elements[order], periodic, tags), order
+
+
+def graded_jittered_box(lx: float, ly: float, nx: int, ny: int, size_range=(100.0, 400.0),
+                        jitter: float = 0.15, seed: int = 0,
+                        sides=(TAG_WALL, TAG_WALL, TAG_WALL, TAG_OPEN)) -> QuadMesh:
+    """A synthetic unstructured-like quad paving of [0, lx]×[0, ly]: a
+    tensor grid whose column widths and row heights are graded smoothly
+    within ``size_range`` (so the aspect ratio stays below max/min), its
+    interior vertices jittered by up to ``jitter`` × the local size with a
+    seeded generator. The element corners stay counter-clockwise and the
+    Jacobians positive (jitter < ¼)."""
+    rng = np.random.default_rng(seed)
+
+    def graded(length, n, phase):
+        t = (np.arange(n) + 0.5) / n
+        lo, hi = size_range
+        w = lo + (hi - lo) * 0.5 * (1.0 + np.sin(2.0 * np.pi * (1.7 * t + phase)))
+        w = w * (length / w.sum())
+        edges = np.concatenate([[0.0], np.cumsum(w)])
+        edges[-1] = length
+        return edges, w
+
+    ex, wx = graded(lx, nx, rng.uniform())
+    ey, wy = graded(ly, ny, rng.uniform())
+    vx = np.tile(ex, ny + 1)
+    vy = np.repeat(ey, nx + 1)
+    # local size at each vertex: the smaller neighbouring width/height
+    sx = np.minimum(np.concatenate([[wx[0]], wx]), np.concatenate([wx, [wx[-1]]]))
+    sy = np.minimum(np.concatenate([[wy[0]], wy]), np.concatenate([wy, [wy[-1]]]))
+    lx_loc = np.tile(sx, ny + 1)
+    ly_loc = np.repeat(sy, nx + 1)
+    ii = np.tile(np.arange(nx + 1), ny + 1)
+    jj = np.repeat(np.arange(ny + 1), nx + 1)
+    interior = (ii > 0) & (ii < nx) & (jj > 0) & (jj < ny)
+    dx = rng.uniform(-jitter, jitter, vx.size) * lx_loc
+    dy = rng.uniform(-jitter, jitter, vy.size) * ly_loc
+    vx = np.where(interior, vx + dx, vx)
+    vy = np.where(interior, vy + dy, vy)
+    verts = np.stack([vx, vy], axis=1)
+    jg, ig = np.meshgrid(np.arange(ny), np.arange(nx), indexing="ij")
+    v0 = (jg * (nx + 1) + ig).ravel().astype(np.int64)
+    elems = np.stack([v0, v0 + 1, v0 + nx + 2, v0 + nx + 1], axis=1)
+    tags = np.tile(np.array(sides, dtype=np.int32), (nx * ny, 1))
+    return QuadMesh(verts, elems, np.zeros((0, 4), np.int64), tags)

@@ -1,0 +1,158 @@
+"""The 2D physics as the device runs it: ``SWEDeviceForm2D``
+(src/physics/device.rs:27-62) as plain host data, turned into the C ABI's
+``dgswe_form`` by :meth:`SWEDeviceForm2D.to_c`.
+
+Defaults follow the reference's case runner (src/case/run.rs:642-787): g =
+9.81, h_min = 1e-6, the `WetDry` split form with subcells below 1 mm, the
+wet/dry correction with h_dry = 1 mm, a 1 s thin-layer time and a 20 m/s
+velocity cap, its positivity-bounded step, and walls (Reflective2D,
+h_min 1e-6) on untagged faces."""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import abi
+from .mesh import TAG_WALL, QuadMesh, node_positions
+
+
+@dataclass
+class WallBoundary:
+    """Reflective2D (src/boundary/boundary_2d.rs:249-300)."""
+
+    h_min: float = 1e-6
+
+
+@dataclass
+class TidalBoundary:
+    """CharacteristicOBC with a uniform HarmonicTide
+    (src/boundary/characteristic.rs:360-437, src/boundary/harmonic_tide.rs)."""
+
+    constituents: list = field(default_factory=list)  # abi.TideConstituent
+    mean_elevation: float = 0.0
+    ramp_duration: float | None = 3600.0
+    incoming_wave: bool = False
+
+
+@dataclass
+class SWEDeviceForm2D:
+    mesh: QuadMesh
+    order: int
+    bathymetry: np.ndarray | None = None  # (n_elements, (N+1)²)
+    g: float = 9.81
+    h_min: float = 1e-6
+    formulation: int = abi.WET_DRY
+    subcell_depth: float = 1e-3
+    subcell_h_dry: float = 1e-3
+    wet_dry: bool = True
+    h_dry: float = 1e-3
+    relaxation_time: float = 1.0
+    max_velocity: float = 20.0
+    positivity_h_dry: float | None = 1e-3
+    manning_n: float | np.ndarray | None = None  # uniform n, or n per node
+    friction_g: float | None = None
+    manning_h_min: float = 1e-6
+    coriolis_f0: float | None = None
+    coriolis_beta: float = 0.0
+    coriolis_y0: float = 0.0
+    boundaries: dict = field(default_factory=lambda: {TAG_WALL: WallBoundary()})
+    numerics: int = abi.NUMERICS_FAST
+
+    @property
+    def n_nodes(self) -> int:
+        return (self.order + 1) ** 2
+
+    @property
+    def n_values(self) -> int:
+        return self.mesh.n_elements * self.n_nodes
+
+    def positions(self):
+        return node_positions(self.mesh, self.order)
+
+    def to_c(self) -> tuple[abi.Form, list]:
+        """The C form and the objects that must outlive it."""
+        keep: list = []
+
+        def arr(a, dtype):
+            a = np.ascontiguousarray(a, dtype=dtype)
+            keep.append(a)
+            return a
+
+        f = abi.Form()
+        f.abi_version = abi.ABI_VERSION
+        f.order = self.order
+        v = arr(self.mesh.vertices, np.float64)
+        f.n_vertices = v.shape[0]
+        f.vertices = v.ctypes.data_as(C.POINTER(C.c_double))
+        e = arr(self.mesh.elements, np.int64)
+        f.n_elements = e.shape[0]
+        f.elements = e.ctypes.data_as(C.POINTER(C.c_int64))
+        p = arr(self.mesh.periodic.reshape(-1, 4), np.int64)
+        f.n_periodic = p.shape[0]
+        f.periodic = p.ctypes.data_as(C.POINTER(C.c_int64)) if p.size else None
+        if self.mesh.face_tags is not None:
+            t = arr(self.mesh.face_tags, np.int32)
+            f.face_tags = t.ctypes.data_as(C.POINTER(C.c_int32))
+        if self.bathymetry is not None:
+            b = arr(self.bathymetry.reshape(-1), np.float64)
+            if b.size != self.n_values:
+                raise ValueError("bathymetry needs one value per node")
+            f.bathymetry = b.ctypes.data_as(C.POINTER(C.c_double))
+        f.g = self.g
+        f.h_min = self.h_min
+        f.formulation = self.formulation
+        f.subcell_depth = self.subcell_depth
+        f.subcell_h_dry = self.subcell_h_dry
+        f.has_wet_dry = 1 if self.wet_dry else 0
+        f.wet_dry_h_dry = self.h_dry
+        f.wet_dry_relaxation_time = self.relaxation_time
+        f.wet_dry_max_velocity = self.max_velocity
+        f.positivity_h_dry = self.positivity_h_dry or 0.0
+        if self.manning_n is None:
+            f.friction = abi.FRICTION_NONE
+        elif np.ndim(self.manning_n) == 0:
+            f.friction = abi.FRICTION_MANNING
+            f.manning_n = float(self.manning_n)
+        else:
+            f.friction = abi.FRICTION_MANNING_NODES
+            n = arr(np.asarray(self.manning_n).reshape(-1), np.float64)
+            if n.size != self.n_values:
+                raise ValueError("per-node Manning needs one value per node")
+            f.manning_n_nodes = n.ctypes.data_as(C.POINTER(C.c_double))
+        f.friction_g = self.g if self.friction_g is None else self.friction_g
+        f.manning_h_min = self.manning_h_min
+        f.has_coriolis = 0 if self.coriolis_f0 is None else 1
+        f.coriolis_f0 = self.coriolis_f0 or 0.0
+        f.coriolis_beta = self.coriolis_beta
+        f.coriolis_y0 = self.coriolis_y0
+        bcs = (abi.Boundary * max(1, len(self.boundaries)))()
+        for i, (tag, bc) in enumerate(sorted(self.boundaries.items())):
+            bcs[i].tag = tag
+            if isinstance(bc, WallBoundary):
+                bcs[i].kind = abi.BC_WALL
+                bcs[i].wall_h_min = bc.h_min
+            else:
+                bcs[i].kind = abi.BC_CHARACTERISTIC
+                bcs[i].elevation_only = abi.INCOMING_WAVE if bc.incoming_wave else abi.AT_REST
+                cons = (abi.TideConstituent * max(1, len(bc.constituents)))(*bc.constituents)
+                keep.append(cons)
+                bcs[i].n_constituents = len(bc.constituents)
+                bcs[i].constituents = cons
+                bcs[i].mean_elevation = bc.mean_elevation
+                bcs[i].ramp_duration = bc.ramp_duration or 0.0
+        keep.append(bcs)
+        f.n_boundaries = len(self.boundaries)
+        f.boundaries = bcs
+        f.numerics = self.numerics
+        return f, keep
+
+
+def at_rest(form: SWEDeviceForm2D, eta: float = 0.0):
+    """Still water at level ``eta``: h = max(0, η − B), no momentum
+    (src/case/run.rs:1157-1170)."""
+    b = np.zeros(form.n_values) if form.bathymetry is None else form.bathymetry.reshape(-1)
+    h = np.maximum(eta - b, 0.0)
+    return h, np.zeros_like(h), np.zeros_like(h)

@@ -1,0 +1,318 @@
+/*
+ * dgswe.h — C ABI of the GB300 (sm_103a) FP64 2D shallow-water nodal-DG
+ * stage: the split-form `WetDry` right-hand side on unstructured quads with
+ * its SSP Runge–Kutta stage update, numerical flux, sources and wet/dry
+ * limiter.
+ *
+ * This is the boundary a host in another language binds (a Rust
+ * `CaseDevice` implementation through `extern "C"`, Python through ctypes):
+ * plain C structs, plain pointers and sizes, `int` status codes, no C++
+ * types and no exceptions across it. Every entry point below names the
+ * reference interface it replaces (EmilLindfors/dgcom, paths relative to
+ * that repository).
+ *
+ * Conventions
+ *  - A solution crosses the ABI as the reference's SoA layout
+ *    (`SWESolution2D::data[var][k·n_nodes + i]`,
+ *    src/solver/core/system_solution.rs:135-142): three arrays h, hu, hv of
+ *    n_elements·(order+1)² doubles, node i = j·(order+1) + a with r fastest
+ *    (src/operators/operators_2d.rs:388-412).
+ *  - Arrays passed in a `dgswe_form` are copied by `dgswe_create`; the caller
+ *    keeps ownership. The handle owns all device memory.
+ *  - A handle is used by one host thread at a time; each handle has its own
+ *    CUDA stream.
+ *  - Every function returns DGSWE_OK (0) or a status; the handle keeps a
+ *    message (`dgswe_last_error`).
+ */
+#ifndef DGSWE_H
+#define DGSWE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DGSWE_ABI_VERSION 1u
+
+/* ---- status codes ------------------------------------------------------ */
+enum dgswe_status {
+    DGSWE_OK = 0,
+    DGSWE_ERR_INVALID = 1,     /* invalid input: form, sizes, pointers, buffer ids */
+    DGSWE_ERR_CUDA = 2,        /* a CUDA call failed (message names it) */
+    DGSWE_ERR_NONFINITE = 3,   /* the state is not finite: the run blew up */
+    DGSWE_ERR_DT_MIN = 4,      /* time step below the run's dt_min */
+    DGSWE_ERR_MAX_STEPS = 5,   /* the run's step limit was reached */
+    DGSWE_ERR_STOPPED = 6,     /* the stop flag was set */
+    DGSWE_ERR_UNSUPPORTED = 7, /* physics this device does not run */
+    DGSWE_ERR_NO_DEVICE = 8    /* no CUDA device (or not the requested one) */
+};
+
+/* ---- physics as data (src/physics/device.rs:27-62) ---------------------- */
+
+/* SWEFormulation2D (src/solver/rhs/swe_2d.rs:42-90): the split forms. */
+enum dgswe_formulation {
+    DGSWE_WET_DRY = 0,
+    DGSWE_ENTROPY_STABLE = 1,
+    DGSWE_ENTROPY_CONSERVATIVE = 2
+};
+
+/* DeviceBoundary2D (src/boundary/boundary_2d.rs:213-231). */
+enum dgswe_boundary_kind {
+    DGSWE_BC_WALL = 0,          /* Reflective2D: free-slip mirror ghost state */
+    DGSWE_BC_CHARACTERISTIC = 1 /* CharacteristicOBC with a uniform harmonic tide */
+};
+
+/* ElevationOnly (src/boundary/characteristic.rs:347-355). */
+enum dgswe_elevation_only {
+    DGSWE_AT_REST = 0,
+    DGSWE_INCOMING_WAVE = 1
+};
+
+/* DeviceFriction2D: Manning (src/source/swe_2d/friction.rs:195-348) or
+ * SpatiallyVaryingManning2D (friction.rs:463-620). */
+enum dgswe_friction {
+    DGSWE_FRICTION_NONE = 0,
+    DGSWE_FRICTION_MANNING = 1,      /* uniform n */
+    DGSWE_FRICTION_MANNING_NODES = 2 /* n per node (manning_n_nodes) */
+};
+
+/* SspScheme (src/time/integrator.rs:226-298). */
+enum dgswe_scheme {
+    DGSWE_SSP_RK3 = 0,
+    DGSWE_SSP_RK43 = 1
+};
+
+/* Device arithmetic. FAST contracts multiply-adds into FMA and evaluates
+ * the Manning rate's h^(-4/3) by FP64 Newton steps from a single-precision
+ * seed; EXACT keeps every multiply and add separately rounded and follows
+ * the reference's cube root (src/source/swe_2d/friction.rs:39-70). Both use
+ * IEEE division and square root and are FP64 throughout. */
+enum dgswe_numerics {
+    DGSWE_NUMERICS_FAST = 0,
+    DGSWE_NUMERICS_EXACT = 1
+};
+
+/* One tidal constituent of a uniform HarmonicTide
+ * (src/boundary/harmonic_tide.rs:124-136) with its nodal drift
+ * (src/tides/astronomy.rs:240-270): its term at time t is
+ *   (f + f_rate·t)·amplitude·cos(2π t/period + phase + (v0_deg + u_deg + u_rate_deg·t)·π/180).
+ * Without nodal corrections f = 1 and the other drift terms are 0. */
+typedef struct dgswe_tide_constituent {
+    double amplitude;  /* m */
+    double period;     /* s */
+    double phase;      /* rad, internal phase φ = −G (Greenwich lag) */
+    double f;          /* nodal factor at t = 0 */
+    double f_rate;     /* its drift per second */
+    double u_deg;      /* nodal phase at t = 0 (deg) */
+    double u_rate_deg; /* its drift per second (deg/s) */
+    double v0_deg;     /* equilibrium argument at t = 0 (deg) */
+} dgswe_tide_constituent;
+
+/* The condition of the boundary faces tagged `tag`. */
+typedef struct dgswe_boundary {
+    int32_t tag;            /* the face tag this condition applies to */
+    int32_t kind;           /* dgswe_boundary_kind */
+    double wall_h_min;      /* Reflective2D::h_min (wall) */
+    int32_t elevation_only; /* dgswe_elevation_only (characteristic) */
+    int32_t n_constituents; /* characteristic: harmonic tide terms */
+    const dgswe_tide_constituent* constituents;
+    double mean_elevation;  /* η₀ (m), not ramped */
+    double ramp_duration;   /* s; ≤ 0: no ramp (src/boundary/harmonic_tide.rs:24-32) */
+} dgswe_boundary;
+
+/* SWEDeviceForm2D (src/physics/device.rs:27-62) as plain data, with the
+ * mesh as Mesh2D::from_quads takes it (src/mesh/core/mesh2d.rs:456-470). */
+typedef struct dgswe_form {
+    uint32_t abi_version;     /* DGSWE_ABI_VERSION */
+    int32_t order;            /* polynomial order N, 1..4 */
+
+    int64_t n_vertices;
+    const double* vertices;   /* [n_vertices][2] x, y */
+    int64_t n_elements;
+    const int64_t* elements;  /* [n_elements][4] vertex indices, counter-clockwise */
+    int64_t n_periodic;
+    const int64_t* periodic;  /* [n_periodic][4] (element_a, face_a, element_b, face_b) */
+    const int32_t* face_tags; /* [n_elements][4] tag of each boundary face; NULL: tag 0 */
+
+    const double* bathymetry; /* [n_elements·(N+1)²] bed elevation B; NULL: flat 0 */
+
+    double g;                 /* gravity (ShallowWater2D::g) */
+    double h_min;             /* velocity threshold (ShallowWater2D::h_min) */
+    int32_t formulation;      /* dgswe_formulation */
+    double subcell_depth;     /* WetDry: subcells where a node is shallower */
+    double subcell_h_dry;     /* WetDry: the subcells' dry-node depth */
+
+    int32_t has_wet_dry;      /* WetDryConfig after every stage (wetting_drying.rs:51-175) */
+    double wet_dry_h_dry;
+    double wet_dry_relaxation_time;
+    double wet_dry_max_velocity;
+    double positivity_h_dry;  /* h_dry of the positivity-bounded step; ≤ 0: no bound */
+
+    int32_t friction;         /* dgswe_friction */
+    double friction_g;        /* the law's g (g·n² per node) */
+    double manning_n;         /* uniform n */
+    double manning_h_min;     /* depth floor of the law */
+    const double* manning_n_nodes; /* [n_elements·(N+1)²] n per node (MANNING_NODES) */
+
+    int32_t has_coriolis;     /* CoriolisSource2D (src/source/swe_2d/coriolis.rs:151-175) */
+    double coriolis_f0;
+    double coriolis_beta;
+    double coriolis_y0;
+
+    int32_t n_boundaries;
+    const dgswe_boundary* boundaries;
+
+    int32_t numerics;         /* dgswe_numerics */
+} dgswe_form;
+
+/* ---- stages and runs ---------------------------------------------------- */
+
+/* Device solution buffers: 0 is the state, 1.. stage values. */
+#define DGSWE_STATE 0
+#define DGSWE_N_BUFFERS 6
+
+/* One stage pass over every element (ElementStage,
+ * src/time/multirate.rs:169-200):
+ *   out = a·base + b·input + c·F(input)   (a term only where its weight ≠ 0),
+ * then the point-implicit damping with weight c, then either
+ *   acc ← w·out + keep·acc   (accumulate ≠ 0; the acc term only if keep ≠ 0)
+ * or the post-processing (wet/dry correction) of out. */
+typedef struct dgswe_stage_plan {
+    int32_t base;       /* buffer id of the step start */
+    int32_t input;      /* buffer id of the RHS argument */
+    int32_t out;        /* buffer id written */
+    int32_t acc;        /* buffer id summed into (accumulate ≠ 0) */
+    double time;        /* stage time (boundary data) */
+    double a, b, c;
+    int32_t accumulate;
+    double w, keep;
+} dgswe_stage_plan;
+
+/* DeviceRun (src/case/run.rs:273-289) as plain data. */
+typedef struct dgswe_run_config {
+    int32_t scheme;            /* dgswe_scheme */
+    double cfl;
+    double t_start, t_end;     /* span (s) */
+    double interval;           /* callback interval (s); ≤ 0: every step */
+    double dt_max;             /* ≤ 0: none */
+    double dt_min;             /* ≤ 0: none */
+    int64_t max_steps;         /* ≤ 0: none */
+    const volatile int32_t* stop; /* nonzero stops the run at its next step; NULL: none */
+} dgswe_run_config;
+
+/* DeviceRunReport (src/case/run.rs:292-300) with its SimulationResult. */
+typedef struct dgswe_report {
+    int32_t success;
+    double final_time;
+    int64_t n_steps;
+    double dt_min_used;
+    double dt_max_used;
+    double wall_time;
+    int64_t negative_depth_clips;
+    char message[256];
+    char device[128];
+} dgswe_report;
+
+/* The run's callback: the state on the host at time t (n values per field).
+ * The arrays are valid during the call only. */
+typedef void (*dgswe_callback)(void* user, double t, const double* h,
+                               const double* hu, const double* hv, int64_t n);
+
+/* Per-kernel timing of device-driven steps (dgswe_profile_steps). */
+typedef struct dgswe_profile {
+    int64_t steps;          /* steps timed */
+    double total_ms;        /* device time from the first launch to the last */
+    double face_ms;         /* summed durations of the face kernels */
+    double stage_ms;        /* of the element stage kernels */
+    double dt_ms;           /* of the element time-step kernels */
+    double control_ms;      /* of the one-thread clock kernels */
+    int64_t face_launches, stage_launches, dt_launches, control_launches;
+    double t_final;         /* model time after the steps */
+} dgswe_profile;
+
+typedef struct dgswe_handle dgswe_handle;
+
+/* ---- entry points ------------------------------------------------------- */
+
+/* ABI version of the library (DGSWE_ABI_VERSION it was built with). */
+uint32_t dgswe_abi_version(void);
+
+/* Text of a status code. */
+const char* dgswe_status_string(int status);
+
+/* The device's physics from `form` on CUDA device `device`: the handle of
+ * a run. Replaces GpuSWE2D::from_form (gpu/src/swe2d.rs:3360) behind
+ * CaseDevice::run_2d (src/case/run.rs:179-192); refuses physics without a
+ * device form as SWEPhysics2D::device_form does (src/physics/device.rs:79-142). */
+int dgswe_create(const dgswe_form* form, int device, dgswe_handle** out);
+
+/* Frees the handle and its device memory. NULL is ignored. */
+void dgswe_destroy(dgswe_handle* handle);
+
+/* The message of the handle's last failure ("" if none). */
+const char* dgswe_last_error(const dgswe_handle* handle);
+
+/* Values per field of a solution: n_elements·(N+1)². */
+int64_t dgswe_n_values(const dgswe_handle* handle);
+
+/* Copies a solution into / out of a device buffer (DGSWE_STATE: the state).
+ * Replaces DeviceState::upload / download (gpu/src/case.rs:36-70). */
+int dgswe_upload(dgswe_handle* handle, int32_t buffer, const double* h,
+                 const double* hu, const double* hv, int64_t n);
+int dgswe_download(dgswe_handle* handle, int32_t buffer, double* h, double* hu,
+                   double* hv, int64_t n);
+
+/* The RHS of buffer `input` at `time` into out_* (host): PhysicsModule::
+ * compute_rhs_into (src/physics/builder.rs:425-434) →
+ * compute_rhs_swe_2d_parallel_into (src/solver/rhs/swe_2d.rs:1478-1488). */
+int dgswe_compute_rhs(dgswe_handle* handle, int32_t input, double time,
+                      double* out_h, double* out_hu, double* out_hv, int64_t n);
+
+/* One stage pass over every element: LocalTimeStepping::stage_where
+ * (src/physics/builder.rs:652-737). */
+int dgswe_stage(dgswe_handle* handle, const dgswe_stage_plan* plan);
+
+/* End of a substep over every element: state ← acc, then the post-processing
+ * (LocalTimeStepping::finish_where, src/physics/builder.rs:739-782). */
+int dgswe_finish(dgswe_handle* handle, int32_t acc);
+
+/* Every element's stable step at `cfl` for `scheme` (element_dt_swe_2d,
+ * src/solver/rhs/swe_2d.rs:2008-2031, with the positivity bound of a
+ * wet/dry run) into dt_elements (n_elements values; may be NULL), and their
+ * minimum (min_element_dt_swe_2d, swe_2d.rs:2045-2068) into dt_min (may be
+ * NULL). Reads the state buffer. */
+int dgswe_element_dt(dgswe_handle* handle, double cfl, int32_t scheme,
+                     double* dt_elements, double* dt_min);
+
+/* One global SSP step of dt from t on the state, the stages fused per
+ * element (MultirateStepper::step with one level,
+ * src/time/multirate.rs:1285-1315). */
+int dgswe_step(dgswe_handle* handle, int32_t scheme, double t, double dt);
+
+/* Simulation::run_with_callback (src/simulation/runner.rs:264-500) on the
+ * state: dt from the positivity-bounded element steps, capped by dt_max,
+ * landing on every callback time and the end; the callback gets the state
+ * on the host at the start, every interval and the end. */
+int dgswe_run(dgswe_handle* handle, const dgswe_run_config* run,
+              dgswe_callback callback, void* user, dgswe_report* report);
+
+/* Elements emptied because their mean depth went negative, summed over
+ * every stage so far (SWEPhysics2D::negative_depth_clips,
+ * src/physics/builder.rs:204). */
+int64_t dgswe_negative_depth_clips(const dgswe_handle* handle);
+
+/* Times n_steps device-driven steps of the state from run->t_start (the
+ * run's scheme, cfl and dt_max; no end time), every kernel bracketed by CUDA
+ * events on the handle's stream, into `out`. The GPU counterpart of the
+ * reference's DG_PROFILE scope timers (src/profiling.rs:1-90); advances the
+ * state like dgswe_run. */
+int dgswe_profile_steps(dgswe_handle* handle, const dgswe_run_config* run,
+                        int64_t n_steps, dgswe_profile* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DGSWE_H */

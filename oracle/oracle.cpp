@@ -1,0 +1,1555 @@
+// Oracle — test infrastructure only (see pointwise.hpp). A CPU restatement
+// of the reference's 2D shallow-water split-form RHS, its fused SSP stage,
+// time-step bound and run loop (EmilLindfors/dgcom), for checking the CUDA
+// library and for timing the CPU baseline. Each function cites the
+// reference file:line it follows. Built with -ffp-contract=off; OpenMP runs
+// the element loops in parallel (each element's result does not depend on
+// the thread count, as in the reference's rayon loops).
+//
+// Parity is pinned only through the reference's own known-answer and
+// property tests: the reference is Rust and no Rust toolchain exists where
+// this is built, so no output of the reference itself was available.
+// The 1D differentiation matrix is the exact Lagrange derivative at the
+// reference's GLL nodes evaluated in long double; the reference inverts a
+// Vandermonde matrix with faer (src/operators/differentiation.rs:19-36), so
+// the last bits of D are not pinned.
+
+#include "oracle.h"
+
+#include <algorithm>
+#include <array>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "pointwise.hpp"
+
+namespace oracle {
+
+static const double INF = std::numeric_limits<double>::infinity();
+
+// ---------------------------------------------------------------------------
+// Operators (src/operators/operators_2d.rs:114-190, src/polynomial/nodes.rs)
+
+// legendre_and_derivative (src/polynomial/legendre.rs:62-94)
+static void legendre_and_derivative(int n, double x, double& p, double& dp) {
+    if (n == 0) {
+        p = 1.0;
+        dp = 0.0;
+        return;
+    }
+    if (n == 1) {
+        p = x;
+        dp = 1.0;
+        return;
+    }
+    double p_prev = 1.0, p_curr = x;
+    for (int k = 1; k < n; ++k) {
+        double p_next = ((double)(2 * k + 1) * x * p_curr - (double)k * p_prev) / (double)(k + 1);
+        p_prev = p_curr;
+        p_curr = p_next;
+    }
+    p = p_curr;
+    if (std::fabs(x - 1.0) < 1e-14)
+        dp = (double)(n * (n + 1)) / 2.0;
+    else if (std::fabs(x + 1.0) < 1e-14)
+        dp = (n % 2 == 0 ? -1.0 : 1.0) * (double)(n * (n + 1)) / 2.0;
+    else
+        dp = (double)n * (x * p_curr - p_prev) / (x * x - 1.0);
+}
+
+static double legendre(int n, double x) {
+    double p, dp;
+    legendre_and_derivative(n, x, p, dp);
+    return p;
+}
+
+struct Ops {
+    int order = 0, n1 = 0, nn = 0;
+    std::vector<double> x1, w1, d1;  // GLL nodes, weights, D row-major
+    std::vector<double> nodes_r, nodes_s, w2;
+    int face_nodes[4][8];
+    std::vector<double> lift;  // [face][node][fi]
+
+    double lift_at(int face, int node, int fi) const { return lift[(face * nn + node) * n1 + fi]; }
+
+    explicit Ops(int order_) : order(order_), n1(order_ + 1), nn((order_ + 1) * (order_ + 1)) {
+        const int n = order;
+        // gauss_lobatto_nodes (src/polynomial/nodes.rs:17-77)
+        x1.resize(n1);
+        for (int j = 0; j <= n; ++j) x1[j] = -std::cos(M_PI * (double)j / (double)n);
+        x1[0] = -1.0;
+        x1[n] = 1.0;
+        for (int j = 1; j < n; ++j) {
+            double x = x1[j];
+            for (int it = 0; it < 100; ++it) {
+                double p, dp;
+                legendre_and_derivative(n, x, p, dp);
+                double update = (1.0 - x * x) * dp / ((double)n * (double)(n + 1) * p);
+                if (std::fabs(update) < 1e-15) break;
+                x += update;
+            }
+            x1[j] = x;
+        }
+        // gauss_lobatto_weights (src/polynomial/nodes.rs:82-103)
+        w1.resize(n1);
+        double denom = (double)(n * (n + 1));
+        for (int j = 0; j < n1; ++j) {
+            double p = legendre(n, x1[j]);
+            w1[j] = 2.0 / (denom * p * p);
+        }
+        // D: exact Lagrange derivative at these nodes (barycentric, long double)
+        d1.assign(n1 * n1, 0.0);
+        std::vector<long double> lam(n1);
+        for (int j = 0; j < n1; ++j) {
+            long double prod = 1.0L;
+            for (int k = 0; k < n1; ++k)
+                if (k != j) prod *= ((long double)x1[j] - (long double)x1[k]);
+            lam[j] = 1.0L / prod;
+        }
+        for (int i = 0; i < n1; ++i) {
+            long double diag = 0.0L;
+            for (int j = 0; j < n1; ++j) {
+                if (j == i) continue;
+                long double dij = (lam[j] / lam[i]) / ((long double)x1[i] - (long double)x1[j]);
+                d1[i * n1 + j] = (double)dij;
+                diag -= dij;
+            }
+            double dd = (double)diag;
+            d1[i * n1 + i] = std::fabs(dd) < 1e-14 ? 0.0 : dd;
+        }
+        // tensor_product_gll_nodes / weights (src/polynomial/legendre_2d.rs:108-144)
+        nodes_r.resize(nn);
+        nodes_s.resize(nn);
+        w2.resize(nn);
+        for (int j = 0; j < n1; ++j)
+            for (int a = 0; a < n1; ++a) {
+                nodes_r[j * n1 + a] = x1[a];
+                nodes_s[j * n1 + a] = x1[j];
+                w2[j * n1 + a] = w1[a] * w1[j];
+            }
+        // compute_face_nodes (src/operators/operators_2d.rs:388-412)
+        for (int a = 0; a < n1; ++a) face_nodes[0][a] = a;
+        for (int j = 0; j < n1; ++j) face_nodes[1][j] = j * n1 + (n1 - 1);
+        for (int q = 0; q < n1; ++q) face_nodes[2][q] = (n1 - 1) * n1 + (n1 - 1 - q);
+        for (int q = 0; q < n1; ++q) face_nodes[3][q] = (n1 - 1 - q) * n1;
+        // compute_lift_matrices (src/operators/operators_2d.rs:445-482):
+        // LIFT[face][i][j] = (1/w_i)·(E_f[j][i]·w1[j])
+        lift.assign(4 * nn * n1, 0.0);
+        for (int face = 0; face < 4; ++face)
+            for (int i = 0; i < nn; ++i)
+                for (int j = 0; j < n1; ++j) {
+                    double e = face_nodes[face][j] == i ? 1.0 : 0.0;
+                    double mass_inv = 1.0 / w2[i];
+                    lift[(face * nn + i) * n1 + j] = mass_inv * (e * w1[j]);
+                }
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Mesh (src/mesh/core/mesh2d.rs:456-620): Mesh2D::from_quads
+
+struct ElementFace {
+    int64_t element;
+    int face;
+};
+
+struct Edge {
+    ElementFace left;
+    ElementFace right;  // element < 0: boundary
+    int32_t tag;
+};
+
+struct Mesh {
+    std::vector<std::array<double, 2>> vertices;
+    std::vector<std::array<int64_t, 4>> elements;
+    std::vector<Edge> edges;
+    std::vector<std::array<int64_t, 4>> element_edges;
+    // FaceLink (src/mesh/core/mesh2d.rs:54-110) unpacked
+    struct Link {
+        int64_t element = -1;  // -1: boundary
+        int face = 0;
+        bool left = false, shared = false;
+    };
+    std::vector<std::array<Link, 4>> links;
+    int64_t n_elements = 0;
+
+    std::array<std::array<double, 2>, 4> corners(int64_t k) const {
+        std::array<std::array<double, 2>, 4> c;
+        for (int i = 0; i < 4; ++i) c[i] = vertices[elements[k][i]];
+        return c;
+    }
+
+    // Mesh2D::neighbor (src/mesh/core/mesh2d.rs:669-678)
+    bool neighbor(int64_t k, int face, ElementFace& nb) const {
+        const Edge& e = edges[element_edges[k][face]];
+        if (e.left.element == k && e.left.face == face) {
+            if (e.right.element < 0) return false;
+            nb = e.right;
+            return true;
+        }
+        nb = e.left;
+        return true;
+    }
+};
+
+static std::string build_mesh(const dgswe_form* f, Mesh& m) {
+    m.n_elements = f->n_elements;
+    m.vertices.resize(f->n_vertices);
+    for (int64_t i = 0; i < f->n_vertices; ++i)
+        m.vertices[i] = {f->vertices[2 * i], f->vertices[2 * i + 1]};
+    m.elements.resize(f->n_elements);
+    for (int64_t k = 0; k < f->n_elements; ++k)
+        for (int c = 0; c < 4; ++c) {
+            int64_t v = f->elements[4 * k + c];
+            if (v < 0 || v >= f->n_vertices) return "element uses a vertex that does not exist";
+            m.elements[k][c] = v;
+        }
+    auto face_vertices = [&](ElementFace fc) {
+        auto q = m.elements[fc.element];
+        return std::make_pair(q[fc.face], q[(fc.face + 1) % 4]);
+    };
+    auto key = [](std::pair<int64_t, int64_t> p) {
+        return std::make_pair(std::min(p.first, p.second), std::max(p.first, p.second));
+    };
+    std::map<std::pair<int64_t, int>, int64_t> pair_of;
+    for (int64_t p = 0; p < f->n_periodic; ++p) {
+        for (int s = 0; s < 2; ++s) {
+            int64_t e = f->periodic[4 * p + 2 * s];
+            int fc = (int)f->periodic[4 * p + 2 * s + 1];
+            if (e < 0 || e >= f->n_elements || fc < 0 || fc >= 4) return "invalid periodic face";
+            if (!pair_of.emplace(std::make_pair(e, fc), p).second) return "periodic face paired twice";
+        }
+    }
+    struct PairHash {
+        size_t operator()(const std::pair<int64_t, int64_t>& p) const {
+            return std::hash<int64_t>()(p.first * 1000003 + p.second);
+        }
+    };
+    std::unordered_map<std::pair<int64_t, int64_t>, int64_t, PairHash> edge_of_key;
+    edge_of_key.reserve(2 * f->n_elements + 16);
+    std::vector<int64_t> edge_of_pair(f->n_periodic, -1);
+    m.element_edges.assign(f->n_elements, {-1, -1, -1, -1});
+    m.edges.reserve(2 * f->n_elements + 64);
+    for (int64_t k = 0; k < f->n_elements; ++k) {
+        for (int fc = 0; fc < 4; ++fc) {
+            ElementFace face{k, fc};
+            auto it = pair_of.find({k, fc});
+            if (it != pair_of.end()) {
+                int64_t p = it->second;
+                if (edge_of_pair[p] < 0) {
+                    ElementFace l{f->periodic[4 * p], (int)f->periodic[4 * p + 1]};
+                    ElementFace r{f->periodic[4 * p + 2], (int)f->periodic[4 * p + 3]};
+                    edge_of_pair[p] = (int64_t)m.edges.size();
+                    m.edges.push_back({l, r, 0});
+                }
+                m.element_edges[k][fc] = edge_of_pair[p];
+                continue;
+            }
+            auto ab = face_vertices(face);
+            auto kk = key(ab);
+            auto found = edge_of_key.find(kk);
+            if (found == edge_of_key.end()) {
+                edge_of_key.emplace(kk, (int64_t)m.edges.size());
+                m.element_edges[k][fc] = (int64_t)m.edges.size();
+                m.edges.push_back({face, {-1, 0}, 0});
+            } else {
+                Edge& e = m.edges[found->second];
+                if (e.right.element >= 0) return "an edge is shared by more than two elements";
+                auto lv = face_vertices(e.left);
+                if (!(lv.first == ab.second && lv.second == ab.first))
+                    return "two faces traverse their shared edge in the same direction";
+                e.right = face;
+                m.element_edges[k][fc] = found->second;
+            }
+        }
+    }
+    for (int64_t p = 0; p < f->n_periodic; ++p)
+        for (int s = 0; s < 2; ++s) {
+            ElementFace fc{f->periodic[4 * p + 2 * s], (int)f->periodic[4 * p + 2 * s + 1]};
+            if (edge_of_key.count(key(face_vertices(fc)))) return "periodic face shared with another";
+        }
+    for (auto& e : m.edges)
+        if (e.right.element < 0)
+            e.tag = f->face_tags ? f->face_tags[4 * e.left.element + e.left.face] : 0;
+    m.links.assign(f->n_elements, {});
+    for (auto& e : m.edges) {
+        if (e.right.element < 0) continue;
+        auto lv = face_vertices(e.left);
+        auto rv = face_vertices(e.right);
+        bool shared = rv.first == lv.second && rv.second == lv.first;
+        m.links[e.left.element][e.left.face] = {e.right.element, e.right.face, true, shared};
+        m.links[e.right.element][e.right.face] = {e.left.element, e.left.face, false, shared};
+    }
+    return "";
+}
+
+// ---------------------------------------------------------------------------
+// Geometry (src/operators/geometric.rs:126-221)
+
+struct Metric {
+    double x_r, x_s, y_r, y_s, det;
+};
+
+// BilinearMetric::at (src/operators/geometric.rs:704-718)
+static Metric bilinear_metric(const std::array<std::array<double, 2>, 4>& v, double r, double s) {
+    double x0 = v[0][0], y0 = v[0][1], x1 = v[1][0], y1 = v[1][1];
+    double x2 = v[2][0], y2 = v[2][1], x3 = v[3][0], y3 = v[3][1];
+    Metric m;
+    m.x_r = 0.25 * ((1.0 - s) * (x1 - x0) + (1.0 + s) * (x2 - x3));
+    m.y_r = 0.25 * ((1.0 - s) * (y1 - y0) + (1.0 + s) * (y2 - y3));
+    m.x_s = 0.25 * ((1.0 - r) * (x3 - x0) + (1.0 + r) * (x2 - x1));
+    m.y_s = 0.25 * ((1.0 - r) * (y3 - y0) + (1.0 + r) * (y2 - y1));
+    m.det = m.x_r * m.y_s - m.x_s * m.y_r;
+    return m;
+}
+
+// is_parallelogram (src/operators/geometric.rs:722-733)
+static bool is_parallelogram(const std::array<std::array<double, 2>, 4>& v) {
+    double bx = v[0][0] - v[1][0] + v[2][0] - v[3][0];
+    double by = v[0][1] - v[1][1] + v[2][1] - v[3][1];
+    double scale = 0.0;
+    for (int i = 0; i < 4; ++i) {
+        auto a = v[i], b = v[(i + 1) % 4];
+        scale = fmax_(scale, std::hypot(b[0] - a[0], b[1] - a[1]));
+    }
+    return std::hypot(bx, by) <= 1.0e-12 * scale;
+}
+
+struct Geometry {
+    int nn = 0, n1 = 0;
+    std::vector<double> rx, ry, sx, sy, det_j, det_j_inv, mass, area;
+    std::vector<double> surface_j, nxv, nyv;  // per face node
+    std::vector<uint8_t> affine;
+
+    size_t fidx(int64_t k, int face, int fi) const { return ((size_t)k * 4 + face) * n1 + fi; }
+    size_t nidx(int64_t k, int i) const { return (size_t)k * nn + i; }
+    // contravariant (src/operators/geometric.rs:309-317)
+    void contravariant(int64_t k, int i, double& rx0, double& rx1, double& sx0, double& sx1) const {
+        size_t n = nidx(k, i);
+        double j = det_j[n];
+        rx0 = j * rx[n];
+        rx1 = j * ry[n];
+        sx0 = j * sx[n];
+        sx1 = j * sy[n];
+    }
+};
+
+static std::string build_geometry(const Mesh& mesh, const Ops& ops, Geometry& g) {
+    int64_t K = mesh.n_elements;
+    g.nn = ops.nn;
+    g.n1 = ops.n1;
+    size_t nv = (size_t)K * ops.nn, nf = (size_t)K * 4 * ops.n1;
+    g.rx.resize(nv);
+    g.ry.resize(nv);
+    g.sx.resize(nv);
+    g.sy.resize(nv);
+    g.det_j.resize(nv);
+    g.det_j_inv.resize(nv);
+    g.mass.resize(nv);
+    g.area.resize(K);
+    g.surface_j.resize(nf);
+    g.nxv.resize(nf);
+    g.nyv.resize(nf);
+    g.affine.resize(K);
+    bool bad = false;
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < K; ++k) {
+        auto v = mesh.corners(k);
+        g.affine[k] = is_parallelogram(v) ? 1 : 0;
+        double area = 0.0;
+        for (int i = 0; i < ops.nn; ++i) {
+            Metric m = bilinear_metric(v, ops.nodes_r[i], ops.nodes_s[i]);
+            if (!(std::isfinite(m.det) && m.det > 0.0)) bad = true;
+            size_t n = g.nidx(k, i);
+            g.rx[n] = m.y_s / m.det;
+            g.ry[n] = -m.x_s / m.det;
+            g.sx[n] = -m.y_r / m.det;
+            g.sy[n] = m.x_r / m.det;
+            g.det_j[n] = m.det;
+            g.det_j_inv[n] = 1.0 / m.det;
+            double mass = ops.w2[i] * m.det;
+            g.mass[n] = mass;
+            area += mass;
+        }
+        g.area[k] = area;
+        for (int face = 0; face < 4; ++face)
+            for (int fi = 0; fi < ops.n1; ++fi) {
+                int node = ops.face_nodes[face][fi];
+                Metric m = bilinear_metric(v, ops.nodes_r[node], ops.nodes_s[node]);
+                double vx, vy;
+                switch (face) {
+                    case 0: vx = m.y_r; vy = -m.x_r; break;
+                    case 1: vx = m.y_s; vy = -m.x_s; break;
+                    case 2: vx = -m.y_r; vy = m.x_r; break;
+                    default: vx = -m.y_s; vy = m.x_s; break;
+                }
+                double s_j = std::sqrt(vx * vx + vy * vy);
+                size_t fn = g.fidx(k, face, fi);
+                g.surface_j[fn] = s_j;
+                g.nxv[fn] = vx / s_j;
+                g.nyv[fn] = vy / s_j;
+            }
+    }
+    if (bad) return "GeometricFactors2D requires a positive finite Jacobian (degenerate, non-convex or clockwise element)";
+    return "";
+}
+
+// ---------------------------------------------------------------------------
+// The model: the form, its boundary conditions and buffers
+
+struct Boundary {
+    int kind = DGSWE_BC_WALL;
+    double wall_h_min = 1e-6;
+    int elevation_only = DGSWE_AT_REST;
+    std::vector<dgswe_tide_constituent> constituents;
+    double mean_elevation = 0.0, ramp_duration = 0.0;
+
+    // HarmonicTide::elevation (src/boundary/harmonic_tide.rs:124-136)
+    double elevation(double t) const {
+        double tide = 0.0;
+        for (const auto& c : constituents) {
+            double f = c.f + c.f_rate * t;
+            double u_deg = c.u_deg + c.u_rate_deg * t;
+            double omega = 2.0 * M_PI / c.period;
+            double offset = (c.v0_deg + u_deg) * (M_PI / 180.0);
+            tide += f * c.amplitude * std::cos(omega * t + c.phase + offset);
+        }
+        return mean_elevation + tidal_ramp(t, ramp_duration) * tide;
+    }
+};
+
+struct Buffer {
+    std::vector<double> h, hu, hv;
+    void resize(size_t n) {
+        h.assign(n, 0.0);
+        hu.assign(n, 0.0);
+        hv.assign(n, 0.0);
+    }
+    State get(size_t i) const { return {h[i], hu[i], hv[i]}; }
+};
+
+struct Model {
+    dgswe_form form;
+    Ops ops;
+    Mesh mesh;
+    Geometry geom;
+    std::vector<double> bed;  // per node (empty: no bathymetry)
+    std::vector<double> g_n2;  // per node (friction)
+    std::map<int32_t, Boundary> boundaries;
+    Buffer buf[DGSWE_N_BUFFERS];
+    std::vector<State> faces;  // face pass output: [edge][side][fi]
+    int64_t clips = 0;
+    std::string error;
+    WetDry wd;
+    bool has_bed = false;
+
+    explicit Model(int order) : ops(order) {}
+    size_t n_values() const { return (size_t)mesh.n_elements * ops.nn; }
+    double bed_at(int64_t k, int i) const { return has_bed ? bed[(size_t)k * ops.nn + i] : 0.0; }
+};
+
+// ---------------------------------------------------------------------------
+// RHS: SplitFormSWE2D (src/solver/rhs/swe_2d_split_form.rs:500-1123)
+
+struct Workspace {
+    std::vector<Node> nodes;
+    std::vector<State> rhs;
+    std::vector<std::pair<double, double>> metric, interfaces;
+    std::vector<std::pair<Side, Side>> faces;
+    struct Outer {
+        bool present = false;
+        Node node;
+        double distance = 0.0;
+    };
+    std::vector<Outer> outer;
+    explicit Workspace(const Ops& ops)
+        : nodes(ops.nn), rhs(ops.nn), metric(ops.n1), interfaces(ops.n1 + 1), faces(ops.n1),
+          outer(4 * ops.n1) {}
+};
+
+enum class SurfaceFlux { EntropyConservative, EntropyStable, HydrostaticHll };
+
+static SurfaceFlux surface_kind(const Model& m) {
+    switch (m.form.formulation) {
+        case DGSWE_ENTROPY_CONSERVATIVE: return SurfaceFlux::EntropyConservative;
+        case DGSWE_ENTROPY_STABLE: return SurfaceFlux::EntropyStable;
+        default: return SurfaceFlux::HydrostaticHll;
+    }
+}
+
+// SplitFormSWE2D::surface_flux (src/solver/rhs/swe_2d_split_form.rs:618-651)
+static void surface_flux(const Model& m, const Node& qa, const Node& qb, double nx, double ny,
+                         State& fa, State& fb) {
+    double g = m.form.g;
+    SurfaceFlux kind = surface_kind(m);
+    if (kind == SurfaceFlux::HydrostaticHll) {
+        State a, b;
+        hydrostatic_hll(side_of(qa), side_of(qb), nx, ny, g, m.form.h_min, a, b);
+        fa = a;
+        fb = -b;
+        return;
+    }
+    State shared = wintermeyer_flux(qa, qb, nx, ny, g);
+    if (kind == SurfaceFlux::EntropyStable) shared = shared + entropy_stable_dissipation(qa, qb, nx, ny, g);
+    fa = shared + bed_interface_term(qa.h, qa.b, qb.b, nx, ny, g);
+    fb = -shared + bed_interface_term(qb.h, qb.b, qa.b, -nx, -ny, g);
+}
+
+static Node node_at(const Model& m, const Buffer& q, int64_t k, int i) {
+    size_t n = (size_t)k * m.ops.nn + i;
+    return make_node(q.get(n), m.bed_at(k, i), m.form.h_min);
+}
+
+// The face normal of an element face node as the kernels read it: a
+// parallelogram's face-node-0 value, else the node's own
+static void face_normal(const Model& m, int64_t k, int face, int fi, double& nx, double& ny,
+                        double& s_j) {
+    const Geometry& g = m.geom;
+    size_t fn = g.affine[k] ? g.fidx(k, face, 0) : g.fidx(k, face, fi);
+    nx = g.nxv[fn];
+    ny = g.nyv[fn];
+    s_j = g.surface_j[fn];
+}
+
+// SplitFormSWE2D::edge_fluxes (src/solver/rhs/swe_2d_split_form.rs:580-616)
+static void edge_fluxes(const Model& m, const Buffer& q, int64_t e, State* out) {
+    const Edge& edge = m.mesh.edges[e];
+    if (edge.right.element < 0) return;
+    int n1 = m.ops.n1;
+    for (int fi = 0; fi < n1; ++fi) {
+        double nx, ny, sj;
+        face_normal(m, edge.left.element, edge.left.face, fi, nx, ny, sj);
+        int left_node = m.ops.face_nodes[edge.left.face][fi];
+        int rfi = n1 - 1 - fi;
+        int right_node = m.ops.face_nodes[edge.right.face][rfi];
+        State fl, fr;
+        surface_flux(m, node_at(m, q, edge.left.element, left_node),
+                     node_at(m, q, edge.right.element, right_node), nx, ny, fl, fr);
+        out[fi] = fl;
+        out[n1 + rfi] = fr;
+    }
+}
+
+// boundary_state (src/solver/rhs/swe_2d.rs:304-327) and
+// SplitFormSWE2D::boundary_flux (src/solver/rhs/swe_2d_split_form.rs:1090-1123)
+static State boundary_flux(const Model& m, int64_t k, int face, int node, const Node& q_int,
+                           double nx, double ny, double time, int32_t tag) {
+    double g = m.form.g, h_min = m.form.h_min;
+    auto it = m.boundaries.find(tag);
+    const Boundary& bc = it->second;
+    State interior{q_int.h, q_int.hu, q_int.hv};
+    if (bc.kind == DGSWE_BC_WALL) {
+        // Reflective2D::ghost_state (src/boundary/boundary_2d.rs:271-283)
+        State ghost;
+        if (interior.h <= bc.wall_h_min) {
+            ghost = {interior.h, 0.0, 0.0};
+        } else {
+            double u, v, ur, vr;
+            velocity_simple(interior, h_min, u, v);  // BCContext2D::interior_velocity
+            reflect_velocity(u, v, nx, ny, ur, vr);
+            ghost = {interior.h, interior.h * ur, interior.h * vr};
+        }
+        Node q_ext = make_node(ghost, q_int.b, h_min);
+        State fa, fb;
+        surface_flux(m, q_int, q_ext, nx, ny, fa, fb);
+        return fa;
+    }
+    // CharacteristicOBC with a uniform tide: characteristic_boundary_state
+    // (src/boundary/characteristic.rs:411-437)
+    double eta = bc.elevation(time);
+    double bathy = q_int.b;
+    double h_e = fmax_(eta - bathy, 0.0);
+    double un_e = 0.0;
+    if (bc.elevation_only == DGSWE_INCOMING_WAVE)
+        un_e = 2.0 * (std::sqrt(g * fmax_(-bathy, 0.0)) - std::sqrt(g * h_e));
+    double u, v;
+    velocity_simple(interior, h_min, u, v);
+    double ut_e = -u * ny + v * nx;
+    State qb = characteristic_state(interior, h_e, un_e, ut_e, nx, ny, g, h_min);
+    Node nb = make_node(qb, q_int.b, h_min);
+    (void)k;
+    (void)face;
+    (void)node;
+    return wintermeyer_flux(nb, nb, nx, ny, g);  // F(q_b)·n
+}
+
+// telescoped_interfaces (src/solver/rhs/subcells.rs:63-92)
+static void telescoped_interfaces(const Ops& ops, const std::vector<std::pair<double, double>>& metric,
+                                  bool affine, std::vector<std::pair<double, double>>& out) {
+    int n1 = ops.n1;
+    if (affine) {
+        for (int a = 0; a <= n1; ++a) out[a] = metric[0];
+        return;
+    }
+    out[0] = metric[0];
+    double m0 = 0.0, m1 = 0.0;
+    for (int a = 0; a < n1 - 1; ++a) {
+        for (int c = 0; c < n1; ++c) {
+            if (c == a) continue;
+            double q2 = 2.0 * ops.w1[a] * ops.d1[a * n1 + c];
+            m0 += q2 * 0.5 * (metric[a].first + metric[c].first);
+            m1 += q2 * 0.5 * (metric[a].second + metric[c].second);
+        }
+        out[a + 1] = {m0, m1};
+    }
+    out[n1] = metric[n1 - 1];
+}
+
+// SplitFormSWE2D::line_volume (src/solver/rhs/swe_2d_split_form.rs:843-894)
+template <class Idx>
+static void line_volume(const Model& m, Workspace& ws, Idx idx, bool affine,
+                        std::pair<double, double> affine_metric) {
+    const Ops& ops = m.ops;
+    int n1 = ops.n1;
+    const std::vector<double>& d1 = ops.d1;
+    double g = m.form.g;
+    for (int a = 0; a < n1; ++a) {
+        int ia = idx(a);
+        Node q_a = ws.nodes[ia];
+        std::pair<double, double> m_a = affine ? affine_metric : ws.metric[a];
+        State acc = (2.0 * d1[a * n1 + a]) * wintermeyer_flux(q_a, q_a, m_a.first, m_a.second, g);
+        for (int c = a + 1; c < n1; ++c) {
+            int ic = idx(c);
+            std::pair<double, double> mm;
+            if (affine) {
+                mm = m_a;
+            } else {
+                auto m_c = ws.metric[c];
+                mm = {0.5 * (m_a.first + m_c.first), 0.5 * (m_a.second + m_c.second)};
+            }
+            State f = wintermeyer_flux(q_a, ws.nodes[ic], mm.first, mm.second, g);
+            acc = acc + (2.0 * d1[a * n1 + c]) * f;
+            ws.rhs[ic] = ws.rhs[ic] - (2.0 * d1[c * n1 + a]) * f;
+        }
+        if (m.has_bed) {
+            double db = 0.0, db_x = 0.0, db_y = 0.0;
+            for (int c = 0; c < n1; ++c) {
+                double d_b = d1[a * n1 + c] * ws.nodes[idx(c)].b;
+                db += d_b;
+                if (!affine) {
+                    db_x += d_b * ws.metric[c].first;
+                    db_y += d_b * ws.metric[c].second;
+                }
+            }
+            double bx, by;
+            if (affine) {
+                bx = db * m_a.first;
+                by = db * m_a.second;
+            } else {
+                bx = 0.5 * (db * m_a.first + db_x);
+                by = 0.5 * (db * m_a.second + db_y);
+            }
+            double force = g * q_a.h;
+            acc = acc + State{0.0, force * bx, force * by};
+        }
+        ws.rhs[ia] = ws.rhs[ia] - acc;
+    }
+}
+
+// SplitFormSWE2D::line_subcells (src/solver/rhs/swe_2d_split_form.rs:938-1035)
+template <class Idx>
+static void line_subcells(const Model& m, Workspace& ws, Idx idx, const Workspace::Outer& end0,
+                          const Workspace::Outer& end1, bool affine) {
+    const Ops& ops = m.ops;
+    int n1 = ops.n1;
+    const std::vector<double>& w = ops.w1;
+    const std::vector<double>& xi = ops.x1;
+    double g = m.form.g, h_min = m.form.h_min;
+    double h_dry = m.form.subcell_h_dry;
+    telescoped_interfaces(ops, ws.metric, affine, ws.interfaces);
+    int first = idx(0), last = idx(n1 - 1);
+    Node q_first = ws.nodes[first], q_last = ws.nodes[last];
+    auto m_first = ws.metric[0], m_last = ws.metric[n1 - 1];
+    ws.rhs[first] = ws.rhs[first] +
+                    (1.0 / w[0]) * wintermeyer_flux(q_first, q_first, m_first.first, m_first.second, g);
+    ws.rhs[last] = ws.rhs[last] -
+                   (1.0 / w[n1 - 1]) * wintermeyer_flux(q_last, q_last, m_last.first, m_last.second, g);
+    double x_left = -1.0;
+    for (int a = 0; a < n1; ++a) {
+        Side q = side_of(ws.nodes[idx(a)]);
+        double x_right = x_left + w[a];
+        bool have_l, have_r;
+        Side l, r;
+        double x_l = 0.0, x_r = 0.0;
+        if (a > 0) {
+            have_l = true;
+            l = side_of(ws.nodes[idx(a - 1)]);
+            x_l = xi[a - 1];
+        } else {
+            have_l = end0.present;
+            if (have_l) {
+                l = side_of(end0.node);
+                x_l = -1.0 - end0.distance;
+            }
+        }
+        if (a + 1 < n1) {
+            have_r = true;
+            r = side_of(ws.nodes[idx(a + 1)]);
+            x_r = xi[a + 1];
+        } else {
+            have_r = end1.present;
+            if (have_r) {
+                r = side_of(end1.node);
+                x_r = 1.0 + end1.distance;
+            }
+        }
+        if (have_l && have_r) {
+            Side nodes[3] = {l, q, r};
+            double xs[3] = {x_l, xi[a], x_r};
+            reconstruct_subcell(nodes, xs, x_left, x_right, h_dry, ws.faces[a].first, ws.faces[a].second);
+        } else {
+            ws.faces[a] = {q, q};
+        }
+        x_left = x_right;
+    }
+    for (int a = 0; a < n1 - 1; ++a) {
+        int ia = idx(a), ib = idx(a + 1);
+        auto mm = ws.interfaces[a + 1];
+        State f_a, f_b;
+        hydrostatic_hll(ws.faces[a].second, ws.faces[a + 1].first, mm.first, mm.second, g, h_min, f_a, f_b);
+        ws.rhs[ia] = ws.rhs[ia] - (1.0 / w[a]) * f_a;
+        ws.rhs[ib] = ws.rhs[ib] + (1.0 / w[a + 1]) * f_b;
+    }
+    for (int a = 0; a < n1; ++a) {
+        int ia = idx(a);
+        const Side& left = ws.faces[a].first;
+        const Side& right = ws.faces[a].second;
+        double w_a = w[a];
+        double bed = -0.5 * g * (left.h + right.h) * (right.b - left.b) / w_a;
+        double fx, fy;
+        if (affine) {
+            auto m0 = ws.metric[0];
+            fx = bed * m0.first;
+            fy = bed * m0.second;
+        } else {
+            auto m_l = ws.interfaces[a], m_r = ws.interfaces[a + 1];
+            double h_a = ws.nodes[ia].h, b_a = ws.nodes[ia].b;
+            double metric = 0.25 * g *
+                            ((right.h + h_a) * (b_a - right.b) + (left.h + h_a) * (b_a - left.b)) / w_a;
+            fx = bed * 0.5 * (m_l.first + m_r.first) + metric * (m_r.first - m_l.first);
+            fy = bed * 0.5 * (m_l.second + m_r.second) + metric * (m_r.second - m_l.second);
+        }
+        ws.rhs[ia] = ws.rhs[ia] + State{0.0, fx, fy};
+    }
+}
+
+// SplitFormSWE2D::outer_node (src/solver/rhs/swe_2d_split_form.rs:1048-1085)
+static Workspace::Outer outer_node(const Model& m, const Buffer& q, int64_t k, int face, int fi) {
+    const Ops& ops = m.ops;
+    const Geometry& g = m.geom;
+    int n1 = ops.n1;
+    Workspace::Outer out;
+    ElementFace nb;
+    if (!m.mesh.neighbor(k, face, nb)) return out;
+    auto height = [&](int64_t e, int f, int fidx, int node) {
+        if (g.affine[e]) return g.det_j[g.nidx(e, 0)] / g.surface_j[g.fidx(e, f, 0)];
+        return g.det_j[g.nidx(e, node)] / g.surface_j[g.fidx(e, f, fidx)];
+    };
+    int nb_node = ops.face_nodes[nb.face][n1 - 1 - fi];
+    int inner;
+    switch (nb.face) {
+        case 0: inner = nb_node + n1; break;
+        case 1: inner = nb_node - 1; break;
+        case 2: inner = nb_node - n1; break;
+        default: inner = nb_node + 1; break;
+    }
+    int own_node = ops.face_nodes[face][fi];
+    double distance = (ops.x1[1] - ops.x1[0]) * height(nb.element, nb.face, n1 - 1 - fi, nb_node) /
+                      height(k, face, fi, own_node);
+    out.present = true;
+    out.node = node_at(m, q, nb.element, inner);
+    out.distance = distance;
+    return out;
+}
+
+// SplitFormSWE2D::element_rhs (src/solver/rhs/swe_2d_split_form.rs:665-820)
+// then SWE2DRhsKernel::source_terms (src/solver/rhs/swe_2d.rs:929-973)
+static void element_rhs(const Model& m, const Buffer& q, int64_t k, double time, Workspace& ws,
+                        double* out_h, double* out_hu, double* out_hv) {
+    const Ops& ops = m.ops;
+    const Geometry& g = m.geom;
+    int n1 = ops.n1, nn = ops.nn;
+    for (int i = 0; i < nn; ++i) {
+        ws.nodes[i] = node_at(m, q, k, i);
+        ws.rhs[i] = State{0.0, 0.0, 0.0};
+    }
+    bool subcells = false;
+    if (m.form.formulation == DGSWE_WET_DRY)
+        for (int i = 0; i < nn; ++i) subcells = subcells || (ws.nodes[i].h < m.form.subcell_depth);
+    if (subcells)
+        for (int face = 0; face < 4; ++face)
+            for (int fi = 0; fi < n1; ++fi) ws.outer[face * n1 + fi] = outer_node(m, q, k, face, fi);
+    bool affine = g.affine[k] != 0;
+    double ar0, ar1, as0, as1;
+    g.contravariant(k, 0, ar0, ar1, as0, as1);
+    for (int line = 0; line < n1; ++line) {
+        auto r_line = [&](int a) { return line * n1 + a; };
+        auto s_line = [&](int j) { return j * n1 + line; };
+        int rev = n1 - 1 - line, fwd = line;
+        for (int a = 0; a < n1; ++a) {
+            if (affine) {
+                ws.metric[a] = {ar0, ar1};
+            } else {
+                double r0, r1, s0, s1;
+                g.contravariant(k, r_line(a), r0, r1, s0, s1);
+                ws.metric[a] = {r0, r1};
+            }
+        }
+        if (subcells)
+            line_subcells(m, ws, r_line, ws.outer[3 * n1 + rev], ws.outer[n1 + fwd], affine);
+        else
+            line_volume(m, ws, r_line, affine, {ar0, ar1});
+        for (int j = 0; j < n1; ++j) {
+            if (affine) {
+                ws.metric[j] = {as0, as1};
+            } else {
+                double r0, r1, s0, s1;
+                g.contravariant(k, s_line(j), r0, r1, s0, s1);
+                ws.metric[j] = {s0, s1};
+            }
+        }
+        if (subcells)
+            line_subcells(m, ws, s_line, ws.outer[fwd], ws.outer[2 * n1 + rev], affine);
+        else
+            line_volume(m, ws, s_line, affine, {as0, as1});
+    }
+    // Surface terms (src/solver/rhs/swe_2d_split_form.rs:777-807)
+    for (int face = 0; face < 4; ++face) {
+        int64_t e = m.mesh.element_edges[k][face];
+        const Edge& edge = m.mesh.edges[e];
+        bool interior = edge.right.element >= 0;
+        int side = (edge.left.element != k || edge.left.face != face) ? 1 : 0;
+        for (int fi = 0; fi < n1; ++fi) {
+            int node = ops.face_nodes[face][fi];
+            double nx, ny, scale;
+            face_normal(m, k, face, fi, nx, ny, scale);
+            const Node& q_int = ws.nodes[node];
+            State f_star = interior ? m.faces[(2 * e + side) * n1 + fi]
+                                    : boundary_flux(m, k, face, node, q_int, nx, ny, time, edge.tag);
+            State flux_diff = wintermeyer_flux(q_int, q_int, nx, ny, m.form.g) - f_star;
+            ws.rhs[node] = ws.rhs[node] + (scale * ops.lift_at(face, node, fi)) * flux_diff;
+        }
+    }
+    for (int i = 0; i < nn; ++i) {
+        double j_inv = affine ? g.det_j_inv[g.nidx(k, 0)] : g.det_j_inv[g.nidx(k, i)];
+        out_h[i] = j_inv * ws.rhs[i].h;
+        out_hu[i] = j_inv * ws.rhs[i].hu;
+        out_hv[i] = j_inv * ws.rhs[i].hv;
+    }
+    // CoriolisSource2D::add_element (src/source/swe_2d/coriolis.rs:151-175)
+    if (m.form.has_coriolis) {
+        auto v = m.mesh.corners(k);
+        for (int i = 0; i < nn; ++i) {
+            double f = m.form.coriolis_f0;
+            if (m.form.coriolis_beta != 0.0) {
+                // Mesh2D::bilinear (src/mesh/core/mesh2d.rs:644-660)
+                double r = ops.nodes_r[i], s = ops.nodes_s[i];
+                double n0 = (1.0 - r) * (1.0 - s) / 4.0, n1b = (1.0 + r) * (1.0 - s) / 4.0;
+                double n2 = (1.0 + r) * (1.0 + s) / 4.0, n3 = (1.0 - r) * (1.0 + s) / 4.0;
+                double y = n0 * v[0][1] + n1b * v[1][1] + n2 * v[2][1] + n3 * v[3][1];
+                f = m.form.coriolis_f0 + m.form.coriolis_beta * (y - m.form.coriolis_y0);
+            }
+            State st = q.get((size_t)k * nn + i);
+            out_hu[i] += f * st.hv;
+            out_hv[i] += -f * st.hu;
+        }
+    }
+}
+
+// The face pass over every interior edge (compute_rhs_swe_2d_*: face_fluxes,
+// src/solver/rhs/swe_2d.rs:619-646)
+static void face_pass(Model& m, const Buffer& q) {
+    int64_t n_edges = (int64_t)m.mesh.edges.size();
+    m.faces.assign((size_t)2 * n_edges * m.ops.n1, State{});
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < n_edges; ++e) edge_fluxes(m, q, e, &m.faces[(size_t)2 * e * m.ops.n1]);
+}
+
+// ---------------------------------------------------------------------------
+// Physics: damping, wet/dry correction, stages (src/physics/builder.rs)
+
+// damp_node (src/solver/algorithms/wetting_drying.rs:324-357); the block
+// path of damp_wet_block gives the same bits (wetting_drying.rs:775-822)
+static void damp_node(const Model& m, size_t node, double h, double& hu, double& hv, State from,
+                      double dt) {
+    if (h <= 0.0) {
+        hu = 0.0;
+        hv = 0.0;
+        return;
+    }
+    double rate = 0.0;
+    if (m.form.friction != DGSWE_FRICTION_NONE) {
+        double u, v;
+        if (m.form.has_wet_dry)
+            m.wd.desingularized_velocity(from.h, from.hu, from.hv, u, v);
+        else
+            state_velocity(from, m.form.h_min, u, v);
+        double speed = std::sqrt(u * u + v * v);
+        if (speed > 0.0) rate += manning_rate(m.g_n2[node], fmax_(h, m.form.manning_h_min), speed);
+    }
+    if (m.form.has_wet_dry) rate += m.wd.thin_layer_rate(h);
+    double factor = 1.0 / (1.0 + dt * rate);
+    hu *= factor;
+    hv *= factor;
+}
+
+// wet_dry_element (src/solver/algorithms/wetting_drying.rs:194-215) with
+// element_mean and positivity_limit_element (src/solver/limiters/swe_2d.rs:135-203)
+static bool wet_dry_element(const Model& m, int64_t k, double* h, double* hu, double* hv) {
+    const Geometry& g = m.geom;
+    int nn = m.ops.nn;
+    const double* mass = &g.mass[g.nidx(k, 0)];
+    double inv_area = 1.0 / g.area[k];
+    double h_dry = m.wd.h_dry;
+    bool needs = false;
+    for (int i = 0; i < nn; ++i) needs = needs || (h[i] < h_dry);
+    bool clipped = false;
+    if (needs) {
+        double sh = 0.0, shu = 0.0, shv = 0.0;
+        for (int i = 0; i < nn; ++i) {
+            sh += mass[i] * h[i];
+            shu += mass[i] * hu[i];
+            shv += mass[i] * hv[i];
+        }
+        double h_avg = sh * inv_area, hu_avg = shu * inv_area, hv_avg = shv * inv_area;
+        if (h_avg <= 0.0) {
+            for (int i = 0; i < nn; ++i) h[i] = hu[i] = hv[i] = 0.0;
+            clipped = h_avg < 0.0;
+        } else {
+            double h_min_elem = INF;
+            for (int i = 0; i < nn; ++i) h_min_elem = fmin_(h_min_elem, h[i]);
+            if (h_min_elem < 0.0) {
+                // compute_theta_positivity (src/solver/limiters/swe_2d.rs:98-106)
+                double theta = h_avg / (h_avg - h_min_elem);
+                theta = theta < 0.0 ? 0.0 : (theta > 1.0 ? 1.0 : theta);
+                for (int i = 0; i < nn; ++i) {
+                    h[i] = theta * (h[i] - h_avg) + h_avg;
+                    hu[i] = theta * (hu[i] - hu_avg) + hu_avg;
+                    hv[i] = theta * (hv[i] - hv_avg) + hv_avg;
+                }
+                for (int i = 0; i < nn; ++i) h[i] = fmax_(h[i], 0.0);
+            }
+            if (h_avg < h_dry)
+                for (int i = 0; i < nn; ++i) hu[i] = hv[i] = 0.0;
+        }
+    }
+    for (int i = 0; i < nn; ++i) m.wd.correct_node(h[i], hu[i], hv[i]);
+    return clipped;
+}
+
+// SWEPhysics2D::post_process_element (src/physics/builder.rs:266-278): the
+// positivity pass of a wet/dry run is the redundant one
+static bool post_process_element(const Model& m, int64_t k, double* h, double* hu, double* hv) {
+    if (!m.form.has_wet_dry) return false;
+    return wet_dry_element(m, k, h, hu, hv);
+}
+
+static std::string check_buffer(const Model& m, int32_t b) {
+    if (b < 0 || b >= DGSWE_N_BUFFERS) return "buffer id out of range";
+    (void)m;
+    return "";
+}
+
+// stage_where over every element (src/physics/builder.rs:652-737) with
+// compute_rhs_swe_2d_subset_then (src/solver/rhs/swe_2d.rs:1759-1996)
+static void stage_all(Model& m, const dgswe_stage_plan& p) {
+    const Buffer& input = m.buf[p.input];
+    face_pass(m, input);
+    int nn = m.ops.nn;
+    Buffer& out = m.buf[p.out];
+    const Buffer& base = m.buf[p.base];
+    Buffer* acc = p.accumulate ? &m.buf[p.acc] : nullptr;
+    int64_t clips = 0;
+#pragma omp parallel reduction(+ : clips)
+    {
+        Workspace ws(m.ops);
+        std::vector<double> rh(nn), rhu(nn), rhv(nn);
+#pragma omp for schedule(static)
+        for (int64_t k = 0; k < m.mesh.n_elements; ++k) {
+            element_rhs(m, input, k, p.time, ws, rh.data(), rhu.data(), rhv.data());
+            size_t o = (size_t)k * nn;
+            double* rows[3] = {rh.data(), rhu.data(), rhv.data()};
+            const std::vector<double>* bases[3] = {&base.h, &base.hu, &base.hv};
+            const std::vector<double>* inputs[3] = {&input.h, &input.hu, &input.hv};
+            for (int var = 0; var < 3; ++var)
+                for (int i = 0; i < nn; ++i) {
+                    double s = (*bases[var])[o + i], x = (*inputs[var])[o + i], f = rows[var][i];
+                    double v = p.a != 0.0 ? p.a * s : 0.0;
+                    if (p.b != 0.0) v += p.b * x;
+                    if (p.c != 0.0) v += p.c * f;
+                    rows[var][i] = v;
+                }
+            // ImplicitDamping2D::damp_element (src/solver/algorithms/wetting_drying.rs:582-592)
+            if (m.form.friction != DGSWE_FRICTION_NONE || m.form.has_wet_dry)
+                for (int i = 0; i < nn; ++i)
+                    damp_node(m, o + i, rh[i], rhu[i], rhv[i], input.get(o + i), p.c);
+            if (p.accumulate) {
+                double* sums[3] = {&acc->h[o], &acc->hu[o], &acc->hv[o]};
+                for (int var = 0; var < 3; ++var)
+                    for (int i = 0; i < nn; ++i)
+                        sums[var][i] = p.keep != 0.0 ? p.w * rows[var][i] + p.keep * sums[var][i]
+                                                     : p.w * rows[var][i];
+            } else {
+                clips += post_process_element(m, k, rh.data(), rhu.data(), rhv.data()) ? 1 : 0;
+            }
+            std::memcpy(&out.h[o], rh.data(), nn * sizeof(double));
+            std::memcpy(&out.hu[o], rhu.data(), nn * sizeof(double));
+            std::memcpy(&out.hv[o], rhv.data(), nn * sizeof(double));
+        }
+    }
+    m.clips += clips;
+}
+
+// finish_where over every element (src/physics/builder.rs:739-782)
+static void finish_all(Model& m, int32_t acc_id) {
+    int nn = m.ops.nn;
+    Buffer& s = m.buf[DGSWE_STATE];
+    const Buffer& acc = m.buf[acc_id];
+    int64_t clips = 0;
+#pragma omp parallel for schedule(static) reduction(+ : clips)
+    for (int64_t k = 0; k < m.mesh.n_elements; ++k) {
+        size_t o = (size_t)k * nn;
+        for (int i = 0; i < nn; ++i) {
+            s.h[o + i] = acc.h[o + i];
+            s.hu[o + i] = acc.hu[o + i];
+            s.hv[o + i] = acc.hv[o + i];
+        }
+        clips += post_process_element(m, k, &s.h[o], &s.hu[o], &s.hv[o]) ? 1 : 0;
+    }
+    m.clips += clips;
+}
+
+// SspScheme::stages (src/time/integrator.rs:239-263): (start, input, beta, c)
+struct ShuOsher {
+    double start, input, beta, c;
+};
+static int scheme_stages(int scheme, ShuOsher* out) {
+    if (scheme == DGSWE_SSP_RK43) {
+        out[0] = {1.0, 0.0, 0.5, 0.0};
+        out[1] = {0.0, 1.0, 0.5, 0.5};
+        out[2] = {2.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0, 1.0};
+        out[3] = {0.0, 1.0, 0.5, 0.5};
+        return 4;
+    }
+    out[0] = {1.0, 0.0, 1.0, 0.0};
+    out[1] = {0.75, 0.25, 0.25, 1.0};
+    out[2] = {1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0, 0.5};
+    return 3;
+}
+
+// MultirateStepper::step with one level (src/time/multirate.rs:1285-1315)
+// and element_stage (multirate.rs:169-200): stage s reads the previous
+// stage's value, the last sums into acc, then finish_where
+static void step_one_level(Model& m, int scheme, double t, double dt) {
+    ShuOsher st[4];
+    int n = scheme_stages(scheme, st);
+    // buffers: values 1..n-1, last n, acc n+1
+    int last = n, acc = n + 1;
+    for (int s = 0; s < n; ++s) {
+        dgswe_stage_plan p{};
+        p.base = DGSWE_STATE;
+        p.input = s == 0 ? DGSWE_STATE : s;
+        p.time = t + st[s].c * dt;
+        p.a = st[s].start;
+        p.b = st[s].input;
+        p.c = st[s].beta * dt;
+        if (s + 1 < n) {
+            p.out = s + 1;
+            p.accumulate = 0;
+        } else {
+            p.out = last;
+            p.acc = acc;
+            p.accumulate = 1;
+            p.w = 1.0;
+            p.keep = 0.0;
+        }
+        stage_all(m, p);
+    }
+    finish_all(m, acc);
+}
+
+// ---------------------------------------------------------------------------
+// Time step (src/solver/rhs/swe_2d.rs:1238-1367, 2072-2258)
+
+static double positivity_cfl(int order) {
+    double n = (double)order;
+    return (2.0 * n + 1.0) / (2.0 * n * (n + 1.0));
+}
+static double linear_cfl(int order, int scheme) {
+    static const double rk3[4] = {1.6, 1.04, 0.73, 0.56}, rk43[4] = {2.2, 1.51, 1.15, 0.93};
+    if (order < 1 || order > 4) return -1.0;
+    return scheme == DGSWE_SSP_RK43 ? rk43[order - 1] : rk3[order - 1];
+}
+static double linear_cfl_subcells(int order, int scheme) {
+    static const double rk3[4] = {0.94, 0.65, 0.47, 0.36}, rk43[4] = {1.5, 1.1, 0.97, 0.75};
+    if (order < 1 || order > 4) return -1.0;
+    return scheme == DGSWE_SSP_RK43 ? rk43[order - 1] : rk3[order - 1];
+}
+
+// PositivityBound::new (src/solver/rhs/swe_2d.rs:2194-2212)
+struct PositivityBound {
+    double cfl, max_cfl, max_cfl_subcells, h_dry;
+};
+static PositivityBound positivity_bound(int order, int scheme, double h_dry) {
+    double ssp = scheme == DGSWE_SSP_RK43 ? 2.0 : 1.0;
+    double cfl = ssp * positivity_cfl(order);
+    auto cap = [&](double limit) { return limit < 0.0 ? cfl : fmax_(cfl, 0.9 * limit); };
+    return {cfl, cap(linear_cfl(order, scheme)), cap(linear_cfl_subcells(order, scheme)), h_dry};
+}
+
+// node_reference_rate (src/solver/rhs/swe_2d.rs:1346-1357)
+static double node_reference_rate(State s, double gr0, double gr1, double gs0, double gs1,
+                                  double norm_r, double norm_s, double g, double h_min) {
+    double u, v;
+    velocity_simple(s, h_min, u, v);
+    double c = std::sqrt(g * fmax_(s.h, 0.0));
+    double lambda_r = std::fabs(u * gr0 + v * gr1) + c * norm_r;
+    double lambda_s = std::fabs(u * gs0 + v * gs1) + c * norm_s;
+    return 0.25 * (lambda_r + lambda_s);
+}
+
+// element_dt (src/solver/rhs/swe_2d.rs:2072-2115) with
+// element_max_reference_rate (swe_2d.rs:1308-1341) and
+// PositivityBound::element_cfl / positivity_relaxation (swe_2d.rs:2220-2258)
+static double element_dt(const Model& m, const Buffer& q, int64_t k, double cfl, bool positivity,
+                         const PositivityBound& bound) {
+    const Ops& ops = m.ops;
+    const Geometry& g = m.geom;
+    int nn = ops.nn, n1 = ops.n1;
+    double gg = m.form.g, h_min = m.form.h_min;
+    auto norm = [](double a, double b) { return std::sqrt(a * a + b * b); };
+    size_t n0 = g.nidx(k, 0);
+    double rate = 0.0;
+    for (int i = 0; i < nn; ++i) {
+        State s = q.get(g.nidx(k, i));
+        double r;
+        if (s.h <= h_min) {
+            r = 0.0;
+        } else {
+            size_t ni = g.affine[k] ? n0 : g.nidx(k, i);
+            r = node_reference_rate(s, g.rx[ni], g.ry[ni], g.sx[ni], g.sy[ni], norm(g.rx[ni], g.ry[ni]),
+                                    norm(g.sx[ni], g.sy[ni]), gg, h_min);
+        }
+        rate = fmax_(rate, r);
+    }
+    for (int face = 0; face < 4; ++face) {
+        ElementFace nb;
+        if (!m.mesh.neighbor(k, face, nb)) continue;
+        for (int fi = 0; fi < n1; ++fi) {
+            int i = ops.face_nodes[face][fi];
+            int j = ops.face_nodes[nb.face][n1 - 1 - fi];
+            State s = q.get(g.nidx(nb.element, j));
+            if (s.h <= h_min) continue;
+            size_t ni = g.nidx(k, i);
+            rate = fmax_(rate, node_reference_rate(s, g.rx[ni], g.ry[ni], g.sx[ni], g.sy[ni],
+                                                   norm(g.rx[ni], g.ry[ni]), norm(g.sx[ni], g.sy[ni]),
+                                                   gg, h_min));
+        }
+    }
+    if (positivity) {
+        double shallow = 100.0 * bound.h_dry;
+        double water = 0.0, water_b = 0.0, weight = 0.0, weight_b = 0.0;
+        bool is_shallow = false;
+        int last = n1 - 1;
+        for (int i = 0; i < nn; ++i) {
+            double h = q.h[g.nidx(k, i)], mm = g.mass[g.nidx(k, i)];
+            is_shallow = is_shallow || (h <= shallow);
+            double water_i = mm * fmax_(h, 0.0);
+            water += water_i;
+            weight += mm;
+            int a = i % n1, j = i / n1;
+            if (a == 0 || a == last || j == 0 || j == last) {
+                water_b += water_i;
+                weight_b += mm;
+            }
+        }
+        double ratio = fmin_(water / water_b, weight / weight_b);
+        double rho = fmax_(0.9 * ratio, 1.0);
+        double cap = is_shallow ? bound.max_cfl_subcells : bound.max_cfl;
+        cfl = fmin_(cfl, fmin_(bound.cfl * rho, cap));
+    }
+    // dt_from_reference_rate (src/solver/rhs/swe_2d.rs:1362-1367)
+    if (rate < 1e-14) return INF;
+    return cfl / ((2.0 * (double)ops.order + 1.0) * rate);
+}
+
+static double min_element_dt(Model& m, double cfl, int scheme, double* dt_el) {
+    bool positivity = m.form.positivity_h_dry > 0.0;
+    PositivityBound bound = positivity_bound(m.ops.order, scheme, m.form.positivity_h_dry);
+    const Buffer& q = m.buf[DGSWE_STATE];
+    double dt_min = INF;
+#pragma omp parallel for schedule(static) reduction(min : dt_min)
+    for (int64_t k = 0; k < m.mesh.n_elements; ++k) {
+        double dt = element_dt(m, q, k, cfl, positivity, bound);
+        if (dt_el) dt_el[k] = dt;
+        dt_min = fmin_(dt_min, dt);
+    }
+    return dt_min;
+}
+
+static bool state_is_finite(const Model& m) {
+    const Buffer& s = m.buf[DGSWE_STATE];
+    size_t n = m.n_values();
+    bool ok = true;
+#pragma omp parallel for schedule(static) reduction(&& : ok)
+    for (size_t i = 0; i < n; ++i)
+        ok = ok && std::isfinite(s.h[i]) && std::isfinite(s.hu[i]) && std::isfinite(s.hv[i]);
+    return ok;
+}
+
+}  // namespace oracle
+
+// ---------------------------------------------------------------------------
+// C API (oracle.h): the library's entry points on the CPU
+
+using namespace oracle;
+
+struct oracle_handle {
+    Model* m;
+};
+
+extern "C" {
+
+int oracle_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+    return omp_get_max_threads();
+#else
+    (void)n;
+    return 1;
+#endif
+}
+
+int oracle_create(const dgswe_form* f, int device, oracle_handle** out) {
+    (void)device;
+    if (!f || !out) return DGSWE_ERR_INVALID;
+    *out = nullptr;
+    if (f->abi_version != DGSWE_ABI_VERSION || f->order < 1 || f->order > 4 || f->n_elements <= 0 ||
+        !f->vertices || !f->elements)
+        return DGSWE_ERR_INVALID;
+    Model* m = new Model(f->order);
+    m->form = *f;
+    std::string err = build_mesh(f, m->mesh);
+    if (err.empty()) err = build_geometry(m->mesh, m->ops, m->geom);
+    if (!err.empty()) {
+        delete m;
+        return DGSWE_ERR_INVALID;
+    }
+    size_t nv = m->n_values();
+    m->has_bed = f->bathymetry != nullptr;
+    if (m->has_bed) m->bed.assign(f->bathymetry, f->bathymetry + nv);
+    if (f->friction == DGSWE_FRICTION_MANNING) {
+        double g_n2 = f->friction_g * f->manning_n * f->manning_n;
+        m->g_n2.assign(nv, g_n2);
+    } else if (f->friction == DGSWE_FRICTION_MANNING_NODES) {
+        m->g_n2.resize(nv);
+        for (size_t i = 0; i < nv; ++i)
+            m->g_n2[i] = f->friction_g * f->manning_n_nodes[i] * f->manning_n_nodes[i];
+    }
+    m->wd.h_dry = f->wet_dry_h_dry;
+    m->wd.relaxation_time = f->wet_dry_relaxation_time;
+    m->wd.max_velocity = f->wet_dry_max_velocity;
+    for (int b = 0; b < f->n_boundaries; ++b) {
+        const dgswe_boundary& in = f->boundaries[b];
+        Boundary bc;
+        bc.kind = in.kind;
+        bc.wall_h_min = in.wall_h_min;
+        bc.elevation_only = in.elevation_only;
+        bc.constituents.assign(in.constituents, in.constituents + in.n_constituents);
+        bc.mean_elevation = in.mean_elevation;
+        bc.ramp_duration = in.ramp_duration;
+        m->boundaries[in.tag] = bc;
+    }
+    for (auto& e : m->mesh.edges)
+        if (e.right.element < 0 && !m->boundaries.count(e.tag)) {
+            delete m;
+            return DGSWE_ERR_INVALID;
+        }
+    m->form.boundaries = nullptr;
+    m->form.bathymetry = nullptr;
+    m->form.manning_n_nodes = nullptr;
+    m->form.vertices = nullptr;
+    m->form.elements = nullptr;
+    m->form.periodic = nullptr;
+    m->form.face_tags = nullptr;
+    for (auto& b : m->buf) b.resize(nv);
+    *out = new oracle_handle{m};
+    return DGSWE_OK;
+}
+
+void oracle_destroy(oracle_handle* h) {
+    if (!h) return;
+    delete h->m;
+    delete h;
+}
+
+int64_t oracle_n_values(const oracle_handle* h) { return (int64_t)h->m->n_values(); }
+
+int oracle_upload(oracle_handle* h, int32_t b, const double* hh, const double* hu, const double* hv,
+                  int64_t n) {
+    if (!check_buffer(*h->m, b).empty() || n != (int64_t)h->m->n_values()) return DGSWE_ERR_INVALID;
+    Buffer& buf = h->m->buf[b];
+    std::memcpy(buf.h.data(), hh, n * 8);
+    std::memcpy(buf.hu.data(), hu, n * 8);
+    std::memcpy(buf.hv.data(), hv, n * 8);
+    return DGSWE_OK;
+}
+
+int oracle_download(oracle_handle* h, int32_t b, double* hh, double* hu, double* hv, int64_t n) {
+    if (!check_buffer(*h->m, b).empty() || n != (int64_t)h->m->n_values()) return DGSWE_ERR_INVALID;
+    const Buffer& buf = h->m->buf[b];
+    std::memcpy(hh, buf.h.data(), n * 8);
+    std::memcpy(hu, buf.hu.data(), n * 8);
+    std::memcpy(hv, buf.hv.data(), n * 8);
+    return DGSWE_OK;
+}
+
+int oracle_compute_rhs(oracle_handle* h, int32_t input, double time, double* oh, double* ohu,
+                       double* ohv, int64_t n) {
+    Model& m = *h->m;
+    if (!check_buffer(m, input).empty() || n != (int64_t)m.n_values()) return DGSWE_ERR_INVALID;
+    const Buffer& q = m.buf[input];
+    face_pass(m, q);
+    int nn = m.ops.nn;
+#pragma omp parallel
+    {
+        Workspace ws(m.ops);
+#pragma omp for schedule(static)
+        for (int64_t k = 0; k < m.mesh.n_elements; ++k) {
+            size_t o = (size_t)k * nn;
+            element_rhs(m, q, k, time, ws, oh + o, ohu + o, ohv + o);
+        }
+    }
+    return DGSWE_OK;
+}
+
+int oracle_stage(oracle_handle* h, const dgswe_stage_plan* p) {
+    Model& m = *h->m;
+    if (!p) return DGSWE_ERR_INVALID;
+    for (int32_t b : {p->base, p->input, p->out})
+        if (!check_buffer(m, b).empty()) return DGSWE_ERR_INVALID;
+    if (p->accumulate && !check_buffer(m, p->acc).empty()) return DGSWE_ERR_INVALID;
+    stage_all(m, *p);
+    return DGSWE_OK;
+}
+
+int oracle_finish(oracle_handle* h, int32_t acc) {
+    if (!check_buffer(*h->m, acc).empty()) return DGSWE_ERR_INVALID;
+    finish_all(*h->m, acc);
+    return DGSWE_OK;
+}
+
+int oracle_element_dt(oracle_handle* h, double cfl, int32_t scheme, double* dt_el, double* dt_min) {
+    double d = min_element_dt(*h->m, cfl, scheme, dt_el);
+    if (dt_min) *dt_min = d;
+    return DGSWE_OK;
+}
+
+int oracle_step(oracle_handle* h, int32_t scheme, double t, double dt) {
+    step_one_level(*h->m, scheme, t, dt);
+    return DGSWE_OK;
+}
+
+int64_t oracle_negative_depth_clips(const oracle_handle* h) { return h->m->clips; }
+
+// Simulation::run_with_callback (src/simulation/runner.rs:264-500) with
+// fused one-level stages
+int oracle_run(oracle_handle* h, const dgswe_run_config* run, dgswe_callback cb, void* user,
+               dgswe_report* report) {
+    Model& m = *h->m;
+    if (!run || !report) return DGSWE_ERR_INVALID;
+    std::memset(report, 0, sizeof(*report));
+    std::snprintf(report->device, sizeof(report->device), "cpu (oracle)");
+    auto start = std::chrono::steady_clock::now();
+    const double LANDING_SLACK = 1e-9;
+    double t_start = run->t_start, t_end = run->t_end, t = t_start;
+    int64_t n_steps = 0;
+    double dt_min_used = INF, dt_max_used = 0.0;
+    uint64_t callbacks_done = 0;
+    bool has_interval = run->interval > 0.0;
+    auto next_callback = [&](uint64_t k) { return t_start + (double)(k + 1) * run->interval; };
+    size_t n = m.n_values();
+    const Buffer& s = m.buf[DGSWE_STATE];
+    auto call = [&](double time) {
+        if (cb) cb(user, time, s.h.data(), s.hu.data(), s.hv.data(), (int64_t)n);
+    };
+    auto finish = [&](int status, const char* msg) {
+        report->success = status == DGSWE_OK;
+        report->final_time = t;
+        report->n_steps = n_steps;
+        report->dt_min_used = dt_min_used;
+        report->dt_max_used = dt_max_used;
+        report->wall_time =
+            std::chrono::duration<double>(std::chrono::steady_clock::now() - start).count();
+        report->negative_depth_clips = m.clips;
+        std::snprintf(report->message, sizeof(report->message), "%s", msg);
+        return status;
+    };
+    call(t);
+    char msg[200];
+    while (t < t_end) {
+        if (run->max_steps > 0 && n_steps >= run->max_steps) {
+            std::snprintf(msg, sizeof msg, "Maximum step limit (%lld) reached", (long long)run->max_steps);
+            return finish(DGSWE_ERR_MAX_STEPS, msg);
+        }
+        if (run->stop && *run->stop) {
+            std::snprintf(msg, sizeof msg, "Stopped at t = %.1f s", t);
+            return finish(DGSWE_ERR_STOPPED, msg);
+        }
+        double target = has_interval ? fmin_(next_callback(callbacks_done), t_end) : t_end;
+        double dt = min_element_dt(m, run->cfl, run->scheme, nullptr);
+        if (run->dt_max > 0.0) dt = fmin_(dt, run->dt_max);
+        if (run->dt_min > 0.0 && dt < run->dt_min) {
+            std::snprintf(msg, sizeof msg, "Time step (%.2e) below minimum (%.2e)", dt, run->dt_min);
+            return finish(DGSWE_ERR_DT_MIN, msg);
+        }
+        dt_min_used = fmin_(dt_min_used, dt);
+        dt_max_used = fmax_(dt_max_used, dt);
+        bool landed = t + dt * (1.0 + LANDING_SLACK) >= target;
+        if (landed) dt = target - t;
+        step_one_level(m, run->scheme, t, dt);
+        t = landed ? target : t + dt;
+        n_steps += 1;
+        if (!state_is_finite(m)) {
+            std::snprintf(msg, sizeof msg, "The state is not finite at t = %.1f s: it has blown up", t);
+            return finish(DGSWE_ERR_NONFINITE, msg);
+        }
+        if (has_interval) {
+            if (t >= next_callback(callbacks_done)) {
+                call(t);
+                callbacks_done += 1;
+            }
+        } else {
+            call(t);
+        }
+    }
+    return finish(DGSWE_OK, "");
+}
+
+// ---- pointwise entry points for the known-answer tests -------------------
+
+double oracle_manning_cbrt(double x) { return manning_cbrt(x); }
+double oracle_tidal_ramp(double t, double duration) { return tidal_ramp(t, duration); }
+
+void oracle_characteristic_state(const double interior[3], double h_e, double un_e, double ut_e,
+                                 double nx, double ny, double g, double h_min, double out[3]) {
+    State s = characteristic_state({interior[0], interior[1], interior[2]}, h_e, un_e, ut_e, nx, ny, g,
+                                   h_min);
+    out[0] = s.h;
+    out[1] = s.hu;
+    out[2] = s.hv;
+}
+
+void oracle_desingularized_velocity(double h_dry, double h, double hu, double hv, double out[2]) {
+    WetDry wd;
+    wd.h_dry = h_dry;
+    wd.desingularized_velocity(h, hu, hv, out[0], out[1]);
+}
+
+double oracle_thin_layer_rate(double h_dry, double relaxation_time, double h) {
+    WetDry wd;
+    wd.h_dry = h_dry;
+    wd.relaxation_time = relaxation_time;
+    return wd.thin_layer_rate(h);
+}
+
+void oracle_correct_node(double h_dry, double max_velocity, double h, double io[2]) {
+    WetDry wd;
+    wd.h_dry = h_dry;
+    wd.max_velocity = max_velocity;
+    wd.correct_node(fmax_(h, 0.0), io[0], io[1]);
+}
+
+void oracle_wintermeyer_flux(const double l[6], const double r[6], double m0, double m1, double g,
+                             double out[3]) {
+    Node a{l[0], l[1], l[2], l[3], l[4], l[5]}, b{r[0], r[1], r[2], r[3], r[4], r[5]};
+    State f = wintermeyer_flux(a, b, m0, m1, g);
+    out[0] = f.h;
+    out[1] = f.hu;
+    out[2] = f.hv;
+}
+
+void oracle_hydrostatic_hll(const double a[4], const double b[4], double m0, double m1, double g,
+                            double h_min, double fa[3], double fb[3]) {
+    State x, y;
+    hydrostatic_hll({a[0], a[1], a[2], a[3]}, {b[0], b[1], b[2], b[3]}, m0, m1, g, h_min, x, y);
+    fa[0] = x.h;
+    fa[1] = x.hu;
+    fa[2] = x.hv;
+    fb[0] = y.h;
+    fb[1] = y.hu;
+    fb[2] = y.hv;
+}
+
+void oracle_gll(int order, double* nodes, double* weights, double* d) {
+    Ops ops(order);
+    for (int i = 0; i < ops.n1; ++i) {
+        nodes[i] = ops.x1[i];
+        weights[i] = ops.w1[i];
+    }
+    for (int i = 0; i < ops.n1 * ops.n1; ++i) d[i] = ops.d1[i];
+}
+
+double oracle_positivity_cfl(int order) { return positivity_cfl(order); }
+
+void oracle_positivity_bound(int order, int scheme, double out[3]) {
+    PositivityBound b = positivity_bound(order, scheme, 1e-3);
+    out[0] = b.cfl;
+    out[1] = b.max_cfl;
+    out[2] = b.max_cfl_subcells;
+}
+
+// The element-wise wet/dry correction of one element with nodal masses
+// `mass` (wet_dry_element, src/solver/algorithms/wetting_drying.rs:194-215)
+int oracle_wet_dry_element(int nn, double* h, double* hu, double* hv, const double* mass,
+                           double h_dry, double max_velocity) {
+    Model m(1);
+    m.form.has_wet_dry = 1;
+    m.wd.h_dry = h_dry;
+    m.wd.max_velocity = max_velocity;
+    m.ops.nn = nn;
+    m.geom.nn = nn;
+    m.geom.mass.assign(mass, mass + nn);
+    double area = 0.0;
+    for (int i = 0; i < nn; ++i) area += mass[i];
+    m.geom.area.assign(1, area);
+    return wet_dry_element(m, 0, h, hu, hv) ? 1 : 0;
+}
+
+// The point-implicit damping of nodes (damp_node,
+// src/solver/algorithms/wetting_drying.rs:324-357) under uniform Manning
+// `manning_n` (≤ 0: none) and the wet/dry thin layer (h_dry ≤ 0: none)
+void oracle_damp_nodes(int64_t n, const double* h, double* hu, double* hv, const double* fh,
+                       const double* fhu, const double* fhv, double dt, double g, double manning_n,
+                       double h_dry, double relaxation_time) {
+    Model m(1);
+    m.form.friction = manning_n > 0.0 ? DGSWE_FRICTION_MANNING : DGSWE_FRICTION_NONE;
+    m.form.manning_h_min = 1e-6;
+    m.form.h_min = 1e-6;
+    m.form.has_wet_dry = h_dry > 0.0;
+    m.wd.h_dry = h_dry;
+    m.wd.relaxation_time = relaxation_time;
+    m.g_n2.assign(n, g * manning_n * manning_n);
+    for (int64_t i = 0; i < n; ++i) damp_node(m, i, h[i], hu[i], hv[i], {fh[i], fhu[i], fhv[i]}, dt);
+}
+
+double oracle_tide_elevation(const dgswe_boundary* b, double t) {
+    Boundary bc;
+    bc.constituents.assign(b->constituents, b->constituents + b->n_constituents);
+    bc.mean_elevation = b->mean_elevation;
+    bc.ramp_duration = b->ramp_duration;
+    return bc.elevation(t);
+}
+
+}  // extern "C"
