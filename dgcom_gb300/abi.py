@@ -183,6 +183,9 @@ CUDA_ONLY = {
     "status_string": (C.c_char_p, [C.c_int]),
     "last_error": (C.c_char_p, [C.c_void_p]),
     "profile_steps": (C.c_int, [C.c_void_p, C.POINTER(RunConfig), C.c_int64, C.POINTER(Profile)]),
+    # device pointers in and out; working memory in the library's own array
+    "compute_rhs_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
+                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]),
 }
 
 

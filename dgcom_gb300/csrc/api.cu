@@ -824,4 +824,61 @@ int dgswe_profile_steps(dgswe_handle* h, const dgswe_run_config* run, int64_t n_
     return DGSWE_OK;
 }
 
+// ---------------------------------------------------------------------------
+// dgswe_compute_rhs_noalloc: the RHS with the library's own scratch array,
+// for callers that cannot allocate device memory while they step.
+
+namespace {
+
+// The working memory of dgswe_compute_rhs_noalloc: 64 MiB, 256-byte aligned.
+// In host code this name stands for the array; its device address comes
+// from cudaGetSymbolAddress, once per device.
+constexpr size_t kNoAllocBytes = size_t(64) << 20;
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocBytes / sizeof(double)];
+
+constexpr int kMaxNoAllocDevices = 64;
+double* g_noalloc_ptr[kMaxNoAllocDevices] = {};
+
+}  // namespace
+
+int dgswe_compute_rhs_noalloc(dgswe_handle* h, const double* hh, const double* hu,
+                              const double* hv, double time, double* out_h, double* out_hu,
+                              double* out_hv, int64_t n) {
+    if (!h) return DGSWE_ERR_INVALID;
+    if (n != h->n_values || !hh || !hu || !hv || !out_h || !out_hu || !out_hv)
+        return fail(h, DGSWE_ERR_INVALID, "compute_rhs_noalloc: %lld values (expected %lld), or a NULL pointer",
+                    (long long)n, (long long)h->n_values);
+    if (h->device < 0 || h->device >= kMaxNoAllocDevices)
+        return fail(h, DGSWE_ERR_INVALID, "compute_rhs_noalloc: device %d", h->device);
+    // face fluxes (3 × n_elements·4·(N+1)) and node velocities (2 × n)
+    const size_t nf = (size_t)h->K * 4 * h->n1;
+    const size_t need = (3 * nf + 2 * (size_t)n) * sizeof(double);
+    if (need > kNoAllocBytes)
+        return fail(h, DGSWE_ERR_INVALID,
+                    "compute_rhs_noalloc: the mesh needs %zu bytes of working memory, more than "
+                    "the %zu-byte array holds (use dgswe_compute_rhs)",
+                    need, kNoAllocBytes);
+    CK(cudaSetDevice(h->device));
+    double*& base = g_noalloc_ptr[h->device];
+    if (!base) {
+        void* p = nullptr;
+        CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        base = (double*)p;
+    }
+    double* fb_h = base;
+    double* fb_hu = fb_h + nf;
+    double* fb_hv = fb_hu + nf;
+    DevBuf in{const_cast<double*>(hh), const_cast<double*>(hu), const_cast<double*>(hv),
+              fb_hv + nf, fb_hv + nf + n};
+    DevBuf out{out_h, out_hu, out_hv, nullptr, nullptr};
+    if (int s = write_host_args(h, StageArgs{time, 0.0, 0.0, 1.0, 1.0, 0.0})) return s;
+    h->ks->velocity(in, n, h->P.h_min, h->stream);
+    h->ks->face(h->n1, h->T, h->P, in, fb_h, fb_hu, fb_hv, h->ctl, kHostSlot, always(h),
+                h->stream);
+    h->ks->stage(h->n1, h->T, h->P, h->X, in, in, out, out, fb_h, fb_hu, fb_hv, h->ctl, kHostSlot,
+                 kModeRhsOnly, 0, always(h), h->stream);
+    CK(cudaGetLastError());
+    return sync(h);
+}
+
 }  // extern "C"

@@ -311,6 +311,27 @@ int64_t dgswe_negative_depth_clips(const dgswe_handle* handle);
 int dgswe_profile_steps(dgswe_handle* handle, const dgswe_run_config* run,
                         int64_t n_steps, dgswe_profile* out);
 
+/* The RHS of a state already on the device, without allocating anything.
+ * No counterpart in the reference: it exists for callers that cannot call
+ * cudaMalloc while they step — a host that hands the whole device budget to
+ * its own pool up front, or a hot loop where an allocation would synchronise
+ * the device or fail halfway through a run. h/hu/hv and out_* are device
+ * pointers of n = dgswe_n_values() doubles each, owned by the caller; the
+ * result is dgswe_compute_rhs's. Its working memory (the face fluxes and the
+ * node velocities, n_elements·(12(N+1) + 2(N+1)²) doubles) lives in one
+ * 64 MiB array inside the library, so meshes up to ≈ 104,000 elements at
+ * N = 3 (≈ 155,000 at N = 2) fit; larger ones are refused with
+ * DGSWE_ERR_INVALID. Every GPU on which the library's device code is loaded
+ * holds that array until the process exits. Every call shares it: calls that
+ * overlap on the GPU (other streams, other handles, other host threads)
+ * race. Each call writes every value it reads, so nothing needs clearing
+ * between calls. The first call on a device looks up the array's address
+ * with that device current (cudaGetSymbolAddress): make that first call
+ * before any stream capture. Returns when the RHS is complete. */
+int dgswe_compute_rhs_noalloc(dgswe_handle* handle, const double* h, const double* hu,
+                              const double* hv, double time, double* out_h, double* out_hu,
+                              double* out_hv, int64_t n);
+
 #ifdef __cplusplus
 }
 #endif
