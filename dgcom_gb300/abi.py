@@ -160,6 +160,19 @@ class Profile(C.Structure):
     ]
 
 
+class FormInfo(C.Structure):
+    _fields_ = [
+        ("n_elements", C.c_int64),
+        ("n_interior_edges", C.c_int64),
+        ("n_periodic_edges", C.c_int64),
+        ("n_boundary_faces", C.c_int64),
+        ("n_affine", C.c_int64),
+        ("min_jacobian", C.c_double),
+        ("area", C.c_double),
+        ("table_checksum", C.c_double),
+    ]
+
+
 CALLBACK = C.CFUNCTYPE(None, C.c_void_p, C.c_double, _dp, _dp, _dp, C.c_int64)
 
 # entry points shared by every library with this ABI: name → (restype, argtypes)
@@ -180,6 +193,7 @@ ENTRY_POINTS = {
 # the CUDA library's own
 CUDA_ONLY = {
     "abi_version": (C.c_uint32, []),
+    "check_form": (C.c_int, [C.POINTER(Form), C.POINTER(FormInfo), C.c_char_p, C.c_size_t]),
     "status_string": (C.c_char_p, [C.c_int]),
     "last_error": (C.c_char_p, [C.c_void_p]),
     "profile_steps": (C.c_int, [C.c_void_p, C.POINTER(RunConfig), C.c_int64, C.POINTER(Profile)]),

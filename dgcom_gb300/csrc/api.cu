@@ -282,6 +282,54 @@ extern "C" {
 
 uint32_t dgswe_abi_version(void) { return DGSWE_ABI_VERSION; }
 
+int dgswe_check_form(const dgswe_form* f, dgswe_form_info* info, char* message,
+                     size_t message_size) {
+    auto say = [&](int status, const std::string& why) {
+        if (message && message_size > 0) std::snprintf(message, message_size, "%s", why.c_str());
+        return status;
+    };
+    std::string why;
+    if (int s = check_form(f, why)) return say(s, why);
+    Operators ops(f->order);
+    Topology topo;
+    std::string err = build_topology(*f, topo);
+    if (!err.empty()) return say(DGSWE_ERR_INVALID, err);
+    std::vector<int32_t> tags, cond_index;
+    for (int b = 0; b < f->n_boundaries; ++b) {
+        tags.push_back(f->boundaries[b].tag);
+        cond_index.push_back(b);
+    }
+    Tables t;
+    err = build_tables(*f, ops, topo, tags, cond_index, t);
+    if (!err.empty()) return say(DGSWE_ERR_INVALID, err);
+    if (info) {
+        std::memset(info, 0, sizeof(*info));
+        info->n_elements = f->n_elements;
+        info->n_interior_edges = (int64_t)t.edge_left.size();
+        info->n_boundary_faces = (int64_t)t.bface.size();
+        for (int64_t k = 0; k < topo.n_elements; ++k)
+            for (int face = 0; face < 4; ++face) {
+                const Link& L = topo.link[k][face];
+                if (L.element >= 0 && L.left && !L.shared) info->n_periodic_edges += 1;
+            }
+        double min_j = INFINITY, area = 0.0;
+        for (int64_t k = 0; k < topo.n_elements; ++k) {
+            info->n_affine += t.affine[k];
+            area += 1.0 / t.inv_area[k];
+            for (int i = 0; i < ops.nn; ++i) min_j = std::fmin(min_j, 1.0 / t.jinv[k * ops.nn + i]);
+        }
+        info->min_jacobian = min_j;
+        info->area = area;
+        double sum = 0.0;
+        for (const auto* v : {&t.bed, &t.jinv, &t.pair_hm, &t.gdb, &t.contra, &t.lift_scale,
+                              &t.outer_dist, &t.mass, &t.inv_area, &t.weight_ratio, &t.dtm_own,
+                              &t.dtm_face, &t.edge_geo, &t.bface_geo})
+            for (double x : *v) sum += x;
+        info->table_checksum = sum;
+    }
+    return say(DGSWE_OK, "");
+}
+
 const char* dgswe_status_string(int status) {
     switch (status) {
         case DGSWE_OK: return "ok";

@@ -1051,6 +1051,10 @@ __device__ __forceinline__ double node_rate(double h, double u, double v, const 
 }
 
 template <int N1>
+__device__ double element_dt(const DevTables& T, const Physics& P, const DtParams& D, int64_t k,
+                             int e, const double* s_h, unsigned long long rate_bits);
+
+template <int N1>
 __global__ void __launch_bounds__(Cfg<N1>::THREADS)
     dt_kernel(DevTables T, Physics P, DevBuf q, DtParams D, double* dt_el, StepCtl* ctl,
               const int* active) {
@@ -1058,6 +1062,7 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS)
     constexpr int NN = C::NN, EPB = C::EPB;
     __shared__ unsigned long long s_rate[EPB];
     __shared__ double s_h[EPB][NN];
+    __shared__ unsigned long long s_dt;  // the block's smallest dt (bits)
     if (!*active) return;
     const int tid = threadIdx.x;
     const int e = tid / NN, i = tid % NN;
@@ -1066,6 +1071,7 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS)
     const int64_t gi = k * NN + i;
     const double g = P.g, h_min = P.h_min;
     if (i == 0) s_rate[e] = 0ull;
+    if (tid == 0) s_dt = 0x7FF0000000000000ull;
     __syncthreads();
     double rate = 0.0;
     if (valid) {
@@ -1083,8 +1089,24 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS)
         atomicMax(&s_rate[e], (unsigned long long)__double_as_longlong(rate));
     }
     __syncthreads();
-    if (!valid || i != 0) return;
-    const double rmax = __longlong_as_double((long long)s_rate[e]);
+    if (valid && i == 0) {
+        const double dt = element_dt<N1>(T, P, D, k, e, s_h[e], s_rate[e]);
+        if (dt_el) dt_el[k] = dt;
+        atomicMin(&s_dt, (unsigned long long)__double_as_longlong(dt));
+    }
+    __syncthreads();
+    // one global atomic per block: dt ≥ 0, so its bits order as the values
+    if (tid == 0) atomicMin(&ctl->dt_bits, s_dt);
+}
+
+// The element's dt from its largest wave rate (bits of a non-negative
+// double) and its depths, with the positivity bound of a wet/dry run
+template <int N1>
+__device__ double element_dt(const DevTables& T, const Physics& P, const DtParams& D, int64_t k,
+                             int e, const double* s_h, unsigned long long rate_bits) {
+    constexpr int NN = N1 * N1;
+    (void)e;
+    const double rmax = __longlong_as_double((long long)rate_bits);
     double cfl = D.cfl;
     if (D.positivity) {
         // PositivityBound::element_cfl / positivity_relaxation, in node order
@@ -1092,7 +1114,7 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS)
         double water = 0.0, water_b = 0.0;
         bool shallow = false;
         for (int p = 0; p < NN; ++p) {
-            const double hp = s_h[e][p];
+            const double hp = s_h[p];
             shallow = shallow || (hp <= D.shallow);
             const double wi = mass[p] * fmax(hp, 0.0);
             water += wi;
@@ -1104,9 +1126,7 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS)
         const double cap = shallow ? D.max_cfl_subcells : D.max_cfl;
         cfl = fmin(cfl, fmin(D.bound_cfl * rho, cap));
     }
-    const double dt = rmax < 1e-14 ? INFINITY : cfl / ((2.0 * (double)P.order + 1.0) * rmax);
-    if (dt_el) dt_el[k] = dt;
-    atomicMin(&ctl->dt_bits, (unsigned long long)__double_as_longlong(dt));
+    return rmax < 1e-14 ? INFINITY : cfl / ((2.0 * (double)P.order + 1.0) * rmax);
 }
 
 // ---------------------------------------------------------------------------

@@ -234,3 +234,20 @@ def graded_jittered_box(lx: float, ly: float, nx: int, ny: int, size_range=(100.
     elems = np.stack([v0, v0 + 1, v0 + nx + 2, v0 + nx + 1], axis=1)
     tags = np.tile(np.array(sides, dtype=np.int32), (nx * ny, 1))
     return QuadMesh(verts, elems, np.zeros((0, 4), np.int64), tags)
+
+
+def node_mass(mesh: QuadMesh, order: int) -> np.ndarray:
+    """GLL weight × J at every node, (n_elements, (N+1)²): the diagonal mass
+    matrix of GeometricFactors2D::compute (src/operators/geometric.rs:160-176)."""
+    r, s = reference_nodes(order)
+    w = gll_weights(order)
+    n1 = order + 1
+    w2 = np.tile(w, n1) * np.repeat(w, n1)  # w_r · w_s at node j·n1 + a
+    c = mesh.corners()
+    x0, y0, x1, y1 = c[:, 0:1, 0], c[:, 0:1, 1], c[:, 1:2, 0], c[:, 1:2, 1]
+    x2, y2, x3, y3 = c[:, 2:3, 0], c[:, 2:3, 1], c[:, 3:4, 0], c[:, 3:4, 1]
+    x_r = 0.25 * ((1.0 - s) * (x1 - x0) + (1.0 + s) * (x2 - x3))
+    y_r = 0.25 * ((1.0 - s) * (y1 - y0) + (1.0 + s) * (y2 - y3))
+    x_s = 0.25 * ((1.0 - r) * (x3 - x0) + (1.0 + r) * (x2 - x1))
+    y_s = 0.25 * ((1.0 - r) * (y3 - y0) + (1.0 + r) * (y2 - y1))
+    return w2 * (x_r * y_s - x_s * y_r)

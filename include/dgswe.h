@@ -232,9 +232,28 @@ typedef struct dgswe_profile {
     double t_final;         /* model time after the steps */
 } dgswe_profile;
 
+/* What dgswe_check_form found in a form (no device involved). */
+typedef struct dgswe_form_info {
+    int64_t n_elements;
+    int64_t n_interior_edges;  /* each counted once */
+    int64_t n_periodic_edges;  /* interior edges whose faces do not share vertices */
+    int64_t n_boundary_faces;
+    int64_t n_affine;          /* parallelogram elements */
+    double min_jacobian;       /* smallest J at any node */
+    double area;               /* Σ of the element areas (Σ w_i J_i) */
+    double table_checksum;     /* Σ of every static device table value */
+} dgswe_form_info;
+
 typedef struct dgswe_handle dgswe_handle;
 
 /* ---- entry points ------------------------------------------------------- */
+
+/* Validates `form` and builds its connectivity, geometry and static tables
+ * on the host only, without touching a device, into `info` (may be NULL);
+ * `message` (may be NULL) receives the reason of a failure. The device
+ * path's counterpart of `dgcom check` (src/case/cli.rs:126-134). */
+int dgswe_check_form(const dgswe_form* form, dgswe_form_info* info, char* message,
+                     size_t message_size);
 
 /* ABI version of the library (DGSWE_ABI_VERSION it was built with). */
 uint32_t dgswe_abi_version(void);
@@ -279,7 +298,7 @@ int dgswe_stage(dgswe_handle* handle, const dgswe_stage_plan* plan);
 int dgswe_finish(dgswe_handle* handle, int32_t acc);
 
 /* Every element's stable step at `cfl` for `scheme` (element_dt_swe_2d,
- * src/solver/rhs/swe_2d.rs:2008-2031, with the positivity bound of a
+ * src/solver/rhs/swe_2d.rs:2018-2043, with the positivity bound of a
  * wet/dry run) into dt_elements (n_elements values; may be NULL), and their
  * minimum (min_element_dt_swe_2d, swe_2d.rs:2045-2068) into dt_min (may be
  * NULL). Reads the state buffer. */

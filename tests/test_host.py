@@ -1,0 +1,81 @@
+"""Host-side logic: meshes, Hilbert order, node geometry, tides and the
+workload generators."""
+
+import math
+
+import numpy as np
+
+from dgcom_gb300 import cases, tides
+from dgcom_gb300.mesh import (graded_jittered_box, hilbert_index, in_hilbert_order, node_mass,
+                              node_positions, uniform_periodic, uniform_rectangle)
+
+
+def test_uniform_rectangle_matches_the_reference_numbering():
+    m = uniform_rectangle(0.0, 3.0, 0.0, 2.0, 3, 2)
+    assert m.vertices.shape == (12, 2) and m.elements.shape == (6, 4)
+    # element 0: vertices 0, 1, 5, 4 counter-clockwise (src/mesh/core/mesh2d.rs:244-250)
+    assert list(m.elements[0]) == [0, 1, 5, 4]
+    assert list(m.elements[4]) == [5, 6, 10, 9]
+
+
+def test_periodic_pairs():
+    m = uniform_periodic(0.0, 1.0, 0.0, 1.0, 3, 2)
+    assert [tuple(p) for p in m.periodic] == [(2, 1, 0, 3), (5, 1, 3, 3), (3, 2, 0, 0),
+                                             (4, 2, 1, 0), (5, 2, 2, 0)]
+
+
+def test_hilbert_curve_visits_neighbours():
+    cells = sorted((int(hilbert_index(np.array([x]), np.array([y]), 3)[0]), x, y)
+                   for x in range(8) for y in range(8))
+    for i, (a, b) in enumerate(zip(cells, cells[1:])):
+        assert a[0] == i
+        assert abs(a[1] - b[1]) + abs(a[2] - b[2]) == 1
+    m = uniform_rectangle(0.0, 16.0, 0.0, 16.0, 16, 16)
+    sorted_mesh, old = in_hilbert_order(m)
+    assert sorted(old) == list(range(256))
+    c = sorted_mesh.corners().mean(axis=1)
+    steps = np.abs(np.diff(c, axis=0)).sum(axis=1)
+    assert np.allclose(steps, 1.0)
+
+
+def test_node_mass_sums_to_the_area():
+    m = graded_jittered_box(2000.0, 1500.0, 20, 15, size_range=(80.0, 120.0), seed=3)
+    for order in (1, 2, 3, 4):
+        assert abs(node_mass(m, order).sum() - 2000.0 * 1500.0) < 1e-6 * 3e6
+        x, y = node_positions(m, order)
+        assert x.min() >= 0.0 and x.max() <= 2000.0 and y.min() >= 0.0 and y.max() <= 1500.0
+
+
+def test_jittered_box_has_positive_jacobians():
+    m = graded_jittered_box(20_000.0, 15_000.0, 60, 45, size_range=(250.0, 450.0), seed=11)
+    assert (node_mass(m, 3) > 0.0).all()
+
+
+def test_constituent_periods():
+    # Schureman's speeds (deg/h): M2 28.9841042, S2 30, N2 28.4397295, K1 15.0410686
+    for name, speed in (("M2", 28.9841042), ("S2", 30.0), ("N2", 28.4397295), ("K1", 15.0410686)):
+        assert abs(tides.angular_speed(name) - speed) < 1e-6
+    c = tides.constituent("M2", 1.0, 90.0)
+    assert abs(tides.elevation([c], 0.25 * c.period) - 1.0) < 1e-12
+    assert tides.elevation([c], 1800.0, ramp=3600.0) == 0.5 * tides.elevation([c], 1800.0)
+
+
+def test_channel_workload():
+    case = cases.tidal_channel()
+    form = case.form
+    assert form.mesh.n_elements == 4000 and form.order == 2
+    b = form.bathymetry
+    assert abs(b.min() + 20.0) < 1e-12 and abs(b.max() - 1.0) < 1e-12
+    h = case.state[0]
+    assert (h >= 0).all() and (h == 0).any()  # the head is dry at rest
+    assert abs(form.boundaries[1].constituents[0].period / 3600.0 - 12.4206012) < 1e-6
+
+
+def test_coastal_workload_is_seeded():
+    a = cases.coastal_box(n_elements=5_000, order=3)
+    b = cases.coastal_box(n_elements=5_000, order=3)
+    assert np.array_equal(a.form.bathymetry, b.form.bathymetry)
+    assert np.array_equal(a.form.mesh.vertices, b.form.mesh.vertices)
+    assert a.form.bathymetry.min() >= -300.0 - 1e-9
+    assert (a.state[0] == 0).any() and (a.state[0] > 0).any()
+    assert abs(a.form.coriolis_f0 - 2 * 7.292115e-5 * math.sin(math.radians(63.0))) < 1e-18
