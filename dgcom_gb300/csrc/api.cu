@@ -433,6 +433,9 @@ int create_impl(dgswe_handle* h, const dgswe_form* f, int device) {
     UP(sched_owned, owned);
     UP(sched_slot, sched.accum_slot);
     UP(sched_coef, sched.accum_coef);
+    std::vector<double> hcoef(sched.accum_coef.size());
+    for (size_t q = 0; q < hcoef.size(); ++q) hcoef[q] = 0.5 * sched.accum_coef[q];
+    UP(sched_hcoef, hcoef);
 #undef UP
 
     Physics& P = h->P;
@@ -442,6 +445,9 @@ int create_impl(dgswe_handle* h, const dgswe_form* f, int device) {
     P.formulation = f->formulation;
     P.g = f->g;
     P.h_min = f->h_min;
+    P.sqrt_g = std::sqrt(f->g);  // correctly rounded, as the device's sqrt
+    P.half_g = 0.5 * f->g;
+    P.two_g = 2.0 * f->g;
     P.subcell_depth = f->subcell_depth;
     P.subcell_h_dry = f->subcell_h_dry;
     P.has_bed = f->bathymetry ? 1 : 0;

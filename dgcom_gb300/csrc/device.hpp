@@ -34,6 +34,7 @@ struct DevTables {
     const int8_t* sched_owned;  // [nn][n1-1][5]
     const int32_t* sched_slot;  // [nn][2(n1-1)]
     const double* sched_coef;   // [nn][2(n1-1)]
+    const double* sched_hcoef;  // [nn][2(n1-1)] sched_coef / 2
 };
 
 struct Constituent {
@@ -53,6 +54,7 @@ struct Physics {
     int order, n1, nn;
     int formulation;
     double g, h_min;
+    double sqrt_g, half_g, two_g;  // √g, g/2 and 2g, computed once on the host
     double subcell_depth, subcell_h_dry;
     int has_bed;
     int has_wet_dry;

@@ -36,6 +36,7 @@
 #include <stdint.h>
 
 #include "device.hpp"
+#include "fp64_bits.hpp"
 
 namespace dgswe {
 namespace DGSWE_NS {
@@ -47,9 +48,13 @@ enum StageMode { kRhsOnly = 0, kPost = 1, kAccumulate = 2 };
 
 // ---------------------------------------------------------------------------
 // arithmetic
+//
+// Every compare, minimum and maximum of doubles on the per-node paths goes
+// through fp:: (fp64_bits.hpp): the same result on the integer pipes, which
+// leaves the FP64 pipe, the stage's bound, to arithmetic.
 
-__device__ __forceinline__ double lmax(double a, double b) { return a > b ? a : b; }
-__device__ __forceinline__ double lmin(double a, double b) { return a < b ? a : b; }
+using fp::lmax;
+using fp::lmin;
 
 struct Q {
     double h, hu, hv, u, v, b;
@@ -66,7 +71,7 @@ __device__ __forceinline__ Sd side(const Q& q) { return {q.h, q.u, q.v, q.b}; }
 // node velocity (src/flux/swe_2d_entropy.rs:106-116)
 __device__ __forceinline__ void node_velocity(double h, double hu, double hv, double h_min,
                                               double& u, double& v) {
-    const bool wet = h > h_min;
+    const bool wet = fp::gt(h, h_min);
     const double inv_h = 1.0 / h;
     u = wet ? hu * inv_h : 0.0;
     v = wet ? hv * inv_h : 0.0;
@@ -86,17 +91,17 @@ __device__ __forceinline__ F3 wflux(const Q& l, const Q& r, double m0, double m1
 __device__ __forceinline__ F3 hll_aligned(double h_l, double hun_l, double hut_l, double un_l,
                                           double ut_l, double h_r, double hun_r, double hut_r,
                                           double un_r, double ut_r, double g, double sqrt_g,
-                                          double h_min) {
-    const bool dry = (h_l <= h_min) && (h_r <= h_min);
-    const double sh_l = sqrt(lmax(h_l, 0.0)), sh_r = sqrt(lmax(h_r, 0.0));
+                                          double half_g, double h_min) {
+    const bool dry = fp::le(h_l, h_min) && fp::le(h_r, h_min);
+    const double sh_l = sqrt(fp::max0(h_l)), sh_r = sqrt(fp::max0(h_r));
     const double c_l = sqrt_g * sh_l, c_r = sqrt_g * sh_r;
-    const bool roe = (sh_l + sh_r) > 1e-10;
+    const double sh_sum = sh_l + sh_r;
+    const bool roe = fp::gt(sh_sum, 1e-10);
     const double h_roe = 0.5 * (h_l + h_r);
-    const double un_roe = roe ? (sh_l * un_l + sh_r * un_r) / (sh_l + sh_r) : 0.0;
+    const double un_roe = roe ? (sh_l * un_l + sh_r * un_r) / sh_sum : 0.0;
     const double c_roe = roe ? sqrt(g * h_roe) : 0.0;
-    const double s_l = h_l > h_min ? lmin(un_l - c_l, un_roe - c_roe) : un_r - 2.0 * c_r;
-    const double s_r = h_r > h_min ? lmax(un_r + c_r, un_roe + c_roe) : un_l + 2.0 * c_l;
-    const double half_g = 0.5 * g;
+    const double s_l = fp::gt(h_l, h_min) ? lmin(un_l - c_l, un_roe - c_roe) : un_r - 2.0 * c_r;
+    const double s_r = fp::gt(h_r, h_min) ? lmax(un_r + c_r, un_roe + c_roe) : un_l + 2.0 * c_l;
     const double fl_h = h_l * un_l, fl_hu = h_l * un_l * un_l + half_g * h_l * h_l,
                  fl_hv = h_l * un_l * ut_l;
     const double fr_h = h_r * un_r, fr_hu = h_r * un_r * un_r + half_g * h_r * h_r,
@@ -106,7 +111,7 @@ __device__ __forceinline__ F3 hll_aligned(double h_l, double hun_l, double hut_l
     const double st_h = inv_ds * (s_r * fl_h - s_l * fr_h + s_lr * (h_r - h_l));
     const double st_hu = inv_ds * (s_r * fl_hu - s_l * fr_hu + s_lr * (hun_r - hun_l));
     const double st_hv = inv_ds * (s_r * fl_hv - s_l * fr_hv + s_lr * (hut_r - hut_l));
-    const bool from_l = s_l >= 0.0, from_r = s_r <= 0.0;
+    const bool from_l = fp::ge0(s_l), from_r = fp::le0(s_r);
     F3 f;
     f.h = dry ? 0.0 : (from_l ? fl_h : (from_r ? fr_h : st_h));
     f.hu = dry ? 0.0 : (from_l ? fl_hu : (from_r ? fr_hu : st_hu));
@@ -116,42 +121,42 @@ __device__ __forceinline__ F3 hll_aligned(double h_l, double hun_l, double hut_l
 
 // wall_ram_pressure (src/solver/rhs/swe_2d_split_form.rs:147-156)
 __device__ __forceinline__ double wall_ram(double h, double un, double sill, double g) {
-    un = lmax(un, 0.0);
+    un = fp::max0(un);
     const double head = un * un * (0.5 / g);
     const double ram = (1.0 - head / sill) * h * un * (2.0 * un + sqrt(g * h));
-    return sill > head ? ram : 0.0;
+    return fp::gt(sill, head) ? ram : 0.0;
 }
 
 // hydrostatic_hll (src/solver/rhs/swe_2d_split_form.rs:336-402) along m with
 // |m| = norm and m/|m| = (nx, ny): the flux seen from side a and from side b
 __device__ __forceinline__ void hydro_hll(const Sd& qa, const Sd& qb, double m0, double m1,
                                           double norm, double nx, double ny, double g,
-                                          double sqrt_g, double h_min, F3& fa, F3& fb) {
+                                          double sqrt_g, double half_g, double h_min, F3& fa,
+                                          F3& fb) {
     const double b_face = lmax(qa.b, qb.b);
-    const double hs_a = lmax(qa.h + qa.b - b_face, 0.0);
-    const double hs_b = lmax(qb.h + qb.b - b_face, 0.0);
-    const bool wet_a = qa.h > h_min, wet_b = qb.h > h_min;
+    const double hs_a = fp::max0(qa.h + qa.b - b_face);
+    const double hs_b = fp::max0(qb.h + qb.b - b_face);
+    const bool wet_a = fp::gt(qa.h, h_min), wet_b = fp::gt(qb.h, h_min);
     const double ua = wet_a ? qa.u : 0.0, va = wet_a ? qa.v : 0.0;
     const double ub = wet_b ? qb.u : 0.0, vb = wet_b ? qb.v : 0.0;
     const double un_a = ua * nx + va * ny, ut_a = -ua * ny + va * nx;
     const double un_b = ub * nx + vb * ny, ut_b = -ub * ny + vb * nx;
-    const bool sw_a = hs_a > h_min, sw_b = hs_b > h_min;
+    const bool sw_a = fp::gt(hs_a, h_min), sw_b = fp::gt(hs_b, h_min);
     const F3 r = hll_aligned(hs_a, hs_a * un_a, hs_a * ut_a, sw_a ? un_a : 0.0, sw_a ? ut_a : 0.0,
                              hs_b, hs_b * un_b, hs_b * ut_b, sw_b ? un_b : 0.0, sw_b ? ut_b : 0.0,
-                             g, sqrt_g, h_min);
+                             g, sqrt_g, half_g, h_min);
     // rotate back (src/flux/swe_2d.rs:38-44), times |m|
     const double f_h = norm * r.h;
     const double f_hu = norm * (r.hu * nx - r.hv * ny);
     const double f_hv = norm * (r.hu * ny + r.hv * nx);
-    const bool hll_dry = (hs_a <= h_min) && (hs_b <= h_min);
+    const bool hll_dry = fp::le(hs_a, h_min) && fp::le(hs_b, h_min);
     const double hsa = hll_dry ? 0.0 : hs_a, hsb = hll_dry ? 0.0 : hs_b;
     double wall_a = 0.0, wall_b = 0.0;
     if (hll_dry) {
-        if (qa.h > h_min) wall_a = wall_ram(qa.h, qa.u * nx + qa.v * ny, b_face - (qa.h + qa.b), g);
-        if (qb.h > h_min)
+        if (wet_a) wall_a = wall_ram(qa.h, qa.u * nx + qa.v * ny, b_face - (qa.h + qa.b), g);
+        if (wet_b)
             wall_b = wall_ram(qb.h, -1.0 * (qb.u * nx + qb.v * ny), b_face - (qb.h + qb.b), g);
     }
-    const double half_g = 0.5 * g;
     const double dp_a = half_g * (qa.h * qa.h - hsa * hsa) + wall_a;
     const double dp_b = half_g * (qb.h * qb.h - hsb * hsb) + wall_b;
     fa = {f_h, f_hu + dp_a * m0, f_hv + dp_a * m1};
@@ -172,9 +177,9 @@ __device__ double tide_elevation(const Condition& c, double t) {
         tide += f * k.amplitude * cos(k.omega * t + k.phase + offset);
     }
     double ramp = 1.0;
-    if (c.ramp > 0.0) {
+    if (fp::gt0(c.ramp)) {
         double tau = t / c.ramp;
-        tau = tau < 0.0 ? 0.0 : (tau > 1.0 ? 1.0 : tau);
+        tau = fp::lt0(tau) ? 0.0 : (fp::gt(tau, 1.0) ? 1.0 : tau);
         ramp = tau * tau * (3.0 - 2.0 * tau);
     }
     return c.mean + ramp * tide;
@@ -226,7 +231,7 @@ __global__ void __launch_bounds__(256) face_kernel(DevTables T, Physics P, DevBu
     const int64_t n_int = T.n_edges * N1;
     if (item >= n_int + T.n_bfaces * N1) return;
     constexpr int NN = N1 * N1;
-    const double g = P.g, h_min = P.h_min, sqrt_g = sqrt(P.g);
+    const double g = P.g, h_min = P.h_min, sqrt_g = P.sqrt_g, half_g = P.half_g;
     if (item < n_int) {
         const int64_t e = item / N1;
         const int fi = (int)(item % N1);
@@ -239,8 +244,8 @@ __global__ void __launch_bounds__(256) face_kernel(DevTables T, Physics P, DevBu
         const double* geo = &T.edge_geo[e * 5];
         F3 fa, fbb;
         if (P.formulation == kWetDry) {
-            hydro_hll(side(ql), side(qr), geo[0], geo[1], geo[2], geo[3], geo[4], g, sqrt_g, h_min,
-                      fa, fbb);
+            hydro_hll(side(ql), side(qr), geo[0], geo[1], geo[2], geo[3], geo[4], g, sqrt_g, half_g,
+                      h_min, fa, fbb);
             fbb = {-fbb.h, -fbb.hu, -fbb.hv};
         } else {
             entropy_surface(ql, qr, geo[0], geo[1], P, fa, fbb);
@@ -269,7 +274,7 @@ __global__ void __launch_bounds__(256) face_kernel(DevTables T, Physics P, DevBu
     F3 fs;
     // the interior velocity of BCContext2D (velocity_simple)
     double u = 0.0, v = 0.0;
-    if (qi.h > h_min) {
+    if (fp::gt(qi.h, h_min)) {
         const double inv = 1.0 / qi.h;
         u = qi.hu * inv;
         v = qi.hv * inv;
@@ -277,7 +282,7 @@ __global__ void __launch_bounds__(256) face_kernel(DevTables T, Physics P, DevBu
     if (c.kind == kBcWall) {
         // Reflective2D mirror ghost (src/boundary/boundary_2d.rs:271-283)
         double gh = qi.h, ghu = 0.0, ghv = 0.0;
-        if (!(qi.h <= c.wall_h_min)) {
+        if (!fp::le(qi.h, c.wall_h_min)) {
             const double un = u * nx + v * ny;
             ghu = qi.h * (u - 2.0 * un * nx);
             ghv = qi.h * (v - 2.0 * un * ny);
@@ -290,8 +295,8 @@ __global__ void __launch_bounds__(256) face_kernel(DevTables T, Physics P, DevBu
         node_velocity(gh, ghu, ghv, h_min, qe.u, qe.v);
         F3 fdummy;
         if (P.formulation == kWetDry)
-            hydro_hll(side(qi), side(qe), nx, ny, geo[2], geo[3], geo[4], g, sqrt_g, h_min, fs,
-                      fdummy);
+            hydro_hll(side(qi), side(qe), nx, ny, geo[2], geo[3], geo[4], g, sqrt_g, half_g, h_min,
+                      fs, fdummy);
         else
             entropy_surface(qi, qe, nx, ny, P, fs, fdummy);
     } else {
@@ -395,7 +400,7 @@ struct DampIn {
 // damp_node (src/solver/algorithms/wetting_drying.rs:324-357)
 __device__ __forceinline__ void damp(const Physics& P, double g_n2, double h, double& hu,
                                      double& hv, const DampIn& from, double dt) {
-    if (h <= 0.0) {
+    if (fp::le0(h)) {
         hu = 0.0;
         hv = 0.0;
         return;
@@ -406,10 +411,10 @@ __device__ __forceinline__ void damp(const Physics& P, double g_n2, double h, do
         if (P.has_wet_dry) {
             // desingularized_velocity (wetting_drying.rs:115-130): the node
             // velocity where h ≥ h_dry (> h_min)
-            if (from.h <= 0.0) {
+            if (fp::le0(from.h)) {
                 u = v = 0.0;
-            } else if (from.h >= P.h_dry) {
-                if (P.h_dry > P.h_min) {
+            } else if (fp::ge(from.h, P.h_dry)) {
+                if (fp::gt(P.h_dry, P.h_min)) {
                     u = from.u;
                     v = from.v;
                 } else {
@@ -426,16 +431,16 @@ __device__ __forceinline__ void damp(const Physics& P, double g_n2, double h, do
             }
         } else {
             // SWEState2D::velocity (src/solver/state/swe_2d.rs:54-61)
-            const double h_reg = fmax(from.h, P.h_min);
+            const double h_reg = lmax(from.h, P.h_min);
             const double inv_d = 1.0 / (from.h * from.h + h_reg * h_reg);
             const double factor = 2.0 * from.h * inv_d;
             u = from.hu * factor;
             v = from.hv * factor;
         }
         const double speed = sqrt(u * u + v * v);
-        if (speed > 0.0) rate += manning_rate(g_n2, fmax(h, P.manning_h_min), speed);
+        if (fp::gt0(speed)) rate += manning_rate(g_n2, lmax(h, P.manning_h_min), speed);
     }
-    if (P.has_wet_dry && h < P.h_dry) {
+    if (P.has_wet_dry && fp::lt(h, P.h_dry)) {
         // thin_layer_rate (wetting_drying.rs:135-146); h > 0 here
         const double excess = P.h_dry / h - 1.0;
         rate += excess * excess / P.relaxation_time;
@@ -447,12 +452,12 @@ __device__ __forceinline__ void damp(const Physics& P, double g_n2, double h, do
 
 // correct_node (src/solver/algorithms/wetting_drying.rs:148-165)
 __device__ __forceinline__ void correct_node(const Physics& P, double h, double& hu, double& hv) {
-    if (h <= 0.0) {
+    if (fp::le0(h)) {
         hu = 0.0;
         hv = 0.0;
         return;
     }
-    if (h < P.h_dry) {
+    if (fp::lt(h, P.h_dry)) {
         const double r = h / P.h_dry;
         const double factor = 1.4142135623730951 * r / (P.h_dry * sqrt(1.0 + r * r * r * r));
         hu = h * (factor * hu);
@@ -461,9 +466,9 @@ __device__ __forceinline__ void correct_node(const Physics& P, double h, double&
     // |hu| > h·u_max; the square root only near the cap
     const double m2 = hu * hu + hv * hv;
     const double cap = P.max_velocity * h;
-    if (m2 > 0.99 * (cap * cap)) {
+    if (fp::gt(m2, 0.99 * (cap * cap))) {
         const double momentum = sqrt(m2);
-        if (momentum > cap) {
+        if (fp::gt(momentum, cap)) {
             const double scale = cap / momentum;
             hu *= scale;
             hv *= scale;
@@ -539,11 +544,11 @@ __device__ __forceinline__ void line_metric(const DevTables& T, int64_t k, int d
 __device__ __forceinline__ double limited_slope(double q0, double q1, double q2, double ic,
                                                 double im, double ip) {
     const double dm = q1 - q0, dp = q2 - q1;
-    const bool extremum = (dm * dp) <= 0.0;
+    const bool extremum = fp::le0(dm * dp);
     const double central = (q2 - q0) * ic;
-    const double bound = lmin(fabs(dm * im), fabs(dp * ip));
-    const double sign = central < 0.0 ? -1.0 : 1.0;
-    return extremum ? 0.0 : sign * lmin(fabs(central), bound);
+    const double bound = fp::min_nn(fabs(dm * im), fabs(dp * ip));
+    const double sign = fp::lt0(central) ? -1.0 : 1.0;
+    return extremum ? 0.0 : sign * fp::min_nn(fabs(central), bound);
 }
 
 // reconstruct_subcell (src/solver/rhs/swe_2d_split_form.rs:279-317)
@@ -552,24 +557,25 @@ __device__ __forceinline__ void reconstruct(const Sd& m, const Sd& c, const Sd& 
                                             double h_dry, Sd& left, Sd& right) {
     const double e0 = m.h + m.b, e1 = c.h + c.b, e2 = p.h + p.b;
     double ws = -INFINITY;
-    ws = (m.h >= h_dry && e0 > ws) ? e0 : ws;
-    ws = (c.h >= h_dry && e1 > ws) ? e1 : ws;
-    ws = (p.h >= h_dry && e2 > ws) ? e2 : ws;
-    const bool flooding =
-        (m.h < h_dry && e0 < ws) || (c.h < h_dry && e1 < ws) || (p.h < h_dry && e2 < ws);
-    const double fm = x1 - xl, fp = xr - x1;
+    ws = (fp::ge(m.h, h_dry) && fp::gt(e0, ws)) ? e0 : ws;
+    ws = (fp::ge(c.h, h_dry) && fp::gt(e1, ws)) ? e1 : ws;
+    ws = (fp::ge(p.h, h_dry) && fp::gt(e2, ws)) ? e2 : ws;
+    const bool flooding = (fp::lt(m.h, h_dry) && fp::lt(e0, ws)) ||
+                          (fp::lt(c.h, h_dry) && fp::lt(e1, ws)) ||
+                          (fp::lt(p.h, h_dry) && fp::lt(e2, ws));
+    const double fm = x1 - xl, fpd = xr - x1;
     const double ic = 1.0 / (x2 - x0);
-    const double im = 1.0 / (fm > 0.0 ? fm : 0.5 * (x1 - x0));
-    const double ip = 1.0 / (fp > 0.0 ? fp : 0.5 * (x2 - x1));
+    const double im = 1.0 / (fp::gt0(fm) ? fm : 0.5 * (x1 - x0));
+    const double ip = 1.0 / (fp::gt0(fpd) ? fpd : 0.5 * (x2 - x1));
     const double s_h = limited_slope(m.h, c.h, p.h, ic, im, ip);
     const double s_eta = flooding ? 0.0 : limited_slope(e0, e1, e2, ic, im, ip);
     const double s_u = limited_slope(m.u, c.u, p.u, ic, im, ip);
     const double s_v = limited_slope(m.v, c.v, p.v, ic, im, ip);
     double d = xl - x1;
-    double hh = lmax(c.h + s_h * d, 0.0);
+    double hh = fp::max0(c.h + s_h * d);
     left = {hh, c.u + s_u * d, c.v + s_v * d, e1 + s_eta * d - hh};
     d = xr - x1;
-    hh = lmax(c.h + s_h * d, 0.0);
+    hh = fp::max0(c.h + s_h * d);
     right = {hh, c.u + s_u * d, c.v + s_v * d, e1 + s_eta * d - hh};
 }
 
@@ -593,7 +599,7 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS)
     const bool valid = k < T.K;
     const int64_t gi = k * NN + i;
     const int a = i % N1, j = i / N1;
-    const double g = P.g, h_min = P.h_min, sqrt_g = sqrt(P.g);
+    const double g = P.g, h_min = P.h_min, sqrt_g = P.sqrt_g, half_g = P.half_g;
 
     if (i == 0) {
         s_flag[e][0] = 0;
@@ -615,7 +621,8 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS)
     s_q[e][4][i] = v;
     s_q[e][5][i] = b;
     __syncthreads();
-    if (valid && P.formulation == kWetDry && h < P.subcell_depth) atomicOr(&s_flag[e][0], 1);
+    if (valid && P.formulation == kWetDry && fp::lt(h, P.subcell_depth))
+        atomicOr(&s_flag[e][0], 1);
     __syncthreads();
     const bool sub = s_flag[e][0] != 0;
     double rh = 0.0, rhu = 0.0, rhv = 0.0;
@@ -629,7 +636,7 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS)
 
     // ---- phase A: pair fluxes, or the subcells' reconstructed faces ----
     if (valid && !sub) {
-        const double two_g = 2.0 * g;
+        const double two_g = P.two_g;
 #pragma unroll
         for (int q = 0; q < NP; ++q) {
             const int8_t* own = &T.sched_owned[(i * NP + q) * 5];
@@ -710,7 +717,7 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS)
         for (int q = 0; q < NA; ++q) {
             const int slot_id = T.sched_slot[i * NA + q];
             const double coef = T.sched_coef[i * NA + q];
-            const double hcoef = 0.5 * coef;
+            const double hcoef = T.sched_hcoef[i * NA + q];  // coef / 2
             const double* f = &s_x[e][slot_id * 3];
             rh -= coef * f[0];
             rhu -= hcoef * f[1];
@@ -736,7 +743,7 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS)
             const double* fb_ = &faces[((dir * N1 + line) * N1 + pos + 1) * 8];   // left face of pos+1
             F3 fa, fb;
             hydro_hll(Sd{fa_[0], fa_[1], fa_[2], fa_[3]}, Sd{fb_[0], fb_[1], fb_[2], fb_[3]}, mx, my,
-                      norm, mx * inv, my * inv, g, sqrt_g, h_min, fa, fb);
+                      norm, mx * inv, my * inv, g, sqrt_g, half_g, h_min, fa, fb);
             double* o = &ifl[((dir * N1 + line) * (N1 - 1) + pos) * 6];
             o[0] = fa.h;
             o[1] = fa.hu;
@@ -844,17 +851,17 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS)
     const StageArgs sa = ctl->stage[slot];
     double vh = 0.0, vhu = 0.0, vhv = 0.0;
     if (valid) {
-        if (sa.a != 0.0) {
+        if (fp::nz(sa.a)) {
             vh = sa.a * base.h[gi];
             vhu = sa.a * base.hu[gi];
             vhv = sa.a * base.hv[gi];
         }
-        if (sa.b != 0.0) {
+        if (fp::nz(sa.b)) {
             vh += sa.b * h;
             vhu += sa.b * hu;
             vhv += sa.b * hv;
         }
-        if (sa.c != 0.0) {
+        if (fp::nz(sa.c)) {
             vh += sa.c * Fh;
             vhu += sa.c * Fhu;
             vhv += sa.c * Fhv;
@@ -871,7 +878,7 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS)
             out.hu[gi] = vhu;
             out.hv[gi] = vhv;
             const double w = sa.w, keep = sa.keep;
-            if (keep != 0.0) {
+            if (fp::nz(keep)) {
                 acc.h[gi] = w * vh + keep * acc.h[gi];
                 acc.hu[gi] = w * vhu + keep * acc.hu[gi];
                 acc.hv[gi] = w * vhv + keep * acc.hv[gi];
@@ -887,7 +894,7 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS)
     // ---- wet/dry correction (wetting_drying.rs:194-215) ----
     if (P.has_wet_dry) {
         __syncthreads();  // s_q is free again
-        if (valid && vh < P.h_dry) atomicOr(&s_flag[e][1], 1);
+        if (valid && fp::lt(vh, P.h_dry)) atomicOr(&s_flag[e][1], 1);
         s_q[e][0][i] = vh;
         s_q[e][1][i] = vhu;
         s_q[e][2][i] = vhv;
@@ -902,7 +909,7 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS)
                 sh += mass[p] * s_q[e][0][p];
                 shu += mass[p] * s_q[e][1][p];
                 shv += mass[p] * s_q[e][2][p];
-                hmin = fmin(hmin, s_q[e][0][p]);
+                hmin = lmin(s_q[e][0][p], hmin);
             }
             const double inv_area = T.inv_area[k];
             const double h_avg = sh * inv_area;
@@ -910,28 +917,28 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS)
             s_red[e][1] = shu * inv_area;
             s_red[e][2] = shv * inv_area;
             double theta = 1.0;
-            if (h_avg > 0.0 && hmin < 0.0) {
+            if (fp::gt0(h_avg) && fp::lt0(hmin)) {
                 theta = h_avg / (h_avg - hmin);
-                theta = theta < 0.0 ? 0.0 : (theta > 1.0 ? 1.0 : theta);
+                theta = fp::lt0(theta) ? 0.0 : (fp::gt(theta, 1.0) ? 1.0 : theta);
             }
             s_red[e][3] = theta;
             s_red[e][4] = hmin;
-            if (h_avg < 0.0) atomicAdd((unsigned long long*)&ctl->clips, 1ull);
+            if (fp::lt0(h_avg)) atomicAdd((unsigned long long*)&ctl->clips, 1ull);
         }
         __syncthreads();
         if (valid && needs) {
             const double h_avg = s_red[e][0];
-            if (h_avg <= 0.0) {
+            if (fp::le0(h_avg)) {
                 vh = vhu = vhv = 0.0;
             } else {
-                if (s_red[e][4] < 0.0) {
+                if (fp::lt0(s_red[e][4])) {
                     const double th = s_red[e][3];
                     vh = th * (vh - h_avg) + h_avg;
                     vhu = th * (vhu - s_red[e][1]) + s_red[e][1];
                     vhv = th * (vhv - s_red[e][2]) + s_red[e][2];
-                    vh = fmax(vh, 0.0);
+                    vh = fp::max0(vh);
                 }
-                if (h_avg < P.h_dry) vhu = vhv = 0.0;
+                if (fp::lt(h_avg, P.h_dry)) vhu = vhv = 0.0;
             }
         }
         if (valid) correct_node(P, vh, vhu, vhv);
@@ -944,7 +951,8 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS)
         node_velocity(vh, vhu, vhv, h_min, uo, vo);
         out.u[gi] = uo;
         out.v[gi] = vo;
-        if (check_finite && !(isfinite(vh) && isfinite(vhu) && isfinite(vhv))) ctl->nonfinite = 1;
+        if (check_finite && !(fp::finite(vh) && fp::finite(vhu) && fp::finite(vhv)))
+            ctl->nonfinite = 1;
     }
 }
 
@@ -974,7 +982,7 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS)
     s_v[e][2][i] = vhv;
     __syncthreads();
     if (P.has_wet_dry) {
-        if (valid && vh < P.h_dry) atomicOr(&s_flag[e], 1);
+        if (valid && fp::lt(vh, P.h_dry)) atomicOr(&s_flag[e], 1);
         __syncthreads();
         const bool needs = s_flag[e] != 0;
         if (valid && needs && i == 0) {
@@ -984,7 +992,7 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS)
                 sh += mass[p] * s_v[e][0][p];
                 shu += mass[p] * s_v[e][1][p];
                 shv += mass[p] * s_v[e][2][p];
-                hmin = fmin(hmin, s_v[e][0][p]);
+                hmin = lmin(s_v[e][0][p], hmin);
             }
             const double inv_area = T.inv_area[k];
             const double h_avg = sh * inv_area;
@@ -992,28 +1000,28 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS)
             s_red[e][1] = shu * inv_area;
             s_red[e][2] = shv * inv_area;
             double theta = 1.0;
-            if (h_avg > 0.0 && hmin < 0.0) {
+            if (fp::gt0(h_avg) && fp::lt0(hmin)) {
                 theta = h_avg / (h_avg - hmin);
-                theta = theta < 0.0 ? 0.0 : (theta > 1.0 ? 1.0 : theta);
+                theta = fp::lt0(theta) ? 0.0 : (fp::gt(theta, 1.0) ? 1.0 : theta);
             }
             s_red[e][3] = theta;
             s_red[e][4] = hmin;
-            if (h_avg < 0.0) atomicAdd((unsigned long long*)&ctl->clips, 1ull);
+            if (fp::lt0(h_avg)) atomicAdd((unsigned long long*)&ctl->clips, 1ull);
         }
         __syncthreads();
         if (valid && needs) {
             const double h_avg = s_red[e][0];
-            if (h_avg <= 0.0) {
+            if (fp::le0(h_avg)) {
                 vh = vhu = vhv = 0.0;
             } else {
-                if (s_red[e][4] < 0.0) {
+                if (fp::lt0(s_red[e][4])) {
                     const double th = s_red[e][3];
                     vh = th * (vh - h_avg) + h_avg;
                     vhu = th * (vhu - s_red[e][1]) + s_red[e][1];
                     vhv = th * (vhv - s_red[e][2]) + s_red[e][2];
-                    vh = fmax(vh, 0.0);
+                    vh = fp::max0(vh);
                 }
-                if (h_avg < P.h_dry) vhu = vhv = 0.0;
+                if (fp::lt(h_avg, P.h_dry)) vhu = vhv = 0.0;
             }
         }
         if (valid) correct_node(P, vh, vhu, vhv);
@@ -1042,91 +1050,115 @@ __global__ void velocity_kernel(DevBuf b, int64_t n, double h_min) {
 // ---------------------------------------------------------------------------
 // the time step (src/solver/rhs/swe_2d.rs:2072-2115, 1346-1367, 2165-2258)
 
+// node_reference_rate (swe_2d.rs:1346-1357) with the mean's ¼ folded into
+// the metric table m (¼∇r, ¼∇s, ¼|∇r|, ¼|∇s|): a power-of-two scaling, so
+// lr + ls here has exactly the bits of ¼(lr + ls) from unscaled metrics
 __device__ __forceinline__ double node_rate(double h, double u, double v, const double* m,
                                             double g) {
-    const double c = sqrt(g * fmax(h, 0.0));
+    const double c = sqrt(g * fp::max0(h));
     const double lr = fabs(u * m[0] + v * m[1]) + c * m[4];
     const double ls = fabs(u * m[2] + v * m[3]) + c * m[5];
-    return 0.25 * (lr + ls);
+    return lr + ls;
+}
+
+// The dt pass stages each node's rate, depth and mass weight per element,
+// then one lane per element takes the maximum and the positivity sums in
+// node order, the reference's order: a sum spread over an element's lanes
+// would serialise on one lane per element and hold the FP64 pipe for the
+// whole warp each step.
+template <int N1>
+struct DtCfg {
+    static constexpr int NN = N1 * N1;
+    static constexpr int EPB = 32;  // elements per block: one lane of warp 0 each
+    static constexpr int THREADS = EPB * NN;
+    static constexpr int PITCH = NN + 1;  // odd row pitch: lanes spread over the banks
+};
+
+// The element's dt from its nodes' rates, depths and mass weights
+// (element_dt, swe_2d.rs:2072-2115, with PositivityBound::element_cfl and
+// positivity_relaxation, swe_2d.rs:2220-2258)
+template <int N1>
+__device__ __forceinline__ double element_dt(const DtParams& D, int order, double weight_ratio,
+                                             const double* rate, const double* h,
+                                             const double* mass) {
+    constexpr int NN = N1 * N1;
+    double rmax = 0.0;
+#pragma unroll
+    for (int p = 0; p < NN; ++p) rmax = fp::max_nn(rate[p], rmax);  // rates are ≥ +0
+    double cfl = D.cfl;
+    if (D.positivity) {
+        double water = 0.0, water_b = 0.0;
+        bool shallow = false;
+#pragma unroll
+        for (int p = 0; p < NN; ++p) {
+            const double hp = h[p];
+            shallow = shallow || fp::le(hp, D.shallow);
+            const double wi = mass[p] * fp::max0(hp);
+            water += wi;
+            constexpr int last = N1 - 1;
+            if (p % N1 == 0 || p % N1 == last || p / N1 == 0 || p / N1 == last) water_b += wi;
+        }
+        // f64::min drops the NaN of 0/0
+        const double ratio =
+            fp::le0(water_b) ? weight_ratio : lmin(water / water_b, weight_ratio);
+        const double rho = lmax(0.9 * ratio, 1.0);
+        const double cap = shallow ? D.max_cfl_subcells : D.max_cfl;
+        cfl = lmin(cfl, lmin(D.bound_cfl * rho, cap));
+    }
+    return fp::lt(rmax, 1e-14) ? INFINITY : cfl / ((2.0 * (double)order + 1.0) * rmax);
 }
 
 template <int N1>
-__device__ double element_dt(const DevTables& T, const Physics& P, const DtParams& D, int64_t k,
-                             int e, const double* s_h, unsigned long long rate_bits);
-
-template <int N1>
-__global__ void __launch_bounds__(Cfg<N1>::THREADS)
+__global__ void __launch_bounds__(DtCfg<N1>::THREADS)
     dt_kernel(DevTables T, Physics P, DevBuf q, DtParams D, double* dt_el, StepCtl* ctl,
               const int* active) {
-    using C = Cfg<N1>;
-    constexpr int NN = C::NN, EPB = C::EPB;
-    __shared__ unsigned long long s_rate[EPB];
-    __shared__ double s_h[EPB][NN];
-    __shared__ unsigned long long s_dt;  // the block's smallest dt (bits)
+    using C = DtCfg<N1>;
+    constexpr int NN = C::NN, EPB = C::EPB, PITCH = C::PITCH;
+    __shared__ double s_rate[EPB * PITCH];
+    __shared__ double s_h[EPB * PITCH];
+    __shared__ double s_mass[EPB * PITCH];
     if (!*active) return;
     const int tid = threadIdx.x;
     const int e = tid / NN, i = tid % NN;
-    const int64_t k = (int64_t)blockIdx.x * EPB + e;
-    const bool valid = k < T.K;
+    const int64_t k0 = (int64_t)blockIdx.x * EPB;
+    const int64_t k = k0 + e;
     const int64_t gi = k * NN + i;
     const double g = P.g, h_min = P.h_min;
-    if (i == 0) s_rate[e] = 0ull;
-    if (tid == 0) s_dt = 0x7FF0000000000000ull;
-    __syncthreads();
-    double rate = 0.0;
-    if (valid) {
-        const double h = q.h[gi];
-        s_h[e][i] = h;
-        if (h > h_min) rate = node_rate(h, q.u[gi], q.v[gi], &T.dtm_own[gi * 6], g);
+    double rate = 0.0, h = 0.0, mass = 0.0;
+    if (k < T.K) {
+        h = q.h[gi];
+        mass = T.mass[gi];
+        if (fp::gt(h, h_min)) rate = node_rate(h, q.u[gi], q.v[gi], &T.dtm_own[gi * 6], g);
         for (int it = i; it < 4 * N1; it += NN) {
             const int64_t o = k * 4 * N1 + it;
             const int64_t nb = T.nb_face_node[o];
             if (nb < 0) continue;
             const double hn = q.h[nb];
-            if (hn <= h_min) continue;
-            rate = fmax(rate, node_rate(hn, q.u[nb], q.v[nb], &T.dtm_face[o * 6], g));
+            if (!fp::gt(hn, h_min)) continue;
+            rate = fp::max_nn(node_rate(hn, q.u[nb], q.v[nb], &T.dtm_face[o * 6], g), rate);
         }
-        atomicMax(&s_rate[e], (unsigned long long)__double_as_longlong(rate));
     }
+    s_rate[e * PITCH + i] = rate;
+    s_h[e * PITCH + i] = h;
+    s_mass[e * PITCH + i] = mass;
     __syncthreads();
-    if (valid && i == 0) {
-        const double dt = element_dt<N1>(T, P, D, k, e, s_h[e], s_rate[e]);
-        if (dt_el) dt_el[k] = dt;
-        atomicMin(&s_dt, (unsigned long long)__double_as_longlong(dt));
+    if (tid >= 32) return;  // warp 0: lane l finishes element k0 + l
+    const int64_t kl = k0 + tid;
+    unsigned long long dt_bits = 0x7FF0000000000000ull;  // +∞
+    if (kl < T.K) {
+        const double dt = element_dt<N1>(D, P.order, T.weight_ratio[kl], &s_rate[tid * PITCH],
+                                         &s_h[tid * PITCH], &s_mass[tid * PITCH]);
+        if (dt_el) dt_el[kl] = dt;
+        dt_bits = (unsigned long long)fp::bits(dt);
     }
-    __syncthreads();
-    // one global atomic per block: dt ≥ 0, so its bits order as the values
-    if (tid == 0) atomicMin(&ctl->dt_bits, s_dt);
-}
-
-// The element's dt from its largest wave rate (bits of a non-negative
-// double) and its depths, with the positivity bound of a wet/dry run
-template <int N1>
-__device__ double element_dt(const DevTables& T, const Physics& P, const DtParams& D, int64_t k,
-                             int e, const double* s_h, unsigned long long rate_bits) {
-    constexpr int NN = N1 * N1;
-    (void)e;
-    const double rmax = __longlong_as_double((long long)rate_bits);
-    double cfl = D.cfl;
-    if (D.positivity) {
-        // PositivityBound::element_cfl / positivity_relaxation, in node order
-        const double* mass = &T.mass[k * NN];
-        double water = 0.0, water_b = 0.0;
-        bool shallow = false;
-        for (int p = 0; p < NN; ++p) {
-            const double hp = s_h[p];
-            shallow = shallow || (hp <= D.shallow);
-            const double wi = mass[p] * fmax(hp, 0.0);
-            water += wi;
-            const int pa = p % N1, pj = p / N1;
-            if (pa == 0 || pa == N1 - 1 || pj == 0 || pj == N1 - 1) water_b += wi;
-        }
-        const double ratio = fmin(water / water_b, T.weight_ratio[k]);
-        const double rho = fmax(0.9 * ratio, 1.0);
-        const double cap = shallow ? D.max_cfl_subcells : D.max_cfl;
-        cfl = fmin(cfl, fmin(D.bound_cfl * rho, cap));
+    // the warp's smallest step, then one atomic per block: dt ≥ 0, so its
+    // bits order as the values
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const unsigned long long o = __shfl_xor_sync(0xffffffffu, dt_bits, off);
+        dt_bits = o < dt_bits ? o : dt_bits;
     }
-    return rmax < 1e-14 ? INFINITY : cfl / ((2.0 * (double)P.order + 1.0) * rmax);
+    if (tid == 0) atomicMin(&ctl->dt_bits, dt_bits);
 }
 
 // ---------------------------------------------------------------------------

@@ -40,7 +40,7 @@ static void finish_n(const DevTables& T, const Physics& P, const DevBuf& acc, co
 template <int N1>
 static void dt_n(const DevTables& T, const Physics& P, const DevBuf& q, const DtParams& D,
                  double* dt_el, StepCtl* ctl, const int* active, cudaStream_t s) {
-    using C = Cfg<N1>;
+    using C = DtCfg<N1>;
     const unsigned blocks = (unsigned)((T.K + C::EPB - 1) / C::EPB);
     dt_kernel<N1><<<blocks, C::THREADS, 0, s>>>(T, P, q, D, dt_el, ctl, active);
 }

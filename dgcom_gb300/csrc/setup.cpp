@@ -428,6 +428,7 @@ std::string build_tables(const dgswe_form& f, const Operators& ops, const Topolo
             m[3] = G.sy[src];
             m[4] = std::sqrt(m[0] * m[0] + m[1] * m[1]);
             m[5] = std::sqrt(m[2] * m[2] + m[3] * m[3]);
+            for (int c = 0; c < 6; ++c) m[c] *= 0.25;  // the rate's ¼, exact
             if (!t.fcor.empty()) {
                 double r = ops.r[i], s = ops.s[i];
                 const auto& c = topo.corners[k];
@@ -504,6 +505,7 @@ std::string build_tables(const dgswe_form& f, const Operators& ops, const Topolo
                 m[3] = G.sy[node];
                 m[4] = std::sqrt(m[0] * m[0] + m[1] * m[1]);
                 m[5] = std::sqrt(m[2] * m[2] + m[3] * m[3]);
+                for (int c = 0; c < 6; ++c) m[c] *= 0.25;  // the rate's ¼, exact
                 if (L.element < 0) continue;
                 const ElementGeometry& NB = geo[L.element];
                 int nb_node = ops.face_node[L.face][n1 - 1 - fi];

@@ -104,7 +104,7 @@ struct Tables {
     std::vector<double> mass;       // [K·nn]
     std::vector<double> inv_area;   // [K]
     std::vector<double> weight_ratio; // [K] W/W∂
-    std::vector<double> dtm_own;    // [K·nn·6] ∇r, ∇s, |∇r|, |∇s| of own nodes
+    std::vector<double> dtm_own;    // [K·nn·6] ¼ of ∇r, ∇s, |∇r|, |∇s| of own nodes
     std::vector<double> dtm_face;   // [K·4·n1·6] the same at face nodes (own node's stored)
     std::vector<int64_t> nb_face_node; // [K·4·n1] neighbour's coincident node (global) or −1
     // faces

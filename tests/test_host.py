@@ -79,3 +79,24 @@ def test_coastal_workload_is_seeded():
     assert a.form.bathymetry.min() >= -300.0 - 1e-9
     assert (a.state[0] == 0).any() and (a.state[0] > 0).any()
     assert abs(a.form.coriolis_f0 - 2 * 7.292115e-5 * math.sin(math.radians(63.0))) < 1e-18
+
+
+def test_integer_pipe_compares_match_ieee(tmp_path):
+    """The kernels' fp:: compares, minima and maxima give the IEEE result."""
+    import shutil
+    import subprocess
+    from pathlib import Path
+
+    gxx = shutil.which("g++")
+    if gxx is None:
+        import pytest
+
+        pytest.skip("g++ not available")
+    here = Path(__file__).resolve().parent
+    exe = tmp_path / "fp64_bits_check"
+    subprocess.run([gxx, "-O2", "-std=c++17", "-ffp-contract=off",
+                    "-I", str(here.parent / "dgcom_gb300" / "csrc"),
+                    str(here / "fp64_bits_check.cpp"), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert out.stdout.startswith("ok ")
