@@ -10,11 +10,13 @@
 //  - face_kernel: the numerical flux F* of every interior edge node once,
 //    from the edge's left side with that side's normal (the reference's
 //    edge_fluxes, src/solver/rhs/swe_2d_split_form.rs:580-616), and of every
-//    boundary face node (wall or characteristic open boundary), scaled by
-//    each side's sJ·LIFT and stored per element face node;
+//    boundary face node (wall or characteristic open boundary), stored per
+//    element face node as each side sees it;
 //  - stage_kernel<N1>: per element, the split-form volume term (flux
 //    differencing on wet elements, subcell finite volumes on elements with a
-//    node shallower than the subcell depth), the lifted face fluxes, 1/J,
+//    node shallower than the subcell depth), the face fluxes lifted by each
+//    face node's sJ·LIFT (a multiply-add in the stage, not a multiply in
+//    the face pass), 1/J,
 //    Coriolis, the Shu–Osher combination, the point-implicit damping and the
 //    wet/dry correction or the accumulation (the reference's fused
 //    stage_where, src/physics/builder.rs:652-737), and the node velocities
@@ -56,6 +58,63 @@ enum StageMode { kRhsOnly = 0, kPost = 1, kAccumulate = 2 };
 using fp::lmax;
 using fp::lmin;
 
+// Square roots and reciprocals. DGSWE_FAST: faithful (within an ulp of the
+// correctly rounded value) from a single-precision seed refined in FP64,
+// ≈ 5 FP64-pipe operations against ≈ 8 for sqrt and ≈ 5 for 1/y measured
+// on GB300; the float views of the seed are built on the integer pipes,
+// since F2F conversions run on the FP64 pipe. Arguments outside the seed's
+// range (zero, subnormal, negative, huge, non-finite) take the IEEE
+// operation. Otherwise, and always without DGSWE_FAST, the IEEE operation.
+#if DGSWE_FAST
+// The float at or below a positive double in [2^-126, 2^128): the exponent
+// rebiased, the mantissa truncated
+__device__ __forceinline__ float f32_seed(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    return __uint_as_float((unsigned int)(b >> 29) - (896u << 23));
+}
+// The double of a positive normal float
+__device__ __forceinline__ double f64_of(float f) {
+    return __longlong_as_double(
+        (long long)(((unsigned long long)__float_as_uint(f) << 29) + (896ull << 52)));
+}
+#endif
+
+__device__ __forceinline__ double vsqrt(double x) {
+#if DGSWE_FAST
+    const int64_t b = fp::bits(x);
+    if (b < 0x3810000000000000ll || b >= 0x47E0000000000000ll) return sqrt(x);  // 2^-126, 2^127
+    const float r0 = rsqrtf(f32_seed(x));
+    const double h0 = f64_of(0.5f * r0);  // 1/(2√x), single precision
+    double c = x * f64_of(r0);
+    c = fma(h0, fma(-c, c, x), c);     // relative error ≈ 2^-42
+    return fma(h0, fma(-c, c, x), c);  // ≈ 2^-63 before the last rounding
+#else
+    return sqrt(x);
+#endif
+}
+
+__device__ __forceinline__ double vrcp(double y) {
+#if DGSWE_FAST
+    const int64_t b = fp::bits(y);
+    if (b < 0x3820000000000000ll || b >= 0x47C0000000000000ll) return 1.0 / y;  // 2^-125, 2^125
+    double r = f64_of(__frcp_rn(f32_seed(y)));
+    double e = fma(-y, r, 1.0);
+    r = fma(r, e, r);  // Newton: relative error ≈ 2^-44
+    e = fma(-y, r, 1.0);
+    return fma(r, e, r);
+#else
+    return 1.0 / y;
+#endif
+}
+
+__device__ __forceinline__ double vdiv(double x, double y) {
+#if DGSWE_FAST
+    return x * vrcp(y);
+#else
+    return x / y;
+#endif
+}
+
 struct Q {
     double h, hu, hv, u, v, b;
 };
@@ -72,7 +131,7 @@ __device__ __forceinline__ Sd side(const Q& q) { return {q.h, q.u, q.v, q.b}; }
 __device__ __forceinline__ void node_velocity(double h, double hu, double hv, double h_min,
                                               double& u, double& v) {
     const bool wet = fp::gt(h, h_min);
-    const double inv_h = 1.0 / h;
+    const double inv_h = vrcp(h);
     u = wet ? hu * inv_h : 0.0;
     v = wet ? hv * inv_h : 0.0;
 }
@@ -93,20 +152,20 @@ __device__ __forceinline__ F3 hll_aligned(double h_l, double hun_l, double hut_l
                                           double un_r, double ut_r, double g, double sqrt_g,
                                           double half_g, double h_min) {
     const bool dry = fp::le(h_l, h_min) && fp::le(h_r, h_min);
-    const double sh_l = sqrt(fp::max0(h_l)), sh_r = sqrt(fp::max0(h_r));
+    const double sh_l = vsqrt(fp::max0(h_l)), sh_r = vsqrt(fp::max0(h_r));
     const double c_l = sqrt_g * sh_l, c_r = sqrt_g * sh_r;
     const double sh_sum = sh_l + sh_r;
     const bool roe = fp::gt(sh_sum, 1e-10);
     const double h_roe = 0.5 * (h_l + h_r);
-    const double un_roe = roe ? (sh_l * un_l + sh_r * un_r) / sh_sum : 0.0;
-    const double c_roe = roe ? sqrt(g * h_roe) : 0.0;
+    const double un_roe = roe ? vdiv(sh_l * un_l + sh_r * un_r, sh_sum) : 0.0;
+    const double c_roe = roe ? vsqrt(g * h_roe) : 0.0;
     const double s_l = fp::gt(h_l, h_min) ? lmin(un_l - c_l, un_roe - c_roe) : un_r - 2.0 * c_r;
     const double s_r = fp::gt(h_r, h_min) ? lmax(un_r + c_r, un_roe + c_roe) : un_l + 2.0 * c_l;
     const double fl_h = h_l * un_l, fl_hu = h_l * un_l * un_l + half_g * h_l * h_l,
                  fl_hv = h_l * un_l * ut_l;
     const double fr_h = h_r * un_r, fr_hu = h_r * un_r * un_r + half_g * h_r * h_r,
                  fr_hv = h_r * un_r * ut_r;
-    const double inv_ds = 1.0 / (s_r - s_l);
+    const double inv_ds = vrcp(s_r - s_l);
     const double s_lr = s_l * s_r;
     const double st_h = inv_ds * (s_r * fl_h - s_l * fr_h + s_lr * (h_r - h_l));
     const double st_hu = inv_ds * (s_r * fl_hu - s_l * fr_hu + s_lr * (hun_r - hun_l));
@@ -251,13 +310,12 @@ __global__ void __launch_bounds__(256) face_kernel(DevTables T, Physics P, DevBu
             entropy_surface(ql, qr, geo[0], geo[1], P, fa, fbb);
         }
         const int64_t sl = (L * N1) + fi, sr = (R * N1) + rfi;
-        const double cl = T.lift_scale[sl], cr = T.lift_scale[sr];
-        fb_h[sl] = cl * fa.h;
-        fb_hu[sl] = cl * fa.hu;
-        fb_hv[sl] = cl * fa.hv;
-        fb_h[sr] = cr * fbb.h;
-        fb_hu[sr] = cr * fbb.hu;
-        fb_hv[sr] = cr * fbb.hv;
+        fb_h[sl] = fa.h;
+        fb_hu[sl] = fa.hu;
+        fb_hv[sl] = fa.hv;
+        fb_h[sr] = fbb.h;
+        fb_hu[sr] = fbb.hu;
+        fb_hv[sr] = fbb.hv;
         return;
     }
     // boundary face node (src/solver/rhs/swe_2d_split_form.rs:1090-1123)
@@ -353,10 +411,9 @@ __global__ void __launch_bounds__(256) face_kernel(DevTables T, Physics P, DevBu
         fs = wflux(qb, qb, nx, ny, g);  // F(q_b)·n
     }
     const int64_t sl = B * N1 + fi;
-    const double cl = T.lift_scale[sl];
-    fb_h[sl] = cl * fs.h;
-    fb_hu[sl] = cl * fs.hu;
-    fb_hv[sl] = cl * fs.hv;
+    fb_h[sl] = fs.h;
+    fb_hu[sl] = fs.hu;
+    fb_hv[sl] = fs.hv;
 }
 
 // ---------------------------------------------------------------------------
@@ -378,14 +435,15 @@ __device__ __forceinline__ double ref_cbrt(double x) {
 // Manning's rate g n² |u| / h^{4/3} at a floored depth h
 __device__ __forceinline__ double manning_rate(double g_n2, double h, double speed) {
 #if DGSWE_FAST
-    // h^{-1/3} by Newton steps z ← z + z(1 − h z³)/3 from a single-precision
-    // seed; then the rate is g n² |u| z⁴, no division
-    double z = (double)rcbrtf((float)h);
-#pragma unroll
-    for (int i = 0; i < 2; ++i) {
-        const double e = 1.0 - h * (z * z * z);
-        z = z + z * e * (1.0 / 3.0);
-    }
+    // h^{-1/3} from a single-precision seed (relative error δ ≈ 2^-22) and
+    // one step of third order, z ← z(1 + e/3 + 2e²/9) with e = 1 − h z³
+    // (error ≈ 5δ³ ≈ 2^-61); then the rate is g n² |u| z⁴, no division
+    const int64_t b = fp::bits(h);
+    double z = (b >= 0x3820000000000000ll && b < 0x47C0000000000000ll)  // 2^-125, 2^125
+                   ? f64_of(rcbrtf(f32_seed(h)))
+                   : 1.0 / cbrt(h);
+    const double e = fma(-h, z * z * z, 1.0);
+    z = fma(z * e, fma(e, 2.0 / 9.0, 1.0 / 3.0), z);
     const double z2 = z * z;
     return g_n2 * speed * (z2 * z2);
 #else
@@ -437,7 +495,7 @@ __device__ __forceinline__ void damp(const Physics& P, double g_n2, double h, do
             u = from.hu * factor;
             v = from.hv * factor;
         }
-        const double speed = sqrt(u * u + v * v);
+        const double speed = vsqrt(u * u + v * v);
         if (fp::gt0(speed)) rate += manning_rate(g_n2, lmax(h, P.manning_h_min), speed);
     }
     if (P.has_wet_dry && fp::lt(h, P.h_dry)) {
@@ -445,7 +503,7 @@ __device__ __forceinline__ void damp(const Physics& P, double g_n2, double h, do
         const double excess = P.h_dry / h - 1.0;
         rate += excess * excess / P.relaxation_time;
     }
-    const double factor = 1.0 / (1.0 + dt * rate);
+    const double factor = vrcp(1.0 + dt * rate);
     hu *= factor;
     hv *= factor;
 }
@@ -463,7 +521,15 @@ __device__ __forceinline__ void correct_node(const Physics& P, double h, double&
         hu = h * (factor * hu);
         hv = h * (factor * hv);
     }
-    // |hu| > h·u_max; the square root only near the cap
+    // |hu| > h·u_max; the square root only near the cap. First a test on
+    // the exponent fields alone (integer pipes): with E the biased exponent,
+    // |m| < √2·2^(max(E_hu, E_hv) − 1022) and h·u_max ≥ 2^(E_h + E_u − 2046)
+    // for normal h and u_max, so max(E_hu, E_hv) + 1025 ≤ E_h + E_u means
+    // |m|² < 0.99·cap² and the exact test below would be false.
+    const int e_h = (int)((fp::bits(h) >> 52) & 0x7FF);
+    const int e_u = (int)((fp::bits(P.max_velocity) >> 52) & 0x7FF);
+    const int e_hu = (int)((fp::bits(hu) >> 52) & 0x7FF), e_hv = (int)((fp::bits(hv) >> 52) & 0x7FF);
+    if (e_h >= 1 && e_u >= 1 && (e_hu > e_hv ? e_hu : e_hv) + 1025 <= e_h + e_u) return;
     const double m2 = hu * hu + hv * hv;
     const double cap = P.max_velocity * h;
     if (fp::gt(m2, 0.99 * (cap * cap))) {
@@ -486,6 +552,11 @@ struct Cfg {
     static constexpr int NA = 2 * (N1 - 1);  // pairs a node is in
     static constexpr int EPB = (128 / NN) > 0 ? (128 / NN) : 1;
     static constexpr int THREADS = EPB * NN;
+    // stage_kernel blocks per SM: 5 caps it at ≤ 102 registers (96 at
+    // N1 = 4, no spills) for 20 warps per SM; it is bound by the FP64 pipe
+    // and waits on it, so more warps keep it busier (measured 5 % faster
+    // on the 1 M-quad N = 3 case than 4 blocks)
+    static constexpr int MIN_BLOCKS = 5;
     static constexpr int PAIR_DOUBLES = NN * NP * 3;
     static constexpr int FACE_DOUBLES = 2 * NN * 8;           // reconstructed faces
     static constexpr int IFL_DOUBLES = 2 * N1 * (N1 - 1) * 6;  // subcell interface fluxes
@@ -564,9 +635,9 @@ __device__ __forceinline__ void reconstruct(const Sd& m, const Sd& c, const Sd& 
                           (fp::lt(c.h, h_dry) && fp::lt(e1, ws)) ||
                           (fp::lt(p.h, h_dry) && fp::lt(e2, ws));
     const double fm = x1 - xl, fpd = xr - x1;
-    const double ic = 1.0 / (x2 - x0);
-    const double im = 1.0 / (fp::gt0(fm) ? fm : 0.5 * (x1 - x0));
-    const double ip = 1.0 / (fp::gt0(fpd) ? fpd : 0.5 * (x2 - x1));
+    const double ic = vrcp(x2 - x0);
+    const double im = vrcp(fp::gt0(fm) ? fm : 0.5 * (x1 - x0));
+    const double ip = vrcp(fp::gt0(fpd) ? fpd : 0.5 * (x2 - x1));
     const double s_h = limited_slope(m.h, c.h, p.h, ic, im, ip);
     const double s_eta = flooding ? 0.0 : limited_slope(e0, e1, e2, ic, im, ip);
     const double s_u = limited_slope(m.u, c.u, p.u, ic, im, ip);
@@ -580,7 +651,7 @@ __device__ __forceinline__ void reconstruct(const Sd& m, const Sd& c, const Sd& 
 }
 
 template <int N1>
-__global__ void __launch_bounds__(Cfg<N1>::THREADS)
+__global__ void __launch_bounds__(Cfg<N1>::THREADS, Cfg<N1>::MIN_BLOCKS)
     stage_kernel(DevTables T, Physics P, StageExtra X, DevBuf in, DevBuf base, DevBuf out,
                  DevBuf acc, const double* __restrict__ fb_h, const double* __restrict__ fb_hu,
                  const double* __restrict__ fb_hv, StepCtl* ctl, int slot, int mode,
@@ -737,8 +808,8 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS)
             line_metric<N1>(T, k, dir, line, m0, m1);
             telescoped<N1>(P, m0, m1, affine, i0, i1);
             const double mx = i0[pos + 1], my = i1[pos + 1];
-            const double norm = sqrt(mx * mx + my * my);
-            const double inv = 1.0 / norm;
+            const double norm = vsqrt(mx * mx + my * my);
+            const double inv = vrcp(norm);
             const double* fa_ = &faces[((dir * N1 + line) * N1 + pos) * 8 + 4];   // right face of pos
             const double* fb_ = &faces[((dir * N1 + line) * N1 + pos + 1) * 8];   // left face of pos+1
             F3 fa, fb;
@@ -777,7 +848,12 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS)
             const double* f = &faces[((dir * N1 + line) * N1 + pos) * 8];
             const double lh = f[0], lb = f[3], rhh = f[4], rb = f[7];
             const double w_a = P.w[pos];
+#if DGSWE_FAST
+            (void)w_a;
+            const double bed = -0.5 * g * (lh + rhh) * (rb - lb) * iw;  // iw = 1/w_a
+#else
             const double bed = -0.5 * g * (lh + rhh) * (rb - lb) / w_a;
+#endif
             double m0[N1], m1[N1];
             line_metric<N1>(T, k, dir, line, m0, m1);
             double fx, fy;
@@ -789,7 +865,11 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS)
                 telescoped<N1>(P, m0, m1, false, i0, i1);
                 const double ml0 = i0[pos], ml1 = i1[pos], mr0 = i0[pos + 1], mr1 = i1[pos + 1];
                 const double metric =
+#if DGSWE_FAST
+                    0.25 * g * ((rhh + h) * (b - rb) + (lh + h) * (b - lb)) * iw;
+#else
                     0.25 * g * ((rhh + h) * (b - rb) + (lh + h) * (b - lb)) / w_a;
+#endif
                 fx = bed * 0.5 * (ml0 + mr0) + metric * (mr0 - ml0);
                 fy = bed * 0.5 * (ml1 + mr1) + metric * (mr1 - ml1);
             }
@@ -799,32 +879,44 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS)
     }
 
     // ---- surface: −LIFT·sJ·F* of the node's faces ----
+    // A node lies on at most one s-face (0 or 2) and one r-face (1 or 3).
+    // Every lane takes two slots in face order, a missing one as zero, so
+    // the warp's FP64 instructions run on all lanes instead of once per
+    // face with only that face's nodes active. Subtracting +0 is exact.
     if (valid) {
+        int f_a = j == 0 ? 0 : (j == N1 - 1 ? 2 : -1);
+        int f_b = a == N1 - 1 ? 1 : (a == 0 ? 3 : -1);
+        if (f_a == 2 && f_b == 1) {  // the reference's face order
+            f_a = 1;
+            f_b = 2;
+        }
         const int64_t fbase = k * 4 * N1;
-        if (j == 0) {
-            const int64_t s = fbase + 0 * N1 + a;
-            rh -= fb_h[s];
-            rhu -= fb_hu[s];
-            rhv -= fb_hv[s];
+        auto slot = [&](int f) -> int64_t {
+            const int fi = f == 0 ? a : (f == 1 ? j : (f == 2 ? N1 - 1 - a : N1 - 1 - j));
+            return fbase + f * N1 + fi;
+        };
+        double c_a = 0.0, h_a = 0.0, hu_a = 0.0, hv_a = 0.0;
+        double c_b = 0.0, h_b = 0.0, hu_b = 0.0, hv_b = 0.0;
+        if (f_a >= 0) {
+            const int64_t s_a = slot(f_a);
+            c_a = T.lift_scale[s_a];
+            h_a = fb_h[s_a];
+            hu_a = fb_hu[s_a];
+            hv_a = fb_hv[s_a];
         }
-        if (a == N1 - 1) {
-            const int64_t s = fbase + 1 * N1 + j;
-            rh -= fb_h[s];
-            rhu -= fb_hu[s];
-            rhv -= fb_hv[s];
+        if (f_b >= 0) {
+            const int64_t s_b = slot(f_b);
+            c_b = T.lift_scale[s_b];
+            h_b = fb_h[s_b];
+            hu_b = fb_hu[s_b];
+            hv_b = fb_hv[s_b];
         }
-        if (j == N1 - 1) {
-            const int64_t s = fbase + 2 * N1 + (N1 - 1 - a);
-            rh -= fb_h[s];
-            rhu -= fb_hu[s];
-            rhv -= fb_hv[s];
-        }
-        if (a == 0) {
-            const int64_t s = fbase + 3 * N1 + (N1 - 1 - j);
-            rh -= fb_h[s];
-            rhu -= fb_hu[s];
-            rhv -= fb_hv[s];
-        }
+        rh -= c_a * h_a;
+        rhu -= c_a * hu_a;
+        rhv -= c_a * hv_a;
+        rh -= c_b * h_b;
+        rhu -= c_b * hu_b;
+        rhv -= c_b * hv_b;
     }
 
     // ---- 1/J and the sources ----
@@ -1055,7 +1147,7 @@ __global__ void velocity_kernel(DevBuf b, int64_t n, double h_min) {
 // lr + ls here has exactly the bits of ¼(lr + ls) from unscaled metrics
 __device__ __forceinline__ double node_rate(double h, double u, double v, const double* m,
                                             double g) {
-    const double c = sqrt(g * fp::max0(h));
+    const double c = vsqrt(g * fp::max0(h));
     const double lr = fabs(u * m[0] + v * m[1]) + c * m[4];
     const double ls = fabs(u * m[2] + v * m[3]) + c * m[5];
     return lr + ls;
