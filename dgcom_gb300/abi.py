@@ -200,6 +200,16 @@ CUDA_ONLY = {
     # device pointers in and out; working memory in the library's own array
     "compute_rhs_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]),
+    # ensembles of independent members
+    "ensemble_create": (C.c_int, [C.POINTER(Form), C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    "ensemble_destroy": (None, [C.c_void_p]),
+    "ensemble_last_error": (C.c_char_p, [C.c_void_p]),
+    "ensemble_n_members": (C.c_int, [C.c_void_p]),
+    "ensemble_n_values": (C.c_int64, [C.c_void_p, C.c_int]),
+    "ensemble_upload": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, C.c_int64]),
+    "ensemble_download": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, C.c_int64]),
+    "ensemble_run": (C.c_int, [C.c_void_p, C.POINTER(RunConfig), C.c_int64, C.POINTER(Report),
+                               C.POINTER(Profile)]),
 }
 
 

@@ -98,7 +98,8 @@ def _bilinear_grid(field: np.ndarray, spacing: float, x: np.ndarray, y: np.ndarr
 
 
 def coastal_bed(x: np.ndarray, y: np.ndarray, lx: float, ly: float, seed: int,
-                n_islands: int = 30) -> np.ndarray:
+                n_islands: int = 30, island_radius: tuple[float, float] = (1000.0, 5000.0)
+                ) -> np.ndarray:
     """Bed elevation B at (x, y): a seeded Gaussian random field (5 km
     correlation, on a 1 km grid, bilinear to the points) mapped to depths of
     2–300 m, with ``n_islands`` Gaussian islands (radius 1–5 km) whose crests
@@ -114,7 +115,7 @@ def coastal_bed(x: np.ndarray, y: np.ndarray, lx: float, ly: float, seed: int,
     bed = -depth
     cx = rng.uniform(0.15 * lx, 0.95 * lx, n_islands)
     cy = rng.uniform(0.05 * ly, 0.95 * ly, n_islands)
-    radius = rng.uniform(1000.0, 5000.0, n_islands)
+    radius = rng.uniform(island_radius[0], island_radius[1], n_islands)
     crest = rng.uniform(2.0, 20.0, n_islands)
     centre_depth = _bilinear_grid(depth_grid, spacing, cx, cy)
     for i in range(n_islands):
@@ -123,9 +124,18 @@ def coastal_bed(x: np.ndarray, y: np.ndarray, lx: float, ly: float, seed: int,
     return bed
 
 
+COASTAL_TIDE = (("M2", 1.0), ("S2", 0.35), ("N2", 0.2), ("K1", 0.1))
+
+
 def coastal_box(n_elements: int = 1_000_000, order: int = 3, seed: int = 2026,
                 numerics: int = abi.NUMERICS_FAST, lx: float = 200_000.0,
-                ly: float = 150_000.0) -> Case:
+                ly: float = 150_000.0, n_islands: int = 30,
+                island_radius: tuple[float, float] = (1000.0, 5000.0),
+                tide: tuple = COASTAL_TIDE, manning_n: float = 0.02) -> Case:
+    """The 1 M-quad coastal box: a graded, jittered quad paving of lx × ly
+    (element size 100–400 m at the default size), Hilbert-ordered, with the
+    seeded coastal bed, walls on three sides and a tide on the open western
+    side, Manning's n and Coriolis at 63° N, from rest."""
     nx = max(2, int(round(math.sqrt(n_elements * lx / ly))))
     ny = max(2, int(round(n_elements / nx)))
     mean = lx / nx
@@ -136,15 +146,45 @@ def coastal_box(n_elements: int = 1_000_000, order: int = 3, seed: int = 2026,
     mesh, _ = in_hilbert_order(mesh)
     form = SWEDeviceForm2D(mesh=mesh, order=order, numerics=numerics)
     x, y = node_positions(mesh, order)
-    form.bathymetry = coastal_bed(x, y, lx, ly, seed)
-    form.manning_n = 0.02
+    form.bathymetry = coastal_bed(x, y, lx, ly, seed, n_islands, island_radius)
+    form.manning_n = manning_n
     form.coriolis_f0 = coriolis_parameter(63.0)
     rng = np.random.default_rng(seed + 1)
-    phases = rng.uniform(0.0, 360.0, 4)
-    cons = [tides.constituent(name, amp, ph) for (name, amp), ph in
-            zip([("M2", 1.0), ("S2", 0.35), ("N2", 0.2), ("K1", 0.1)], phases)]
+    phases = rng.uniform(0.0, 360.0, len(tide))
+    cons = [tides.constituent(name, amp, ph) for (name, amp), ph in zip(tide, phases)]
     form.boundaries = {TAG_WALL: WallBoundary(), TAG_OPEN: TidalBoundary(cons, ramp_duration=3600.0)}
     return Case(form, at_rest(form), 0.5, abi.SSP_RK3, 2000.0)
+
+
+def ensemble_member(n_elements: int, order: int, seed: int, manning_n: float,
+                    m2_amplitude: float, numerics: int = abi.NUMERICS_FAST) -> Case:
+    """One member of a batched ensemble: the coastal-box generator scaled to
+    ``n_elements`` quads of the same element sizes (mean 173 m, 4:3 box),
+    with islands in proportion to the area (at least one, radii at most a
+    tenth of the box) and an M2 tide of ``m2_amplitude``."""
+    mean = 173.0
+    area = n_elements * mean * mean
+    lx = math.sqrt(area * 4.0 / 3.0)
+    ly = 0.75 * lx
+    n_islands = max(1, int(round(30.0 * area / (200_000.0 * 150_000.0))))
+    radius = (min(1000.0, 0.05 * ly), min(5000.0, 0.1 * ly))
+    return coastal_box(n_elements, order, seed, numerics, lx, ly, n_islands, radius,
+                       (("M2", m2_amplitude),), manning_n)
+
+
+def ensemble_members(n_members: int = 256, seed: int = 2027,
+                     k_range: tuple[int, int] = (5_000, 200_000), orders: tuple = (2, 3),
+                     numerics: int = abi.NUMERICS_FAST) -> list[Case]:
+    """The batched-ensemble workload: element counts log-uniform over
+    ``k_range``, orders drawn from ``orders``, Manning n ~ U(0.015, 0.035)
+    and M2 amplitude ~ U(0.5, 1.5) m per member, every draw seeded."""
+    rng = np.random.default_rng(seed)
+    k = np.exp(rng.uniform(math.log(k_range[0]), math.log(k_range[1]), n_members))
+    order = rng.choice(np.asarray(orders), n_members)
+    manning = rng.uniform(0.015, 0.035, n_members)
+    amp = rng.uniform(0.5, 1.5, n_members)
+    return [ensemble_member(int(round(k[i])), int(order[i]), seed * 1000 + i, float(manning[i]),
+                            float(amp[i]), numerics) for i in range(n_members)]
 
 
 # -- the reference's split-form test setups ------------------------------------

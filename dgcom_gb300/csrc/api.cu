@@ -17,6 +17,7 @@
 
 #include "../../include/dgswe.h"
 #include "device.hpp"
+#include "host_common.hpp"
 #include "kernel_set.hpp"
 #include "setup.hpp"
 
@@ -113,43 +114,6 @@ int ensure_buffer(dgswe_handle* h, int id) {
 
 bool valid_buffer(int id) { return id >= 0 && id < DGSWE_N_BUFFERS; }
 
-// SspScheme::stages (src/time/integrator.rs:239-263): (start, input, beta, c)
-int scheme_table(int scheme, double st[4][4]) {
-    if (scheme == DGSWE_SSP_RK43) {
-        const double t[4][4] = {{1.0, 0.0, 0.5, 0.0},
-                                {0.0, 1.0, 0.5, 0.5},
-                                {2.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0, 1.0},
-                                {0.0, 1.0, 0.5, 0.5}};
-        std::memcpy(st, t, sizeof t);
-        return 4;
-    }
-    const double t[3][4] = {{1.0, 0.0, 1.0, 0.0}, {0.75, 0.25, 0.25, 1.0},
-                            {1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0, 0.5}};
-    std::memcpy(st, t, sizeof t);
-    return 3;
-}
-
-// PositivityBound::new (src/solver/rhs/swe_2d.rs:2194-2212) with the linear
-// limits of linear_cfl_swe_2d / linear_cfl_subcells_swe_2d (swe_2d.rs:1263-1300)
-DtParams dt_params(const dgswe_handle* h, double cfl, int scheme) {
-    DtParams d{};
-    d.cfl = cfl;
-    d.positivity = h->form.positivity_h_dry > 0.0 ? 1 : 0;
-    const int order = h->form.order;
-    const double n = (double)order;
-    const double ssp = scheme == DGSWE_SSP_RK43 ? 2.0 : 1.0;
-    const double bound = ssp * ((2.0 * n + 1.0) / (2.0 * n * (n + 1.0)));
-    static const double lin3[4] = {1.6, 1.04, 0.73, 0.56}, lin43[4] = {2.2, 1.51, 1.15, 0.93};
-    static const double sub3[4] = {0.94, 0.65, 0.47, 0.36}, sub43[4] = {1.5, 1.1, 0.97, 0.75};
-    const double lin = scheme == DGSWE_SSP_RK43 ? lin43[order - 1] : lin3[order - 1];
-    const double sub = scheme == DGSWE_SSP_RK43 ? sub43[order - 1] : sub3[order - 1];
-    d.bound_cfl = bound;
-    d.max_cfl = std::fmax(bound, 0.9 * lin);
-    d.max_cfl_subcells = std::fmax(bound, 0.9 * sub);
-    d.shallow = 100.0 * h->form.positivity_h_dry;
-    return d;
-}
-
 int sync(dgswe_handle* h) {
     CK(cudaStreamSynchronize(h->stream));
     CK(cudaGetLastError());
@@ -174,42 +138,6 @@ int write_host_args(dgswe_handle* h, const StageArgs& a) {
 }
 
 const int* always(dgswe_handle* h) { return &h->ctl->always; }
-
-int check_form(const dgswe_form* f, std::string& why) {
-    if (!f) return why = "form is NULL", DGSWE_ERR_INVALID;
-    if (f->abi_version != DGSWE_ABI_VERSION) return why = "ABI version mismatch", DGSWE_ERR_INVALID;
-    if (f->order < 1 || f->order > 4) return why = "order must be 1..4", DGSWE_ERR_UNSUPPORTED;
-    if (f->n_elements <= 0 || f->n_vertices <= 0 || !f->vertices || !f->elements)
-        return why = "the mesh is empty", DGSWE_ERR_INVALID;
-    if (f->n_elements >= (1ll << 40)) return why = "too many elements", DGSWE_ERR_INVALID;
-    if (f->n_periodic < 0 || (f->n_periodic > 0 && !f->periodic))
-        return why = "periodic pairs without data", DGSWE_ERR_INVALID;
-    if (f->formulation < DGSWE_WET_DRY || f->formulation > DGSWE_ENTROPY_CONSERVATIVE)
-        return why = "unknown formulation", DGSWE_ERR_UNSUPPORTED;
-    if (!(f->g > 0.0) || !(f->h_min >= 0.0)) return why = "g and h_min", DGSWE_ERR_INVALID;
-    if (f->friction < DGSWE_FRICTION_NONE || f->friction > DGSWE_FRICTION_MANNING_NODES)
-        return why = "unknown friction law", DGSWE_ERR_UNSUPPORTED;
-    if (f->friction == DGSWE_FRICTION_MANNING_NODES && !f->manning_n_nodes)
-        return why = "per-node Manning without data", DGSWE_ERR_INVALID;
-    if (f->has_wet_dry && !(f->wet_dry_h_dry > 0.0 && f->wet_dry_relaxation_time > 0.0))
-        return why = "the wet/dry depth and relaxation time must be positive", DGSWE_ERR_INVALID;
-    if (f->n_boundaries < 0 || f->n_boundaries > kMaxConditions ||
-        (f->n_boundaries > 0 && !f->boundaries))
-        return why = "boundary conditions", DGSWE_ERR_INVALID;
-    for (int b = 0; b < f->n_boundaries; ++b) {
-        const dgswe_boundary& c = f->boundaries[b];
-        if (c.kind != DGSWE_BC_WALL && c.kind != DGSWE_BC_CHARACTERISTIC)
-            return why = "a boundary condition without a device form", DGSWE_ERR_UNSUPPORTED;
-        if (c.n_constituents < 0 || c.n_constituents > kMaxConstituents ||
-            (c.n_constituents > 0 && !c.constituents))
-            return why = "tide constituents", DGSWE_ERR_INVALID;
-        for (int i = 0; i < c.n_constituents; ++i)
-            if (!(c.constituents[i].period > 0.0)) return why = "a tide period", DGSWE_ERR_INVALID;
-    }
-    if (f->numerics != DGSWE_NUMERICS_FAST && f->numerics != DGSWE_NUMERICS_EXACT)
-        return why = "unknown numerics", DGSWE_ERR_INVALID;
-    return DGSWE_OK;
-}
 
 // The device clock of a run from run->t_start towards `target`
 int begin_run(dgswe_handle* h, const dgswe_run_config* run, double target) {
@@ -253,19 +181,19 @@ int run_device_step_graph(dgswe_handle* h, int scheme, double cfl) {
     const int n = scheme_table(scheme, st);
     for (int b = 1; b < n; ++b)
         if (int s = ensure_buffer(h, b)) return s;
-    const DtParams D = dt_params(h, cfl, scheme);
+    const DtParams D = dt_params(h->form, cfl, scheme);
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     const int* active = &h->ctl->active;
-    h->ks->step_begin(h->ctl, h->stream);
+    h->ks->step_begin(h->ctl, 1, h->stream);
     h->ks->dt(h->n1, h->T, h->P, h->buf[DGSWE_STATE].view, D, nullptr, h->ctl, active, h->stream);
-    h->ks->step_dt(h->ctl, h->stream);
+    h->ks->step_dt(h->ctl, 1, h->stream);
     for (int s = 0; s < n; ++s) {
         const int in = s == 0 ? DGSWE_STATE : s;
         const int out = s + 1 < n ? s + 1 : DGSWE_STATE;
         launch_stage(h, in, DGSWE_STATE, out, DGSWE_STATE, s, kModePost, s + 1 == n, active);
     }
-    h->ks->step_end(h->ctl, h->stream);
+    h->ks->step_end(h->ctl, 1, h->stream);
     cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
     if (e != cudaSuccess) return fail(h, DGSWE_ERR_CUDA, "stream capture: %s", cudaGetErrorString(e));
     e = cudaGraphInstantiate(&h->step_graph, graph, 0);
@@ -438,62 +366,9 @@ int create_impl(dgswe_handle* h, const dgswe_form* f, int device) {
     UP(sched_hcoef, hcoef);
 #undef UP
 
-    Physics& P = h->P;
-    P.order = f->order;
-    P.n1 = ops.n1;
-    P.nn = ops.nn;
-    P.formulation = f->formulation;
-    P.g = f->g;
-    P.h_min = f->h_min;
-    P.sqrt_g = std::sqrt(f->g);  // correctly rounded, as the device's sqrt
-    P.half_g = 0.5 * f->g;
-    P.two_g = 2.0 * f->g;
-    P.subcell_depth = f->subcell_depth;
-    P.subcell_h_dry = f->subcell_h_dry;
-    P.has_bed = f->bathymetry ? 1 : 0;
-    P.has_wet_dry = f->has_wet_dry ? 1 : 0;
-    P.h_dry = f->wet_dry_h_dry;
-    P.relaxation_time = f->wet_dry_relaxation_time;
-    P.max_velocity = f->wet_dry_max_velocity;
-    P.friction = f->friction;
-    P.g_n2 = f->friction_g * f->manning_n * f->manning_n;
-    P.manning_h_min = f->manning_h_min;
-    P.has_coriolis = f->has_coriolis ? 1 : 0;
-    P.coriolis_field = t.fcor.empty() ? 0 : 1;
-    P.f0 = f->coriolis_f0;
-    P.n_conditions = f->n_boundaries;
-    for (int b = 0; b < f->n_boundaries; ++b) {
-        const dgswe_boundary& in = f->boundaries[b];
-        Condition& c = P.cond[b];
-        c.kind = in.kind;
-        c.elevation_only = in.elevation_only;
-        c.n_constituents = in.n_constituents;
-        c.wall_h_min = in.wall_h_min;
-        c.mean = in.mean_elevation;
-        c.ramp = in.ramp_duration;
-        for (int i = 0; i < in.n_constituents; ++i) {
-            const dgswe_tide_constituent& k = in.constituents[i];
-            // TidalConstituent::angular_frequency (src/boundary/tidal.rs:40-43)
-            c.c[i] = {k.amplitude, 2.0 * M_PI / k.period, k.phase, k.f,
-                      k.f_rate,    k.u_deg,                k.u_rate_deg, k.v0_deg};
-        }
-    }
-    for (int i = 0; i < ops.n1; ++i) {
-        P.x[i] = ops.x[i];
-        P.w[i] = ops.w[i];
-    }
-    for (int i = 0; i < ops.n1 * ops.n1; ++i) P.d[i] = ops.d[i];
-    for (int face = 0; face < 4; ++face)
-        for (int fi = 0; fi < ops.n1; ++fi) P.face_node[face][fi] = ops.face_node[face][fi];
-    // subcell bounds as the reference sums them (swe_2d_split_form.rs:968-990)
-    double x_left = -1.0;
-    for (int a = 0; a < ops.n1; ++a) {
-        const double x_right = x_left + ops.w[a];
-        h->X.xl[a] = x_left;
-        h->X.xr[a] = x_right;
-        h->X.inv_w[a] = 1.0 / ops.w[a];
-        x_left = x_right;
-    }
+    fill_physics(*f, ops, !t.fcor.empty(), h->P, h->X);
+    h->P.n_conditions = f->n_boundaries;
+    for (int b = 0; b < f->n_boundaries; ++b) h->P.cond[b] = make_condition(f->boundaries[b]);
 
     // buffers, faces, control
     if ((s = ensure_buffer(h, DGSWE_STATE))) return bail(s);
@@ -662,7 +537,7 @@ int dgswe_element_dt(dgswe_handle* h, double cfl, int32_t scheme, double* dt_ele
     const unsigned long long inf_bits = 0x7FF0000000000000ull;
     CK(cudaMemcpyAsync(&h->ctl->dt_bits, &inf_bits, sizeof inf_bits, cudaMemcpyHostToDevice,
                        h->stream));
-    const DtParams D = dt_params(h, cfl, scheme);
+    const DtParams D = dt_params(h->form, cfl, scheme);
     h->ks->dt(h->n1, h->T, h->P, h->buf[DGSWE_STATE].view, D, h->dt_el, h->ctl, always(h),
               h->stream);
     CK(cudaGetLastError());
@@ -749,8 +624,10 @@ int dgswe_run(dgswe_handle* h, const dgswe_run_config* run, dgswe_callback callb
     };
     if (int s = call(c.t)) return s;
     // steps launched between host checks: one when the host acts after
-    // every step (callbacks every step, a stop flag)
-    const int chunk = (!has_interval || run->stop) ? 1 : 4;
+    // every step (callbacks every step, a stop flag); with no host action
+    // due, many. The device's step_begin stops at the target, the step
+    // limit or a failure, so graphs launched past that point do nothing.
+    const int chunk = run->stop || (callback && !has_interval) ? 1 : (has_interval ? 4 : 64);
     char msg[256];
     while (c.t < run->t_end) {
         if (run->stop && *run->stop) {
@@ -804,7 +681,7 @@ int dgswe_profile_steps(dgswe_handle* h, const dgswe_run_config* run, int64_t n_
     for (int b = 1; b < n; ++b)
         if (int s = ensure_buffer(h, b)) return s;
     if (int s = begin_run(h, run, INFINITY)) return s;
-    const DtParams D = dt_params(h, run->cfl, run->scheme);
+    const DtParams D = dt_params(h->form, run->cfl, run->scheme);
     const int* active = &h->ctl->active;
     // per step: begin, dt, fit, n × (face, stage), end → 4 + 2n kernels
     const int per_step = 4 + 2 * n;
@@ -817,12 +694,12 @@ int dgswe_profile_steps(dgswe_handle* h, const dgswe_run_config* run, int64_t n_
     size_t q = 0;
     for (int64_t step = 0; step < n_steps; ++step) {
         CK(cudaEventRecord(ev[q++], h->stream));
-        h->ks->step_begin(h->ctl, h->stream);
+        h->ks->step_begin(h->ctl, 1, h->stream);
         CK(cudaEventRecord(ev[q++], h->stream));
         h->ks->dt(h->n1, h->T, h->P, h->buf[DGSWE_STATE].view, D, nullptr, h->ctl, active,
                   h->stream);
         CK(cudaEventRecord(ev[q++], h->stream));
-        h->ks->step_dt(h->ctl, h->stream);
+        h->ks->step_dt(h->ctl, 1, h->stream);
         CK(cudaEventRecord(ev[q++], h->stream));
         for (int s = 0; s < n; ++s) {
             const int in = s == 0 ? DGSWE_STATE : s;
@@ -835,7 +712,7 @@ int dgswe_profile_steps(dgswe_handle* h, const dgswe_run_config* run, int64_t n_
                          h->ctl, s, kModePost, s + 1 == n, active, h->stream);
             CK(cudaEventRecord(ev[q++], h->stream));
         }
-        h->ks->step_end(h->ctl, h->stream);
+        h->ks->step_end(h->ctl, 1, h->stream);
     }
     const size_t last = q;
     CK(cudaEventRecord(ev[q++], h->stream));

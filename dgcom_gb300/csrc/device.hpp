@@ -35,6 +35,11 @@ struct DevTables {
     const int32_t* sched_slot;  // [nn][2(n1-1)]
     const double* sched_coef;   // [nn][2(n1-1)]
     const double* sched_hcoef;  // [nn][2(n1-1)] sched_coef / 2
+    // An ensemble's concatenated members: each element's member (its
+    // StepCtl is ctl[member]) and the members' boundary conditions, which
+    // bface_cond indexes. Both null for one mesh (ctl[0], Physics::cond).
+    const int32_t* elem_member = nullptr;
+    const struct Condition* cond = nullptr;
 };
 
 struct Constituent {

@@ -1,0 +1,165 @@
+// Host-side pieces shared by one mesh's handle (api.cu) and the ensemble
+// (ensemble.cu): form checks, the SSP schemes' tables, the dt parameters and
+// the device physics constants of a form.
+#pragma once
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/dgswe.h"
+#include "device.hpp"
+#include "setup.hpp"
+
+namespace dgswe {
+
+// SspScheme::stages (src/time/integrator.rs:239-263): (start, input, beta, c)
+inline int scheme_table(int scheme, double st[4][4]) {
+    if (scheme == DGSWE_SSP_RK43) {
+        const double t[4][4] = {{1.0, 0.0, 0.5, 0.0},
+                                {0.0, 1.0, 0.5, 0.5},
+                                {2.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0, 1.0},
+                                {0.0, 1.0, 0.5, 0.5}};
+        std::memcpy(st, t, sizeof t);
+        return 4;
+    }
+    const double t[3][4] = {{1.0, 0.0, 1.0, 0.0}, {0.75, 0.25, 0.25, 1.0},
+                            {1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0, 0.5}};
+    std::memcpy(st, t, sizeof t);
+    return 3;
+}
+
+// PositivityBound::new (src/solver/rhs/swe_2d.rs:2194-2212) with the linear
+// limits of linear_cfl_swe_2d / linear_cfl_subcells_swe_2d (swe_2d.rs:1263-1300)
+inline DtParams dt_params(const dgswe_form& f, double cfl, int scheme) {
+    DtParams d{};
+    d.cfl = cfl;
+    d.positivity = f.positivity_h_dry > 0.0 ? 1 : 0;
+    const int order = f.order;
+    const double n = (double)order;
+    const double ssp = scheme == DGSWE_SSP_RK43 ? 2.0 : 1.0;
+    const double bound = ssp * ((2.0 * n + 1.0) / (2.0 * n * (n + 1.0)));
+    static const double lin3[4] = {1.6, 1.04, 0.73, 0.56}, lin43[4] = {2.2, 1.51, 1.15, 0.93};
+    static const double sub3[4] = {0.94, 0.65, 0.47, 0.36}, sub43[4] = {1.5, 1.1, 0.97, 0.75};
+    const double lin = scheme == DGSWE_SSP_RK43 ? lin43[order - 1] : lin3[order - 1];
+    const double sub = scheme == DGSWE_SSP_RK43 ? sub43[order - 1] : sub3[order - 1];
+    d.bound_cfl = bound;
+    d.max_cfl = std::fmax(bound, 0.9 * lin);
+    d.max_cfl_subcells = std::fmax(bound, 0.9 * sub);
+    d.shallow = 100.0 * f.positivity_h_dry;
+    return d;
+}
+
+inline int check_form(const dgswe_form* f, std::string& why) {
+    if (!f) return why = "form is NULL", DGSWE_ERR_INVALID;
+    if (f->abi_version != DGSWE_ABI_VERSION) return why = "ABI version mismatch", DGSWE_ERR_INVALID;
+    if (f->order < 1 || f->order > 4) return why = "order must be 1..4", DGSWE_ERR_UNSUPPORTED;
+    if (f->n_elements <= 0 || f->n_vertices <= 0 || !f->vertices || !f->elements)
+        return why = "the mesh is empty", DGSWE_ERR_INVALID;
+    if (f->n_elements >= (1ll << 40)) return why = "too many elements", DGSWE_ERR_INVALID;
+    if (f->n_periodic < 0 || (f->n_periodic > 0 && !f->periodic))
+        return why = "periodic pairs without data", DGSWE_ERR_INVALID;
+    if (f->formulation < DGSWE_WET_DRY || f->formulation > DGSWE_ENTROPY_CONSERVATIVE)
+        return why = "unknown formulation", DGSWE_ERR_UNSUPPORTED;
+    if (!(f->g > 0.0) || !(f->h_min >= 0.0)) return why = "g and h_min", DGSWE_ERR_INVALID;
+    if (f->friction < DGSWE_FRICTION_NONE || f->friction > DGSWE_FRICTION_MANNING_NODES)
+        return why = "unknown friction law", DGSWE_ERR_UNSUPPORTED;
+    if (f->friction == DGSWE_FRICTION_MANNING_NODES && !f->manning_n_nodes)
+        return why = "per-node Manning without data", DGSWE_ERR_INVALID;
+    if (f->has_wet_dry && !(f->wet_dry_h_dry > 0.0 && f->wet_dry_relaxation_time > 0.0))
+        return why = "the wet/dry depth and relaxation time must be positive", DGSWE_ERR_INVALID;
+    if (f->n_boundaries < 0 || f->n_boundaries > kMaxConditions ||
+        (f->n_boundaries > 0 && !f->boundaries))
+        return why = "boundary conditions", DGSWE_ERR_INVALID;
+    for (int b = 0; b < f->n_boundaries; ++b) {
+        const dgswe_boundary& c = f->boundaries[b];
+        if (c.kind != DGSWE_BC_WALL && c.kind != DGSWE_BC_CHARACTERISTIC)
+            return why = "a boundary condition without a device form", DGSWE_ERR_UNSUPPORTED;
+        if (c.n_constituents < 0 || c.n_constituents > kMaxConstituents ||
+            (c.n_constituents > 0 && !c.constituents))
+            return why = "tide constituents", DGSWE_ERR_INVALID;
+        for (int i = 0; i < c.n_constituents; ++i)
+            if (!(c.constituents[i].period > 0.0)) return why = "a tide period", DGSWE_ERR_INVALID;
+    }
+    if (f->numerics != DGSWE_NUMERICS_FAST && f->numerics != DGSWE_NUMERICS_EXACT)
+        return why = "unknown numerics", DGSWE_ERR_INVALID;
+    return DGSWE_OK;
+}
+
+// A boundary condition's device form; TidalConstituent::angular_frequency
+// (src/boundary/tidal.rs:40-43) for each constituent
+inline Condition make_condition(const dgswe_boundary& in) {
+    Condition c{};
+    c.kind = in.kind;
+    c.elevation_only = in.elevation_only;
+    c.n_constituents = in.n_constituents;
+    c.wall_h_min = in.wall_h_min;
+    c.mean = in.mean_elevation;
+    c.ramp = in.ramp_duration;
+    for (int i = 0; i < in.n_constituents; ++i) {
+        const dgswe_tide_constituent& k = in.constituents[i];
+        c.c[i] = {k.amplitude, 2.0 * M_PI / k.period, k.phase, k.f,
+                  k.f_rate,    k.u_deg,                k.u_rate_deg, k.v0_deg};
+    }
+    return c;
+}
+
+// The device physics of a form, without its boundary conditions, and the
+// subcell bounds of its operators
+inline void fill_physics(const dgswe_form& f, const Operators& ops, bool coriolis_field,
+                         Physics& P, StageExtra& X) {
+    P.order = ops.order;  // the operators' order (an ensemble group's, not member 0's)
+    P.n1 = ops.n1;
+    P.nn = ops.nn;
+    P.formulation = f.formulation;
+    P.g = f.g;
+    P.h_min = f.h_min;
+    P.sqrt_g = std::sqrt(f.g);  // correctly rounded, as the device's sqrt
+    P.half_g = 0.5 * f.g;
+    P.two_g = 2.0 * f.g;
+    P.subcell_depth = f.subcell_depth;
+    P.subcell_h_dry = f.subcell_h_dry;
+    P.has_bed = f.bathymetry ? 1 : 0;
+    P.has_wet_dry = f.has_wet_dry ? 1 : 0;
+    P.h_dry = f.wet_dry_h_dry;
+    P.relaxation_time = f.wet_dry_relaxation_time;
+    P.max_velocity = f.wet_dry_max_velocity;
+    P.friction = f.friction;
+    P.g_n2 = f.friction_g * f.manning_n * f.manning_n;
+    P.manning_h_min = f.manning_h_min;
+    P.has_coriolis = f.has_coriolis ? 1 : 0;
+    P.coriolis_field = coriolis_field ? 1 : 0;
+    P.f0 = f.coriolis_f0;
+    for (int i = 0; i < ops.n1; ++i) {
+        P.x[i] = ops.x[i];
+        P.w[i] = ops.w[i];
+    }
+    for (int i = 0; i < ops.n1 * ops.n1; ++i) P.d[i] = ops.d[i];
+    for (int face = 0; face < 4; ++face)
+        for (int fi = 0; fi < ops.n1; ++fi) P.face_node[face][fi] = ops.face_node[face][fi];
+    // subcell bounds as the reference sums them (swe_2d_split_form.rs:968-990)
+    double x_left = -1.0;
+    for (int a = 0; a < ops.n1; ++a) {
+        const double x_right = x_left + ops.w[a];
+        X.xl[a] = x_left;
+        X.xr[a] = x_right;
+        X.inv_w[a] = 1.0 / ops.w[a];
+        x_left = x_right;
+    }
+}
+
+// The owned pairs of a schedule as the device reads them (a, c, dir, pa, pc)
+inline std::vector<int8_t> owned_table(const PairSchedule& sched) {
+    std::vector<int8_t> owned;
+    for (const PairSlot& p : sched.owned) {
+        owned.push_back(p.a);
+        owned.push_back(p.c);
+        owned.push_back(p.dir);
+        owned.push_back(p.pa);
+        owned.push_back(p.pc);
+    }
+    return owned;
+}
+
+}  // namespace dgswe

@@ -21,9 +21,10 @@ struct KernelSet {
     void (*dt)(int n1, const DevTables&, const Physics&, const DevBuf& q, const DtParams&,
                double* dt_el, StepCtl* ctl, const int* active, cudaStream_t);
     void (*velocity)(const DevBuf&, int64_t n, double h_min, cudaStream_t);
-    void (*step_begin)(StepCtl*, cudaStream_t);
-    void (*step_dt)(StepCtl*, cudaStream_t);
-    void (*step_end)(StepCtl*, cudaStream_t);
+    // the run's clock, one thread per StepCtl of ctl[0..n)
+    void (*step_begin)(StepCtl*, int n, cudaStream_t);
+    void (*step_dt)(StepCtl*, int n, cudaStream_t);
+    void (*step_end)(StepCtl*, int n, cudaStream_t);
 };
 
 // kernels_fast.cu: FMA contraction, division-free Manning rate

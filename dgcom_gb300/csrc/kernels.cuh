@@ -328,7 +328,7 @@ __global__ void __launch_bounds__(256) face_kernel(DevTables T, Physics P, DevBu
     const Q qi = load_q(in, T, P, k * NN + node);
     const double* geo = &T.bface_geo[bfi * 5];
     const double nx = geo[0], ny = geo[1];
-    const Condition& c = P.cond[T.bface_cond[bfi]];
+    const Condition& c = T.cond ? T.cond[T.bface_cond[bfi]] : P.cond[T.bface_cond[bfi]];
     F3 fs;
     // the interior velocity of BCContext2D (velocity_simple)
     double u = 0.0, v = 0.0;
@@ -360,7 +360,8 @@ __global__ void __launch_bounds__(256) face_kernel(DevTables T, Physics P, DevBu
     } else {
         // CharacteristicOBC with a uniform harmonic tide
         // (src/boundary/characteristic.rs:411-437, 481-520)
-        const double eta = tide_elevation(c, ctl->stage[slot].time);
+        const int member = T.elem_member ? T.elem_member[k] : 0;
+        const double eta = tide_elevation(c, ctl[member].stage[slot].time);
         const double bathy = qi.b;
         const double h_e = fmax(eta - bathy, 0.0);
         double un_e = 0.0;
@@ -667,7 +668,10 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS, Cfg<N1>::MIN_BLOCKS)
     const int tid = threadIdx.x;
     const int e = tid / NN, i = tid % NN;
     const int64_t k = (int64_t)blockIdx.x * EPB + e;
-    const bool valid = k < T.K;
+    // the element's member (its StepCtl); an ensemble member that has
+    // stopped keeps its state: its elements take no part
+    StepCtl* const cm = ctl + ((T.elem_member && k < T.K) ? T.elem_member[k] : 0);
+    const bool valid = k < T.K && (!T.elem_member || cm->active);
     const int64_t gi = k * NN + i;
     const int a = i % N1, j = i / N1;
     const double g = P.g, h_min = P.h_min, sqrt_g = P.sqrt_g, half_g = P.half_g;
@@ -940,7 +944,7 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS, Cfg<N1>::MIN_BLOCKS)
     if (mode == kRhsOnly) return;  // uniform: no barrier follows for this mode
 
     // ---- stage combination and damping ----
-    const StageArgs sa = ctl->stage[slot];
+    const StageArgs sa = cm->stage[slot];
     double vh = 0.0, vhu = 0.0, vhv = 0.0;
     if (valid) {
         if (fp::nz(sa.a)) {
@@ -1015,7 +1019,7 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS, Cfg<N1>::MIN_BLOCKS)
             }
             s_red[e][3] = theta;
             s_red[e][4] = hmin;
-            if (fp::lt0(h_avg)) atomicAdd((unsigned long long*)&ctl->clips, 1ull);
+            if (fp::lt0(h_avg)) atomicAdd((unsigned long long*)&cm->clips, 1ull);
         }
         __syncthreads();
         if (valid && needs) {
@@ -1044,7 +1048,7 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS, Cfg<N1>::MIN_BLOCKS)
         out.u[gi] = uo;
         out.v[gi] = vo;
         if (check_finite && !(fp::finite(vh) && fp::finite(vhu) && fp::finite(vhv)))
-            ctl->nonfinite = 1;
+            cm->nonfinite = 1;
     }
 }
 
@@ -1062,6 +1066,7 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS)
     const int64_t k = (int64_t)blockIdx.x * EPB + e;
     const bool valid = k < T.K;
     const int64_t gi = k * NN + i;
+    StepCtl* const cm = ctl + ((T.elem_member && valid) ? T.elem_member[k] : 0);  // the member's
     if (i == 0) s_flag[e] = 0;
     double vh = 0, vhu = 0, vhv = 0;
     if (valid) {
@@ -1098,7 +1103,7 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS)
             }
             s_red[e][3] = theta;
             s_red[e][4] = hmin;
-            if (fp::lt0(h_avg)) atomicAdd((unsigned long long*)&ctl->clips, 1ull);
+            if (fp::lt0(h_avg)) atomicAdd((unsigned long long*)&cm->clips, 1ull);
         }
         __syncthreads();
         if (valid && needs) {
@@ -1237,20 +1242,26 @@ __global__ void __launch_bounds__(DtCfg<N1>::THREADS)
     if (tid >= 32) return;  // warp 0: lane l finishes element k0 + l
     const int64_t kl = k0 + tid;
     unsigned long long dt_bits = 0x7FF0000000000000ull;  // +∞
+    int member = -1;
     if (kl < T.K) {
         const double dt = element_dt<N1>(D, P.order, T.weight_ratio[kl], &s_rate[tid * PITCH],
                                          &s_h[tid * PITCH], &s_mass[tid * PITCH]);
         if (dt_el) dt_el[kl] = dt;
         dt_bits = (unsigned long long)fp::bits(dt);
+        member = T.elem_member ? T.elem_member[kl] : 0;
     }
-    // the warp's smallest step, then one atomic per block: dt ≥ 0, so its
-    // bits order as the values
+    // Each member's smallest step over the warp, then one atomic per member
+    // present: members are contiguous element ranges, so lane l gathers the
+    // lanes above it while they share its member, and the first lane of each
+    // run holds that run's minimum. dt ≥ 0, so its bits order as the values.
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        const unsigned long long o = __shfl_xor_sync(0xffffffffu, dt_bits, off);
-        dt_bits = o < dt_bits ? o : dt_bits;
+    for (int off = 1; off < 32; off <<= 1) {
+        const unsigned long long o = __shfl_down_sync(0xffffffffu, dt_bits, off);
+        const int om = __shfl_down_sync(0xffffffffu, member, off);
+        if (tid + off < 32 && om == member && o < dt_bits) dt_bits = o;
     }
-    if (tid == 0) atomicMin(&ctl->dt_bits, dt_bits);
+    const int below = __shfl_up_sync(0xffffffffu, member, 1);
+    if (member >= 0 && (tid == 0 || below != member)) atomicMin(&ctl[member].dt_bits, dt_bits);
 }
 
 // ---------------------------------------------------------------------------
@@ -1260,7 +1271,10 @@ __global__ void __launch_bounds__(DtCfg<N1>::THREADS)
 constexpr int kFailDtMin = 4, kFailMaxSteps = 5, kFailNonFinite = 3;
 
 // Whether the step runs: no failure, time left before the target, steps left
-__global__ void step_begin(StepCtl* c) {
+__global__ void step_begin(StepCtl* ctl, int n) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n) return;
+    StepCtl* c = ctl + m;
     c->dt_bits = 0x7FF0000000000000ull;  // +∞
     bool run = c->failure == 0 && c->t < c->target;
     if (run && c->max_steps > 0 && c->steps >= c->max_steps) {
@@ -1272,7 +1286,10 @@ __global__ void step_begin(StepCtl* c) {
 
 // dt from the element steps, capped, checked, fitted to land on the target;
 // the stages' times and weights (element_stage, src/time/multirate.rs:169-200)
-__global__ void step_dt(StepCtl* c) {
+__global__ void step_dt(StepCtl* ctl, int n) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n) return;
+    StepCtl* c = ctl + m;
     if (!c->active) return;
     double dt = __longlong_as_double((long long)c->dt_bits);
     if (c->dt_max > 0.0) dt = fmin(dt, c->dt_max);
@@ -1299,7 +1316,10 @@ __global__ void step_dt(StepCtl* c) {
     }
 }
 
-__global__ void step_end(StepCtl* c) {
+__global__ void step_end(StepCtl* ctl, int n) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n) return;
+    StepCtl* c = ctl + m;
     if (!c->active) return;
     c->t = c->landed ? c->target : c->t + c->dt;
     c->steps += 1;

@@ -84,9 +84,17 @@ static void velocity(const DevBuf& b, int64_t n, double h_min, cudaStream_t s) {
     velocity_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b, n, h_min);
 }
 
-static void begin(StepCtl* c, cudaStream_t s) { step_begin<<<1, 1, 0, s>>>(c); }
-static void dt_fit(StepCtl* c, cudaStream_t s) { step_dt<<<1, 1, 0, s>>>(c); }
-static void end(StepCtl* c, cudaStream_t s) { step_end<<<1, 1, 0, s>>>(c); }
+// one thread per member's StepCtl
+static unsigned member_blocks(int n) { return (unsigned)((n + 127) / 128); }
+static void begin(StepCtl* c, int n, cudaStream_t s) {
+    step_begin<<<member_blocks(n), 128, 0, s>>>(c, n);
+}
+static void dt_fit(StepCtl* c, int n, cudaStream_t s) {
+    step_dt<<<member_blocks(n), 128, 0, s>>>(c, n);
+}
+static void end(StepCtl* c, int n, cudaStream_t s) {
+    step_end<<<member_blocks(n), 128, 0, s>>>(c, n);
+}
 
 static const KernelSet kSet = {face, stage, finish, dt, velocity, begin, dt_fit, end};
 

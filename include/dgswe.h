@@ -84,11 +84,13 @@ enum dgswe_scheme {
     DGSWE_SSP_RK43 = 1
 };
 
-/* Device arithmetic. FAST contracts multiply-adds into FMA and evaluates
- * the Manning rate's h^(-4/3) by FP64 Newton steps from a single-precision
- * seed; EXACT keeps every multiply and add separately rounded and follows
- * the reference's cube root (src/source/swe_2d/friction.rs:39-70). Both use
- * IEEE division and square root and are FP64 throughout. */
+/* Device arithmetic, FP64 throughout. FAST contracts multiply-adds into FMA,
+ * takes square roots and reciprocals within an ulp of the correctly rounded
+ * value (a single-precision seed refined in FP64) and the Manning rate's
+ * h^(-4/3) from one third-order FP64 step, with no division; EXACT keeps
+ * every multiply and add separately rounded, uses IEEE division and square
+ * root and follows the reference's cube root
+ * (src/source/swe_2d/friction.rs:39-70). */
 enum dgswe_numerics {
     DGSWE_NUMERICS_FAST = 0,
     DGSWE_NUMERICS_EXACT = 1
@@ -350,6 +352,47 @@ int dgswe_profile_steps(dgswe_handle* handle, const dgswe_run_config* run,
 int dgswe_compute_rhs_noalloc(dgswe_handle* handle, const double* h, const double* hu,
                               const double* hv, double time, double* out_h, double* out_hu,
                               double* out_hv, int64_t n);
+
+/* ---------------------------------------------------------------------------
+ * Ensembles: independent runs advanced together.
+ *
+ * No counterpart in the reference, which runs one case per
+ * CaseDevice::run_2d call (src/case/run.rs:179-212); a member is what one
+ * such call would run. Members may differ in mesh (size and shape), order,
+ * bathymetry, Manning coefficient (uniform or per node) and boundary data
+ * (tide constituents, walls); every other physics option must equal member
+ * 0's, or create fails with DGSWE_ERR_INVALID. Each member takes its own
+ * time step from its own CFL limit. All members' device data lives in one
+ * set of tables per order, and one CUDA graph advances every member by one
+ * step. A member's result equals a dgswe_run of that member alone over the
+ * same steps, bit for bit. */
+typedef struct dgswe_ensemble dgswe_ensemble;
+
+/* Copies n_members forms (the same rules as dgswe_create for each) to the
+ * device. *out is set even on failure, for dgswe_ensemble_last_error;
+ * destroy it either way. */
+int dgswe_ensemble_create(const dgswe_form* forms, int n_members, int device,
+                          dgswe_ensemble** out);
+void dgswe_ensemble_destroy(dgswe_ensemble* ensemble);
+const char* dgswe_ensemble_last_error(const dgswe_ensemble* ensemble);
+int dgswe_ensemble_n_members(const dgswe_ensemble* ensemble);
+/* Values per variable of one member: its n_elements·(order+1)² */
+int64_t dgswe_ensemble_n_values(const dgswe_ensemble* ensemble, int member);
+/* One member's state, host or device pointers, n = dgswe_ensemble_n_values */
+int dgswe_ensemble_upload(dgswe_ensemble* ensemble, int member, const double* h,
+                          const double* hu, const double* hv, int64_t n);
+int dgswe_ensemble_download(dgswe_ensemble* ensemble, int member, double* h, double* hu,
+                            double* hv, int64_t n);
+/* Advances every member by n_steps SSP steps (run->scheme, run->cfl,
+ * run->dt_max, run->dt_min; t_end, interval and stop are not used), all
+ * from run->t_start, or each from its own time (0 before its first run)
+ * when run->t_start is NaN: two runs of n steps with the second from NaN
+ * equal one run of 2n. Negative-depth clips add up over runs. reports (n_members entries) and profile may be NULL;
+ * profile->total_ms is the device time of all the steps. A member whose
+ * step fails (non-finite state, dt below dt_min) stops there and the others
+ * go on; the call then returns that member's status. */
+int dgswe_ensemble_run(dgswe_ensemble* ensemble, const dgswe_run_config* run, int64_t n_steps,
+                       dgswe_report* reports, dgswe_profile* profile);
 
 #ifdef __cplusplus
 }

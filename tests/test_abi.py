@@ -114,3 +114,39 @@ def test_create_without_a_gpu_says_so(cuda_lib):
     assert status == abi.ERR_NO_DEVICE
     assert "no CUDA device" in cuda_lib.last_error(handle).decode()
     cuda_lib.destroy(handle)
+
+
+def test_ensemble_create_checks_the_members_before_the_device():
+    """Members must share every physics option but the mesh, bed, Manning
+    and boundary data; the check needs no GPU."""
+    import ctypes as C
+
+    from dgcom_gb300 import cases
+
+    lib = abi.cuda_library()
+    a = cases.tidal_channel(nx=4, ny=2)
+    b = cases.tidal_channel(nx=6, ny=2, order=3)
+    b.form.manning_n = 0.03
+    keep = []
+    forms = (abi.Form * 2)()
+    for i, c in enumerate((a, b)):
+        f, k = c.form.to_c()
+        forms[i] = f
+        keep.append(k)
+    handle = C.c_void_p()
+    status = lib.ensemble_create(forms, 2, 0, C.byref(handle))
+    # the same physics: only the device can refuse (no GPU here), or it runs
+    assert status in (abi.OK, abi.ERR_NO_DEVICE)
+    lib.ensemble_destroy(handle)
+    c2 = cases.tidal_channel(nx=6, ny=2)
+    c2.form.h_min = 2e-6
+    f, k = c2.form.to_c()
+    forms[1] = f
+    keep.append(k)
+    handle = C.c_void_p()
+    status = lib.ensemble_create(forms, 2, 0, C.byref(handle))
+    assert status == abi.ERR_INVALID
+    assert b"physics options differ" in lib.ensemble_last_error(handle)
+    lib.ensemble_destroy(handle)
+    assert lib.ensemble_create(forms, 0, 0, C.byref(handle)) == abi.ERR_INVALID
+    lib.ensemble_destroy(handle)
