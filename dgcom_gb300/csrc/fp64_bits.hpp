@@ -37,6 +37,16 @@ DG_HD int64_t bits(double x) {
 #endif
 }
 
+DG_HD double from_bits(int64_t b) {
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double((long long)b);
+#else
+    double x;
+    memcpy(&x, &b, sizeof x);
+    return x;
+#endif
+}
+
 // A signed key in the order of the values: the sign-magnitude pattern as a
 // two's-complement integer, with −0 and +0 both mapped to 0
 DG_HD int64_t key(double x) {

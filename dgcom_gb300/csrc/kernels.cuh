@@ -39,210 +39,12 @@
 
 #include "device.hpp"
 #include "fp64_bits.hpp"
+#include "point.cuh"
 
 namespace dgswe {
 namespace DGSWE_NS {
 
-constexpr int kWetDry = 0, kEntropyStable = 1, kEntropyConservative = 2;
-constexpr int kBcWall = 0;
-constexpr int kIncomingWave = 1;
 enum StageMode { kRhsOnly = 0, kPost = 1, kAccumulate = 2 };
-
-// ---------------------------------------------------------------------------
-// arithmetic
-//
-// Every compare, minimum and maximum of doubles on the per-node paths goes
-// through fp:: (fp64_bits.hpp): the same result on the integer pipes, which
-// leaves the FP64 pipe, the stage's bound, to arithmetic.
-
-using fp::lmax;
-using fp::lmin;
-
-// Square roots and reciprocals. DGSWE_FAST: faithful (within an ulp of the
-// correctly rounded value) from a single-precision seed refined in FP64,
-// ≈ 5 FP64-pipe operations against ≈ 8 for sqrt and ≈ 5 for 1/y measured
-// on GB300; the float views of the seed are built on the integer pipes,
-// since F2F conversions run on the FP64 pipe. Arguments outside the seed's
-// range (zero, subnormal, negative, huge, non-finite) take the IEEE
-// operation. Otherwise, and always without DGSWE_FAST, the IEEE operation.
-#if DGSWE_FAST
-// The float at or below a positive double in [2^-126, 2^128): the exponent
-// rebiased, the mantissa truncated
-__device__ __forceinline__ float f32_seed(double x) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    return __uint_as_float((unsigned int)(b >> 29) - (896u << 23));
-}
-// The double of a positive normal float
-__device__ __forceinline__ double f64_of(float f) {
-    return __longlong_as_double(
-        (long long)(((unsigned long long)__float_as_uint(f) << 29) + (896ull << 52)));
-}
-#endif
-
-__device__ __forceinline__ double vsqrt(double x) {
-#if DGSWE_FAST
-    const int64_t b = fp::bits(x);
-    if (b < 0x3810000000000000ll || b >= 0x47E0000000000000ll) return sqrt(x);  // 2^-126, 2^127
-    const float r0 = rsqrtf(f32_seed(x));
-    const double h0 = f64_of(0.5f * r0);  // 1/(2√x), single precision
-    double c = x * f64_of(r0);
-    c = fma(h0, fma(-c, c, x), c);     // relative error ≈ 2^-42
-    return fma(h0, fma(-c, c, x), c);  // ≈ 2^-63 before the last rounding
-#else
-    return sqrt(x);
-#endif
-}
-
-__device__ __forceinline__ double vrcp(double y) {
-#if DGSWE_FAST
-    const int64_t b = fp::bits(y);
-    if (b < 0x3820000000000000ll || b >= 0x47C0000000000000ll) return 1.0 / y;  // 2^-125, 2^125
-    double r = f64_of(__frcp_rn(f32_seed(y)));
-    double e = fma(-y, r, 1.0);
-    r = fma(r, e, r);  // Newton: relative error ≈ 2^-44
-    e = fma(-y, r, 1.0);
-    return fma(r, e, r);
-#else
-    return 1.0 / y;
-#endif
-}
-
-__device__ __forceinline__ double vdiv(double x, double y) {
-#if DGSWE_FAST
-    return x * vrcp(y);
-#else
-    return x / y;
-#endif
-}
-
-struct Q {
-    double h, hu, hv, u, v, b;
-};
-struct Sd {
-    double h, u, v, b;
-};
-struct F3 {
-    double h, hu, hv;
-};
-
-__device__ __forceinline__ Sd side(const Q& q) { return {q.h, q.u, q.v, q.b}; }
-
-// node velocity (src/flux/swe_2d_entropy.rs:106-116)
-__device__ __forceinline__ void node_velocity(double h, double hu, double hv, double h_min,
-                                              double& u, double& v) {
-    const bool wet = fp::gt(h, h_min);
-    const double inv_h = vrcp(h);
-    u = wet ? hu * inv_h : 0.0;
-    v = wet ? hv * inv_h : 0.0;
-}
-
-// Two-point flux F#(q_l, q_r)·m (src/flux/swe_2d_entropy.rs:140-160)
-__device__ __forceinline__ F3 wflux(const Q& l, const Q& r, double m0, double m1, double g) {
-    const double mass = 0.5 * ((l.hu + r.hu) * m0 + (l.hv + r.hv) * m1);
-    const double pressure = (0.5 * g) * (l.h * r.h);
-    const double u_avg = 0.5 * (l.u + r.u), v_avg = 0.5 * (l.v + r.v);
-    return {mass, mass * u_avg + pressure * m0, mass * v_avg + pressure * m1};
-}
-
-// HLL in face-aligned components with Einfeldt speeds
-// (src/flux/swe_2d.rs:277-375); l/r: depth, normal and tangential momentum,
-// and the velocities (zero on a dry side)
-__device__ __forceinline__ F3 hll_aligned(double h_l, double hun_l, double hut_l, double un_l,
-                                          double ut_l, double h_r, double hun_r, double hut_r,
-                                          double un_r, double ut_r, double g, double sqrt_g,
-                                          double half_g, double h_min) {
-    const bool dry = fp::le(h_l, h_min) && fp::le(h_r, h_min);
-    const double sh_l = vsqrt(fp::max0(h_l)), sh_r = vsqrt(fp::max0(h_r));
-    const double c_l = sqrt_g * sh_l, c_r = sqrt_g * sh_r;
-    const double sh_sum = sh_l + sh_r;
-    const bool roe = fp::gt(sh_sum, 1e-10);
-    const double h_roe = 0.5 * (h_l + h_r);
-    const double un_roe = roe ? vdiv(sh_l * un_l + sh_r * un_r, sh_sum) : 0.0;
-    const double c_roe = roe ? vsqrt(g * h_roe) : 0.0;
-    const double s_l = fp::gt(h_l, h_min) ? lmin(un_l - c_l, un_roe - c_roe) : un_r - 2.0 * c_r;
-    const double s_r = fp::gt(h_r, h_min) ? lmax(un_r + c_r, un_roe + c_roe) : un_l + 2.0 * c_l;
-    const double fl_h = h_l * un_l, fl_hu = h_l * un_l * un_l + half_g * h_l * h_l,
-                 fl_hv = h_l * un_l * ut_l;
-    const double fr_h = h_r * un_r, fr_hu = h_r * un_r * un_r + half_g * h_r * h_r,
-                 fr_hv = h_r * un_r * ut_r;
-    const double inv_ds = vrcp(s_r - s_l);
-    const double s_lr = s_l * s_r;
-    const double st_h = inv_ds * (s_r * fl_h - s_l * fr_h + s_lr * (h_r - h_l));
-    const double st_hu = inv_ds * (s_r * fl_hu - s_l * fr_hu + s_lr * (hun_r - hun_l));
-    const double st_hv = inv_ds * (s_r * fl_hv - s_l * fr_hv + s_lr * (hut_r - hut_l));
-    const bool from_l = fp::ge0(s_l), from_r = fp::le0(s_r);
-    F3 f;
-    f.h = dry ? 0.0 : (from_l ? fl_h : (from_r ? fr_h : st_h));
-    f.hu = dry ? 0.0 : (from_l ? fl_hu : (from_r ? fr_hu : st_hu));
-    f.hv = dry ? 0.0 : (from_l ? fl_hv : (from_r ? fr_hv : st_hv));
-    return f;
-}
-
-// wall_ram_pressure (src/solver/rhs/swe_2d_split_form.rs:147-156)
-__device__ __forceinline__ double wall_ram(double h, double un, double sill, double g) {
-    un = fp::max0(un);
-    const double head = un * un * (0.5 / g);
-    const double ram = (1.0 - head / sill) * h * un * (2.0 * un + sqrt(g * h));
-    return fp::gt(sill, head) ? ram : 0.0;
-}
-
-// hydrostatic_hll (src/solver/rhs/swe_2d_split_form.rs:336-402) along m with
-// |m| = norm and m/|m| = (nx, ny): the flux seen from side a and from side b
-__device__ __forceinline__ void hydro_hll(const Sd& qa, const Sd& qb, double m0, double m1,
-                                          double norm, double nx, double ny, double g,
-                                          double sqrt_g, double half_g, double h_min, F3& fa,
-                                          F3& fb) {
-    const double b_face = lmax(qa.b, qb.b);
-    const double hs_a = fp::max0(qa.h + qa.b - b_face);
-    const double hs_b = fp::max0(qb.h + qb.b - b_face);
-    const bool wet_a = fp::gt(qa.h, h_min), wet_b = fp::gt(qb.h, h_min);
-    const double ua = wet_a ? qa.u : 0.0, va = wet_a ? qa.v : 0.0;
-    const double ub = wet_b ? qb.u : 0.0, vb = wet_b ? qb.v : 0.0;
-    const double un_a = ua * nx + va * ny, ut_a = -ua * ny + va * nx;
-    const double un_b = ub * nx + vb * ny, ut_b = -ub * ny + vb * nx;
-    const bool sw_a = fp::gt(hs_a, h_min), sw_b = fp::gt(hs_b, h_min);
-    const F3 r = hll_aligned(hs_a, hs_a * un_a, hs_a * ut_a, sw_a ? un_a : 0.0, sw_a ? ut_a : 0.0,
-                             hs_b, hs_b * un_b, hs_b * ut_b, sw_b ? un_b : 0.0, sw_b ? ut_b : 0.0,
-                             g, sqrt_g, half_g, h_min);
-    // rotate back (src/flux/swe_2d.rs:38-44), times |m|
-    const double f_h = norm * r.h;
-    const double f_hu = norm * (r.hu * nx - r.hv * ny);
-    const double f_hv = norm * (r.hu * ny + r.hv * nx);
-    const bool hll_dry = fp::le(hs_a, h_min) && fp::le(hs_b, h_min);
-    const double hsa = hll_dry ? 0.0 : hs_a, hsb = hll_dry ? 0.0 : hs_b;
-    double wall_a = 0.0, wall_b = 0.0;
-    if (hll_dry) {
-        if (wet_a) wall_a = wall_ram(qa.h, qa.u * nx + qa.v * ny, b_face - (qa.h + qa.b), g);
-        if (wet_b)
-            wall_b = wall_ram(qb.h, -1.0 * (qb.u * nx + qb.v * ny), b_face - (qb.h + qb.b), g);
-    }
-    const double dp_a = half_g * (qa.h * qa.h - hsa * hsa) + wall_a;
-    const double dp_b = half_g * (qb.h * qb.h - hsb * hsb) + wall_b;
-    fa = {f_h, f_hu + dp_a * m0, f_hv + dp_a * m1};
-    fb = {f_h, f_hu + dp_b * m0, f_hv + dp_b * m1};
-}
-
-// ---------------------------------------------------------------------------
-// face kernel
-
-// HarmonicTide::elevation (src/boundary/harmonic_tide.rs:124-136)
-__device__ double tide_elevation(const Condition& c, double t) {
-    double tide = 0.0;
-    for (int i = 0; i < c.n_constituents; ++i) {
-        const Constituent& k = c.c[i];
-        const double f = k.f + k.f_rate * t;
-        const double u_deg = k.u_deg + k.u_rate_deg * t;
-        const double offset = (k.v0_deg + u_deg) * (M_PI / 180.0);
-        tide += f * k.amplitude * cos(k.omega * t + k.phase + offset);
-    }
-    double ramp = 1.0;
-    if (fp::gt0(c.ramp)) {
-        double tau = t / c.ramp;
-        tau = fp::lt0(tau) ? 0.0 : (fp::gt(tau, 1.0) ? 1.0 : tau);
-        ramp = tau * tau * (3.0 - 2.0 * tau);
-    }
-    return c.mean + ramp * tide;
-}
 
 __device__ __forceinline__ Q load_q(const DevBuf& in, const DevTables& T, const Physics& P,
                                     int64_t g) {
@@ -330,27 +132,10 @@ __global__ void __launch_bounds__(256) face_kernel(DevTables T, Physics P, DevBu
     const double nx = geo[0], ny = geo[1];
     const Condition& c = T.cond ? T.cond[T.bface_cond[bfi]] : P.cond[T.bface_cond[bfi]];
     F3 fs;
-    // the interior velocity of BCContext2D (velocity_simple)
-    double u = 0.0, v = 0.0;
-    if (fp::gt(qi.h, h_min)) {
-        const double inv = 1.0 / qi.h;
-        u = qi.hu * inv;
-        v = qi.hv * inv;
-    }
+    double u, v;
+    interior_velocity(qi, h_min, u, v);
     if (c.kind == kBcWall) {
-        // Reflective2D mirror ghost (src/boundary/boundary_2d.rs:271-283)
-        double gh = qi.h, ghu = 0.0, ghv = 0.0;
-        if (!fp::le(qi.h, c.wall_h_min)) {
-            const double un = u * nx + v * ny;
-            ghu = qi.h * (u - 2.0 * un * nx);
-            ghv = qi.h * (v - 2.0 * un * ny);
-        }
-        Q qe;
-        qe.h = gh;
-        qe.hu = ghu;
-        qe.hv = ghv;
-        qe.b = qi.b;
-        node_velocity(gh, ghu, ghv, h_min, qe.u, qe.v);
+        const Q qe = wall_ghost(qi, u, v, nx, ny, c.wall_h_min, h_min);
         F3 fdummy;
         if (P.formulation == kWetDry)
             hydro_hll(side(qi), side(qe), nx, ny, geo[2], geo[3], geo[4], g, sqrt_g, half_g, h_min,
@@ -358,189 +143,16 @@ __global__ void __launch_bounds__(256) face_kernel(DevTables T, Physics P, DevBu
         else
             entropy_surface(qi, qe, nx, ny, P, fs, fdummy);
     } else {
-        // CharacteristicOBC with a uniform harmonic tide
-        // (src/boundary/characteristic.rs:411-437, 481-520)
+        // CharacteristicOBC with a uniform harmonic tide, flux F(q_b)·n
         const int member = T.elem_member ? T.elem_member[k] : 0;
         const double eta = tide_elevation(c, ctl[member].stage[slot].time);
-        const double bathy = qi.b;
-        const double h_e = fmax(eta - bathy, 0.0);
-        double un_e = 0.0;
-        if (c.elevation_only == kIncomingWave)
-            un_e = 2.0 * (sqrt(g * fmax(-bathy, 0.0)) - sqrt(g * h_e));
-        const double ut_e = -u * ny + v * nx;
-        const double h_i = fmax(qi.h, 0.0);
-        double un_i = 0.0, ut_i = 0.0;
-        if (h_i > h_min) {
-            const double ui = qi.hu / h_i, vi = qi.hv / h_i;
-            un_i = ui * nx + vi * ny;
-            ut_i = -ui * ny + vi * nx;
-        }
-        const double c_i = sqrt(g * h_i), c_e = sqrt(g * h_e);
-        const double w_out = un_i + 2.0 * c_i, w_in = un_e - 2.0 * c_e;
-        const bool wi = h_i > h_min, we = h_e > h_min;
-        double h_b, un_b;
-        if (!wi && !we) {
-            h_b = 0.0;
-            un_b = 0.0;
-        } else if (wi && un_i >= c_i) {
-            h_b = h_i;
-            un_b = un_i;
-        } else if (we && un_e <= -c_e) {
-            h_b = h_e;
-            un_b = un_e;
-        } else if (wi && !we) {
-            const double cc = fmax(w_out / 3.0, 0.0);
-            h_b = cc * cc / g;
-            un_b = cc;
-        } else if (!wi && we) {
-            const double cc = fmax(-w_in / 3.0, 0.0);
-            h_b = cc * cc / g;
-            un_b = -cc;
-        } else {
-            const double cc = fmax(0.25 * (w_out - w_in), 0.0);
-            h_b = cc * cc / g;
-            un_b = 0.5 * (w_out + w_in);
-        }
-        const double ut_b = un_b > 0.0 ? ut_i : ut_e;
-        const double ub = un_b * nx - ut_b * ny, vb = un_b * ny + ut_b * nx;
-        Q qb;
-        qb.h = h_b;
-        qb.hu = h_b * ub;
-        qb.hv = h_b * vb;
-        qb.b = qi.b;
-        node_velocity(qb.h, qb.hu, qb.hv, h_min, qb.u, qb.v);
-        fs = wflux(qb, qb, nx, ny, g);  // F(q_b)·n
+        const Q qb = characteristic_state(qi, u, v, eta, nx, ny, c.elevation_only, g, h_min);
+        fs = wflux(qb, qb, nx, ny, g);
     }
     const int64_t sl = B * N1 + fi;
     fb_h[sl] = fs.h;
     fb_hu[sl] = fs.hu;
     fb_hv[sl] = fs.hv;
-}
-
-// ---------------------------------------------------------------------------
-// damping and the wet/dry correction
-
-// The reference's cube root (src/source/swe_2d/friction.rs:39-70)
-__device__ __forceinline__ double ref_cbrt(double x) {
-    if (!(x >= 2.2250738585072014e-308 && x <= 1.7976931348623157e308)) return cbrt(x);
-    unsigned long long bits = (unsigned long long)__double_as_longlong(x);
-    double y = __longlong_as_double((long long)(bits / 3ull + 0x2A9F7893782DA1CEull));
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        const double y3 = y * y * y;
-        y += y * ((x - y3) / (2.0 * y3 + x));
-    }
-    return y;
-}
-
-// Manning's rate g n² |u| / h^{4/3} at a floored depth h
-__device__ __forceinline__ double manning_rate(double g_n2, double h, double speed) {
-#if DGSWE_FAST
-    // h^{-1/3} from a single-precision seed (relative error δ ≈ 2^-22) and
-    // one step of third order, z ← z(1 + e/3 + 2e²/9) with e = 1 − h z³
-    // (error ≈ 5δ³ ≈ 2^-61); then the rate is g n² |u| z⁴, no division
-    const int64_t b = fp::bits(h);
-    double z = (b >= 0x3820000000000000ll && b < 0x47C0000000000000ll)  // 2^-125, 2^125
-                   ? f64_of(rcbrtf(f32_seed(h)))
-                   : 1.0 / cbrt(h);
-    const double e = fma(-h, z * z * z, 1.0);
-    z = fma(z * e, fma(e, 2.0 / 9.0, 1.0 / 3.0), z);
-    const double z2 = z * z;
-    return g_n2 * speed * (z2 * z2);
-#else
-    return g_n2 * speed / (ref_cbrt(h) * h);
-#endif
-}
-
-struct DampIn {
-    double h, hu, hv, u, v;  // the RHS input (u, v: node velocity)
-};
-
-// damp_node (src/solver/algorithms/wetting_drying.rs:324-357)
-__device__ __forceinline__ void damp(const Physics& P, double g_n2, double h, double& hu,
-                                     double& hv, const DampIn& from, double dt) {
-    if (fp::le0(h)) {
-        hu = 0.0;
-        hv = 0.0;
-        return;
-    }
-    double rate = 0.0;
-    if (P.friction) {
-        double u, v;
-        if (P.has_wet_dry) {
-            // desingularized_velocity (wetting_drying.rs:115-130): the node
-            // velocity where h ≥ h_dry (> h_min)
-            if (fp::le0(from.h)) {
-                u = v = 0.0;
-            } else if (fp::ge(from.h, P.h_dry)) {
-                if (fp::gt(P.h_dry, P.h_min)) {
-                    u = from.u;
-                    v = from.v;
-                } else {
-                    const double inv = 1.0 / from.h;
-                    u = from.hu * inv;
-                    v = from.hv * inv;
-                }
-            } else {
-                const double r = from.h / P.h_dry;
-                const double factor =
-                    1.4142135623730951 * r / (P.h_dry * sqrt(1.0 + r * r * r * r));
-                u = factor * from.hu;
-                v = factor * from.hv;
-            }
-        } else {
-            // SWEState2D::velocity (src/solver/state/swe_2d.rs:54-61)
-            const double h_reg = lmax(from.h, P.h_min);
-            const double inv_d = 1.0 / (from.h * from.h + h_reg * h_reg);
-            const double factor = 2.0 * from.h * inv_d;
-            u = from.hu * factor;
-            v = from.hv * factor;
-        }
-        const double speed = vsqrt(u * u + v * v);
-        if (fp::gt0(speed)) rate += manning_rate(g_n2, lmax(h, P.manning_h_min), speed);
-    }
-    if (P.has_wet_dry && fp::lt(h, P.h_dry)) {
-        // thin_layer_rate (wetting_drying.rs:135-146); h > 0 here
-        const double excess = P.h_dry / h - 1.0;
-        rate += excess * excess / P.relaxation_time;
-    }
-    const double factor = vrcp(1.0 + dt * rate);
-    hu *= factor;
-    hv *= factor;
-}
-
-// correct_node (src/solver/algorithms/wetting_drying.rs:148-165)
-__device__ __forceinline__ void correct_node(const Physics& P, double h, double& hu, double& hv) {
-    if (fp::le0(h)) {
-        hu = 0.0;
-        hv = 0.0;
-        return;
-    }
-    if (fp::lt(h, P.h_dry)) {
-        const double r = h / P.h_dry;
-        const double factor = 1.4142135623730951 * r / (P.h_dry * sqrt(1.0 + r * r * r * r));
-        hu = h * (factor * hu);
-        hv = h * (factor * hv);
-    }
-    // |hu| > h·u_max; the square root only near the cap. First a test on
-    // the exponent fields alone (integer pipes): with E the biased exponent,
-    // |m| < √2·2^(max(E_hu, E_hv) − 1022) and h·u_max ≥ 2^(E_h + E_u − 2046)
-    // for normal h and u_max, so max(E_hu, E_hv) + 1025 ≤ E_h + E_u means
-    // |m|² < 0.99·cap² and the exact test below would be false.
-    const int e_h = (int)((fp::bits(h) >> 52) & 0x7FF);
-    const int e_u = (int)((fp::bits(P.max_velocity) >> 52) & 0x7FF);
-    const int e_hu = (int)((fp::bits(hu) >> 52) & 0x7FF), e_hv = (int)((fp::bits(hv) >> 52) & 0x7FF);
-    if (e_h >= 1 && e_u >= 1 && (e_hu > e_hv ? e_hu : e_hv) + 1025 <= e_h + e_u) return;
-    const double m2 = hu * hu + hv * hv;
-    const double cap = P.max_velocity * h;
-    if (fp::gt(m2, 0.99 * (cap * cap))) {
-        const double momentum = sqrt(m2);
-        if (fp::gt(momentum, cap)) {
-            const double scale = cap / momentum;
-            hu *= scale;
-            hv *= scale;
-        }
-    }
 }
 
 // ---------------------------------------------------------------------------
@@ -610,45 +222,6 @@ __device__ __forceinline__ void line_metric(const DevTables& T, int64_t k, int d
         m0[p] = T.contra[g * 4 + 2 * dir];
         m1[p] = T.contra[g * 4 + 2 * dir + 1];
     }
-}
-
-// limited_slope with SlopeDistances (src/solver/rhs/swe_2d_split_form.rs:168-203)
-__device__ __forceinline__ double limited_slope(double q0, double q1, double q2, double ic,
-                                                double im, double ip) {
-    const double dm = q1 - q0, dp = q2 - q1;
-    const bool extremum = fp::le0(dm * dp);
-    const double central = (q2 - q0) * ic;
-    const double bound = fp::min_nn(fabs(dm * im), fabs(dp * ip));
-    const double sign = fp::lt0(central) ? -1.0 : 1.0;
-    return extremum ? 0.0 : sign * fp::min_nn(fabs(central), bound);
-}
-
-// reconstruct_subcell (src/solver/rhs/swe_2d_split_form.rs:279-317)
-__device__ __forceinline__ void reconstruct(const Sd& m, const Sd& c, const Sd& p, double x0,
-                                            double x1, double x2, double xl, double xr,
-                                            double h_dry, Sd& left, Sd& right) {
-    const double e0 = m.h + m.b, e1 = c.h + c.b, e2 = p.h + p.b;
-    double ws = -INFINITY;
-    ws = (fp::ge(m.h, h_dry) && fp::gt(e0, ws)) ? e0 : ws;
-    ws = (fp::ge(c.h, h_dry) && fp::gt(e1, ws)) ? e1 : ws;
-    ws = (fp::ge(p.h, h_dry) && fp::gt(e2, ws)) ? e2 : ws;
-    const bool flooding = (fp::lt(m.h, h_dry) && fp::lt(e0, ws)) ||
-                          (fp::lt(c.h, h_dry) && fp::lt(e1, ws)) ||
-                          (fp::lt(p.h, h_dry) && fp::lt(e2, ws));
-    const double fm = x1 - xl, fpd = xr - x1;
-    const double ic = vrcp(x2 - x0);
-    const double im = vrcp(fp::gt0(fm) ? fm : 0.5 * (x1 - x0));
-    const double ip = vrcp(fp::gt0(fpd) ? fpd : 0.5 * (x2 - x1));
-    const double s_h = limited_slope(m.h, c.h, p.h, ic, im, ip);
-    const double s_eta = flooding ? 0.0 : limited_slope(e0, e1, e2, ic, im, ip);
-    const double s_u = limited_slope(m.u, c.u, p.u, ic, im, ip);
-    const double s_v = limited_slope(m.v, c.v, p.v, ic, im, ip);
-    double d = xl - x1;
-    double hh = fp::max0(c.h + s_h * d);
-    left = {hh, c.u + s_u * d, c.v + s_v * d, e1 + s_eta * d - hh};
-    d = xr - x1;
-    hh = fp::max0(c.h + s_h * d);
-    right = {hh, c.u + s_u * d, c.v + s_v * d, e1 + s_eta * d - hh};
 }
 
 template <int N1>
@@ -1146,17 +719,6 @@ __global__ void velocity_kernel(DevBuf b, int64_t n, double h_min) {
 
 // ---------------------------------------------------------------------------
 // the time step (src/solver/rhs/swe_2d.rs:2072-2115, 1346-1367, 2165-2258)
-
-// node_reference_rate (swe_2d.rs:1346-1357) with the mean's ¼ folded into
-// the metric table m (¼∇r, ¼∇s, ¼|∇r|, ¼|∇s|): a power-of-two scaling, so
-// lr + ls here has exactly the bits of ¼(lr + ls) from unscaled metrics
-__device__ __forceinline__ double node_rate(double h, double u, double v, const double* m,
-                                            double g) {
-    const double c = vsqrt(g * fp::max0(h));
-    const double lr = fabs(u * m[0] + v * m[1]) + c * m[4];
-    const double ls = fabs(u * m[2] + v * m[3]) + c * m[5];
-    return lr + ls;
-}
 
 // The dt pass stages each node's rate, depth and mass weight per element,
 // then one lane per element takes the maximum and the positivity sums in

@@ -100,3 +100,25 @@ def test_integer_pipe_compares_match_ieee(tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True)
     assert out.returncode == 0, out.stdout + out.stderr
     assert out.stdout.startswith("ok ")
+
+
+def test_reverse_point_functions_match_finite_differences(tmp_path):
+    """Every reverse function of the adjoint (adjoint_point.cuh) against
+    central differences of its forward function (point.cuh), host build."""
+    import shutil
+    import subprocess
+    from pathlib import Path
+
+    gxx = shutil.which("g++")
+    if gxx is None:
+        import pytest
+
+        pytest.skip("g++ not available")
+    here = Path(__file__).resolve().parent
+    exe = tmp_path / "adjoint_point_check"
+    subprocess.run([gxx, "-O2", "-std=c++17", "-ffp-contract=off",
+                    "-I", str(here.parent / "dgcom_gb300" / "csrc"),
+                    str(here / "adjoint_point_check.cpp"), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert out.stdout.strip().endswith("all ok")
