@@ -173,6 +173,35 @@ class FormInfo(C.Structure):
     ]
 
 
+MAX_CONSTITUENTS = 8  # DGSWE_MAX_CONSTITUENTS
+
+
+class AdjointConfig(C.Structure):
+    _fields_ = [
+        ("scheme", C.c_int32),
+        ("cfl", C.c_double),
+        ("t_start", C.c_double),
+        ("n_steps", C.c_int64),
+        ("n_stations", C.c_int32),
+        ("stations", _dp),
+        ("memory_budget", C.c_double),
+    ]
+
+
+class AdjointStats(C.Structure):
+    _fields_ = [
+        ("J", C.c_double),
+        ("forward_ms", C.c_double),
+        ("reverse_ms", C.c_double),
+        ("forward_wall_s", C.c_double),
+        ("reverse_wall_s", C.c_double),
+        ("stride", C.c_int64),
+        ("recomputed_steps", C.c_int64),
+        ("stored_states", C.c_int64),
+        ("stored_bytes", C.c_double),
+    ]
+
+
 CALLBACK = C.CFUNCTYPE(None, C.c_void_p, C.c_double, _dp, _dp, _dp, C.c_int64)
 
 # entry points shared by every library with this ABI: name → (restype, argtypes)
@@ -210,6 +239,16 @@ CUDA_ONLY = {
     "ensemble_download": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, C.c_int64]),
     "ensemble_run": (C.c_int, [C.c_void_p, C.POINTER(RunConfig), C.c_int64, C.POINTER(Report),
                                C.POINTER(Profile)]),
+    # the discrete adjoint
+    "adjoint_create": (C.c_int, [C.POINTER(Form), C.c_int, C.POINTER(AdjointConfig),
+                                 C.POINTER(C.c_void_p)]),
+    "adjoint_destroy": (None, [C.c_void_p]),
+    "adjoint_last_error": (C.c_char_p, [C.c_void_p]),
+    "adjoint_n_values": (C.c_int64, [C.c_void_p]),
+    "adjoint_stations": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), _dp]),
+    "adjoint_forward": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "adjoint_reverse": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "adjoint_get_stats": (C.c_int, [C.c_void_p, C.POINTER(AdjointStats)]),
 }
 
 

@@ -17,58 +17,15 @@
 
 #include "../../include/dgswe.h"
 #include "device.hpp"
+#include "handle.hpp"
 #include "host_common.hpp"
 #include "kernel_set.hpp"
 #include "setup.hpp"
 
 using namespace dgswe;
 
-namespace {
-
-constexpr int kRhsBuffer = DGSWE_N_BUFFERS;  // scratch buffer of dgswe_compute_rhs
-
-struct DeviceBuffer {
-    double* base = nullptr;  // one allocation of 5 fields
-    DevBuf view{};
-};
-
-}  // namespace
-
-struct dgswe_handle {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    std::string error;
-    dgswe_form form{};
-    std::vector<dgswe_tide_constituent> constituents;
-    Operators* ops = nullptr;
-    int n1 = 0, nn = 0;
-    int64_t K = 0, n_values = 0;
-    const KernelSet* ks = nullptr;
-    DevTables T{};
-    Physics P{};
-    StageExtra X{};
-    std::vector<void*> allocations;
-    DeviceBuffer buf[DGSWE_N_BUFFERS + 1];
-    double *fb_h = nullptr, *fb_hu = nullptr, *fb_hv = nullptr;
-    double* dt_el = nullptr;
-    StepCtl* ctl = nullptr;    // device
-    StepCtl* h_ctl = nullptr;  // pinned host mirror
-    std::string device_name;
-    // graph of one device-driven step
-    cudaGraphExec_t step_graph = nullptr;
-    int graph_scheme = -1;
-    double graph_cfl = -1.0;
-
-    ~dgswe_handle() {
-        if (step_graph) cudaGraphExecDestroy(step_graph);
-        for (void* p : allocations) cudaFree(p);
-        if (h_ctl) cudaFreeHost(h_ctl);
-        if (stream) cudaStreamDestroy(stream);
-        delete ops;
-    }
-};
-
-namespace {
+namespace dgswe {
+namespace host {
 
 int fail(dgswe_handle* h, int status, const char* fmt, ...) {
     char msg[512];
@@ -80,12 +37,6 @@ int fail(dgswe_handle* h, int status, const char* fmt, ...) {
     return status;
 }
 
-#define CK(call)                                                                             \
-    do {                                                                                     \
-        cudaError_t err_ = (call);                                                           \
-        if (err_ != cudaSuccess)                                                             \
-            return fail(h, DGSWE_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(err_)); \
-    } while (0)
 
 template <class T>
 int upload_vec(dgswe_handle* h, const std::vector<T>& v, const T** out) {
@@ -204,7 +155,10 @@ int run_device_step_graph(dgswe_handle* h, int scheme, double cfl) {
     return DGSWE_OK;
 }
 
-}  // namespace
+}  // namespace host
+}  // namespace dgswe
+
+using namespace dgswe::host;
 
 extern "C" {
 

@@ -111,4 +111,18 @@ struct StepCtl {
     double st_start[kMaxStages], st_input[kMaxStages], st_beta[kMaxStages], st_c[kMaxStages];
 };
 
+// The adjoint of one stage (adjoint_kernels.cuh): λ arrays per node, or per
+// face slot for the face fluxes
+struct AdjStage {
+    const double *lo_h, *lo_hu, *lo_hv;          // of the stage output (read)
+    double *li_h, *li_hu, *li_hv, *li_u, *li_v;  // of the stage input, own element (written)
+    double *lb_h, *lb_hu, *lb_hv;                // of the stage's base state (added)
+    double *lf_h, *lf_hu, *lf_hv;                // of the face fluxes, per face slot (written)
+    double *lx_h, *lx_hu, *lx_hv, *lx_u, *lx_v;  // of the stage input from faces and
+                                                 // neighbouring elements (atomic)
+    double* lbed;                                // of the bed elevation (atomic)
+    double* lgn2;                                // of g·n² per node (added)
+    double* ltide;                               // [condition][constituent][amplitude, phase]
+};
+
 }  // namespace dgswe

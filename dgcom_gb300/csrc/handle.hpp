@@ -1,0 +1,93 @@
+// The internals of a dgswe handle, shared by the C ABI of one mesh (api.cu)
+// and the adjoint driver (adjoint.cu), which works on a handle's tables,
+// buffers and step control.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/dgswe.h"
+#include "device.hpp"
+#include "kernel_set.hpp"
+#include "setup.hpp"
+
+namespace dgswe {
+namespace host {
+
+constexpr int kRhsBuffer = DGSWE_N_BUFFERS;  // scratch buffer of dgswe_compute_rhs
+
+struct DeviceBuffer {
+    double* base = nullptr;  // one allocation of 5 fields
+    DevBuf view{};
+};
+
+}  // namespace host
+}  // namespace dgswe
+
+struct dgswe_handle {
+    using Operators = dgswe::Operators;
+    using KernelSet = dgswe::KernelSet;
+    using DevTables = dgswe::DevTables;
+    using Physics = dgswe::Physics;
+    using StageExtra = dgswe::StageExtra;
+    using StepCtl = dgswe::StepCtl;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string error;
+    dgswe_form form{};
+    std::vector<dgswe_tide_constituent> constituents;
+    Operators* ops = nullptr;
+    int n1 = 0, nn = 0;
+    int64_t K = 0, n_values = 0;
+    const KernelSet* ks = nullptr;
+    DevTables T{};
+    Physics P{};
+    StageExtra X{};
+    std::vector<void*> allocations;
+    dgswe::host::DeviceBuffer buf[DGSWE_N_BUFFERS + 1];
+    double *fb_h = nullptr, *fb_hu = nullptr, *fb_hv = nullptr;
+    double* dt_el = nullptr;
+    StepCtl* ctl = nullptr;    // device
+    StepCtl* h_ctl = nullptr;  // pinned host mirror
+    std::string device_name;
+    // graph of one device-driven step
+    cudaGraphExec_t step_graph = nullptr;
+    int graph_scheme = -1;
+    double graph_cfl = -1.0;
+
+    ~dgswe_handle() {
+        if (step_graph) cudaGraphExecDestroy(step_graph);
+        for (void* p : allocations) cudaFree(p);
+        if (h_ctl) cudaFreeHost(h_ctl);
+        if (stream) cudaStreamDestroy(stream);
+        delete ops;
+    }
+};
+
+
+namespace dgswe {
+namespace host {
+
+// Records `status` and the message on the handle; returns the status
+int fail(dgswe_handle* h, int status, const char* fmt, ...);
+// Allocates buffer `id` (5 fields of n_values doubles) on first use
+int ensure_buffer(dgswe_handle* h, int id);
+int sync(dgswe_handle* h);
+// One stage: the face pass, then the element stage
+void launch_stage(dgswe_handle* h, int in, int base, int out, int acc, int slot, int mode,
+                  int check_finite, const int* active);
+const int* always(dgswe_handle* h);
+// The device clock of a run from run->t_start towards `target`
+int begin_run(dgswe_handle* h, const dgswe_run_config* run, double target);
+
+}  // namespace host
+}  // namespace dgswe
+
+#define CK(call)                                                                             \
+    do {                                                                                     \
+        cudaError_t err_ = (call);                                                           \
+        if (err_ != cudaSuccess)                                                             \
+            return fail(h, DGSWE_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(err_)); \
+    } while (0)

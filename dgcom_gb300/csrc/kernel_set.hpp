@@ -21,6 +21,25 @@ struct KernelSet {
     void (*dt)(int n1, const DevTables&, const Physics&, const DevBuf& q, const DtParams&,
                double* dt_el, StepCtl* ctl, const int* active, cudaStream_t);
     void (*velocity)(const DevBuf&, int64_t n, double h_min, cudaStream_t);
+    // a kPost stage that also keeps the combination and the damped momentum
+    // (the adjoint's recomputation)
+    void (*stage_keep)(int n1, const DevTables&, const Physics&, const StageExtra&,
+                       const DevBuf& in, const DevBuf& base, const DevBuf& out, const double* fh,
+                       const double* fhu, const double* fhv, StepCtl* ctl, int slot,
+                       int check_finite, const DevBuf& keep, cudaStream_t);
+    // the adjoint of one stage (adjoint_kernels.cuh)
+    void (*stage_adjoint)(int n1, const DevTables&, const Physics&, const StageExtra&,
+                          const DevBuf& in, const DevBuf& keep, const AdjStage&,
+                          const StepCtl* ctl, int slot, cudaStream_t);
+    void (*face_adjoint)(int n1, const DevTables&, const Physics&, const DevBuf& in,
+                         const AdjStage&, const StepCtl* ctl, int slot, cudaStream_t);
+    void (*adjoint_combine)(const DevBuf& in, const AdjStage&, double* out_h, double* out_hu,
+                            double* out_hv, int64_t n, double h_min, cudaStream_t);
+    void (*station_eval)(const double* h, const double* bed, const int64_t* node0,
+                         const double* w, int n_stations, int nn, double* eta, cudaStream_t);
+    void (*station_seed)(const double* eta, const double* obs, const int64_t* node0,
+                         const double* w, int n_stations, int nn, double* lh, double* lbed,
+                         cudaStream_t);
     // the run's clock, one thread per StepCtl of ctl[0..n)
     void (*step_begin)(StepCtl*, int n, cudaStream_t);
     void (*step_dt)(StepCtl*, int n, cudaStream_t);

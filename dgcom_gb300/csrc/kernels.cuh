@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS, Cfg<N1>::MIN_BLOCKS)
     stage_kernel(DevTables T, Physics P, StageExtra X, DevBuf in, DevBuf base, DevBuf out,
                  DevBuf acc, const double* __restrict__ fb_h, const double* __restrict__ fb_hu,
                  const double* __restrict__ fb_hv, StepCtl* ctl, int slot, int mode,
-                 int check_finite, const int* active) {
+                 int check_finite, const int* active, DevBuf keep) {
     using C = Cfg<N1>;
     constexpr int NN = C::NN, NP = C::NP, NA = C::NA, EPB = C::EPB;
     __shared__ double s_q[EPB][6][NN];
@@ -535,9 +535,19 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS, Cfg<N1>::MIN_BLOCKS)
             vhu += sa.c * Fhu;
             vhv += sa.c * Fhv;
         }
+        // for the adjoint: the combination, then the damped momentum
+        if (keep.h) {
+            keep.h[gi] = vh;
+            keep.hu[gi] = vhu;
+            keep.hv[gi] = vhv;
+        }
         if (P.friction || P.has_wet_dry) {
             const double g_n2 = P.friction == 2 ? T.g_n2[gi] : P.g_n2;
             damp(P, g_n2, vh, vhu, vhv, DampIn{h, hu, hv, u, v}, sa.c);
+        }
+        if (keep.h) {
+            keep.u[gi] = vhu;
+            keep.v[gi] = vhv;
         }
     }
 

@@ -4,6 +4,7 @@
 #define DGSWE_FAST 0
 #define DGSWE_NS exact
 #include "kernels.cuh"
+#include "adjoint_kernels.cuh"
 #include "launch.cuh"
 
 namespace dgswe {

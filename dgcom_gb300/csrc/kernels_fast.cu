@@ -3,6 +3,7 @@
 #define DGSWE_FAST 1
 #define DGSWE_NS fast
 #include "kernels.cuh"
+#include "adjoint_kernels.cuh"
 #include "launch.cuh"
 
 namespace dgswe {

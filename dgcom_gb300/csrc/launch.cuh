@@ -22,11 +22,11 @@ template <int N1>
 static void stage_n(const DevTables& T, const Physics& P, const StageExtra& X, const DevBuf& in,
                     const DevBuf& base, const DevBuf& out, const DevBuf& acc, const double* fh,
                     const double* fhu, const double* fhv, StepCtl* ctl, int slot, int mode,
-                    int check_finite, const int* active, cudaStream_t s) {
+                    int check_finite, const int* active, const DevBuf& keep, cudaStream_t s) {
     using C = Cfg<N1>;
     const unsigned blocks = (unsigned)((T.K + C::EPB - 1) / C::EPB);
     stage_kernel<N1><<<blocks, C::THREADS, 0, s>>>(T, P, X, in, base, out, acc, fh, fhu, fhv, ctl,
-                                                   slot, mode, check_finite, active);
+                                                   slot, mode, check_finite, active, keep);
 }
 
 template <int N1>
@@ -64,7 +64,15 @@ static void stage(int n1, const DevTables& T, const Physics& P, const StageExtra
                   const double* fh, const double* fhu, const double* fhv, StepCtl* ctl, int slot,
                   int mode, int check_finite, const int* active, cudaStream_t s) {
     DGSWE_BY_ORDER(stage_n, T, P, X, in, base, out, acc, fh, fhu, fhv, ctl, slot, mode,
-                   check_finite, active, s);
+                   check_finite, active, DevBuf{}, s);
+}
+
+static void stage_keep(int n1, const DevTables& T, const Physics& P, const StageExtra& X,
+                       const DevBuf& in, const DevBuf& base, const DevBuf& out, const double* fh,
+                       const double* fhu, const double* fhv, StepCtl* ctl, int slot,
+                       int check_finite, const DevBuf& keep, cudaStream_t s) {
+    DGSWE_BY_ORDER(stage_n, T, P, X, in, base, out, base, fh, fhu, fhv, ctl, slot, kPost,
+                   check_finite, &ctl->always, keep, s);
 }
 
 static void finish(int n1, const DevTables& T, const Physics& P, const DevBuf& acc,
@@ -77,7 +85,58 @@ static void dt(int n1, const DevTables& T, const Physics& P, const DevBuf& q, co
     DGSWE_BY_ORDER(dt_n, T, P, q, D, dt_el, ctl, active, s);
 }
 
+template <int N1>
+static void stage_adjoint_n(const DevTables& T, const Physics& P, const StageExtra& X,
+                            const DevBuf& in, const DevBuf& keep, const AdjStage& A,
+                            const StepCtl* ctl, int slot, cudaStream_t s) {
+    using C = AdjCfg<N1>;
+    const unsigned blocks = (unsigned)((T.K + C::EPB - 1) / C::EPB);
+    stage_adjoint_kernel<N1><<<blocks, C::THREADS, 0, s>>>(T, P, X, in, keep, A, ctl, slot);
+}
+
+template <int N1>
+static void face_adjoint_n(const DevTables& T, const Physics& P, const DevBuf& in,
+                           const AdjStage& A, const StepCtl* ctl, int slot, cudaStream_t s) {
+    const int64_t items = (T.n_edges + T.n_bfaces) * N1;
+    if (items == 0) return;
+    face_adjoint_kernel<N1><<<(unsigned)((items + 255) / 256), 256, 0, s>>>(T, P, in, A, ctl, slot);
+}
+
+static void stage_adjoint(int n1, const DevTables& T, const Physics& P, const StageExtra& X,
+                          const DevBuf& in, const DevBuf& keep, const AdjStage& A,
+                          const StepCtl* ctl, int slot, cudaStream_t s) {
+    DGSWE_BY_ORDER(stage_adjoint_n, T, P, X, in, keep, A, ctl, slot, s);
+}
+
+static void face_adjoint(int n1, const DevTables& T, const Physics& P, const DevBuf& in,
+                         const AdjStage& A, const StepCtl* ctl, int slot, cudaStream_t s) {
+    DGSWE_BY_ORDER(face_adjoint_n, T, P, in, A, ctl, slot, s);
+}
+
 #undef DGSWE_BY_ORDER
+
+static void adjoint_combine(const DevBuf& in, const AdjStage& A, double* out_h, double* out_hu,
+                            double* out_hv, int64_t n, double h_min, cudaStream_t s) {
+    if (n == 0) return;
+    adjoint_combine_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(in, A, out_h, out_hu,
+                                                                        out_hv, n, h_min);
+}
+
+static void station_eval(const double* h, const double* bed, const int64_t* node0, const double* w,
+                         int n_stations, int nn, double* eta, cudaStream_t s) {
+    if (n_stations == 0) return;
+    station_eval_kernel<<<(n_stations + 127) / 128, 128, 0, s>>>(h, bed, node0, w, n_stations, nn,
+                                                                  eta);
+}
+
+static void station_seed(const double* eta, const double* obs, const int64_t* node0,
+                         const double* w, int n_stations, int nn, double* lh, double* lbed,
+                         cudaStream_t s) {
+    const int n = n_stations * nn;
+    if (n == 0) return;
+    station_seed_kernel<<<(n + 127) / 128, 128, 0, s>>>(eta, obs, node0, w, n_stations, nn, lh,
+                                                         lbed);
+}
 
 static void velocity(const DevBuf& b, int64_t n, double h_min, cudaStream_t s) {
     if (n == 0) return;
@@ -96,7 +155,10 @@ static void end(StepCtl* c, int n, cudaStream_t s) {
     step_end<<<member_blocks(n), 128, 0, s>>>(c, n);
 }
 
-static const KernelSet kSet = {face, stage, finish, dt, velocity, begin, dt_fit, end};
+static const KernelSet kSet = {face,          stage,         finish,          dt,
+                                velocity,      stage_keep,    stage_adjoint,   face_adjoint,
+                                adjoint_combine, station_eval, station_seed,   begin,
+                                dt_fit,        end};
 
 }  // namespace DGSWE_NS
 }  // namespace dgswe

@@ -394,6 +394,73 @@ int dgswe_ensemble_download(dgswe_ensemble* ensemble, int member, double* h, dou
 int dgswe_ensemble_run(dgswe_ensemble* ensemble, const dgswe_run_config* run, int64_t n_steps,
                        dgswe_report* reports, dgswe_profile* profile);
 
+/* ---------------------------------------------------------------------------
+ * The discrete adjoint of a WetDry SSP-RK3 run.
+ *
+ * No counterpart in the reference, which has no adjoint. The functional is
+ * a station misfit, J = Σ_{n=1..N} Σ_s (η_s(q_n) − η_obs[n][s])², with
+ * η = h + B interpolated at station s inside its element and q_n the state
+ * after step n. The reverse sweep gives ∂J/∂ of the initial state, of the
+ * bed elevation B per node, of Manning's n per node (per element: sum an
+ * element's nodes) and of each boundary condition's tide constituents
+ * (amplitude and phase). These are exact derivatives of the steps the
+ * forward sweep took: its time steps and every branch (wet/dry tests, the
+ * limiter, the HLL wave speeds) stay fixed. Where the bed of coincident
+ * nodes of two elements is equal, the face bed max(B⁻, B⁺) has a kink; the
+ * derivative given is exact for perturbations that keep coincident nodes
+ * equal (a continuous bed). Step-start states are stored in HBM within
+ * memory_budget; when all N do not fit, a two-level checkpointing stores
+ * every s-th one and recomputes each segment once. */
+#define DGSWE_MAX_CONSTITUENTS 8
+
+typedef struct dgswe_adjoint dgswe_adjoint;
+
+typedef struct dgswe_adjoint_config {
+    int32_t scheme;           /* DGSWE_SSP_RK3 */
+    double cfl;               /* the forward's CFL when no time steps are given */
+    double t_start;
+    int64_t n_steps;          /* N */
+    int32_t n_stations;
+    const double* stations;   /* [n_stations][2] x, y; copied */
+    double memory_budget;     /* bytes of HBM for stored states; ≤ 0: free memory − 2 GiB */
+} dgswe_adjoint_config;
+
+typedef struct dgswe_adjoint_stats {
+    double J;                 /* of the last forward sweep */
+    double forward_ms;        /* device time of the forward sweep */
+    double reverse_ms;        /* of the reverse sweep */
+    double forward_wall_s, reverse_wall_s;
+    int64_t stride;           /* 1: every step-start state stored */
+    int64_t recomputed_steps; /* forward steps the reverse sweep recomputed */
+    int64_t stored_states;
+    double stored_bytes;
+} dgswe_adjoint_stats;
+
+/* A form (the WetDry formulation) and the run's shape; the stations are
+ * located in the mesh here (DGSWE_ERR_INVALID if one is outside). *out is
+ * set even on failure; destroy it either way. */
+int dgswe_adjoint_create(const dgswe_form* form, int device, const dgswe_adjoint_config* config,
+                         dgswe_adjoint** out);
+void dgswe_adjoint_destroy(dgswe_adjoint* adjoint);
+const char* dgswe_adjoint_last_error(const dgswe_adjoint* adjoint);
+int64_t dgswe_adjoint_n_values(const dgswe_adjoint* adjoint);
+/* Each station's element and its (order+1)² interpolation weights */
+int dgswe_adjoint_stations(const dgswe_adjoint* adjoint, int64_t* element, double* weights);
+/* The forward sweep from (h0, hu0, hv0): N steps of SSP-RK3 with the given
+ * time steps dts[N], or (dts NULL) with the CFL steps, written to dts_out.
+ * eta_obs [N][n_stations] (NULL: zero) enters J; eta_out gets the
+ * stations' η after each step. Any output may be NULL. */
+int dgswe_adjoint_forward(dgswe_adjoint* adjoint, const double* h0, const double* hu0,
+                          const double* hv0, const double* dts, const double* eta_obs,
+                          double* eta_out, double* dts_out, double* J);
+/* The reverse sweep of the last forward sweep: ∂J/∂h0, ∂J/∂hu0, ∂J/∂hv0,
+ * ∂J/∂B and ∂J/∂n per node (n_values each), and ∂J/∂(amplitude, phase)
+ * as [n_boundaries][DGSWE_MAX_CONSTITUENTS][2]. Any output may be NULL. */
+int dgswe_adjoint_reverse(dgswe_adjoint* adjoint, double* grad_h0, double* grad_hu0,
+                          double* grad_hv0, double* grad_bed, double* grad_manning,
+                          double* grad_tide);
+int dgswe_adjoint_get_stats(const dgswe_adjoint* adjoint, dgswe_adjoint_stats* out);
+
 #ifdef __cplusplus
 }
 #endif
