@@ -24,6 +24,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -41,6 +42,9 @@ import numpy as np  # noqa: E402
 METRIC = "FP64 DG SWE DOF-updates/s"
 UNIT = "DOF-updates/s"
 BYTES_PER_NODE_STAGE = {2: 81.8, 3: 77.5}  # algorithmic bytes (state, bed, mesh), N=2 / N=3
+# stage_kernel<4>'s DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per
+# node-stage in one ncu capture of the 200k-quad coastal box, for scaling by nodes
+STAGE_TRAFFIC_PER_NODE_STAGE = {3: 192.1}
 
 
 def peaks():
@@ -313,9 +317,12 @@ def run_ours(args, rank: int, world: int, local: int):
                        "nodes": nodes, "parallelism": f"replicas x{world}",
                        "l2": "inputs larger than L2 (state and tables ≫ 129 MB)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
-                         "kernel": "stage_kernel<4>",
-                         "note": "FP64-pipe bound: see profiles/ for the FP64 fraction"},
+                         "frac": achieved / peak,
+                         "traffic": (STAGE_TRAFFIC_PER_NODE_STAGE[args.order] * nodes
+                                     if args.order in STAGE_TRAFFIC_PER_NODE_STAGE else None),
+                         "peak_kind": peak_kind, "kernel": f"stage_kernel<{args.order + 1}>",
+                         "note": "bound by the FP64 pipe (86.5 % of it in ncu), not HBM; traffic "
+                                 "from an ncu capture at 200k quads scaled by nodes"},
             "kernel_ms": {"stage": timed.stage_ms / args.steps, "face": timed.face_ms / args.steps,
                           "dt": timed.dt_ms / args.steps, "control": timed.control_ms / args.steps},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 3 * 8 * nodes,
@@ -430,6 +437,130 @@ def run_ensemble(args, rank: int, world: int, local: int):
     dist.close()
 
 
+def run_adjoint(args, rank: int, world: int, local: int):
+    """The discrete adjoint on the refined tidal channel: the gradient of a
+    50-station misfit (observations from a forward run with a perturbed
+    friction field) w.r.t. Manning's n per element, the bed, and the M2
+    amplitude and phase; its time against the forward's, at the memory
+    budget that checkpoints about every 45 steps and with every state
+    stored; central differences on random directions, by replaying the
+    forward's steps. One GPU: replicas are independent runs."""
+    import dataclasses
+
+    from dgcom_gb300 import cases
+    from dgcom_gb300.adjoint import Adjoint
+    from dgcom_gb300.physics import TidalBoundary
+
+    dist = Dist(world, "nccl")
+    case, stations, n_obs = cases.adjoint_channel(nx=args.adj_nx, ny=args.adj_ny, order=args.order)
+    form = case.form
+    nn = (args.order + 1) ** 2
+    steps = args.steps
+    state = case.state
+    nodes = form.n_values
+    obs_form = dataclasses.replace(form, manning_n=np.repeat(n_obs, nn))
+    t0 = args.adj_t_start
+    with Adjoint(obs_form, steps, stations, cfl=case.cfl, t_start=t0) as a:
+        _, eta_obs, _ = a.forward(state)
+    state_bytes = 3.0 * 8.0 * nodes
+    results = {}
+    g = None
+    dts = None
+    stride_budget = (math.ceil(steps / 45.0) + 45 + 1) * state_bytes
+    for label, budget in [("stride~45", stride_budget), ("all stored", 0.0)]:
+        with Adjoint(form, steps, stations, cfl=case.cfl, t_start=t0, memory_budget=budget,
+                     device=local) as a:
+            a.forward(state, eta_obs=eta_obs)  # warm-up
+            J, _, dts = a.forward(state, eta_obs=eta_obs)
+            g = a.reverse()
+            st = a.stats()
+        results[label] = {"J": J, "forward_ms": st.forward_ms, "reverse_ms": st.reverse_ms,
+                          "reverse_over_forward": st.reverse_ms / st.forward_ms,
+                          "gradient_over_forward": (st.forward_ms + st.reverse_ms) / st.forward_ms,
+                          "stride": int(st.stride), "stored_gb": st.stored_bytes / 1e9,
+                          "recomputed_steps": int(st.recomputed_steps)}
+    # central differences of the forward (the steps replayed) on random directions
+    rng = np.random.default_rng(7)
+    n0 = np.asarray(form.manning_n)
+    b0 = form.bathymetry.reshape(-1)
+    x, y = form.positions()
+    x = x.reshape(-1)
+    y = y.reshape(-1)
+    OPEN = 1
+    c0 = form.boundaries[OPEN].constituents[0]
+
+    def J_of(f):
+        with Adjoint(f, steps, stations, cfl=case.cfl, t_start=t0, device=local) as a:
+            return a.forward(state, dts=dts, eta_obs=eta_obs)[0]
+
+    def with_tide(amplitude, phase):
+        cons = list(form.boundaries[OPEN].constituents)
+        c = type(cons[0])()
+        for name, _ in type(c)._fields_:
+            setattr(c, name, getattr(cons[0], name))
+        c.amplitude = amplitude
+        c.phase = phase
+        cons[0] = c
+        bc = form.boundaries[OPEN]
+        new = dict(form.boundaries)
+        new[OPEN] = TidalBoundary(cons, mean_elevation=bc.mean_elevation,
+                                  ramp_duration=bc.ramp_duration, incoming_wave=bc.incoming_wave)
+        return dataclasses.replace(form, boundaries=new)
+
+    checks = []
+    for i in range(args.fd_directions):
+        kind = ("manning", "bed", "tide")[i % 3]
+        if kind == "manning":
+            d_el = rng.standard_normal(form.mesh.n_elements)
+            d = np.repeat(d_el, nn)
+            adj = float(np.dot(g.manning_per_element(nn), d_el))
+            eps = 1e-4 * 0.02  # at 1e-6 the difference is within J's rounding
+            make = lambda e, d=d: dataclasses.replace(form, manning_n=n0 + e * d)
+        elif kind == "bed":
+            kx, ky = rng.uniform(1.0, 8.0), rng.uniform(0.5, 3.0)
+            ph = rng.uniform(0.0, 2 * np.pi)
+            d = np.sin(kx * 2 * np.pi * x / 50_000.0 + ph) * np.cos(ky * np.pi * y / 5_000.0)
+            adj = float(np.dot(g.bed, d))
+            eps = 1e-6 * float(np.abs(b0).max())
+            make = lambda e, d=d: dataclasses.replace(
+                form, bathymetry=(b0 + e * d).reshape(form.bathymetry.shape))
+        else:  # a direction in the (amplitude, phase) plane
+            th = rng.uniform(0.0, 2 * np.pi)
+            da, dp = np.cos(th) * c0.amplitude, np.sin(th)
+            adj = float(g.tide[OPEN, 0, 0] * da + g.tide[OPEN, 0, 1] * dp)
+            eps = 1e-6
+            make = lambda e, da=da, dp=dp: with_tide(c0.amplitude + e * da, c0.phase + e * dp)
+        fd = (J_of(make(eps)) - J_of(make(-eps))) / (2.0 * eps)
+        checks.append({"kind": kind, "adjoint": adj, "fd": fd,
+                       "rel": abs(adj - fd) / max(abs(fd), abs(adj), 1e-300)})
+    rels = [c["rel"] for c in checks]
+    headline = results["stride~45"]
+    if rank == 0:
+        line = {
+            "metric": "adjoint time / forward time (discrete adjoint of the FP64 DG SWE run)",
+            "value": headline["reverse_over_forward"], "unit": "ratio", "n_gpus": world,
+            "steps": steps, "warmup": 1, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"tidal channel {form.mesh.n_elements} quads N={args.order} "
+                                   f"(drying flat), {steps} SSP-RK3 steps from rest at t = {t0:g} s "
+                                   f"(past the 1 h tide ramp), {len(stations)} stations; "
+                                   "gradient w.r.t. Manning n per element, bed per node, M2 "
+                                   "amplitude and phase",
+                       "elements": form.mesh.n_elements, "order": args.order, "nodes": nodes,
+                       "parallelism": f"replicas x{world}"},
+            "runs": results,
+            "fd_check": {"directions": len(checks), "what": "central differences of the GPU "
+                         "forward with the adjoint's time steps replayed: Manning n per element "
+                         "(step 1e-4 relative: at 1e-6 the difference is within J's rounding), "
+                         "smooth bed fields and (amplitude, phase) directions (step 1e-6)",
+                         "max_rel": max(rels) if rels else None,
+                         "median_rel": float(np.median(rels)) if rels else None,
+                         "checks": checks},
+        }
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -439,12 +570,17 @@ def main():
     ap.add_argument("--elements", type=int, default=1_000_000)
     ap.add_argument("--order", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="coastal", choices=["coastal", "ensemble"],
+    ap.add_argument("--workload", default="coastal", choices=["coastal", "ensemble", "adjoint"],
                     help="coastal: the 1 M-quad coastal box (the headline); ensemble: batched "
-                         "members against sequential plain runs")
+                         "members against sequential plain runs; adjoint: the discrete "
+                         "adjoint's time against the forward's on the refined channel")
     ap.add_argument("--members", type=int, default=256)
     ap.add_argument("--k-min", type=int, default=5_000)
     ap.add_argument("--k-max", type=int, default=200_000)
+    ap.add_argument("--adj-nx", type=int, default=1000)
+    ap.add_argument("--adj-ny", type=int, default=100)
+    ap.add_argument("--fd-directions", type=int, default=20)
+    ap.add_argument("--adj-t-start", type=float, default=4000.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
@@ -452,6 +588,8 @@ def main():
         run_reference(args, rank, world)
     elif args.workload == "ensemble":
         run_ensemble(args, rank, world, local)
+    elif args.workload == "adjoint":
+        run_adjoint(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)
 

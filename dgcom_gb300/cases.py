@@ -187,6 +187,30 @@ def ensemble_members(n_members: int = 256, seed: int = 2027,
                             float(amp[i]), numerics) for i in range(n_members)]
 
 
+def adjoint_channel(nx: int = 1000, ny: int = 100, order: int = 3, n_stations: int = 50,
+                    seed: int = 2028, numerics: int = abi.NUMERICS_FAST):
+    """The adjoint workload: the tidal channel refined to nx × ny quads
+    (1000 × 100 at 50 m by default), Manning's n per element, seeded
+    stations, and the friction field of the observations,
+    n_obs = 0.02·(1 + 0.2·GRF) with a seeded Gaussian random field (2 km
+    correlation) at the element centres. Returns the case (n = 0.02 per
+    element), the stations [n][2] and n_obs per element."""
+    case = tidal_channel(nx=nx, ny=ny, order=order, numerics=numerics)
+    mesh = case.form.mesh
+    rng = np.random.default_rng(seed)
+    lx, ly = 50_000.0, 5_000.0
+    stations = np.column_stack([rng.uniform(0.02 * lx, 0.98 * lx, n_stations),
+                                rng.uniform(0.05 * ly, 0.95 * ly, n_stations)])
+    centres = mesh.vertices[mesh.elements].mean(axis=1)
+    spacing = 250.0
+    grid = gaussian_random_field(int(lx / spacing) + 2, int(ly / spacing) + 2, spacing, 2_000.0, rng)
+    z = _bilinear_grid(grid, spacing, centres[:, 0], centres[:, 1])
+    nn = (order + 1) ** 2
+    n_obs = 0.02 * (1.0 + 0.2 * z)
+    case.form.manning_n = np.repeat(np.full(mesh.n_elements, 0.02), nn)
+    return case, stations, n_obs
+
+
 # -- the reference's split-form test setups ------------------------------------
 
 L_TEST = 20_000.0
