@@ -249,6 +249,38 @@ int dgswe_adjoint_create(const dgswe_form* f, int device, const dgswe_adjoint_co
     ACK(cudaEventCreate(&a->e0));
     ACK(cudaEventCreate(&a->e1));
     const int64_t nf = h->K * 4 * h->n1;
+    // the bed slope's transpose: for node c, each line partner i's
+    // ∂(g∇B)_i/∂B_c = g·D[pos_i][pos_c]·w(i, c), with w the forward's metric
+    // weight (i's own on an affine element, else the mean of i's and c's)
+    if (h->P.has_bed) {
+        const int n1 = ops.n1;
+        std::vector<double> contra(4 * (size_t)nv), gt(4 * (size_t)n1 * nv);
+        std::vector<uint8_t> aff((size_t)h->K);
+        ACK(cudaMemcpy(contra.data(), h->T.contra, contra.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        ACK(cudaMemcpy(aff.data(), h->T.affine, aff.size(), cudaMemcpyDeviceToHost));
+#pragma omp parallel for schedule(static)
+        for (int64_t k = 0; k < h->K; ++k)
+            for (int c = 0; c < nn; ++c)
+                for (int dir = 0; dir < 2; ++dir) {
+                    const int line = dir == 0 ? c / n1 : c % n1;
+                    const int pc = dir == 0 ? c % n1 : c / n1;
+                    const double* mc = &contra[(k * nn + c) * 4 + 2 * dir];
+                    for (int pa = 0; pa < n1; ++pa) {
+                        const int i = dir == 0 ? line * n1 + pa : pa * n1 + line;
+                        const double* mi = &contra[(k * nn + i) * 4 + 2 * dir];
+                        const double wx = aff[k] ? mi[0] : 0.5 * (mi[0] + mc[0]);
+                        const double wy = aff[k] ? mi[1] : 0.5 * (mi[1] + mc[1]);
+                        const double gd = f->g * ops.d[pa * n1 + pc];
+                        double* o = &gt[(((k * nn + c) * 2 + dir) * n1 + pa) * 2];
+                        o[0] = gd * wx;
+                        o[1] = gd * wy;
+                    }
+                }
+        double* d_gt = nullptr;
+        if (int s = dalloc(a, gt.size(), &d_gt)) return s;
+        ACK(cudaMemcpy(d_gt, gt.data(), gt.size() * sizeof(double), cudaMemcpyHostToDevice));
+        h->T.gdb_t = d_gt;
+    }
     const int n_st = cfg->n_stations;
     std::vector<int64_t> node0(n_st);
     for (int s = 0; s < n_st; ++s) node0[s] = a->st_elem[s] * nn;

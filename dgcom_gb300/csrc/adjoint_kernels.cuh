@@ -34,11 +34,14 @@ struct AdjCfg {
     static constexpr int NA = 2 * (N1 - 1);
     static constexpr int EPB = (64 / NN) > 0 ? (64 / NN) : 1;
     static constexpr int THREADS = EPB * NN;
-    static constexpr int PAIR = NN * NP * 16;                   // λ per slot side (3) and out (5)
+    static constexpr int PAIR = NN * NP * 12 + 2 * NN;          // λ per slot side (3), out (6), bed (2)
     static constexpr int FACES = 2 * NN * 8;                    // subcell faces
     static constexpr int IFL = 2 * N1 * (N1 - 1) * 6;           // subcell interface fluxes
     static constexpr int SUB = 2 * FACES + IFL;                 // faces, their λ, interfaces' λ
     static constexpr int X = PAIR > SUB ? PAIR : SUB;
+    static_assert(X >= 6 * NN, "the limiter's scratch shares s_x");
+    // 8 blocks per SM: ≤ 128 registers; shared memory ≈ 27 KB per block
+    static constexpr int MIN_BLOCKS = 8;
 };
 
 // The node's face slots in the reference's face order (as the forward's lift)
@@ -61,16 +64,14 @@ __device__ __forceinline__ void node_face_slots(int a, int j, int64_t k, int64_t
 }
 
 template <int N1>
-__global__ void __launch_bounds__(AdjCfg<N1>::THREADS)
+__global__ void __launch_bounds__(AdjCfg<N1>::THREADS, AdjCfg<N1>::MIN_BLOCKS)
     stage_adjoint_kernel(DevTables T, Physics P, StageExtra X, DevBuf in, DevBuf keep, AdjStage A,
                          const StepCtl* ctl, int slot) {
     using C = AdjCfg<N1>;
     constexpr int NN = C::NN, NP = C::NP, NA = C::NA, EPB = C::EPB;
     __shared__ double s_q[EPB][6][NN];   // stage input: h, hu, hv, u, v, b
     __shared__ double s_l[EPB][6][NN];   // λ landing from the element's other nodes
-    __shared__ double s_w[EPB][6][NN];   // limiter: damped values, then λ
-    __shared__ double s_ab[EPB][2][NN];  // bed-slope weights −h·λr
-    __shared__ double s_x[EPB][C::X];
+    __shared__ double s_x[EPB][C::X];    // limiter, then the pair or subcell scratch
     __shared__ int s_flag[EPB][2];
     __shared__ double s_red[EPB][12];
     __shared__ int s_arg[EPB];
@@ -130,9 +131,9 @@ __global__ void __launch_bounds__(AdjCfg<N1>::THREADS)
     double ldh = lo_h, ldhu = lo_hu, ldhv = lo_hv;  // λ of (vh, dhu, dhv)
     if (P.has_wet_dry) {
         if (valid && fp::lt(vh, P.h_dry)) atomicOr(&s_flag[e][1], 1);
-        s_w[e][0][i] = vh;
-        s_w[e][1][i] = dhu;
-        s_w[e][2][i] = dhv;
+        s_x[e][0 * NN + i] = vh;
+        s_x[e][1 * NN + i] = dhu;
+        s_x[e][2 * NN + i] = dhv;
         __syncthreads();
         const bool needs = s_flag[e][1] != 0;
         if (valid && needs && i == 0) {
@@ -141,11 +142,11 @@ __global__ void __launch_bounds__(AdjCfg<N1>::THREADS)
             double sh = 0.0, shu = 0.0, shv = 0.0, hmin = INFINITY;
             int arg = 0;
             for (int p = 0; p < NN; ++p) {
-                sh += mass[p] * s_w[e][0][p];
-                shu += mass[p] * s_w[e][1][p];
-                shv += mass[p] * s_w[e][2][p];
-                if (fp::lt(s_w[e][0][p], hmin)) {
-                    hmin = s_w[e][0][p];
+                sh += mass[p] * s_x[e][0 * NN + p];
+                shu += mass[p] * s_x[e][1 * NN + p];
+                shv += mass[p] * s_x[e][2 * NN + p];
+                if (fp::lt(s_x[e][0 * NN + p], hmin)) {
+                    hmin = s_x[e][0 * NN + p];
                     arg = p;
                 }
             }
@@ -202,18 +203,18 @@ __global__ void __launch_bounds__(AdjCfg<N1>::THREADS)
             ldhu = lwhu;
             ldhv = lwhv;
         }
-        s_w[e][3][i] = lpre;
-        s_w[e][4][i] = lwhu;
-        s_w[e][5][i] = lwhv;
+        s_x[e][3 * NN + i] = lpre;
+        s_x[e][4 * NN + i] = lwhu;
+        s_x[e][5 * NN + i] = lwhv;
         __syncthreads();
         if (valid && scaled && i == 0) {
             double tb = 0.0, sp = 0.0, spu = 0.0, spv = 0.0;
             for (int p = 0; p < NN; ++p) {
-                tb += s_w[e][3][p] * (s_w[e][0][p] - h_avg) + s_w[e][4][p] * (s_w[e][1][p] - s_red[e][1]) +
-                      s_w[e][5][p] * (s_w[e][2][p] - s_red[e][2]);
-                sp += s_w[e][3][p];
-                spu += s_w[e][4][p];
-                spv += s_w[e][5][p];
+                tb += s_x[e][3 * NN + p] * (s_x[e][0 * NN + p] - h_avg) + s_x[e][4 * NN + p] * (s_x[e][1 * NN + p] - s_red[e][1]) +
+                      s_x[e][5 * NN + p] * (s_x[e][2 * NN + p] - s_red[e][2]);
+                sp += s_x[e][3 * NN + p];
+                spu += s_x[e][4 * NN + p];
+                spv += s_x[e][5 * NN + p];
             }
             double h_avg_b = (1.0 - theta) * sp, hmin_b = 0.0;
             if (s_red[e][5] != 0.0) {  // dθ: θ = h_avg/(h_avg − hmin)
@@ -303,7 +304,8 @@ __global__ void __launch_bounds__(AdjCfg<N1>::THREADS)
     double* faces_b = &s_x[e][C::FACES];           // their λ
     double* ifl_b = &s_x[e][2 * C::FACES];         // λ of the interface fluxes [..][6]
     double* lf = &s_x[e][0];                       // pair path: [slot][side][3]
-    double* lp = &s_x[e][NN * NP * 6];             // pair path: [slot][side][5]
+    double* lp = &s_x[e][NN * NP * 6];             // pair path: [slot][λh_a, λh_c, λhu, λhv, λu, λv]
+    double* s_ab = &s_x[e][NN * NP * 12];          // pair path: bed-slope weights −h·λr [2][NN]
     auto node_side = [&](int n) {
         return Sd{s_q[e][0][n], s_q[e][3][n], s_q[e][4][n], s_q[e][5][n]};
     };
@@ -312,8 +314,8 @@ __global__ void __launch_bounds__(AdjCfg<N1>::THREADS)
         if (P.has_bed) {
             Lh -= T.gdb[gi * 2] * lrhu + T.gdb[gi * 2 + 1] * lrhv;
         }
-        s_ab[e][0][i] = -h * lrhu;
-        s_ab[e][1][i] = -h * lrhv;
+        s_ab[i] = -h * lrhu;
+        s_ab[NN + i] = -h * lrhv;
 #pragma unroll
         for (int q = 0; q < NA; ++q) {
             const int sl = T.sched_slot[i * NA + q];
@@ -395,14 +397,13 @@ __global__ void __launch_bounds__(AdjCfg<N1>::THREADS)
             const double lmass =
                 f0 + f1 * (s_q[e][3][na] + s_q[e][3][nc]) + f2 * (s_q[e][4][na] + s_q[e][4][nc]);
             const double lgp2 = (f1 * hm0 + f2 * hm1) * two_g;
-            double* pa_ = &lp[(sl * 2) * 5];
-            double* pc_ = &lp[(sl * 2 + 1) * 5];
-            pa_[0] = lgp2 * hc;
-            pc_[0] = lgp2 * ha;
-            pa_[1] = pc_[1] = lmass * hm0;
-            pa_[2] = pc_[2] = lmass * hm1;
-            pa_[3] = pc_[3] = f1 * mass;
-            pa_[4] = pc_[4] = f2 * mass;
+            double* o = &lp[sl * 6];  // both nodes share all but λh
+            o[0] = lgp2 * hc;
+            o[1] = lgp2 * ha;
+            o[2] = lmass * hm0;
+            o[3] = lmass * hm1;
+            o[4] = f1 * mass;
+            o[5] = f2 * mass;
         }
     } else if (valid && sub) {
 #pragma unroll
@@ -478,28 +479,25 @@ __global__ void __launch_bounds__(AdjCfg<N1>::THREADS)
         for (int q = 0; q < NA; ++q) {
             const int sl = T.sched_slot[i * NA + q];
             const int side = T.sched_owned[sl * 5] == i ? 0 : 1;
-            const double* o = &lp[(sl * 2 + side) * 5];
-            Lh += o[0];
-            Lhu += o[1];
-            Lhv += o[2];
-            Lu += o[3];
-            Lv += o[4];
+            const double* o = &lp[sl * 6];
+            Lh += o[side];
+            Lhu += o[2];
+            Lhv += o[3];
+            Lu += o[4];
+            Lv += o[5];
         }
         if (P.has_bed) {
-            // gdb_i = g Σ_dir Σ_c D[pos_i][pos_c] B_c w(i, c): this node as c
-            const double* mc = &T.contra[gi * 4];
+            // gdb_i = g Σ_dir Σ_c D[pos_i][pos_c] B_c w(i, c), transposed: this
+            // node as c, the coefficients from the gdb_t table
+            const double* t = &T.gdb_t[gi * 4 * N1];
 #pragma unroll
             for (int dir = 0; dir < 2; ++dir) {
                 const int line = dir == 0 ? j : a;
-                const int pc = dir == 0 ? a : j;
 #pragma unroll
                 for (int pa = 0; pa < N1; ++pa) {
                     const int n = line_node(N1, dir, line, pa);
-                    const double* mi = &T.contra[(k * NN + n) * 4];
-                    const double wx = affine ? mi[2 * dir] : 0.5 * (mi[2 * dir] + mc[2 * dir]);
-                    const double wy =
-                        affine ? mi[2 * dir + 1] : 0.5 * (mi[2 * dir + 1] + mc[2 * dir + 1]);
-                    Lb += g * P.d[pa * N1 + pc] * (wx * s_ab[e][0][n] + wy * s_ab[e][1][n]);
+                    const double* c = &t[(dir * N1 + pa) * 2];
+                    Lb += c[0] * s_ab[n] + c[1] * s_ab[NN + n];
                 }
             }
         }

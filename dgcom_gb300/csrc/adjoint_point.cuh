@@ -545,7 +545,7 @@ DG_PT void damp_rev(const Physics& P, double g_n2, double h, double hu, double h
             hm_h = fp::gt(h, P.manning_h_min);
             hm = hm_h ? h : P.manning_h_min;
             z4 = manning_z4(hm);
-            rate += manning_rate(g_n2, hm, speed);
+            rate += g_n2 * speed * z4;  // manning_rate's value from the same h^(-4/3)
         }
     }
     const bool thin = P.has_wet_dry && fp::lt(h, P.h_dry);
@@ -560,8 +560,8 @@ DG_PT void damp_rev(const Physics& P, double g_n2, double h, double hu, double h
     if (manning) {
         g_n2b += rateb * speed * z4;
         const double speedb = rateb * g_n2 * z4;
-        if (hm_h) hb += rateb * g_n2 * speed * z4 * (-4.0 / 3.0) / hm;
-        const double inv = 1.0 / speed;
+        if (hm_h) hb += rateb * g_n2 * speed * z4 * (-4.0 / 3.0) * vrcp(hm);
+        const double inv = vrcp(speed);
         damp_velocity_rev(P, from, speedb * u * inv, speedb * v * inv, fromb);
     }
 }

@@ -40,6 +40,10 @@ struct DevTables {
     // bface_cond indexes. Both null for one mesh (ctl[0], Physics::cond).
     const int32_t* elem_member = nullptr;
     const struct Condition* cond = nullptr;
+    // The adjoint's transpose of the bed slope: per node c, for each
+    // direction and line position p, g·D[p][pos_c]·w (x and y) of the node i
+    // at p, so that ∂(g∇B)_i/∂B_c is a table entry (adjoint handles only)
+    const double* gdb_t = nullptr;  // [K·nn][2][n1][2]
 };
 
 struct Constituent {
