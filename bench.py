@@ -561,6 +561,130 @@ def run_adjoint(args, rank: int, world: int, local: int):
     dist.close()
 
 
+def run_adjoint_ensemble(args, rank: int, world: int, local: int):
+    """The batched adjoint ensemble: ``--adj-members`` coastal boxes of
+    ``--adj-k-min``..``--adj-k-max`` quads (log-uniform), each with 30
+    stations, eight tide constituents and Manning's n per element, in one
+    batched forward and reverse sweep within a shared checkpoint budget of
+    ``--adj-budget-gb``. The observations come from a forward run under
+    perturbed forcing (the same step times); the gradient is w.r.t. every
+    member's Manning n per element and constituent amplitudes and phases.
+    Central differences of the batched forward (steps replayed, the
+    parameters moved in place) check random directions. One GPU: replicas
+    are independent runs."""
+    from dgcom_gb300 import cases
+    from dgcom_gb300.adjoint import Adjoint
+    from dgcom_gb300.mesh import TAG_OPEN
+
+    dist = Dist(world, "nccl")
+    t_gen = time.perf_counter()
+    ms = cases.adjoint_ensemble_members(n_members=args.adj_members, seed=2029 + rank,
+                                        k_range=(args.adj_k_min, args.adj_k_max),
+                                        order=args.order, n_stations=30)
+    t_gen = time.perf_counter() - t_gen
+    forms = [m.case.form for m in ms]
+    stations = np.vstack([m.stations for m in ms])
+    member = np.repeat(np.arange(len(ms)), [m.stations.shape[0] for m in ms]).astype(np.int32)
+    state = tuple(np.concatenate([m.case.state[c] for m in ms]) for c in range(3))
+    nn = (args.order + 1) ** 2
+    quads = int(sum(f.mesh.n_elements for f in forms))
+    nodes = quads * nn
+    steps = args.steps
+    t0 = args.adj_ens_t_start
+    budget = args.adj_budget_gb * 1e9
+    t_create = time.perf_counter()
+    ens = Adjoint.ensemble(forms, steps, stations, member, cfl=0.5, t_start=t0,
+                           memory_budget=budget, device=local)
+    t_create = time.perf_counter() - t_create
+    try:
+        tide0 = ens.tide_parameters()
+        n0 = np.concatenate([np.asarray(f.manning_n) for f in forms])
+        tide_obs = tide0.copy()
+        row = 0
+        for m, f in zip(ms, forms):
+            tide_obs[row + sorted(f.boundaries).index(TAG_OPEN)] = m.tide_obs
+            row += len(f.boundaries)
+        n_obs = np.concatenate([m.manning_obs for m in ms])
+        # the CFL steps (also the warm-up), then the observations at the same times
+        _, _, dts = ens.forward(state)
+        ens.set_parameters(manning=n_obs, tide=tide_obs)
+        _, eta_obs, _ = ens.forward(state, dts=dts)
+        ens.set_parameters(manning=n0, tide=tide0)
+        J, _, _ = ens.forward(state, dts=dts, eta_obs=eta_obs)
+        Jm = ens.member_J()
+        g = ens.reverse()
+        st = ens.stats()
+
+        def J_at(manning=None, tide=None):
+            ens.set_parameters(manning=manning, tide=tide)
+            return ens.forward(state, dts=dts, eta_obs=eta_obs)[0]
+
+        rng = np.random.default_rng(17)
+        checks = []
+        for i in range(args.fd_directions):
+            m = int(rng.integers(len(forms)))
+            if i % 2 == 0:  # Manning n per element of one member
+                sl = ens.member_slice(m)
+                d = np.zeros_like(n0)
+                d[sl] = np.repeat(rng.standard_normal((sl.stop - sl.start) // nn), nn)
+                eps = 1e-4 * float(n0[sl].max())
+                fd = (J_at(manning=n0 + eps * d) - J_at(manning=n0 - eps * d)) / (2 * eps)
+                J_at(manning=n0)
+                adj = float(np.dot(g.manning, d))
+                kind = "manning"
+            else:  # the eight constituents' amplitudes and phases of one member
+                r = sum(len(f.boundaries) for f in forms[:m]) + \
+                    sorted(forms[m].boundaries).index(TAG_OPEN)
+                d = np.zeros_like(tide0)
+                d[r] = rng.standard_normal(d[r].shape)
+                eps = 1e-5
+                fd = (J_at(tide=tide0 + eps * d) - J_at(tide=tide0 - eps * d)) / (2 * eps)
+                J_at(tide=tide0)
+                adj = float(np.sum(g.tide * d))
+                kind = "tide"
+            checks.append({"kind": kind, "member": m, "adjoint": adj, "fd": fd,
+                           "rel": abs(adj - fd) / max(abs(fd), abs(adj), 1e-300)})
+    finally:
+        ens.close()
+    rels = [c["rel"] for c in checks]
+    if rank == 0:
+        fwd_s = st.forward_ms / 1e3
+        line = {
+            "metric": "batched adjoint ensemble: adjoint time / forward time",
+            "value": st.reverse_ms / st.forward_ms, "unit": "ratio", "n_gpus": world,
+            "steps": steps, "warmup": 1, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"{len(forms)} coastal boxes of {args.adj_k_min}-"
+                                   f"{args.adj_k_max} quads (log-uniform, {quads} in all), "
+                                   f"N={args.order}, {steps} SSP-RK3 steps from rest at "
+                                   f"t = {t0:g} s, 30 stations each, 8 constituents; gradient "
+                                   "w.r.t. Manning n per element and every constituent's "
+                                   "amplitude and phase, one batched sweep",
+                       "members": len(forms), "elements": quads, "order": args.order,
+                       "nodes": nodes, "checkpoint_budget_gb": args.adj_budget_gb,
+                       "parallelism": f"replicas x{world}"},
+            "forward_ms": st.forward_ms, "reverse_ms": st.reverse_ms,
+            "gradient_over_forward": (st.forward_ms + st.reverse_ms) / st.forward_ms,
+            "forward_dof_updates_per_s": 3.0 * nodes * steps / fwd_s,
+            "gradient_wall_s": st.forward_wall_s + st.reverse_wall_s,
+            "stride": int(st.stride), "stored_gb": st.stored_bytes / 1e9,
+            "recomputed_steps": int(st.recomputed_steps),
+            "J": J, "J_member_min": float(Jm.min()), "J_member_max": float(Jm.max()),
+            "dt_range_s": [float(dts.min()), float(dts.max())],
+            "setup_s": {"generate": t_gen, "create": t_create},
+            "fd_check": {"directions": len(checks), "what": "central differences of the batched "
+                         "GPU forward with the adjoint's time steps replayed and the parameters "
+                         "moved in place: Manning n per element of one member (step 1e-4 "
+                         "relative), all eight constituents' (amplitude, phase) of one member "
+                         "(step 1e-5)",
+                         "max_rel": max(rels) if rels else None,
+                         "median_rel": float(np.median(rels)) if rels else None,
+                         "checks": checks},
+        }
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -570,10 +694,12 @@ def main():
     ap.add_argument("--elements", type=int, default=1_000_000)
     ap.add_argument("--order", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="coastal", choices=["coastal", "ensemble", "adjoint"],
+    ap.add_argument("--workload", default="coastal",
+                    choices=["coastal", "ensemble", "adjoint", "adjoint_ensemble"],
                     help="coastal: the 1 M-quad coastal box (the headline); ensemble: batched "
                          "members against sequential plain runs; adjoint: the discrete "
-                         "adjoint's time against the forward's on the refined channel")
+                         "adjoint's time against the forward's on the refined channel; "
+                         "adjoint_ensemble: the batched adjoint of coastal-box members")
     ap.add_argument("--members", type=int, default=256)
     ap.add_argument("--k-min", type=int, default=5_000)
     ap.add_argument("--k-max", type=int, default=200_000)
@@ -581,6 +707,11 @@ def main():
     ap.add_argument("--adj-ny", type=int, default=100)
     ap.add_argument("--fd-directions", type=int, default=20)
     ap.add_argument("--adj-t-start", type=float, default=4000.0)
+    ap.add_argument("--adj-members", type=int, default=64)
+    ap.add_argument("--adj-k-min", type=int, default=10_000)
+    ap.add_argument("--adj-k-max", type=int, default=150_000)
+    ap.add_argument("--adj-budget-gb", type=float, default=120.0)
+    ap.add_argument("--adj-ens-t-start", type=float, default=0.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
@@ -590,6 +721,8 @@ def main():
         run_ensemble(args, rank, world, local)
     elif args.workload == "adjoint":
         run_adjoint(args, rank, world, local)
+    elif args.workload == "adjoint_ensemble":
+        run_adjoint_ensemble(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)
 

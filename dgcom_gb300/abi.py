@@ -185,6 +185,7 @@ class AdjointConfig(C.Structure):
         ("n_stations", C.c_int32),
         ("stations", _dp),
         ("memory_budget", C.c_double),
+        ("station_member", C.POINTER(C.c_int32)),
     ]
 
 
@@ -242,12 +243,17 @@ CUDA_ONLY = {
     # the discrete adjoint
     "adjoint_create": (C.c_int, [C.POINTER(Form), C.c_int, C.POINTER(AdjointConfig),
                                  C.POINTER(C.c_void_p)]),
+    "adjoint_create_ensemble": (C.c_int, [C.POINTER(Form), C.c_int, C.c_int,
+                                          C.POINTER(AdjointConfig), C.POINTER(C.c_void_p)]),
+    "adjoint_member_offset": (C.c_int64, [C.c_void_p, C.c_int]),
+    "adjoint_member_misfit": (C.c_int, [C.c_void_p, _dp]),
     "adjoint_destroy": (None, [C.c_void_p]),
     "adjoint_last_error": (C.c_char_p, [C.c_void_p]),
     "adjoint_n_values": (C.c_int64, [C.c_void_p]),
     "adjoint_stations": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), _dp]),
     "adjoint_forward": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
     "adjoint_reverse": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "adjoint_set_parameters": (C.c_int, [C.c_void_p, _dp, _dp]),
     "adjoint_get_stats": (C.c_int, [C.c_void_p, C.POINTER(AdjointStats)]),
 }
 

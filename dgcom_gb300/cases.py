@@ -9,6 +9,9 @@
   N = 3, over a seeded Gaussian random bed of 2–300 m with 30 Gaussian
   islands above the datum, under a 4-constituent tide (M2, S2, N2, K1) with
   seeded phases, Manning n = 0.02 and Coriolis at 63° N;
+- :func:`adjoint_channel` and :func:`adjoint_ensemble_members`: the
+  station-misfit adjoint workloads (one channel; a batched ensemble of
+  coastal boxes under eight constituents);
 - :func:`split_form_setup`: the meshes, beds and states of the reference's
   split-form unit tests (src/solver/rhs/swe_2d_split_form.rs:1144-1232).
 
@@ -156,18 +159,24 @@ def coastal_box(n_elements: int = 1_000_000, order: int = 3, seed: int = 2026,
     return Case(form, at_rest(form), 0.5, abi.SSP_RK3, 2000.0)
 
 
-def ensemble_member(n_elements: int, order: int, seed: int, manning_n: float,
-                    m2_amplitude: float, numerics: int = abi.NUMERICS_FAST) -> Case:
-    """One member of a batched ensemble: the coastal-box generator scaled to
-    ``n_elements`` quads of the same element sizes (mean 173 m, 4:3 box),
-    with islands in proportion to the area (at least one, radii at most a
-    tenth of the box) and an M2 tide of ``m2_amplitude``."""
+def _member_box(n_elements: int) -> tuple:
+    """lx, ly, island count and radius range of an ensemble member's box."""
     mean = 173.0
     area = n_elements * mean * mean
     lx = math.sqrt(area * 4.0 / 3.0)
     ly = 0.75 * lx
     n_islands = max(1, int(round(30.0 * area / (200_000.0 * 150_000.0))))
     radius = (min(1000.0, 0.05 * ly), min(5000.0, 0.1 * ly))
+    return lx, ly, n_islands, radius
+
+
+def ensemble_member(n_elements: int, order: int, seed: int, manning_n: float,
+                    m2_amplitude: float, numerics: int = abi.NUMERICS_FAST) -> Case:
+    """One member of a batched ensemble: the coastal-box generator scaled to
+    ``n_elements`` quads of the same element sizes (mean 173 m, 4:3 box),
+    with islands in proportion to the area (at least one, radii at most a
+    tenth of the box) and an M2 tide of ``m2_amplitude``."""
+    lx, ly, n_islands, radius = _member_box(n_elements)
     return coastal_box(n_elements, order, seed, numerics, lx, ly, n_islands, radius,
                        (("M2", m2_amplitude),), manning_n)
 
@@ -209,6 +218,79 @@ def adjoint_channel(nx: int = 1000, ny: int = 100, order: int = 3, n_stations: i
     n_obs = 0.02 * (1.0 + 0.2 * z)
     case.form.manning_n = np.repeat(np.full(mesh.n_elements, 0.02), nn)
     return case, stations, n_obs
+
+
+# the eight constituents of the batched adjoint, with typical amplitude ratios
+ADJOINT_TIDE = (("M2", 1.0), ("S2", 0.35), ("N2", 0.2), ("K2", 0.1), ("K1", 0.1),
+                ("O1", 0.08), ("P1", 0.03), ("Q1", 0.02))
+
+
+@dataclass
+class AdjointMember:
+    """One member of the batched adjoint: its case (Manning's n per node),
+    its stations [n][2], and the forcing of its observations (Manning's n
+    per node and the tide's (amplitude, phase) [MAX_CONSTITUENTS][2], in
+    the adjoint's parameter layout)."""
+    case: Case
+    stations: np.ndarray
+    manning_obs: np.ndarray
+    tide_obs: np.ndarray
+
+
+def adjoint_ensemble_members(n_members: int = 64, seed: int = 2029,
+                             k_range: tuple[int, int] = (10_000, 150_000), order: int = 3,
+                             n_stations: int = 30,
+                             numerics: int = abi.NUMERICS_FAST) -> list[AdjointMember]:
+    """The batched-adjoint workload: ``n_members`` coastal boxes of
+    log-uniform element counts over ``k_range`` (the ensemble generator's
+    meshes and beds), order ``order``, each under the eight constituents of
+    ``ADJOINT_TIDE`` scaled by U(0.5, 1.5) with seeded phases, with Manning's
+    n per element n₀·(1 + 0.2·GRF), n₀ ~ U(0.015, 0.035) (5 km correlation),
+    and ``n_stations`` stations at least 5 m deep. The observations' forcing
+    perturbs each element's n by a factor 1 + 0.1·GRF and each constituent's
+    amplitude by 5 % and phase by 3° (normal draws); a forward run under it
+    gives the observed η."""
+    rng = np.random.default_rng(seed)
+    k = np.exp(rng.uniform(math.log(k_range[0]), math.log(k_range[1]), n_members))
+    scale = rng.uniform(0.5, 1.5, n_members)
+    n0 = rng.uniform(0.015, 0.035, n_members)
+    out = []
+    for m in range(n_members):
+        mseed = seed * 1000 + m
+        tide = tuple((name, amp * float(scale[m])) for name, amp in ADJOINT_TIDE)
+        case = ensemble_member(int(round(k[m])), order, mseed, float(n0[m]), 1.0, numerics)
+        mesh = case.form.mesh
+        bc = case.form.boundaries[TAG_OPEN]
+        mr = np.random.default_rng(mseed + 7)
+        phases = mr.uniform(0.0, 360.0, len(tide))
+        bc.constituents = [tides.constituent(name, amp, ph) for (name, amp), ph in zip(tide, phases)]
+        # Manning's n per element, as a per-node field
+        lx, ly, n_islands, radius = _member_box(int(round(k[m])))
+        centres = mesh.vertices[mesh.elements].mean(axis=1)
+        spacing = 1000.0
+        nn = (order + 1) ** 2
+
+        def field():
+            g = gaussian_random_field(int(lx / spacing) + 2, int(ly / spacing) + 2, spacing,
+                                      5_000.0, mr)
+            return _bilinear_grid(g, spacing, centres[:, 0], centres[:, 1])
+
+        n_elem = np.maximum(n0[m] * (1.0 + 0.2 * field()), 0.005)
+        n_obs = np.maximum(n_elem * (1.0 + 0.1 * field()), 0.005)
+        case.form.manning_n = np.repeat(n_elem, nn)
+        # stations in water at least 5 m deep (the member's bed at the point)
+        st = np.zeros((0, 2))
+        while st.shape[0] < n_stations:
+            cand = np.column_stack([mr.uniform(0.02 * lx, 0.98 * lx, 4 * n_stations),
+                                    mr.uniform(0.02 * ly, 0.98 * ly, 4 * n_stations)])
+            bed = coastal_bed(cand[:, 0], cand[:, 1], lx, ly, mseed, n_islands, radius)
+            st = np.vstack([st, cand[bed < -5.0]])
+        tide_obs = np.zeros((abi.MAX_CONSTITUENTS, 2))
+        for i, c in enumerate(bc.constituents):
+            tide_obs[i] = (c.amplitude * (1.0 + 0.05 * mr.standard_normal()),
+                           c.phase + math.radians(3.0) * mr.standard_normal())
+        out.append(AdjointMember(case, st[:n_stations], np.repeat(n_obs, nn), tide_obs))
+    return out
 
 
 # -- the reference's split-form test setups ------------------------------------

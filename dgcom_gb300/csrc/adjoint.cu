@@ -7,6 +7,11 @@
 // the time steps and every branch (wet/dry tests, limiter, HLL wave speeds)
 // are the forward's.
 //
+// It runs on one mesh (a dgswe handle) or on an ensemble of members of one
+// order (the ensemble's concatenated tables; each member its own time steps,
+// stations and J): the same kernels, with each element reading its member's
+// step control.
+//
 // Storage: the state at the start of each step (h, hu, hv) is what the
 // reverse sweep needs; within a step the three stages are recomputed. When
 // all N states fit in the memory budget, the forward sweep keeps them all;
@@ -27,6 +32,7 @@
 
 #include "../../include/dgswe.h"
 #include "device.hpp"
+#include "ensemble_internal.hpp"
 #include "handle.hpp"
 #include "host_common.hpp"
 #include "kernel_set.hpp"
@@ -37,23 +43,57 @@ using namespace dgswe::host;
 
 static_assert(DGSWE_MAX_CONSTITUENTS == kMaxConstituents, "constituent table size");
 
+namespace {
+
+// What the adjoint drives: the tables, physics, buffers and step control of
+// one mesh or of one order group of an ensemble
+struct Target {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    const KernelSet* ks = nullptr;
+    DevTables* T = nullptr;
+    const Physics* P = nullptr;
+    const StageExtra* X = nullptr;
+    StepCtl* ctl = nullptr;
+    int n_members = 1;
+    double *fb_h = nullptr, *fb_hu = nullptr, *fb_hv = nullptr;
+    DevBuf state{};
+    int64_t K = 0, nv = 0;
+    int n1 = 0, nn = 0, order = 0;
+    dgswe_form form0{};
+    std::vector<int64_t> k0, nvals;   // per member: first element, values
+    std::vector<int> cond0, ncond;    // per member: first condition, count
+    int n_cond = 0;
+    // the parameters a calibration changes between sweeps: the tide
+    // constituents (in Physics::cond of one mesh, or the ensemble's device
+    // table) and g·n² per node (null: a uniform coefficient)
+    Physics* cond_host = nullptr;
+    Condition* cond_dev = nullptr;
+    double* g_n2 = nullptr;
+};
+
+}  // namespace
+
 struct dgswe_adjoint {
-    dgswe_handle* h = nullptr;  // the forward: tables, state buffer, step control
+    dgswe_handle* h = nullptr;       // one mesh
+    dgswe_ensemble* ens = nullptr;   // or an ensemble
+    Target tg;
     std::string error;
     dgswe_adjoint_config cfg{};
-    std::vector<double> stations;  // [n][2]
-    std::vector<int64_t> st_elem;
-    std::vector<double> st_w;      // [n][nn]
-    std::vector<double> manning_n; // n per node (for ∂J/∂n)
+    std::vector<double> stations;    // [n][2]
+    std::vector<int32_t> st_member;
+    std::vector<int64_t> st_elem;    // global element
+    std::vector<double> st_w;        // [n][nn]
+    std::vector<double> manning_n;   // n per node, concatenated
     double friction_g = 0.0;
-    int n_cond = 0;
+    std::vector<double> J_member;
     // device
     std::vector<void*> allocations;
     int64_t* d_node0 = nullptr;
     double* d_w = nullptr;
-    StageArgs* d_args = nullptr;  // [n_steps][3] the forward's stage weights
+    StageArgs* d_args = nullptr;  // [n_steps][n_members][3] the forward's stage weights
     double* d_eta = nullptr;      // [n_steps][n_stations]
-    double* d_obs = nullptr;      // [n_steps][n_stations] or null
+    double* d_obs = nullptr;      // [n_steps][n_stations]
     double* d_ckpt = nullptr;     // stored step-start states, 3·nv doubles each
     double* d_seg = nullptr;      // a segment's step-start states (stride > 1)
     int64_t stride = 1, n_ckpt = 0;
@@ -66,13 +106,14 @@ struct dgswe_adjoint {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
 
     ~dgswe_adjoint() {
-        if (h) {
-            cudaSetDevice(h->device);
+        if (h || ens) {
+            cudaSetDevice(tg.device);
             for (void* p : allocations) cudaFree(p);
             if (e0) cudaEventDestroy(e0);
             if (e1) cudaEventDestroy(e1);
-            dgswe_destroy(h);
         }
+        if (h) dgswe_destroy(h);
+        if (ens) dgswe_ensemble_destroy(ens);
     }
 };
 
@@ -146,6 +187,25 @@ double lagrange(const std::vector<double>& x, int a, double r) {
     return l;
 }
 
+// the element of a form holding (x, y), and the point's reference coordinates
+int64_t find_element(const dgswe_form& f, double x, double y, double& r, double& s) {
+    for (int64_t k = 0; k < f.n_elements; ++k) {
+        double c[8];
+        for (int v = 0; v < 4; ++v) {
+            const int64_t vi = f.elements[k * 4 + v];
+            c[2 * v] = f.vertices[vi * 2];
+            c[2 * v + 1] = f.vertices[vi * 2 + 1];
+        }
+        const double xmin = std::min({c[0], c[2], c[4], c[6]}), xmax = std::max({c[0], c[2], c[4], c[6]});
+        const double ymin = std::min({c[1], c[3], c[5], c[7]}), ymax = std::max({c[1], c[3], c[5], c[7]});
+        if (x < xmin - 1e-9 * (1 + std::fabs(xmin)) || x > xmax + 1e-9 * (1 + std::fabs(xmax)) ||
+            y < ymin - 1e-9 * (1 + std::fabs(ymin)) || y > ymax + 1e-9 * (1 + std::fabs(ymax)))
+            continue;
+        if (locate(c, x, y, r, s)) return k;
+    }
+    return -1;
+}
+
 __global__ void sum_clear_kernel(double* out, const double* a, double* b, int64_t n) {
     const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n) return;
@@ -169,97 +229,80 @@ int unpack(dgswe_adjoint* a, const DevBuf& dst, const double* src, int64_t n, cu
     return DGSWE_OK;
 }
 
+// the stage weights of step n into every member's StepCtl, or back
+int args_to_ctl(dgswe_adjoint* a, int64_t n) {
+    const Target& t = a->tg;
+    ACK(cudaMemcpy2DAsync(t.ctl[0].stage, sizeof(StepCtl), a->d_args + 3 * n * t.n_members,
+                          3 * sizeof(StageArgs), 3 * sizeof(StageArgs), t.n_members,
+                          cudaMemcpyDeviceToDevice, t.stream));
+    return DGSWE_OK;
+}
+int ctl_to_args(dgswe_adjoint* a, int64_t n) {
+    const Target& t = a->tg;
+    ACK(cudaMemcpy2DAsync(a->d_args + 3 * n * t.n_members, 3 * sizeof(StageArgs), t.ctl[0].stage,
+                          sizeof(StepCtl), 3 * sizeof(StageArgs), t.n_members,
+                          cudaMemcpyDeviceToDevice, t.stream));
+    return DGSWE_OK;
+}
+
 // One forward step of the state in `q` (velocities current), with the
-// stage weights already in ctl->stage[0..2]; the state buffers S[1], S[2]
-// take the intermediate stages, the result lands in q
-void forward_step(dgswe_adjoint* a, const DevBuf& q, cudaStream_t st) {
-    dgswe_handle* h = a->h;
-    const int* on = &h->ctl->always;
+// stage weights already in every member's StepCtl; S[1], S[2] take the
+// intermediate stages, the result lands in q
+void forward_step(dgswe_adjoint* a, const DevBuf& q) {
+    const Target& t = a->tg;
+    const int* on = &t.ctl[0].always;
     const DevBuf* ins[3] = {&q, &a->S[1], &a->S[2]};
     const DevBuf* outs[3] = {&a->S[1], &a->S[2], &q};
     for (int s = 0; s < 3; ++s) {
-        h->ks->face(h->n1, h->T, h->P, *ins[s], h->fb_h, h->fb_hu, h->fb_hv, h->ctl, s, on, st);
-        h->ks->stage(h->n1, h->T, h->P, h->X, *ins[s], q, *outs[s], q, h->fb_h, h->fb_hu, h->fb_hv,
-                     h->ctl, s, kModePost, s == 2, on, st);
+        t.ks->face(t.n1, *t.T, *t.P, *ins[s], t.fb_h, t.fb_hu, t.fb_hv, t.ctl, s, on, t.stream);
+        t.ks->stage(t.n1, *t.T, *t.P, *t.X, *ins[s], q, *outs[s], q, t.fb_h, t.fb_hu, t.fb_hv,
+                    t.ctl, s, kModePost, s == 2, on, t.stream);
     }
 }
 
-}  // namespace
-
-extern "C" {
-
-int dgswe_adjoint_create(const dgswe_form* f, int device, const dgswe_adjoint_config* cfg,
-                         dgswe_adjoint** out) {
-    if (!out) return DGSWE_ERR_INVALID;
-    auto* a = new dgswe_adjoint();
-    *out = a;
-    if (!cfg) return afail(a, DGSWE_ERR_INVALID, "no configuration");
-    std::string why;
-    if (int s = check_form(f, why)) return afail(a, s, "%s", why.c_str());
-    if (f->formulation != DGSWE_WET_DRY)
-        return afail(a, DGSWE_ERR_UNSUPPORTED, "the adjoint covers the WetDry formulation");
-    if (cfg->scheme != DGSWE_SSP_RK3)
-        return afail(a, DGSWE_ERR_UNSUPPORTED, "the adjoint covers SSP-RK3");
-    if (cfg->n_steps <= 0 || cfg->n_stations < 0 || (cfg->n_stations > 0 && !cfg->stations))
-        return afail(a, DGSWE_ERR_INVALID, "steps and stations");
-    a->cfg = *cfg;
-    a->stations.assign(cfg->stations, cfg->stations + 2 * (size_t)cfg->n_stations);
-    a->cfg.stations = nullptr;
-    // stations: element and Lagrange weights
-    Operators ops(f->order);
-    const int nn = ops.nn;
+// Everything after the target exists: stations, the bed slope's transpose,
+// buffers, checkpoints
+int setup(dgswe_adjoint* a, const dgswe_form* forms, const dgswe_adjoint_config* cfg) {
+    Target& t = a->tg;
+    const int nn = t.nn, n1 = t.n1;
+    const int64_t nv = t.nv;
+    Operators ops(t.order);
+    // stations: element (global) and Lagrange weights
     for (int s = 0; s < cfg->n_stations; ++s) {
-        const double x = a->stations[2 * s], y = a->stations[2 * s + 1];
-        int64_t found = -1;
+        const int m = a->st_member[s];
         double r = 0, q = 0;
-        for (int64_t k = 0; k < f->n_elements && found < 0; ++k) {
-            double c[8];
-            for (int v = 0; v < 4; ++v) {
-                const int64_t vi = f->elements[k * 4 + v];
-                c[2 * v] = f->vertices[vi * 2];
-                c[2 * v + 1] = f->vertices[vi * 2 + 1];
-            }
-            const double xmin = std::min({c[0], c[2], c[4], c[6]}), xmax = std::max({c[0], c[2], c[4], c[6]});
-            const double ymin = std::min({c[1], c[3], c[5], c[7]}), ymax = std::max({c[1], c[3], c[5], c[7]});
-            if (x < xmin - 1e-9 * (1 + std::fabs(xmin)) || x > xmax + 1e-9 * (1 + std::fabs(xmax)) ||
-                y < ymin - 1e-9 * (1 + std::fabs(ymin)) || y > ymax + 1e-9 * (1 + std::fabs(ymax)))
-                continue;
-            if (locate(c, x, y, r, q)) found = k;
-        }
-        if (found < 0) return afail(a, DGSWE_ERR_INVALID, "station %d is outside the mesh", s);
-        a->st_elem.push_back(found);
+        const int64_t k = find_element(forms[m], a->stations[2 * s], a->stations[2 * s + 1], r, q);
+        if (k < 0) return afail(a, DGSWE_ERR_INVALID, "station %d is outside member %d's mesh", s, m);
+        a->st_elem.push_back(t.k0[m] + k);
         for (int i = 0; i < nn; ++i)
-            a->st_w.push_back(lagrange(ops.x, i % ops.n1, r) * lagrange(ops.x, i / ops.n1, q));
+            a->st_w.push_back(lagrange(ops.x, i % n1, r) * lagrange(ops.x, i / n1, q));
     }
     // Manning's n per node, for ∂J/∂n = ∂J/∂(g n²)·2 g n
-    const int64_t nv = f->n_elements * nn;
-    a->friction_g = f->friction_g;
-    if (f->friction == DGSWE_FRICTION_MANNING_NODES)
-        a->manning_n.assign(f->manning_n_nodes, f->manning_n_nodes + nv);
-    else
-        a->manning_n.assign(nv, f->friction == DGSWE_FRICTION_MANNING ? f->manning_n : 0.0);
-    a->n_cond = f->n_boundaries;
-    dgswe_handle* hd = nullptr;
-    const int st = dgswe_create(f, device, &hd);
-    a->h = hd;
-    if (st != DGSWE_OK)
-        return afail(a, st, "%s", hd ? dgswe_last_error(hd) : "create failed");
-    dgswe_handle* h = hd;
-    ACK(cudaSetDevice(h->device));
+    a->friction_g = forms[0].friction_g;
+    a->manning_n.assign((size_t)nv, 0.0);
+    for (int m = 0; m < t.n_members; ++m) {
+        const dgswe_form& f = forms[m];
+        double* o = &a->manning_n[(size_t)t.k0[m] * nn];
+        for (int64_t i = 0; i < t.nvals[m]; ++i)
+            o[i] = f.friction == DGSWE_FRICTION_MANNING_NODES ? f.manning_n_nodes[i]
+                   : f.friction == DGSWE_FRICTION_MANNING       ? f.manning_n
+                                                                : 0.0;
+    }
+    ACK(cudaSetDevice(t.device));
     ACK(cudaEventCreate(&a->e0));
     ACK(cudaEventCreate(&a->e1));
-    const int64_t nf = h->K * 4 * h->n1;
+    const int64_t nf = t.K * 4 * n1;
     // the bed slope's transpose: for node c, each line partner i's
     // ∂(g∇B)_i/∂B_c = g·D[pos_i][pos_c]·w(i, c), with w the forward's metric
     // weight (i's own on an affine element, else the mean of i's and c's)
-    if (h->P.has_bed) {
-        const int n1 = ops.n1;
+    if (t.P->has_bed) {
         std::vector<double> contra(4 * (size_t)nv), gt(4 * (size_t)n1 * nv);
-        std::vector<uint8_t> aff((size_t)h->K);
-        ACK(cudaMemcpy(contra.data(), h->T.contra, contra.size() * sizeof(double), cudaMemcpyDeviceToHost));
-        ACK(cudaMemcpy(aff.data(), h->T.affine, aff.size(), cudaMemcpyDeviceToHost));
+        std::vector<uint8_t> aff((size_t)t.K);
+        ACK(cudaMemcpy(contra.data(), t.T->contra, contra.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        ACK(cudaMemcpy(aff.data(), t.T->affine, aff.size(), cudaMemcpyDeviceToHost));
+        const double g = forms[0].g;
 #pragma omp parallel for schedule(static)
-        for (int64_t k = 0; k < h->K; ++k)
+        for (int64_t k = 0; k < t.K; ++k)
             for (int c = 0; c < nn; ++c)
                 for (int dir = 0; dir < 2; ++dir) {
                     const int line = dir == 0 ? c / n1 : c % n1;
@@ -270,7 +313,7 @@ int dgswe_adjoint_create(const dgswe_form* f, int device, const dgswe_adjoint_co
                         const double* mi = &contra[(k * nn + i) * 4 + 2 * dir];
                         const double wx = aff[k] ? mi[0] : 0.5 * (mi[0] + mc[0]);
                         const double wy = aff[k] ? mi[1] : 0.5 * (mi[1] + mc[1]);
-                        const double gd = f->g * ops.d[pa * n1 + pc];
+                        const double gd = g * ops.d[pa * n1 + pc];
                         double* o = &gt[(((k * nn + c) * 2 + dir) * n1 + pa) * 2];
                         o[0] = gd * wx;
                         o[1] = gd * wy;
@@ -279,7 +322,7 @@ int dgswe_adjoint_create(const dgswe_form* f, int device, const dgswe_adjoint_co
         double* d_gt = nullptr;
         if (int s = dalloc(a, gt.size(), &d_gt)) return s;
         ACK(cudaMemcpy(d_gt, gt.data(), gt.size() * sizeof(double), cudaMemcpyHostToDevice));
-        h->T.gdb_t = d_gt;
+        t.T->gdb_t = d_gt;
     }
     const int n_st = cfg->n_stations;
     std::vector<int64_t> node0(n_st);
@@ -292,7 +335,7 @@ int dgswe_adjoint_create(const dgswe_form* f, int device, const dgswe_adjoint_co
         ACK(cudaMemcpy(a->d_w, a->st_w.data(), a->st_w.size() * sizeof(double), cudaMemcpyHostToDevice));
     }
     const int64_t N = cfg->n_steps;
-    if ((s = dalloc(a, 3 * (size_t)N, &a->d_args))) return s;
+    if ((s = dalloc(a, 3 * (size_t)N * t.n_members, &a->d_args))) return s;
     if ((s = dalloc(a, (size_t)N * n_st, &a->d_eta))) return s;
     if ((s = dalloc(a, (size_t)N * n_st, &a->d_obs))) return s;
     for (int b = 0; b < 4; ++b)
@@ -324,7 +367,7 @@ int dgswe_adjoint_create(const dgswe_form* f, int device, const dgswe_adjoint_co
     A.lf_hv = p + 2 * nf;
     if ((s = dalloc(a, (size_t)nv, &A.lbed))) return s;
     if ((s = dalloc(a, (size_t)nv, &A.lgn2))) return s;
-    if ((s = dalloc(a, (size_t)std::max(1, a->n_cond) * 2 * kMaxConstituents, &A.ltide))) return s;
+    if ((s = dalloc(a, (size_t)std::max(1, t.n_cond) * 2 * kMaxConstituents, &A.ltide))) return s;
     A.lb_h = a->lam_b[0];
     A.lb_hu = a->lam_b[1];
     A.lb_hv = a->lam_b[2];
@@ -340,9 +383,9 @@ int dgswe_adjoint_create(const dgswe_form* f, int device, const dgswe_adjoint_co
     int64_t stride = 1;
     if ((double)N * sb > budget) {
         stride = 0;
-        for (int64_t t = 2; t <= N; ++t)
-            if ((double)((N + t - 1) / t + t) * sb <= budget) {
-                stride = t;
+        for (int64_t st = 2; st <= N; ++st)
+            if ((double)((N + st - 1) / st + st) * sb <= budget) {
+                stride = st;
                 break;
             }
         if (stride == 0)
@@ -360,74 +403,221 @@ int dgswe_adjoint_create(const dgswe_form* f, int device, const dgswe_adjoint_co
     return DGSWE_OK;
 }
 
+int check_config(dgswe_adjoint* a, const dgswe_form* forms, int n, const dgswe_adjoint_config* cfg) {
+    if (!cfg) return afail(a, DGSWE_ERR_INVALID, "no configuration");
+    for (int m = 0; m < n; ++m) {
+        std::string why;
+        if (int s = check_form(&forms[m], why)) return afail(a, s, "member %d: %s", m, why.c_str());
+        if (forms[m].formulation != DGSWE_WET_DRY)
+            return afail(a, DGSWE_ERR_UNSUPPORTED, "the adjoint covers the WetDry formulation");
+        if (forms[m].order != forms[0].order)
+            return afail(a, DGSWE_ERR_UNSUPPORTED, "an adjoint ensemble has members of one order");
+    }
+    if (cfg->scheme != DGSWE_SSP_RK3)
+        return afail(a, DGSWE_ERR_UNSUPPORTED, "the adjoint covers SSP-RK3");
+    if (cfg->n_steps <= 0 || cfg->n_stations < 0 || (cfg->n_stations > 0 && !cfg->stations))
+        return afail(a, DGSWE_ERR_INVALID, "steps and stations");
+    a->cfg = *cfg;
+    a->stations.assign(cfg->stations, cfg->stations + 2 * (size_t)cfg->n_stations);
+    a->cfg.stations = nullptr;
+    a->st_member.assign((size_t)cfg->n_stations, 0);
+    if (cfg->station_member) {
+        for (int s = 0; s < cfg->n_stations; ++s) {
+            if (cfg->station_member[s] < 0 || cfg->station_member[s] >= n)
+                return afail(a, DGSWE_ERR_INVALID, "station %d's member", s);
+            a->st_member[s] = cfg->station_member[s];
+        }
+    }
+    a->cfg.station_member = nullptr;
+    return DGSWE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dgswe_adjoint_create(const dgswe_form* f, int device, const dgswe_adjoint_config* cfg,
+                         dgswe_adjoint** out) {
+    if (!out) return DGSWE_ERR_INVALID;
+    auto* a = new dgswe_adjoint();
+    *out = a;
+    if (int s = check_config(a, f, 1, cfg)) return s;
+    dgswe_handle* hd = nullptr;
+    const int st = dgswe_create(f, device, &hd);
+    a->h = hd;
+    if (st != DGSWE_OK) return afail(a, st, "%s", hd ? dgswe_last_error(hd) : "create failed");
+    dgswe_handle* h = hd;
+    Target& t = a->tg;
+    t.device = h->device;
+    t.stream = h->stream;
+    t.ks = h->ks;
+    t.T = &h->T;
+    t.P = &h->P;
+    t.X = &h->X;
+    t.ctl = h->ctl;
+    t.n_members = 1;
+    t.fb_h = h->fb_h;
+    t.fb_hu = h->fb_hu;
+    t.fb_hv = h->fb_hv;
+    t.state = h->buf[DGSWE_STATE].view;
+    t.K = h->K;
+    t.nv = h->n_values;
+    t.n1 = h->n1;
+    t.nn = h->nn;
+    t.order = f->order;
+    t.form0 = h->form;
+    t.k0 = {0};
+    t.nvals = {h->n_values};
+    t.cond0 = {0};
+    t.ncond = {f->n_boundaries};
+    t.n_cond = f->n_boundaries;
+    t.cond_host = &h->P;
+    t.g_n2 = const_cast<double*>(h->T.g_n2);
+    return setup(a, f, cfg);
+}
+
+int dgswe_adjoint_create_ensemble(const dgswe_form* forms, int n_members, int device,
+                                  const dgswe_adjoint_config* cfg, dgswe_adjoint** out) {
+    if (!out) return DGSWE_ERR_INVALID;
+    auto* a = new dgswe_adjoint();
+    *out = a;
+    if (!forms || n_members <= 0) return afail(a, DGSWE_ERR_INVALID, "no members");
+    if (int s = check_config(a, forms, n_members, cfg)) return s;
+    dgswe_ensemble* e = nullptr;
+    const int st = dgswe_ensemble_create(forms, n_members, device, &e);
+    a->ens = e;
+    if (st != DGSWE_OK)
+        return afail(a, st, "%s", e ? dgswe_ensemble_last_error(e) : "ensemble create failed");
+    if (e->groups.size() != 1) return afail(a, DGSWE_ERR_UNSUPPORTED, "one order per ensemble");
+    Group& G = e->groups[0];
+    Target& t = a->tg;
+    t.device = e->device;
+    t.stream = e->stream;
+    t.ks = e->ks;
+    t.T = &G.T;
+    t.P = &G.P;
+    t.X = &G.X;
+    t.ctl = e->ctl;
+    t.n_members = n_members;
+    t.fb_h = G.fb_h;
+    t.fb_hu = G.fb_hu;
+    t.fb_hv = G.fb_hv;
+    t.state = G.buf[DGSWE_STATE];
+    t.K = G.K;
+    t.nv = G.n_values;
+    t.n1 = G.n1;
+    t.nn = G.nn;
+    t.order = forms[0].order;
+    t.form0 = e->form0;
+    t.form0.order = forms[0].order;
+    for (int m = 0; m < n_members; ++m) {
+        t.k0.push_back(e->members[m].k0);
+        t.nvals.push_back(e->members[m].n_values);
+        t.cond0.push_back(e->cond_base[m]);
+        t.ncond.push_back(forms[m].n_boundaries);
+        t.n_cond += forms[m].n_boundaries;
+    }
+    t.cond_dev = const_cast<Condition*>(G.T.cond);
+    t.g_n2 = const_cast<double*>(G.T.g_n2);
+    return setup(a, forms, cfg);
+}
+
 void dgswe_adjoint_destroy(dgswe_adjoint* a) { delete a; }
 
 const char* dgswe_adjoint_last_error(const dgswe_adjoint* a) { return a ? a->error.c_str() : ""; }
 
-int64_t dgswe_adjoint_n_values(const dgswe_adjoint* a) { return a && a->h ? a->h->n_values : 0; }
+int64_t dgswe_adjoint_n_values(const dgswe_adjoint* a) { return a ? a->tg.nv : 0; }
+
+int64_t dgswe_adjoint_member_offset(const dgswe_adjoint* a, int member) {
+    if (!a || member < 0 || member >= a->tg.n_members) return -1;
+    return a->tg.k0[member] * a->tg.nn;
+}
 
 int dgswe_adjoint_stations(const dgswe_adjoint* a, int64_t* element, double* weights) {
-    if (!a || !a->h) return DGSWE_ERR_INVALID;
-    const size_t n = a->st_elem.size();
+    if (!a || (!a->h && !a->ens)) return DGSWE_ERR_INVALID;
     if (element) std::copy(a->st_elem.begin(), a->st_elem.end(), element);
     if (weights) std::copy(a->st_w.begin(), a->st_w.end(), weights);
-    (void)n;
     return DGSWE_OK;
 }
 
 int dgswe_adjoint_forward(dgswe_adjoint* a, const double* h0, const double* hu0, const double* hv0,
                           const double* dts, const double* eta_obs, double* eta_out,
                           double* dts_out, double* J) {
-    if (!a || !a->h) return DGSWE_ERR_INVALID;
-    dgswe_handle* h = a->h;
-    ACK(cudaSetDevice(h->device));
-    const int64_t nv = h->n_values, N = a->cfg.n_steps;
-    const int n_st = a->cfg.n_stations, nn = h->nn;
-    cudaStream_t st = h->stream;
-    if (int s = dgswe_upload(h, DGSWE_STATE, h0, hu0, hv0, nv)) return afail(a, s, "%s", h->error.c_str());
+    if (!a || (!a->h && !a->ens)) return DGSWE_ERR_INVALID;
+    if (!h0 || !hu0 || !hv0) return afail(a, DGSWE_ERR_INVALID, "no initial state");
+    Target& t = a->tg;
+    ACK(cudaSetDevice(t.device));
+    const int64_t nv = t.nv, N = a->cfg.n_steps;
+    const int n_st = a->cfg.n_stations, nn = t.nn, M = t.n_members;
+    cudaStream_t st = t.stream;
+    const size_t bv = (size_t)nv * sizeof(double);
+    ACK(cudaMemcpyAsync(t.state.h, h0, bv, cudaMemcpyDefault, st));
+    ACK(cudaMemcpyAsync(t.state.hu, hu0, bv, cudaMemcpyDefault, st));
+    ACK(cudaMemcpyAsync(t.state.hv, hv0, bv, cudaMemcpyDefault, st));
     if (n_st)
-        ACK(eta_obs ? cudaMemcpy(a->d_obs, eta_obs, (size_t)N * n_st * sizeof(double), cudaMemcpyHostToDevice)
-                    : cudaMemset(a->d_obs, 0, (size_t)N * n_st * sizeof(double)));
-    // the run's clock (CFL steps) or the given steps' stage weights
-    dgswe_run_config run{};
-    run.scheme = DGSWE_SSP_RK3;
-    run.cfl = a->cfg.cfl > 0.0 ? a->cfg.cfl : 0.5;
-    run.t_start = a->cfg.t_start;
-    run.t_end = INFINITY;
-    if (int s = begin_run(h, &run, INFINITY)) return afail(a, s, "%s", h->error.c_str());
+        ACK(eta_obs ? cudaMemcpyAsync(a->d_obs, eta_obs, (size_t)N * n_st * sizeof(double),
+                                      cudaMemcpyDefault, st)
+                    : cudaMemsetAsync(a->d_obs, 0, (size_t)N * n_st * sizeof(double), st));
+    // every member's clock (CFL steps), or the given steps' stage weights
     double sc[4][4];
-    scheme_table(DGSWE_SSP_RK3, sc);
-    if (dts) {
-        std::vector<StageArgs> args(3 * (size_t)N);
-        double t = a->cfg.t_start;
-        for (int64_t n = 0; n < N; ++n) {
-            for (int s = 0; s < 3; ++s)
-                args[3 * n + s] = StageArgs{t + sc[s][3] * dts[n], sc[s][0], sc[s][1],
-                                            sc[s][2] * dts[n], 1.0, 0.0};
-            t += dts[n];
+    const int n_stages = scheme_table(DGSWE_SSP_RK3, sc);
+    const double cfl = a->cfg.cfl > 0.0 ? a->cfg.cfl : 0.5;
+    std::vector<StepCtl> c0((size_t)M);
+    for (int m = 0; m < M; ++m) {
+        StepCtl& c = c0[m];
+        std::memset(&c, 0, sizeof c);
+        c.t = a->cfg.t_start;
+        c.t_end = INFINITY;
+        c.target = INFINITY;
+        c.cfl = cfl;
+        c.dt_min_used = INFINITY;
+        c.dt_bits = 0x7FF0000000000000ull;
+        c.always = 1;
+        c.active = 1;
+        c.scheme_stages = n_stages;
+        for (int s = 0; s < n_stages; ++s) {
+            c.st_start[s] = sc[s][0];
+            c.st_input[s] = sc[s][1];
+            c.st_beta[s] = sc[s][2];
+            c.st_c[s] = sc[s][3];
         }
-        ACK(cudaMemcpy(a->d_args, args.data(), args.size() * sizeof(StageArgs), cudaMemcpyHostToDevice));
     }
-    const DtParams D = dt_params(h->form, run.cfl, DGSWE_SSP_RK3);
-    DevBuf q = h->buf[DGSWE_STATE].view;
+    ACK(cudaMemcpyAsync(t.ctl, c0.data(), c0.size() * sizeof(StepCtl), cudaMemcpyHostToDevice, st));
+    t.ks->velocity(t.state, nv, t.P->h_min, st);
+    if (dts) {  // dts[n][m]
+        std::vector<StageArgs> args(3 * (size_t)N * M);
+        for (int m = 0; m < M; ++m) {
+            double tm = a->cfg.t_start;
+            for (int64_t n = 0; n < N; ++n) {
+                const double dt = dts[n * M + m];
+                for (int s = 0; s < 3; ++s)
+                    args[(n * M + m) * 3 + s] =
+                        StageArgs{tm + sc[s][3] * dt, sc[s][0], sc[s][1], sc[s][2] * dt, 1.0, 0.0};
+                tm += dt;
+            }
+        }
+        ACK(cudaMemcpyAsync(a->d_args, args.data(), args.size() * sizeof(StageArgs),
+                            cudaMemcpyHostToDevice, st));
+        ACK(cudaStreamSynchronize(st));  // `args` is pageable and goes out of scope
+    }
+    const DtParams D = dt_params(t.form0, cfl, DGSWE_SSP_RK3);
+    DevBuf q = t.state;
     const auto wall0 = std::chrono::steady_clock::now();
     ACK(cudaEventRecord(a->e0, st));
     for (int64_t n = 0; n < N; ++n) {
         if (n % a->stride == 0)
             if (int s = pack(a, a->d_ckpt + (n / a->stride) * 3 * nv, q, nv, st)) return s;
         if (dts) {
-            ACK(cudaMemcpyAsync(h->ctl->stage, a->d_args + 3 * n, 3 * sizeof(StageArgs),
-                                cudaMemcpyDeviceToDevice, st));
+            if (int s = args_to_ctl(a, n)) return s;
         } else {
-            h->ks->step_begin(h->ctl, 1, st);
-            h->ks->dt(h->n1, h->T, h->P, q, D, nullptr, h->ctl, &h->ctl->active, st);
-            h->ks->step_dt(h->ctl, 1, st);
-            ACK(cudaMemcpyAsync(a->d_args + 3 * n, h->ctl->stage, 3 * sizeof(StageArgs),
-                                cudaMemcpyDeviceToDevice, st));
+            t.ks->step_begin(t.ctl, M, st);
+            t.ks->dt(t.n1, *t.T, *t.P, q, D, nullptr, t.ctl, &t.ctl[0].always, st);
+            t.ks->step_dt(t.ctl, M, st);
+            if (int s = ctl_to_args(a, n)) return s;
         }
-        forward_step(a, q, st);
-        if (!dts) h->ks->step_end(h->ctl, 1, st);
-        h->ks->station_eval(q.h, h->T.bed, a->d_node0, a->d_w, n_st, nn, a->d_eta + n * n_st, st);
+        forward_step(a, q);
+        if (!dts) t.ks->step_end(t.ctl, M, st);
+        t.ks->station_eval(q.h, t.T->bed, a->d_node0, a->d_w, n_st, nn, a->d_eta + n * n_st, st);
     }
     ACK(cudaEventRecord(a->e1, st));
     ACK(cudaStreamSynchronize(st));
@@ -437,37 +627,52 @@ int dgswe_adjoint_forward(dgswe_adjoint* a, const double* h0, const double* hu0,
     a->stats.forward_ms = ms;
     a->stats.forward_wall_s =
         std::chrono::duration<double>(std::chrono::steady_clock::now() - wall0).count();
-    StepCtl c{};
-    ACK(cudaMemcpy(&c, h->ctl, sizeof c, cudaMemcpyDeviceToHost));
-    if (c.nonfinite) return afail(a, DGSWE_ERR_NONFINITE, "the forward state is not finite");
+    ACK(cudaMemcpy(c0.data(), t.ctl, c0.size() * sizeof(StepCtl), cudaMemcpyDeviceToHost));
+    for (int m = 0; m < M; ++m)
+        if (c0[m].nonfinite)
+            return afail(a, DGSWE_ERR_NONFINITE, "member %d's forward state is not finite", m);
     std::vector<double> eta((size_t)N * n_st), obs((size_t)N * n_st, 0.0);
     if (n_st) {
         ACK(cudaMemcpy(eta.data(), a->d_eta, eta.size() * sizeof(double), cudaMemcpyDeviceToHost));
         if (eta_obs) std::copy(eta_obs, eta_obs + obs.size(), obs.begin());
     }
+    a->J_member.assign((size_t)M, 0.0);
     double j = 0.0;
-    for (size_t m = 0; m < eta.size(); ++m) j += (eta[m] - obs[m]) * (eta[m] - obs[m]);
+    for (int64_t n = 0; n < N; ++n)
+        for (int s = 0; s < n_st; ++s) {
+            const size_t i = (size_t)n * n_st + s;
+            const double r = (eta[i] - obs[i]) * (eta[i] - obs[i]);
+            j += r;
+            a->J_member[a->st_member[s]] += r;
+        }
     a->stats.J = j;
     if (J) *J = j;
     if (eta_out) std::copy(eta.begin(), eta.end(), eta_out);
     if (dts_out) {
-        std::vector<StageArgs> args(3 * (size_t)N);
+        std::vector<StageArgs> args(3 * (size_t)N * M);
         ACK(cudaMemcpy(args.data(), a->d_args, args.size() * sizeof(StageArgs), cudaMemcpyDeviceToHost));
-        for (int64_t n = 0; n < N; ++n) dts_out[n] = args[3 * n].c / sc[0][2];
+        for (int64_t n = 0; n < N; ++n)
+            for (int m = 0; m < M; ++m) dts_out[n * M + m] = args[(n * M + m) * 3].c / sc[0][2];
     }
     a->forward_done = true;
     return DGSWE_OK;
 }
 
+int dgswe_adjoint_member_misfit(const dgswe_adjoint* a, double* J) {
+    if (!a || !J || !a->forward_done) return DGSWE_ERR_INVALID;
+    std::copy(a->J_member.begin(), a->J_member.end(), J);
+    return DGSWE_OK;
+}
+
 int dgswe_adjoint_reverse(dgswe_adjoint* a, double* grad_h0, double* grad_hu0, double* grad_hv0,
                           double* grad_bed, double* grad_manning, double* grad_tide) {
-    if (!a || !a->h) return DGSWE_ERR_INVALID;
+    if (!a || (!a->h && !a->ens)) return DGSWE_ERR_INVALID;
     if (!a->forward_done) return afail(a, DGSWE_ERR_INVALID, "run dgswe_adjoint_forward first");
-    dgswe_handle* h = a->h;
-    ACK(cudaSetDevice(h->device));
-    const int64_t nv = h->n_values, N = a->cfg.n_steps, nf = h->K * 4 * h->n1;
-    const int n_st = a->cfg.n_stations, nn = h->nn;
-    cudaStream_t st = h->stream;
+    Target& t = a->tg;
+    ACK(cudaSetDevice(t.device));
+    const int64_t nv = t.nv, N = a->cfg.n_steps;
+    const int n_st = a->cfg.n_stations, nn = t.nn;
+    cudaStream_t st = t.stream;
     const size_t bv = (size_t)nv * sizeof(double);
     for (int c = 0; c < 3; ++c) {
         ACK(cudaMemsetAsync(a->lam[c], 0, bv, st));
@@ -477,9 +682,9 @@ int dgswe_adjoint_reverse(dgswe_adjoint* a, double* grad_h0, double* grad_hu0, d
     ACK(cudaMemsetAsync(A.lx_h, 0, 5 * bv, st));
     ACK(cudaMemsetAsync(A.lbed, 0, bv, st));
     ACK(cudaMemsetAsync(A.lgn2, 0, bv, st));
-    ACK(cudaMemsetAsync(A.ltide, 0, (size_t)std::max(1, a->n_cond) * 2 * kMaxConstituents * sizeof(double), st));
-    (void)nf;
-    const int* on = &h->ctl->always;
+    ACK(cudaMemsetAsync(A.ltide, 0,
+                        (size_t)std::max(1, t.n_cond) * 2 * kMaxConstituents * sizeof(double), st));
+    const int* on = &t.ctl[0].always;
     const auto wall0 = std::chrono::steady_clock::now();
     ACK(cudaEventRecord(a->e0, st));
     int64_t recomputed = 0;
@@ -489,30 +694,28 @@ int dgswe_adjoint_reverse(dgswe_adjoint* a, double* grad_h0, double* grad_hu0, d
         const double* ck = a->d_ckpt + (c0 / a->stride) * 3 * nv;
         if (a->stride > 1) {  // the segment's step-start states, recomputed from its checkpoint
             if (int s = unpack(a, q, ck, nv, st)) return s;
-            h->ks->velocity(q, nv, h->P.h_min, st);
+            t.ks->velocity(q, nv, t.P->h_min, st);
             for (int64_t n = c0; n < c1; ++n) {
                 if (int s = pack(a, a->d_seg + (n - c0) * 3 * nv, q, nv, st)) return s;
                 if (n + 1 == c1) break;  // the last step is recomputed below
-                ACK(cudaMemcpyAsync(h->ctl->stage, a->d_args + 3 * n, 3 * sizeof(StageArgs),
-                                    cudaMemcpyDeviceToDevice, st));
-                forward_step(a, q, st);
+                if (int s = args_to_ctl(a, n)) return s;
+                forward_step(a, q);
                 recomputed += 1;
             }
         }
         for (int64_t n = c1 - 1; n >= c0; --n) {
             // J's dependence on q_{n+1}
-            h->ks->station_seed(a->d_eta + n * n_st, a->d_obs + n * n_st, a->d_node0, a->d_w, n_st,
-                                nn, a->lam[0], h->P.has_bed ? A.lbed : nullptr, st);
+            t.ks->station_seed(a->d_eta + n * n_st, a->d_obs + n * n_st, a->d_node0, a->d_w, n_st,
+                               nn, a->lam[0], t.P->has_bed ? A.lbed : nullptr, st);
             // the step's start state and its stages, recomputed with what the reverse keeps
             const double* q0 = a->stride > 1 ? a->d_seg + (n - c0) * 3 * nv : ck;
             if (int s = unpack(a, q, q0, nv, st)) return s;
-            h->ks->velocity(q, nv, h->P.h_min, st);
-            ACK(cudaMemcpyAsync(h->ctl->stage, a->d_args + 3 * n, 3 * sizeof(StageArgs),
-                                cudaMemcpyDeviceToDevice, st));
+            t.ks->velocity(q, nv, t.P->h_min, st);
+            if (int s = args_to_ctl(a, n)) return s;
             for (int s = 0; s < 3; ++s) {
-                h->ks->face(h->n1, h->T, h->P, a->S[s], h->fb_h, h->fb_hu, h->fb_hv, h->ctl, s, on, st);
-                h->ks->stage_keep(h->n1, h->T, h->P, h->X, a->S[s], q, a->S[s + 1], h->fb_h,
-                                  h->fb_hu, h->fb_hv, h->ctl, s, 0, a->Kp[s], st);
+                t.ks->face(t.n1, *t.T, *t.P, a->S[s], t.fb_h, t.fb_hu, t.fb_hv, t.ctl, s, on, st);
+                t.ks->stage_keep(t.n1, *t.T, *t.P, *t.X, a->S[s], q, a->S[s + 1], t.fb_h, t.fb_hu,
+                                 t.fb_hv, t.ctl, s, 0, a->Kp[s], st);
             }
             // the stages reversed: λ of each stage's input from λ of its output
             for (int s = 2; s >= 0; --s) {
@@ -521,10 +724,10 @@ int dgswe_adjoint_reverse(dgswe_adjoint* a, double* grad_h0, double* grad_hu0, d
                 As.lo_h = lo[0];
                 As.lo_hu = lo[1];
                 As.lo_hv = lo[2];
-                h->ks->stage_adjoint(h->n1, h->T, h->P, h->X, a->S[s], a->Kp[s], As, h->ctl, s, st);
-                h->ks->face_adjoint(h->n1, h->T, h->P, a->S[s], As, h->ctl, s, st);
-                h->ks->adjoint_combine(a->S[s], As, a->lam_t[0], a->lam_t[1], a->lam_t[2], nv,
-                                       h->P.h_min, st);
+                t.ks->stage_adjoint(t.n1, *t.T, *t.P, *t.X, a->S[s], a->Kp[s], As, t.ctl, s, st);
+                t.ks->face_adjoint(t.n1, *t.T, *t.P, a->S[s], As, t.ctl, s, st);
+                t.ks->adjoint_combine(a->S[s], As, a->lam_t[0], a->lam_t[1], a->lam_t[2], nv,
+                                      t.P->h_min, st);
             }
             // λ of q_n: the first stage's input plus the three stages' base terms
             for (int c = 0; c < 3; ++c)
@@ -551,9 +754,50 @@ int dgswe_adjoint_reverse(dgswe_adjoint* a, double* grad_h0, double* grad_hu0, d
         ACK(cudaMemcpy(grad_manning, A.lgn2, bv, cudaMemcpyDeviceToHost));
         for (int64_t i = 0; i < nv; ++i) grad_manning[i] *= 2.0 * a->friction_g * a->manning_n[i];
     }
-    if (grad_tide && a->n_cond > 0)
-        ACK(cudaMemcpy(grad_tide, A.ltide, (size_t)a->n_cond * 2 * kMaxConstituents * sizeof(double),
+    if (grad_tide && t.n_cond > 0)
+        ACK(cudaMemcpy(grad_tide, A.ltide, (size_t)t.n_cond * 2 * kMaxConstituents * sizeof(double),
                        cudaMemcpyDeviceToHost));
+    return DGSWE_OK;
+}
+
+int dgswe_adjoint_set_parameters(dgswe_adjoint* a, const double* manning_n, const double* tide) {
+    if (!a || (!a->h && !a->ens)) return DGSWE_ERR_INVALID;
+    Target& t = a->tg;
+    ACK(cudaSetDevice(t.device));
+    if (manning_n) {
+        if (!t.g_n2)
+            return afail(a, DGSWE_ERR_UNSUPPORTED,
+                         "Manning's n per node needs a per-node friction field (DGSWE_FRICTION_MANNING_NODES)");
+        std::vector<double> gn2((size_t)t.nv);
+        for (int64_t i = 0; i < t.nv; ++i) {
+            if (!(manning_n[i] >= 0.0) || !std::isfinite(manning_n[i]))
+                return afail(a, DGSWE_ERR_INVALID, "Manning's n at node %lld", (long long)i);
+            gn2[i] = a->friction_g * manning_n[i] * manning_n[i];
+        }
+        ACK(cudaMemcpy(t.g_n2, gn2.data(), gn2.size() * sizeof(double), cudaMemcpyHostToDevice));
+        a->manning_n.assign(manning_n, manning_n + t.nv);
+    }
+    if (tide && t.n_cond > 0) {
+        std::vector<Condition> c((size_t)t.n_cond);
+        if (t.cond_dev)
+            ACK(cudaMemcpy(c.data(), t.cond_dev, c.size() * sizeof(Condition), cudaMemcpyDeviceToHost));
+        else
+            std::copy(t.cond_host->cond, t.cond_host->cond + t.n_cond, c.begin());
+        for (int ci = 0; ci < t.n_cond; ++ci)
+            for (int i = 0; i < c[ci].n_constituents; ++i) {
+                const double amp = tide[((size_t)ci * kMaxConstituents + i) * 2];
+                const double ph = tide[((size_t)ci * kMaxConstituents + i) * 2 + 1];
+                if (!std::isfinite(amp) || !std::isfinite(ph))
+                    return afail(a, DGSWE_ERR_INVALID, "condition %d constituent %d", ci, i);
+                c[ci].c[i].amplitude = amp;
+                c[ci].c[i].phase = ph;
+            }
+        if (t.cond_dev)
+            ACK(cudaMemcpy(t.cond_dev, c.data(), c.size() * sizeof(Condition), cudaMemcpyHostToDevice));
+        else
+            std::copy(c.begin(), c.end(), t.cond_host->cond);
+    }
+    a->forward_done = false;
     return DGSWE_OK;
 }
 

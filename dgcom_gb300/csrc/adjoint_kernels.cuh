@@ -110,7 +110,8 @@ __global__ void __launch_bounds__(AdjCfg<N1>::THREADS, AdjCfg<N1>::MIN_BLOCKS)
     __syncthreads();
     const bool sub = s_flag[e][0] != 0;
     const bool affine = valid ? T.affine[k] != 0 : true;
-    const StageArgs sa = ctl->stage[slot];
+    // the element's member's stage weights (an ensemble: one StepCtl each)
+    const StageArgs sa = ctl[(T.elem_member && valid) ? T.elem_member[k] : 0].stage[slot];
 
     // λ of this node's input values (registers)
     double Lh = 0, Lhu = 0, Lhv = 0, Lu = 0, Lv = 0, Lb = 0;
@@ -678,7 +679,7 @@ __global__ void __launch_bounds__(256)
     const double* geo = &T.bface_geo[bfi * 5];
     const double nx = geo[0], ny = geo[1];
     const int ci = T.bface_cond[bfi];
-    const Condition& c = P.cond[ci];
+    const Condition& c = T.cond ? T.cond[ci] : P.cond[ci];
     const int64_t sl = B * N1 + fi;
     const F3 lfs{A.lf_h[sl], A.lf_hu[sl], A.lf_hv[sl]};
     double u, v;
@@ -694,7 +695,7 @@ __global__ void __launch_bounds__(256)
         wall_ghost_rev(qi, u, v, nx, ny, c.wall_h_min, h_min, qe, qeb, qib, ub, vb);
         add(gn, qib.h, qib.hu, qib.hv, ub, vb, qib.b);
     } else {
-        const double t = ctl->stage[slot].time;
+        const double t = ctl[T.elem_member ? T.elem_member[k] : 0].stage[slot].time;
         const double eta = tide_elevation(c, t);
         const Q qb = characteristic_state(qi, u, v, eta, nx, ny, c.elevation_only, g, h_min);
         Q qbb{};

@@ -26,65 +26,13 @@
 
 #include "../../include/dgswe.h"
 #include "device.hpp"
+#include "ensemble_internal.hpp"
 #include "host_common.hpp"
 #include "kernel_set.hpp"
 #include "setup.hpp"
 
 using namespace dgswe;
-
-namespace {
-
-constexpr int kEnsBuffers = 4;  // state and the stage outputs of SSP-RK(4,3)
-
-struct Group {
-    int n1 = 0, nn = 0;
-    int64_t K = 0, n_values = 0;
-    Operators* ops = nullptr;
-    DevTables T{};
-    Physics P{};
-    StageExtra X{};
-    double* buf_base[kEnsBuffers] = {};
-    DevBuf buf[kEnsBuffers]{};
-    double *fb_h = nullptr, *fb_hu = nullptr, *fb_hv = nullptr;
-    std::vector<int> members;
-};
-
-struct Member {
-    int group = -1;
-    int64_t k0 = 0, K = 0, node0 = 0, n_values = 0;
-};
-
-}  // namespace
-
-struct dgswe_ensemble {
-    int device = 0;
-    cudaStream_t stream = nullptr, side = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr, t0 = nullptr, t1 = nullptr;
-    std::string error, device_name;
-    dgswe_form form0{};  // the shared physics (array pointers cleared)
-    const KernelSet* ks = nullptr;
-    int n_members = 0;
-    std::vector<Member> members;
-    std::vector<Group> groups;
-    StepCtl* ctl = nullptr;    // device, one per member
-    StepCtl* h_ctl = nullptr;  // pinned host mirror
-    int* always = nullptr;     // device 1: the launches' activity flag
-    std::vector<void*> allocations;
-    cudaGraphExec_t graph = nullptr;
-    int graph_scheme = -1;
-    double graph_cfl = -1.0;
-
-    ~dgswe_ensemble() {
-        if (graph) cudaGraphExecDestroy(graph);
-        for (void* p : allocations) cudaFree(p);
-        if (h_ctl) cudaFreeHost(h_ctl);
-        for (cudaEvent_t e : {fork, join, t0, t1})
-            if (e) cudaEventDestroy(e);
-        if (side) cudaStreamDestroy(side);
-        if (stream) cudaStreamDestroy(stream);
-        for (Group& g : groups) delete g.ops;
-    }
-};
+using namespace dgswe::host;
 
 namespace {
 
@@ -299,6 +247,7 @@ int create_impl(dgswe_ensemble* h, const dgswe_form* forms, int n, int device) {
         for (int b = 0; b < forms[m].n_boundaries; ++b)
             conds.push_back(make_condition(forms[m].boundaries[b]));
     }
+    h->cond_base = cond_base;
     // order groups, members in the caller's order within each
     for (int order = 1; order <= 4; ++order) {
         std::vector<int> ms;

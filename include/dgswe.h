@@ -423,6 +423,8 @@ typedef struct dgswe_adjoint_config {
     int32_t n_stations;
     const double* stations;   /* [n_stations][2] x, y; copied */
     double memory_budget;     /* bytes of HBM for stored states; ≤ 0: free memory − 2 GiB */
+    const int32_t* station_member; /* [n_stations] each station's member (an ensemble's
+                                      adjoint); NULL: member 0 */
 } dgswe_adjoint_config;
 
 typedef struct dgswe_adjoint_stats {
@@ -441,13 +443,29 @@ typedef struct dgswe_adjoint_stats {
  * set even on failure; destroy it either way. */
 int dgswe_adjoint_create(const dgswe_form* form, int device, const dgswe_adjoint_config* config,
                          dgswe_adjoint** out);
+/* The adjoint of an ensemble run (dgswe_ensemble_create's members, all of
+ * one order) in one batched sweep: each member takes its own CFL steps (or
+ * given ones) and its stations (config->station_member); J is the sum of
+ * the members' misfits. The state, the initial state and the per-node
+ * gradients are the members' arrays concatenated (member m's first value
+ * at dgswe_adjoint_member_offset(m)); time steps are [N][n_members];
+ * tide gradients are per boundary condition, the members' conditions
+ * concatenated in member order. Each member's gradients equal those of its
+ * own single-mesh adjoint. */
+int dgswe_adjoint_create_ensemble(const dgswe_form* forms, int n_members, int device,
+                                  const dgswe_adjoint_config* config, dgswe_adjoint** out);
+/* Member m's first value in the concatenated arrays (−1: no such member) */
+int64_t dgswe_adjoint_member_offset(const dgswe_adjoint* adjoint, int member);
+/* Each member's part of J from the last forward sweep [n_members] */
+int dgswe_adjoint_member_misfit(const dgswe_adjoint* adjoint, double* J);
 void dgswe_adjoint_destroy(dgswe_adjoint* adjoint);
 const char* dgswe_adjoint_last_error(const dgswe_adjoint* adjoint);
 int64_t dgswe_adjoint_n_values(const dgswe_adjoint* adjoint);
 /* Each station's element and its (order+1)² interpolation weights */
 int dgswe_adjoint_stations(const dgswe_adjoint* adjoint, int64_t* element, double* weights);
 /* The forward sweep from (h0, hu0, hv0): N steps of SSP-RK3 with the given
- * time steps dts[N], or (dts NULL) with the CFL steps, written to dts_out.
+ * time steps dts[N] ([N][n_members] for an ensemble), or (dts NULL) with
+ * the CFL steps, written to dts_out.
  * eta_obs [N][n_stations] (NULL: zero) enters J; eta_out gets the
  * stations' η after each step. Any output may be NULL. */
 int dgswe_adjoint_forward(dgswe_adjoint* adjoint, const double* h0, const double* hu0,
@@ -459,6 +477,15 @@ int dgswe_adjoint_forward(dgswe_adjoint* adjoint, const double* h0, const double
 int dgswe_adjoint_reverse(dgswe_adjoint* adjoint, double* grad_h0, double* grad_hu0,
                           double* grad_hv0, double* grad_bed, double* grad_manning,
                           double* grad_tide);
+/* New parameter values for the next forward sweep, in the gradients'
+ * layout: Manning's n per node [n_values] (the form's friction must be
+ * DGSWE_FRICTION_MANNING_NODES, or any Manning law in an ensemble) and the
+ * tide constituents' (amplitude, phase) [n_conditions][DGSWE_MAX_CONSTITUENTS][2]
+ * (the phase as dgswe_tide_constituent.phase; entries beyond a
+ * condition's n_constituents are ignored). Either may be NULL: unchanged.
+ * A calibration loop calls forward, reverse and this in turn. */
+int dgswe_adjoint_set_parameters(dgswe_adjoint* adjoint, const double* manning_n,
+                                 const double* tide);
 int dgswe_adjoint_get_stats(const dgswe_adjoint* adjoint, dgswe_adjoint_stats* out);
 
 #ifdef __cplusplus
