@@ -246,7 +246,8 @@ def adjoint_ensemble_members(n_members: int = 64, seed: int = 2029,
     meshes and beds), order ``order``, each under the eight constituents of
     ``ADJOINT_TIDE`` scaled by U(0.5, 1.5) with seeded phases, with Manning's
     n per element n₀·(1 + 0.2·GRF), n₀ ~ U(0.015, 0.035) (5 km correlation),
-    and ``n_stations`` stations at least 5 m deep. The observations' forcing
+    and ``n_stations`` stations at least 5 m deep (a sixth of them within
+    3 km of the open side, which the tide reaches first). The observations' forcing
     perturbs each element's n by a factor 1 + 0.1·GRF and each constituent's
     amplitude by 5 % and phase by 3° (normal draws); a forward run under it
     gives the observed η."""
@@ -278,13 +279,20 @@ def adjoint_ensemble_members(n_members: int = 64, seed: int = 2029,
         n_elem = np.maximum(n0[m] * (1.0 + 0.2 * field()), 0.005)
         n_obs = np.maximum(n_elem * (1.0 + 0.1 * field()), 0.005)
         case.form.manning_n = np.repeat(n_elem, nn)
-        # stations in water at least 5 m deep (the member's bed at the point)
-        st = np.zeros((0, 2))
-        while st.shape[0] < n_stations:
-            cand = np.column_stack([mr.uniform(0.02 * lx, 0.98 * lx, 4 * n_stations),
-                                    mr.uniform(0.02 * ly, 0.98 * ly, 4 * n_stations)])
-            bed = coastal_bed(cand[:, 0], cand[:, 1], lx, ly, mseed, n_islands, radius)
-            st = np.vstack([st, cand[bed < -5.0]])
+        # stations in water at least 5 m deep (the member's bed at the point),
+        # a sixth of them within 3 km of the open (western) side
+        def deep(n, x_hi):
+            got = np.zeros((0, 2))
+            while got.shape[0] < n:
+                cand = np.column_stack([mr.uniform(0.02 * lx, x_hi, 4 * n),
+                                        mr.uniform(0.02 * ly, 0.98 * ly, 4 * n)])
+                bed = coastal_bed(cand[:, 0], cand[:, 1], lx, ly, mseed, n_islands, radius)
+                got = np.vstack([got, cand[bed < -5.0]])
+            return got[:n]
+
+        n_near = n_stations // 6
+        st = np.vstack([deep(n_near, min(3_000.0, 0.98 * lx)),
+                        deep(n_stations - n_near, 0.98 * lx)])
         tide_obs = np.zeros((abi.MAX_CONSTITUENTS, 2))
         for i, c in enumerate(bc.constituents):
             tide_obs[i] = (c.amplitude * (1.0 + 0.05 * mr.standard_normal()),

@@ -23,15 +23,20 @@ from dgcom_gb300.physics import TidalBoundary
 pytestmark = pytest.mark.gpu
 
 STEPS = 24
-T_START = 3600.0  # the tide fully ramped
+T_START = 3600.0  # the tide fully ramped; from a flowing state (Manning's n matters)
 
 
 def members(n=3, k_range=(300, 900), n_stations=5):
     ms = cases.adjoint_ensemble_members(n_members=n, k_range=k_range, n_stations=n_stations)
     forms = [m.case.form for m in ms]
-    stations = np.vstack([m.stations for m in ms])
-    member = np.repeat(np.arange(n), [m.stations.shape[0] for m in ms]).astype(np.int32)
-    state = tuple(np.concatenate([m.case.state[c] for m in ms]) for c in range(3))
+    # and one station in the first column of elements, which the tide on the
+    # open (western) side reaches within the run
+    own = [np.vstack([m.stations, [[50.0, 0.5 * f.mesh.vertices[:, 1].max()]]])
+           for m, f in zip(ms, forms)]
+    stations = np.vstack(own)
+    member = np.repeat(np.arange(n), [x.shape[0] for x in own]).astype(np.int32)
+    flows = [cases.with_flow(m.case, eta_amp=0.5, u=0.4, v=-0.15) for m in ms]
+    state = tuple(np.concatenate([f[c] for f in flows]) for c in range(3))
     return ms, forms, stations, member, state
 
 
