@@ -699,6 +699,78 @@ def run_adjoint_ensemble(args, rank: int, world: int, local: int):
     dist.close()
 
 
+def run_multirate(args, rank: int, world: int, local: int):
+    """Local time stepping on the coastal box: the same model span with
+    global SSP-RK3 steps and with multirate coarse steps of up to
+    ``--levels`` levels (dgswe_run with DeviceRun::levels), each timed on
+    the host around the run (the multirate run's level planning, on the
+    host, included), after a warm-up of both. The span starts from a
+    flowing state after the tide's ramp. One GPU: replicas are independent."""
+    from dgcom_gb300 import cases
+    from dgcom_gb300.device import DeviceRun, SWEPhysics2D
+
+    dist = Dist(world, "nccl")
+    case = cases.coastal_box(args.elements, args.order)
+    form = case.form
+    nodes = form.n_values
+    state = cases.with_flow(case, eta_amp=0.5, u=0.4, v=-0.15)
+    t0 = 3600.0
+    span = args.lts_span
+    dev = SWEPhysics2D(form, local)
+
+    def run(levels, t_len):
+        dev.upload(*state)
+        rep = dev.run_with_callback(DeviceRun(span=(t0, t0 + t_len), cfl=case.cfl, levels=levels))
+        if not rep.success:
+            raise RuntimeError(rep.message)
+        return rep
+
+    run(0, 2.0)
+    run(args.levels, 2.0)
+    sampler = ClockSampler(local)
+    dist.barrier()
+    sampler.start()
+    g = run(0, span)
+    g_state = dev.download()
+    m = run(args.levels, span)
+    m_state = dev.download()
+    clocks = sampler.stop()
+    dist.barrier()
+    dev.close()
+    s = m.local_time_stepping
+    b = form.bathymetry.reshape(-1)
+    eta_diff = float(np.abs((m_state[0] + b) - (g_state[0] + b))[m_state[0] > 0.0].max())
+    g_rate = 3.0 * nodes * g.n_steps / g.wall_time
+    if rank == 0:
+        line = {
+            "metric": "local time stepping: model time per wall second against global steps",
+            "value": g.wall_time / m.wall_time, "unit": "speedup", "n_gpus": world,
+            "steps": int(s.steps), "warmup": 1, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"coastal box {form.mesh.n_elements} quads N={args.order}, "
+                                   f"{span:g} s of model time from a flowing state at "
+                                   f"t = {t0:g} s, SSP-RK3, up to {args.levels} levels",
+                       "elements": form.mesh.n_elements, "order": args.order, "nodes": nodes,
+                       "levels": args.levels, "parallelism": f"replicas x{world}"},
+            "global": {"steps": g.n_steps, "wall_s": g.wall_time, "dof_updates_per_s": g_rate,
+                       "dt_min": g.dt_min, "dt_max": g.dt_max},
+            "multirate": {"coarse_steps": int(s.steps), "wall_s": m.wall_time,
+                          "finest_level": int(s.finest_level),
+                          "element_evaluations": int(s.element_evaluations),
+                          "global_evaluations_at_finest": int(s.global_evaluations),
+                          "level_evaluations": s.level_evaluations,
+                          "ideal_evaluations": s.ideal_evaluations,
+                          "line_local_elements_per_step": s.line_local_elements / max(1, s.steps),
+                          "coarse_dt_range": [m.dt_min, m.dt_max]},
+            "evaluations_global_over_multirate":
+                (3.0 * form.mesh.n_elements * g.n_steps) / max(1, s.element_evaluations),
+            "max_eta_difference_m": eta_diff,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -709,11 +781,12 @@ def main():
     ap.add_argument("--order", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="coastal",
-                    choices=["coastal", "ensemble", "adjoint", "adjoint_ensemble"],
+                    choices=["coastal", "ensemble", "adjoint", "adjoint_ensemble", "multirate"],
                     help="coastal: the 1 M-quad coastal box (the headline); ensemble: batched "
                          "members against sequential plain runs; adjoint: the discrete "
                          "adjoint's time against the forward's on the refined channel; "
-                         "adjoint_ensemble: the batched adjoint of coastal-box members")
+                         "adjoint_ensemble: the batched adjoint of coastal-box members; "
+                         "multirate: local time stepping against global steps")
     ap.add_argument("--members", type=int, default=256)
     ap.add_argument("--k-min", type=int, default=5_000)
     ap.add_argument("--k-max", type=int, default=200_000)
@@ -726,6 +799,8 @@ def main():
     ap.add_argument("--adj-k-max", type=int, default=150_000)
     ap.add_argument("--adj-budget-gb", type=float, default=120.0)
     ap.add_argument("--adj-ens-t-start", type=float, default=3600.0)
+    ap.add_argument("--levels", type=int, default=4)
+    ap.add_argument("--lts-span", type=float, default=60.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
@@ -737,6 +812,8 @@ def main():
         run_adjoint(args, rank, world, local)
     elif args.workload == "adjoint_ensemble":
         run_adjoint_ensemble(args, rank, world, local)
+    elif args.workload == "multirate":
+        run_multirate(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)
 

@@ -13,7 +13,7 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 LIBRARY_PATH = HERE / "libdgswe.so"
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 
 # dgswe_status
 OK, ERR_INVALID, ERR_CUDA, ERR_NONFINITE, ERR_DT_MIN, ERR_MAX_STEPS, ERR_STOPPED, \
@@ -97,6 +97,8 @@ class Form(C.Structure):
         ("n_boundaries", C.c_int32),
         ("boundaries", C.POINTER(Boundary)),
         ("numerics", C.c_int32),
+        ("has_line_local", C.c_int32),
+        ("line_local_depth", C.c_double),
     ]
 
 
@@ -127,6 +129,34 @@ class RunConfig(C.Structure):
         ("dt_min", C.c_double),
         ("max_steps", C.c_int64),
         ("stop", C.POINTER(C.c_int32)),
+        ("levels", C.c_int32),
+    ]
+
+
+MAX_LEVELS = 8  # DGSWE_MAX_LEVELS
+
+
+class MultirateStats(C.Structure):
+    _fields_ = [
+        ("steps", C.c_int64),
+        ("element_evaluations", C.c_int64),
+        ("global_evaluations", C.c_int64),
+        ("finest_level", C.c_int32),
+        ("model_seconds", C.c_double),
+        ("ideal_evaluations", C.c_double),
+        ("level_evaluations", C.c_double),
+        ("line_local_elements", C.c_int64),
+    ]
+
+
+class PlanResult(C.Structure):
+    _fields_ = [
+        ("dt", C.c_double),
+        ("stable_step", C.c_double),
+        ("finest", C.c_int32),
+        ("evaluations", C.c_int64),
+        ("level_evaluations", C.c_int64),
+        ("inverse_dt_sum", C.c_double),
     ]
 
 
@@ -227,6 +257,15 @@ CUDA_ONLY = {
     "status_string": (C.c_char_p, [C.c_int]),
     "last_error": (C.c_char_p, [C.c_void_p]),
     "profile_steps": (C.c_int, [C.c_void_p, C.POINTER(RunConfig), C.c_int64, C.POINTER(Profile)]),
+    # local time stepping: the last run's work counts; the level planner (host only)
+    "multirate_stats_get": (C.c_int, [C.c_void_p, C.POINTER(MultirateStats)]),
+    "planner_create": (C.c_int, [C.POINTER(Form), C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    "planner_destroy": (None, [C.c_void_p]),
+    "planner_assign": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_uint8), C.c_double, C.c_double,
+                                 C.POINTER(PlanResult), C.POINTER(C.c_uint8),
+                                 C.POINTER(C.c_uint8), C.POINTER(C.c_int32)]),
+    "planner_spread": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint8), C.c_int32,
+                                 C.POINTER(C.c_uint8), C.POINTER(C.c_uint8)]),
     # device pointers in and out; working memory in the library's own array
     "compute_rhs_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]),

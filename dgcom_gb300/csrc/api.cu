@@ -271,6 +271,17 @@ int create_impl(dgswe_handle* h, const dgswe_form* f, int device) {
     Tables t;
     err = build_tables(*f, ops, topo, tags, cond_index, t);
     if (!err.empty()) return bail(fail(h, DGSWE_ERR_INVALID, "%s", err.c_str()));
+    // what the multirate planner reads: the face neighbours and the edges
+    h->nb.resize(h->K);
+    h->nb_face.resize(h->K);
+    for (int64_t k = 0; k < h->K; ++k)
+        for (int face = 0; face < 4; ++face) {
+            h->nb[k][face] = topo.link[k][face].element;
+            h->nb_face[k][face] = (int8_t)topo.link[k][face].face;
+        }
+    h->h_edge_left = t.edge_left;
+    h->h_edge_right = t.edge_right;
+    h->h_bface = t.bface;
     PairSchedule sched(ops);
     std::vector<int8_t> owned;
     for (const PairSlot& p : sched.owned) {
@@ -536,6 +547,10 @@ int dgswe_run(dgswe_handle* h, const dgswe_run_config* run, dgswe_callback callb
         !(run->t_end >= run->t_start))
         return fail(h, DGSWE_ERR_INVALID, "run: cfl %g, scheme %d, span (%g, %g)", run->cfl,
                     run->scheme, run->t_start, run->t_end);
+    if (run->levels < 0 || run->levels > DGSWE_MAX_LEVELS)
+        return fail(h, DGSWE_ERR_INVALID, "run: %d levels of local time stepping (0..%d)",
+                    run->levels, DGSWE_MAX_LEVELS);
+    if (run->levels > 0) return run_multirate(h, run, callback, user, report);
     std::memset(report, 0, sizeof(*report));
     std::snprintf(report->device, sizeof report->device, "%s", h->device_name.c_str());
     CK(cudaSetDevice(h->device));

@@ -96,6 +96,25 @@ struct StageArgs {
     double time, a, b, c, w, keep;
 };
 
+// One pass of a multirate coarse step on the device: a finest substep's
+// stage over the elements whose stage rate is at least the substep's depth
+// (a prefix of the rate-sorted order), with the faces they read, or the end
+// of the substeps of the elements whose level is at least it. Each element
+// takes its stage from its level (element_stage, src/time/multirate.rs:169-200).
+struct LtsPass {
+    const int32_t* list = nullptr;    // the pass's elements
+    int64_t n = 0;
+    const int32_t* edges = nullptr;   // the interior edges they read
+    int64_t n_edges = 0;
+    const int32_t* bfaces = nullptr;  // and boundary faces
+    int64_t n_bfaces = 0;
+    const uint8_t* level = nullptr;   // [K]
+    const uint8_t* rate = nullptr;    // [K] the stage's rates
+    double t = 0.0, dt = 0.0;         // the coarse step
+    int finest = 0, substep = 0, depth = 0, last = 0;
+    double start = 0.0, input = 0.0, beta = 0.0, c = 0.0;  // the stage's Shu–Osher weights
+};
+
 // Step control (device memory): the run's clock, the step's dt and stage
 // arguments, and the failure flags. Written by the step kernels of a
 // device-driven run or by the host between host-driven calls.

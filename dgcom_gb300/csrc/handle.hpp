@@ -11,6 +11,7 @@
 #include "../../include/dgswe.h"
 #include "device.hpp"
 #include "kernel_set.hpp"
+#include "multirate.hpp"
 #include "setup.hpp"
 
 namespace dgswe {
@@ -56,8 +57,20 @@ struct dgswe_handle {
     cudaGraphExec_t step_graph = nullptr;
     int graph_scheme = -1;
     double graph_cfl = -1.0;
+    // local time stepping: the mesh's face neighbours and the device tables'
+    // edges on the host, the level planner and its plan on the device
+    std::vector<std::array<int64_t, 4>> nb;
+    std::vector<std::array<int8_t, 4>> nb_face;
+    std::vector<int64_t> h_edge_left, h_edge_right, h_bface;
+    dgswe::MultiratePlanner* planner = nullptr;
+    int planner_levels = -1, planner_stages = -1;
+    uint64_t plan_uploaded = 0;
+    uint8_t *d_level = nullptr, *d_rate = nullptr, *d_flags = nullptr;
+    int32_t *d_order = nullptr, *d_edges = nullptr, *d_bfaces = nullptr;
+    dgswe_multirate_stats mr_stats{};
 
     ~dgswe_handle() {
+        delete planner;
         if (step_graph) cudaGraphExecDestroy(step_graph);
         for (void* p : allocations) cudaFree(p);
         if (h_ctl) cudaFreeHost(h_ctl);
@@ -81,6 +94,9 @@ void launch_stage(dgswe_handle* h, int in, int base, int out, int acc, int slot,
 const int* always(dgswe_handle* h);
 // The device clock of a run from run->t_start towards `target`
 int begin_run(dgswe_handle* h, const dgswe_run_config* run, double target);
+// dgswe_run with local time stepping (run->levels > 0; multirate_run.cu)
+int run_multirate(dgswe_handle* h, const dgswe_run_config* run, dgswe_callback callback,
+                  void* user, dgswe_report* report);
 
 }  // namespace host
 }  // namespace dgswe

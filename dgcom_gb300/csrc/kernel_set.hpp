@@ -44,6 +44,20 @@ struct KernelSet {
     void (*step_begin)(StepCtl*, int n, cudaStream_t);
     void (*step_dt)(StepCtl*, int n, cudaStream_t);
     void (*step_end)(StepCtl*, int n, cudaStream_t);
+    // a multirate pass (LtsPass): the listed faces, the listed elements'
+    // stage (mode kModePost, or kModeAccumulate for the last stage), the
+    // end of the listed elements' substeps
+    void (*face_listed)(int n1, const DevTables&, const Physics&, const DevBuf& in, double* fh,
+                        double* fhu, double* fhv, StepCtl* ctl, const LtsPass&, cudaStream_t);
+    void (*stage_listed)(int n1, const DevTables&, const Physics&, const StageExtra&,
+                         const DevBuf& in, const DevBuf& base, const DevBuf& out,
+                         const DevBuf& acc, const double* fh, const double* fhu,
+                         const double* fhv, StepCtl* ctl, int mode, const LtsPass&, cudaStream_t);
+    void (*finish_listed)(int n1, const DevTables&, const Physics&, const DevBuf& acc,
+                          const DevBuf& state, StepCtl* ctl, const LtsPass&, cudaStream_t);
+    // per element: every node deeper than d0, d1, d2 (bits 0, 1, 2)
+    void (*depth_flags)(const double* h, int64_t K, int nn, double d0, double d1, double d2,
+                        uint8_t* flags, cudaStream_t);
 };
 
 // kernels_fast.cu: FMA contraction, division-free Manning rate

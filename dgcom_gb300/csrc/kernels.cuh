@@ -58,6 +58,33 @@ __device__ __forceinline__ Q load_q(const DevBuf& in, const DevTables& T, const 
     return q;
 }
 
+// An element's stage in a multirate pass (element_stage,
+// src/time/multirate.rs:169-200), every operation rounded on its own as the
+// reference's are (no contraction): its substep's start time and step, the
+// Shu–Osher weights, and for the last stage the weight of its sum (the mean
+// of the substep's 2^(rate − level) blocks, restarted where the substep
+// starts). dt/2^level and 1/2^(rate − level) are exact.
+__device__ __forceinline__ StageArgs lts_stage(const LtsPass& p, int64_t k) {
+    const int l = p.level[k];
+    const double inv_2l = __longlong_as_double((long long)(1023 - l) << 52);  // 2^-l
+    const double dt_l = __dmul_rn(p.dt, inv_2l);
+    const long long q = (long long)p.substep >> (p.finest - l);
+    const double t_k = __dadd_rn(p.t, __dmul_rn((double)q, dt_l));
+    StageArgs a;
+    a.time = __dadd_rn(t_k, __dmul_rn(p.c, dt_l));
+    a.a = p.start;
+    a.b = p.input;
+    a.c = __dmul_rn(p.beta, dt_l);
+    a.w = 1.0;
+    a.keep = 0.0;
+    if (p.last) {
+        const int blocks = p.rate[k] - l;
+        a.w = __longlong_as_double((long long)(1023 - blocks) << 52);  // 1/2^(rate − level)
+        a.keep = l >= p.depth ? 0.0 : 1.0;
+    }
+    return a;
+}
+
 // The interface flux of the other split forms (EntropyStable / EntropyConservative):
 // F#·n (+ dissipation) with the bed interface term per side
 // (src/solver/rhs/swe_2d_split_form.rs:639-650, src/flux/swe_2d_entropy.rs:166-205)
@@ -82,19 +109,21 @@ __device__ void entropy_surface(const Q& qa, const Q& qb, double nx, double ny, 
     fb = {-s.h + 0.0, -s.hu + fb_b * (-nx), -s.hv + fb_b * (-ny)};
 }
 
-template <int N1>
+// LISTED: a multirate pass's faces (lp's edge and boundary-face lists),
+// each boundary face at its element's stage time
+template <int N1, bool LISTED>
 __global__ void __launch_bounds__(256) face_kernel(DevTables T, Physics P, DevBuf in, double* fb_h,
                                                    double* fb_hu, double* fb_hv,
                                                    const StepCtl* ctl, int slot,
-                                                   const int* active) {
+                                                   const int* active, LtsPass lp) {
     if (!*active) return;
     const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t n_int = T.n_edges * N1;
-    if (item >= n_int + T.n_bfaces * N1) return;
+    const int64_t n_int = (LISTED ? lp.n_edges : T.n_edges) * N1;
+    if (item >= n_int + (LISTED ? lp.n_bfaces : T.n_bfaces) * N1) return;
     constexpr int NN = N1 * N1;
     const double g = P.g, h_min = P.h_min, sqrt_g = P.sqrt_g, half_g = P.half_g;
     if (item < n_int) {
-        const int64_t e = item / N1;
+        const int64_t e = LISTED ? (int64_t)lp.edges[item / N1] : item / N1;
         const int fi = (int)(item % N1);
         const int64_t L = T.edge_left[e], R = T.edge_right[e];
         const int64_t kl = L >> 2, kr = R >> 2;
@@ -121,7 +150,7 @@ __global__ void __launch_bounds__(256) face_kernel(DevTables T, Physics P, DevBu
         return;
     }
     // boundary face node (src/solver/rhs/swe_2d_split_form.rs:1090-1123)
-    const int64_t bfi = (item - n_int) / N1;
+    const int64_t bfi = LISTED ? (int64_t)lp.bfaces[(item - n_int) / N1] : (item - n_int) / N1;
     const int fi = (int)((item - n_int) % N1);
     const int64_t B = T.bface[bfi];
     const int64_t k = B >> 2;
@@ -145,7 +174,8 @@ __global__ void __launch_bounds__(256) face_kernel(DevTables T, Physics P, DevBu
     } else {
         // CharacteristicOBC with a uniform harmonic tide, flux F(q_b)·n
         const int member = T.elem_member ? T.elem_member[k] : 0;
-        const double eta = tide_elevation(c, ctl[member].stage[slot].time);
+        const double eta =
+            tide_elevation(c, LISTED ? lts_stage(lp, k).time : ctl[member].stage[slot].time);
         const Q qb = characteristic_state(qi, u, v, eta, nx, ny, c.elevation_only, g, h_min);
         fs = wflux(qb, qb, nx, ny, g);
     }
@@ -224,12 +254,13 @@ __device__ __forceinline__ void line_metric(const DevTables& T, int64_t k, int d
     }
 }
 
-template <int N1>
+// LISTED: a multirate pass over lp's elements, each with its own stage
+template <int N1, bool LISTED>
 __global__ void __launch_bounds__(Cfg<N1>::THREADS, Cfg<N1>::MIN_BLOCKS)
     stage_kernel(DevTables T, Physics P, StageExtra X, DevBuf in, DevBuf base, DevBuf out,
                  DevBuf acc, const double* __restrict__ fb_h, const double* __restrict__ fb_hu,
                  const double* __restrict__ fb_hv, StepCtl* ctl, int slot, int mode,
-                 int check_finite, const int* active, DevBuf keep) {
+                 int check_finite, const int* active, DevBuf keep, LtsPass lp) {
     using C = Cfg<N1>;
     constexpr int NN = C::NN, NP = C::NP, NA = C::NA, EPB = C::EPB;
     __shared__ double s_q[EPB][6][NN];
@@ -240,7 +271,8 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS, Cfg<N1>::MIN_BLOCKS)
     if (!*active) return;
     const int tid = threadIdx.x;
     const int e = tid / NN, i = tid % NN;
-    const int64_t k = (int64_t)blockIdx.x * EPB + e;
+    int64_t k = (int64_t)blockIdx.x * EPB + e;
+    if (LISTED) k = k < lp.n ? (int64_t)lp.list[k] : T.K;
     // the element's member (its StepCtl); an ensemble member that has
     // stopped keeps its state: its elements take no part
     StepCtl* const cm = ctl + ((T.elem_member && k < T.K) ? T.elem_member[k] : 0);
@@ -517,7 +549,7 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS, Cfg<N1>::MIN_BLOCKS)
     if (mode == kRhsOnly) return;  // uniform: no barrier follows for this mode
 
     // ---- stage combination and damping ----
-    const StageArgs sa = cm->stage[slot];
+    const StageArgs sa = LISTED ? (valid ? lts_stage(lp, k) : StageArgs{}) : cm->stage[slot];
     double vh = 0.0, vhu = 0.0, vhv = 0.0;
     if (valid) {
         if (fp::nz(sa.a)) {
@@ -636,9 +668,11 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS, Cfg<N1>::MIN_BLOCKS)
 }
 
 // finish_where over every element: state ← acc, then the wet/dry correction
-template <int N1>
+// LISTED: the end of the substeps of lp's elements, and a non-finite
+// result flagged in ctl
+template <int N1, bool LISTED>
 __global__ void __launch_bounds__(Cfg<N1>::THREADS)
-    finish_kernel(DevTables T, Physics P, DevBuf acc, DevBuf state, StepCtl* ctl) {
+    finish_kernel(DevTables T, Physics P, DevBuf acc, DevBuf state, StepCtl* ctl, LtsPass lp) {
     using C = Cfg<N1>;
     constexpr int NN = C::NN, EPB = C::EPB;
     __shared__ double s_v[EPB][3][NN];
@@ -646,7 +680,8 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS)
     __shared__ double s_red[EPB][5];
     const int tid = threadIdx.x;
     const int e = tid / NN, i = tid % NN;
-    const int64_t k = (int64_t)blockIdx.x * EPB + e;
+    int64_t k = (int64_t)blockIdx.x * EPB + e;
+    if (LISTED) k = k < lp.n ? (int64_t)lp.list[k] : T.K;
     const bool valid = k < T.K;
     const int64_t gi = k * NN + i;
     StepCtl* const cm = ctl + ((T.elem_member && valid) ? T.elem_member[k] : 0);  // the member's
@@ -714,7 +749,26 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS)
         node_velocity(vh, vhu, vhv, P.h_min, uo, vo);
         state.u[gi] = uo;
         state.v[gi] = vo;
+        if (LISTED && !(fp::finite(vh) && fp::finite(vhu) && fp::finite(vhv))) cm->nonfinite = 1;
     }
+}
+
+// Per element, whether every node is deeper than each of three depths
+// (bits 0, 1, 2): the line-local test and the two depths of the coarse
+// step's bound (SWEPhysics2D::line_local and coarse_step_bound,
+// src/physics/builder.rs:560-632)
+__global__ void depth_flags_kernel(const double* h, int64_t K, int nn, double d0, double d1,
+                                   double d2, uint8_t* flags) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= K) return;
+    bool a = true, b = true, c = true;
+    for (int i = 0; i < nn; ++i) {
+        const double x = h[k * nn + i];
+        a = a && fp::gt(x, d0);
+        b = b && fp::gt(x, d1);
+        c = c && fp::gt(x, d2);
+    }
+    flags[k] = (uint8_t)((a ? 1 : 0) | (b ? 2 : 0) | (c ? 4 : 0));
 }
 
 // node velocities of a buffer (after an upload)
@@ -879,7 +933,7 @@ __global__ void step_dt(StepCtl* ctl, int n) {
     c->dt = dt;
     for (int s = 0; s < c->scheme_stages; ++s) {
         StageArgs& a = c->stage[s];
-        a.time = c->t + c->st_c[s] * dt;
+        a.time = __dadd_rn(c->t, __dmul_rn(c->st_c[s], dt));  // rounded apart, as the reference
         a.a = c->st_start[s];
         a.b = c->st_input[s];
         a.c = c->st_beta[s] * dt;

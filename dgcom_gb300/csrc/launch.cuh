@@ -15,7 +15,20 @@ static void face_n(const DevTables& T, const Physics& P, const DevBuf& in, doubl
     if (items == 0) return;
     const int threads = 256;
     const unsigned blocks = (unsigned)((items + threads - 1) / threads);
-    face_kernel<N1><<<blocks, threads, 0, s>>>(T, P, in, fh, fhu, fhv, ctl, slot, active);
+    face_kernel<N1, false><<<blocks, threads, 0, s>>>(T, P, in, fh, fhu, fhv, ctl, slot, active,
+                                                      LtsPass{});
+}
+
+template <int N1>
+static void face_listed_n(const DevTables& T, const Physics& P, const DevBuf& in, double* fh,
+                          double* fhu, double* fhv, StepCtl* ctl, const LtsPass& lp,
+                          cudaStream_t s) {
+    const int64_t items = (lp.n_edges + lp.n_bfaces) * N1;
+    if (items == 0) return;
+    const int threads = 256;
+    const unsigned blocks = (unsigned)((items + threads - 1) / threads);
+    face_kernel<N1, true><<<blocks, threads, 0, s>>>(T, P, in, fh, fhu, fhv, ctl, 0, &ctl->always,
+                                                     lp);
 }
 
 template <int N1>
@@ -25,8 +38,23 @@ static void stage_n(const DevTables& T, const Physics& P, const StageExtra& X, c
                     int check_finite, const int* active, const DevBuf& keep, cudaStream_t s) {
     using C = Cfg<N1>;
     const unsigned blocks = (unsigned)((T.K + C::EPB - 1) / C::EPB);
-    stage_kernel<N1><<<blocks, C::THREADS, 0, s>>>(T, P, X, in, base, out, acc, fh, fhu, fhv, ctl,
-                                                   slot, mode, check_finite, active, keep);
+    stage_kernel<N1, false><<<blocks, C::THREADS, 0, s>>>(T, P, X, in, base, out, acc, fh, fhu, fhv,
+                                                          ctl, slot, mode, check_finite, active,
+                                                          keep, LtsPass{});
+}
+
+template <int N1>
+static void stage_listed_n(const DevTables& T, const Physics& P, const StageExtra& X,
+                           const DevBuf& in, const DevBuf& base, const DevBuf& out,
+                           const DevBuf& acc, const double* fh, const double* fhu,
+                           const double* fhv, StepCtl* ctl, int mode, const LtsPass& lp,
+                           cudaStream_t s) {
+    using C = Cfg<N1>;
+    if (lp.n == 0) return;
+    const unsigned blocks = (unsigned)((lp.n + C::EPB - 1) / C::EPB);
+    stage_kernel<N1, true><<<blocks, C::THREADS, 0, s>>>(T, P, X, in, base, out, acc, fh, fhu, fhv,
+                                                         ctl, 0, mode, 0, &ctl->always, DevBuf{},
+                                                         lp);
 }
 
 template <int N1>
@@ -34,7 +62,16 @@ static void finish_n(const DevTables& T, const Physics& P, const DevBuf& acc, co
                      StepCtl* ctl, cudaStream_t s) {
     using C = Cfg<N1>;
     const unsigned blocks = (unsigned)((T.K + C::EPB - 1) / C::EPB);
-    finish_kernel<N1><<<blocks, C::THREADS, 0, s>>>(T, P, acc, state, ctl);
+    finish_kernel<N1, false><<<blocks, C::THREADS, 0, s>>>(T, P, acc, state, ctl, LtsPass{});
+}
+
+template <int N1>
+static void finish_listed_n(const DevTables& T, const Physics& P, const DevBuf& acc,
+                            const DevBuf& state, StepCtl* ctl, const LtsPass& lp, cudaStream_t s) {
+    using C = Cfg<N1>;
+    if (lp.n == 0) return;
+    const unsigned blocks = (unsigned)((lp.n + C::EPB - 1) / C::EPB);
+    finish_kernel<N1, true><<<blocks, C::THREADS, 0, s>>>(T, P, acc, state, ctl, lp);
 }
 
 template <int N1>
@@ -83,6 +120,24 @@ static void finish(int n1, const DevTables& T, const Physics& P, const DevBuf& a
 static void dt(int n1, const DevTables& T, const Physics& P, const DevBuf& q, const DtParams& D,
                double* dt_el, StepCtl* ctl, const int* active, cudaStream_t s) {
     DGSWE_BY_ORDER(dt_n, T, P, q, D, dt_el, ctl, active, s);
+}
+
+static void face_listed(int n1, const DevTables& T, const Physics& P, const DevBuf& in,
+                        double* fh, double* fhu, double* fhv, StepCtl* ctl, const LtsPass& lp,
+                        cudaStream_t s) {
+    DGSWE_BY_ORDER(face_listed_n, T, P, in, fh, fhu, fhv, ctl, lp, s);
+}
+
+static void stage_listed(int n1, const DevTables& T, const Physics& P, const StageExtra& X,
+                         const DevBuf& in, const DevBuf& base, const DevBuf& out,
+                         const DevBuf& acc, const double* fh, const double* fhu, const double* fhv,
+                         StepCtl* ctl, int mode, const LtsPass& lp, cudaStream_t s) {
+    DGSWE_BY_ORDER(stage_listed_n, T, P, X, in, base, out, acc, fh, fhu, fhv, ctl, mode, lp, s);
+}
+
+static void finish_listed(int n1, const DevTables& T, const Physics& P, const DevBuf& acc,
+                          const DevBuf& state, StepCtl* ctl, const LtsPass& lp, cudaStream_t s) {
+    DGSWE_BY_ORDER(finish_listed_n, T, P, acc, state, ctl, lp, s);
 }
 
 template <int N1>
@@ -138,6 +193,12 @@ static void station_seed(const double* eta, const double* obs, const int64_t* no
                                                          lbed);
 }
 
+static void depth_flags(const double* h, int64_t K, int nn, double d0, double d1, double d2,
+                        uint8_t* flags, cudaStream_t s) {
+    if (K == 0) return;
+    depth_flags_kernel<<<(unsigned)((K + 255) / 256), 256, 0, s>>>(h, K, nn, d0, d1, d2, flags);
+}
+
 static void velocity(const DevBuf& b, int64_t n, double h_min, cudaStream_t s) {
     if (n == 0) return;
     velocity_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b, n, h_min);
@@ -158,7 +219,8 @@ static void end(StepCtl* c, int n, cudaStream_t s) {
 static const KernelSet kSet = {face,          stage,         finish,          dt,
                                 velocity,      stage_keep,    stage_adjoint,   face_adjoint,
                                 adjoint_combine, station_eval, station_seed,   begin,
-                                dt_fit,        end};
+                                dt_fit,        end,           face_listed,     stage_listed,
+                                finish_listed, depth_flags};
 
 }  // namespace DGSWE_NS
 }  // namespace dgswe

@@ -47,6 +47,9 @@ class DeviceRun:
     max_steps: int | None = None
     scheme: int = abi.SSP_RK3
     stop: C.c_int32 | None = None  # set .value = 1 to stop at the next step
+    # local time stepping's levels below the coarsest (Multirate on the
+    # stepper), 0 for global steps
+    levels: int = 0
 
 
 @dataclass
@@ -62,6 +65,9 @@ class DeviceRunReport:
     negative_depth_clips: int
     message: str
     device: str
+    # MultirateStats of a run with local time stepping (SimulationResult::
+    # local_time_stepping, src/simulation/runner.rs:89-90)
+    local_time_stepping: abi.MultirateStats | None = None
 
 
 class SWEPhysics2D:
@@ -166,6 +172,7 @@ class SWEPhysics2D:
         cfg.dt_min = run.dt_min or 0.0
         cfg.max_steps = run.max_steps or 0
         cfg.stop = C.pointer(run.stop) if run.stop is not None else None
+        cfg.levels = run.levels
 
         def trampoline(_user, t, h, hu, hv, count):
             if callback is not None:
@@ -183,6 +190,10 @@ class SWEPhysics2D:
                           abi.ERR_STOPPED):
             self._check(status, "run")
         result.status = status
+        if run.levels > 0:
+            stats = abi.MultirateStats()
+            self._check(self.lib.multirate_stats_get(self.handle, C.byref(stats)), "stats")
+            result.local_time_stepping = stats
         return result
 
 

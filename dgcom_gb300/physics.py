@@ -10,6 +10,8 @@ h_min 1e-6) on untagged faces."""
 
 from __future__ import annotations
 
+import math
+
 import ctypes as C
 from dataclasses import dataclass, field
 
@@ -60,6 +62,21 @@ class SWEDeviceForm2D:
     coriolis_y0: float = 0.0
     boundaries: dict = field(default_factory=lambda: {TAG_WALL: WallBoundary()})
     numerics: int = abi.NUMERICS_FAST
+    # Local time stepping: the depth below which a node takes its element out
+    # of the line-local form (SWEDeviceForm2D::line_local_depth,
+    # src/physics/device.rs:62-66); None: no element is line-local; "auto":
+    # SWEPhysics2D::line_local_depth's value for this form
+    # (src/physics/builder.rs:296-322), the WetDry subcells' depth and the
+    # wet/dry correction's h_dry, whichever is deeper
+    line_local_depth: float | None | str = "auto"
+
+    def local_depth(self) -> float | None:
+        """The line-local depth the C form carries (None: none)."""
+        if self.line_local_depth != "auto":
+            return self.line_local_depth
+        if self.formulation != abi.WET_DRY or self.order < 1:
+            return None
+        return max(self.subcell_depth, self.h_dry if self.wet_dry else -math.inf)
 
     @property
     def n_nodes(self) -> int:
@@ -147,6 +164,9 @@ class SWEDeviceForm2D:
         f.n_boundaries = len(self.boundaries)
         f.boundaries = bcs
         f.numerics = self.numerics
+        depth = self.local_depth()
+        f.has_line_local = 0 if depth is None else 1
+        f.line_local_depth = 0.0 if depth is None else float(depth)
         return f, keep
 
 

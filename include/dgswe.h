@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define DGSWE_ABI_VERSION 1u
+#define DGSWE_ABI_VERSION 2u
 
 /* ---- status codes ------------------------------------------------------ */
 enum dgswe_status {
@@ -167,6 +167,14 @@ typedef struct dgswe_form {
     const dgswe_boundary* boundaries;
 
     int32_t numerics;         /* dgswe_numerics */
+
+    /* Local time stepping (SWEDeviceForm2D::line_local_depth,
+     * src/physics/device.rs:62-66): elements whose every node is deeper than
+     * line_local_depth + 1 m read only their GLL lines in a stage, so the
+     * stage rates spread node by node; has_line_local = 0: no element does
+     * (the rates spread one face per stage). */
+    int32_t has_line_local;
+    double line_local_depth;
 } dgswe_form;
 
 /* ---- stages and runs ---------------------------------------------------- */
@@ -202,7 +210,11 @@ typedef struct dgswe_run_config {
     double dt_min;             /* ≤ 0: none */
     int64_t max_steps;         /* ≤ 0: none */
     const volatile int32_t* stop; /* nonzero stops the run at its next step; NULL: none */
+    int32_t levels;            /* local time stepping: levels below the coarsest
+                                  (DeviceRun::levels, ≤ DGSWE_MAX_LEVELS); 0: global steps */
 } dgswe_run_config;
+
+#define DGSWE_MAX_LEVELS 8
 
 /* DeviceRunReport (src/case/run.rs:292-300) with its SimulationResult. */
 typedef struct dgswe_report {
@@ -323,6 +335,64 @@ int dgswe_run(dgswe_handle* handle, const dgswe_run_config* run,
  * every stage so far (SWEPhysics2D::negative_depth_clips,
  * src/physics/builder.rs:204). */
 int64_t dgswe_negative_depth_clips(const dgswe_handle* handle);
+
+/* ---- local time stepping -------------------------------------------------
+ * dgswe_run with run->levels > 0 takes multirate coarse steps (Multirate on
+ * the scheme, src/time/multirate.rs): every element steps at dt/2^level of
+ * the coarse step dt, levels from the element steps every coarse step (the
+ * host plans, as the reference's MultirateStepper does; the device runs each
+ * finest substep's stage passes over prefixes of level-sorted element and
+ * face lists). One level is the global scheme, bit for bit. */
+
+/* MultirateStats (src/time/multirate.rs:785-860) of the handle's last run */
+typedef struct dgswe_multirate_stats {
+    int64_t steps;                /* coarse steps */
+    int64_t element_evaluations;  /* element RHS evaluations */
+    int64_t global_evaluations;   /* those of global steps at the finest level */
+    int32_t finest_level;         /* largest level used */
+    double model_seconds;
+    double ideal_evaluations;     /* every element at its own stable step */
+    double level_evaluations;     /* every stage at the element's level */
+    int64_t line_local_elements;  /* summed over the coarse steps */
+} dgswe_multirate_stats;
+
+int dgswe_multirate_stats_get(const dgswe_handle* handle, dgswe_multirate_stats* out);
+
+/* The level planner alone, on the host (no device): MultirateStepper's
+ * level assignment (assign_levels, the landing fit, the jump limit, the
+ * stage rates and the kept plan) on a form's mesh, for the scheme's stages
+ * and up to max_levels levels. */
+typedef struct dgswe_planner dgswe_planner;
+
+typedef struct dgswe_plan_result {
+    double dt;                 /* the coarse step, fitted to the landing */
+    double stable_step;        /* the step the elements (and the cap) allow */
+    int32_t finest;            /* finest level */
+    int64_t evaluations;       /* element RHS evaluations per coarse step */
+    int64_t level_evaluations; /* the same with every stage at the element's level */
+    double inverse_dt_sum;     /* Σ 1/element dt over the finite ones */
+} dgswe_plan_result;
+
+int dgswe_planner_create(const dgswe_form* form, int32_t max_levels, int32_t scheme,
+                         dgswe_planner** out);
+void dgswe_planner_destroy(dgswe_planner* planner);
+/* element_dt [n_elements] (∞: unlimited); line_local [n_elements] flags or
+ * NULL (no line-local elements: the rates spread one face per stage);
+ * dt_cap, landing ≤ 0: none. levels [n_elements], rates
+ * [n_stages][n_elements] and order [(n_stages + 1)][n_elements] (each key's
+ * elements, largest key first: the device's pass order; key j < n_stages is
+ * stage j's rate, the last the level) may be NULL. */
+int dgswe_planner_assign(dgswe_planner* planner, const double* element_dt,
+                         const uint8_t* line_local, double dt_cap, double landing,
+                         dgswe_plan_result* result, uint8_t* levels, uint8_t* rates,
+                         int32_t* order);
+/* The planner's pieces on given levels [n_elements]: with limit ≠ 0 the
+ * jump limit first (face neighbours' levels differ by at most one, the
+ * coarser side refined; `levels` is updated), then every stage's rates into
+ * rates [n_stages][n_elements] (may be NULL), node by node over the GLL
+ * lines where line_local marks an element (NULL: one face per stage). */
+int dgswe_planner_spread(dgswe_planner* planner, uint8_t* levels, int32_t limit,
+                         const uint8_t* line_local, uint8_t* rates);
 
 /* Times n_steps device-driven steps of the state from run->t_start (the
  * run's scheme, cfl and dt_max; no end time), every kernel bracketed by CUDA

@@ -1208,6 +1208,359 @@ static bool state_is_finite(const Model& m) {
     return ok;
 }
 
+// ---------------------------------------------------------------------------
+// Local time stepping (src/time/multirate.rs): MultirateStepper's levels,
+// stage rates and schedule, and the element subsets' stages and finishes of
+// SWEPhysics2D's LocalTimeStepping (src/physics/builder.rs:546-782)
+
+struct Multirate {
+    int max_levels = 0, n_stages = 3;
+    int finest = 0;
+    double stable_step = INF;
+    std::vector<uint8_t> level;
+    std::vector<uint8_t> rate[4];
+    // MultirateStats (multirate.rs:785-860)
+    int64_t steps = 0, element_evaluations = 0, global_evaluations = 0;
+    int finest_used = 0;
+    double model_seconds = 0.0, ideal_evaluations = 0.0, level_evaluations = 0.0;
+    int64_t line_local_elements = 0;
+    int64_t evaluations_per_step = 0, level_evaluations_per_step = 0;
+    double inverse_dt_sum = 0.0;
+    int64_t n_line_local = 0;
+};
+
+// assign_levels (multirate.rs:527-568)
+static double mr_assign_levels(const std::vector<double>& element_dt, int max_levels,
+                               double dt_cap, std::vector<uint8_t>& level, int& finest) {
+    double dt_min = INF, dt_max = 0.0;
+    for (double d : element_dt)
+        if (std::isfinite(d)) {
+            dt_min = fmin_(dt_min, d);
+            dt_max = fmax_(dt_max, d);
+        }
+    level.assign(element_dt.size(), 0);
+    finest = 0;
+    if (!std::isfinite(dt_min)) return INF;
+    while (finest < max_levels) {
+        double coarser = dt_min * (double)(2ull << finest);
+        if (coarser > dt_max || (dt_cap > 0.0 && coarser > dt_cap)) break;
+        finest += 1;
+    }
+    double dt = dt_min * (double)(1ull << finest);
+    for (size_t k = 0; k < element_dt.size(); ++k) {
+        int l = 0;
+        double dt_l = dt;
+        while (l < finest && dt_l > element_dt[k]) {
+            dt_l *= 0.5;
+            l += 1;
+        }
+        level[k] = (uint8_t)l;
+    }
+    return dt;
+}
+
+// levels_for_step (multirate.rs:570-583)
+static int mr_levels_for_step(const std::vector<double>& element_dt, double dt, int max_levels,
+                              std::vector<uint8_t>& level) {
+    int finest = 0;
+    for (size_t k = 0; k < element_dt.size(); ++k) {
+        int l = 0;
+        double dt_l = dt;
+        while (l < max_levels && dt_l > element_dt[k]) {
+            dt_l *= 0.5;
+            l += 1;
+        }
+        level[k] = (uint8_t)l;
+        finest = std::max(finest, l);
+    }
+    return finest;
+}
+
+// spread_to_neighbours (multirate.rs:592-615): to[k] = max(from[k],
+// from[j] − drop) over the face neighbours j; whether any changed
+static bool mr_spread(const Mesh& mesh, const std::vector<uint8_t>& from, std::vector<uint8_t>& to,
+                      int drop) {
+    bool changed = false;
+    to.assign(from.size(), 0);
+    for (int64_t k = 0; k < mesh.n_elements; ++k) {
+        int best = from[k];
+        for (int face = 0; face < 4; ++face) {
+            ElementFace nb;
+            if (!mesh.neighbor(k, face, nb)) continue;
+            best = std::max(best, std::max((int)from[nb.element] - drop, 0));
+        }
+        to[k] = (uint8_t)best;
+        changed = changed || to[k] != from[k];
+    }
+    return changed;
+}
+
+// spread_over_lines (multirate.rs:678-743) of one stage
+static void mr_spread_lines(const Model& m, const std::vector<uint8_t>& line_local,
+                            const std::vector<uint8_t>& from, std::vector<uint8_t>& to,
+                            std::vector<uint8_t>& rate) {
+    const Ops& ops = m.ops;
+    const int n1 = ops.n1, nn = ops.nn;
+    to.assign(from.size(), 0);
+    rate.assign((size_t)m.mesh.n_elements, 0);
+    auto inner = [&](int face, int node) {
+        return face == 0 ? node + n1 : face == 1 ? node - 1 : face == 2 ? node - n1 : node + 1;
+    };
+    for (int64_t k = 0; k < m.mesh.n_elements; ++k) {
+        const uint8_t* own = &from[(size_t)k * nn];
+        uint8_t* t = &to[(size_t)k * nn];
+        if (!line_local[k]) {
+            int finest = 0;
+            for (int i = 0; i < nn; ++i) finest = std::max(finest, (int)own[i]);
+            for (int face = 0; face < 4; ++face) {
+                ElementFace nb;
+                if (!m.mesh.neighbor(k, face, nb)) continue;
+                const uint8_t* other = &from[(size_t)nb.element * nn];
+                for (int fi = 0; fi < n1; ++fi) {
+                    int node = ops.face_nodes[nb.face][fi];
+                    finest = std::max(finest, std::max((int)other[node], (int)other[inner(nb.face, node)]));
+                }
+            }
+            for (int i = 0; i < nn; ++i) t[i] = (uint8_t)finest;
+            rate[k] = (uint8_t)finest;
+            continue;
+        }
+        for (int j = 0; j < n1; ++j) {
+            int mx = 0;
+            for (int i = 0; i < n1; ++i) mx = std::max(mx, (int)own[j * n1 + i]);
+            for (int i = 0; i < n1; ++i) t[j * n1 + i] = (uint8_t)mx;
+        }
+        for (int i = 0; i < n1; ++i) {
+            int mx = 0;
+            for (int j = 0; j < n1; ++j) mx = std::max(mx, (int)own[j * n1 + i]);
+            for (int j = 0; j < n1; ++j) t[j * n1 + i] = (uint8_t)std::max((int)t[j * n1 + i], mx);
+        }
+        for (int face = 0; face < 4; ++face) {
+            ElementFace nb;
+            if (!m.mesh.neighbor(k, face, nb)) continue;
+            const uint8_t* other = &from[(size_t)nb.element * nn];
+            for (int fi = 0; fi < n1; ++fi) {
+                int node = ops.face_nodes[face][fi];
+                int o = other[ops.face_nodes[nb.face][n1 - 1 - fi]];
+                t[node] = (uint8_t)std::max((int)t[node], o);
+            }
+        }
+        int mx = 0;
+        for (int i = 0; i < nn; ++i) mx = std::max(mx, (int)t[i]);
+        rate[k] = (uint8_t)mx;
+    }
+}
+
+// MultirateStepper::assign (multirate.rs:1044-1157) without the kept plan
+// (which gives what a fresh one gives) and the longest step (off)
+static double mr_assign(const Model& m, Multirate& mr, const std::vector<double>& element_dt,
+                        const std::vector<uint8_t>* line_local, double dt_cap, double landing) {
+    const int64_t K = m.mesh.n_elements;
+    int finest = 0;
+    double dt = mr_assign_levels(element_dt, mr.max_levels, dt_cap, mr.level, finest);
+    mr.stable_step = dt;
+    if (finest > 0 && landing > 0.0 && std::isfinite(dt)) {
+        double steps = std::ceil(landing / (dt * (1.0 + 1e-9)));
+        if (steps < 1.0) steps = 1.0;
+        double fitted = landing / steps;
+        if (fitted < dt) {
+            dt = fitted;
+            finest = mr_levels_for_step(element_dt, dt, mr.max_levels, mr.level);
+        }
+    }
+    mr.finest = finest;
+    mr.inverse_dt_sum = 0.0;
+    for (double d : element_dt)
+        if (std::isfinite(d)) mr.inverse_dt_sum += 1.0 / d;
+    // limit_level_jumps (multirate.rs:745-752)
+    std::vector<uint8_t> scratch;
+    while (mr_spread(m.mesh, mr.level, scratch, 1)) std::swap(mr.level, scratch);
+    int64_t lev = 0;
+    for (int64_t k = 0; k < K; ++k) lev += (int64_t)1 << mr.level[k];
+    mr.level_evaluations_per_step = (int64_t)mr.n_stages * lev;
+    mr.n_line_local = 0;
+    if (line_local) {
+        for (int64_t k = 0; k < K; ++k) mr.n_line_local += (*line_local)[k] ? 1 : 0;
+        const int nn = m.ops.nn;
+        std::vector<uint8_t> from((size_t)K * nn), to;
+        for (int64_t k = 0; k < K; ++k)
+            for (int i = 0; i < nn; ++i) from[(size_t)k * nn + i] = mr.level[k];
+        for (int s = 0; s < mr.n_stages; ++s) {
+            mr_spread_lines(m, *line_local, from, to, mr.rate[s]);
+            std::swap(from, to);
+        }
+    } else {
+        for (int s = 0; s < mr.n_stages; ++s)
+            mr_spread(m.mesh, s == 0 ? mr.level : mr.rate[s - 1], mr.rate[s], 0);
+    }
+    mr.evaluations_per_step = 0;
+    for (int s = 0; s < mr.n_stages; ++s)
+        for (int64_t k = 0; k < K; ++k) mr.evaluations_per_step += (int64_t)1 << mr.rate[s][k];
+    return dt;
+}
+
+// depth (multirate.rs:771-778)
+static int mr_depth(int64_t p, int finest) {
+    if (p == 0 || p == ((int64_t)1 << finest)) return 0;
+    int tz = 0;
+    while (((p >> tz) & 1) == 0) ++tz;
+    return finest - tz;
+}
+
+// element_stage (multirate.rs:169-200)
+struct ElementStage {
+    double time, a, b, c;
+    bool accumulate;
+    double w, keep;
+};
+static ElementStage mr_element_stage(double t, double dt, int finest, int64_t substep, int depth,
+                                     const ShuOsher& st, bool last, int level, int rate) {
+    double dt_l = dt / (double)(1ull << level);
+    int64_t q = substep >> (finest - level);
+    double t_k = t + (double)q * dt_l;
+    ElementStage e{};
+    e.time = t_k + st.c * dt_l;
+    e.a = st.start;
+    e.b = st.input;
+    e.c = st.beta * dt_l;
+    e.accumulate = last;
+    if (last) {
+        uint64_t blocks = 1ull << (rate - level);
+        e.w = 1.0 / (double)blocks;
+        e.keep = level >= depth ? 0.0 : 1.0;
+    }
+    return e;
+}
+
+// stage_where (builder.rs:652-737) on the elements whose stage rate is at
+// least the pass's depth
+static void mr_stage(Model& m, const Multirate& mr, int s, const ShuOsher& st, bool last,
+                     double t, double dt, int64_t p, int d, int32_t input_id, int32_t out_id,
+                     int32_t acc_id) {
+    const Buffer& input = m.buf[input_id];
+    face_pass(m, input);
+    const int nn = m.ops.nn;
+    Buffer& out = m.buf[out_id];
+    const Buffer& base = m.buf[DGSWE_STATE];
+    Buffer& acc = m.buf[acc_id];
+    int64_t clips = 0;
+#pragma omp parallel reduction(+ : clips)
+    {
+        Workspace ws(m.ops);
+        std::vector<double> rh(nn), rhu(nn), rhv(nn);
+#pragma omp for schedule(static)
+        for (int64_t k = 0; k < m.mesh.n_elements; ++k) {
+            if (mr.rate[s][k] < d) continue;
+            ElementStage e = mr_element_stage(t, dt, mr.finest, p, d, st, last, mr.level[k],
+                                              mr.rate[s][k]);
+            element_rhs(m, input, k, e.time, ws, rh.data(), rhu.data(), rhv.data());
+            size_t o = (size_t)k * nn;
+            double* rows[3] = {rh.data(), rhu.data(), rhv.data()};
+            const std::vector<double>* bases[3] = {&base.h, &base.hu, &base.hv};
+            const std::vector<double>* inputs[3] = {&input.h, &input.hu, &input.hv};
+            for (int var = 0; var < 3; ++var)
+                for (int i = 0; i < nn; ++i) {
+                    double sv = (*bases[var])[o + i], x = (*inputs[var])[o + i], f = rows[var][i];
+                    double v = e.a != 0.0 ? e.a * sv : 0.0;
+                    if (e.b != 0.0) v += e.b * x;
+                    if (e.c != 0.0) v += e.c * f;
+                    rows[var][i] = v;
+                }
+            if (m.form.friction != DGSWE_FRICTION_NONE || m.form.has_wet_dry)
+                for (int i = 0; i < nn; ++i)
+                    damp_node(m, o + i, rh[i], rhu[i], rhv[i], input.get(o + i), e.c);
+            if (e.accumulate) {
+                double* sums[3] = {&acc.h[o], &acc.hu[o], &acc.hv[o]};
+                for (int var = 0; var < 3; ++var)
+                    for (int i = 0; i < nn; ++i)
+                        sums[var][i] = e.keep != 0.0 ? e.w * rows[var][i] + e.keep * sums[var][i]
+                                                     : e.w * rows[var][i];
+            } else {
+                clips += post_process_element(m, k, rh.data(), rhu.data(), rhv.data()) ? 1 : 0;
+            }
+            std::memcpy(&out.h[o], rh.data(), nn * sizeof(double));
+            std::memcpy(&out.hu[o], rhu.data(), nn * sizeof(double));
+            std::memcpy(&out.hv[o], rhv.data(), nn * sizeof(double));
+        }
+    }
+    m.clips += clips;
+}
+
+// finish_where (builder.rs:739-782) on the elements whose level is at least d
+static void mr_finish(Model& m, const Multirate& mr, int d, int32_t acc_id) {
+    const int nn = m.ops.nn;
+    Buffer& st = m.buf[DGSWE_STATE];
+    const Buffer& acc = m.buf[acc_id];
+    int64_t clips = 0;
+#pragma omp parallel for schedule(static) reduction(+ : clips)
+    for (int64_t k = 0; k < m.mesh.n_elements; ++k) {
+        if (mr.level[k] < d) continue;
+        size_t o = (size_t)k * nn;
+        for (int i = 0; i < nn; ++i) {
+            st.h[o + i] = acc.h[o + i];
+            st.hu[o + i] = acc.hu[o + i];
+            st.hv[o + i] = acc.hv[o + i];
+        }
+        clips += post_process_element(m, k, &st.h[o], &st.hu[o], &st.hv[o]) ? 1 : 0;
+    }
+    m.clips += clips;
+}
+
+// MultirateStepper::step (multirate.rs:1285-1315) over schedule
+// (multirate.rs:1249-1283): buffers 1..n−1 the stage values, n the last
+// stage's, n + 1 the substeps' sums
+static void mr_step(Model& m, Multirate& mr, int scheme, double t, double dt) {
+    ShuOsher st[4];
+    const int n = scheme_stages(scheme, st);
+    const int last = n, acc = n + 1;
+    for (int64_t p = 0; p < ((int64_t)1 << mr.finest); ++p) {
+        const int d = mr_depth(p, mr.finest);
+        for (int s = 0; s < n; ++s)
+            mr_stage(m, mr, s, st[s], s + 1 == n, t, dt, p, d, s == 0 ? DGSWE_STATE : s,
+                     s + 1 < n ? s + 1 : last, acc);
+        mr_finish(m, mr, mr_depth(p + 1, mr.finest), acc);
+    }
+    mr.steps += 1;
+    mr.element_evaluations += mr.evaluations_per_step;
+    mr.global_evaluations += (int64_t)n * m.mesh.n_elements * ((int64_t)1 << mr.finest);
+    mr.finest_used = std::max(mr.finest_used, mr.finest);
+    mr.model_seconds += dt;
+    mr.ideal_evaluations += (double)n * mr.inverse_dt_sum * dt;
+    mr.level_evaluations += (double)mr.level_evaluations_per_step;
+    mr.line_local_elements += mr.n_line_local;
+}
+
+// SWEPhysics2D::line_local and coarse_step_bound (builder.rs:560-632) of the
+// state: the line-local flags (null: none) and the bound
+static double mr_flags(const Model& m, const std::vector<double>& element_dt,
+                       std::vector<uint8_t>& line_local, bool& has_lines) {
+    const int nn = m.ops.nn;
+    const int64_t K = m.mesh.n_elements;
+    const Buffer& q = m.buf[DGSWE_STATE];
+    auto all_deeper = [&](int64_t k, double depth) {
+        for (int i = 0; i < nn; ++i)
+            if (!(q.h[(size_t)k * nn + i] > depth)) return false;
+        return true;
+    };
+    has_lines = m.form.has_line_local != 0 && m.ops.n1 >= 2;
+    if (has_lines) {
+        double depth = m.form.line_local_depth;
+        if (!(std::isinf(depth) && depth < 0.0)) depth += 1.0;  // LINE_LOCAL_HEADROOM
+        line_local.assign(K, 0);
+        for (int64_t k = 0; k < K; ++k) line_local[k] = all_deeper(k, depth) ? 1 : 0;
+    }
+    if (!(m.form.positivity_h_dry > 0.0)) return INF;
+    const double h_dry = m.form.positivity_h_dry;
+    for (double shallow : {100.0 * h_dry, h_dry}) {
+        double longest = 0.0;
+        for (int64_t k = 0; k < K; ++k)
+            if (std::isfinite(element_dt[k]) && all_deeper(k, shallow))
+                longest = fmax_(longest, element_dt[k]);
+        if (longest > 0.0) return longest;
+    }
+    return INF;
+}
+
 }  // namespace oracle
 
 // ---------------------------------------------------------------------------
@@ -1217,6 +1570,7 @@ using namespace oracle;
 
 struct oracle_handle {
     Model* m;
+    Multirate mr;
 };
 
 extern "C" {
@@ -1396,6 +1750,19 @@ int oracle_run(oracle_handle* h, const dgswe_run_config* run, dgswe_callback cb,
         std::snprintf(report->message, sizeof(report->message), "%s", msg);
         return status;
     };
+    const bool multirate = run->levels > 0;
+    if (run->levels < 0 || run->levels > DGSWE_MAX_LEVELS) return DGSWE_ERR_INVALID;
+    if (multirate) {
+        h->mr = Multirate{};
+        h->mr.max_levels = run->levels;
+        ShuOsher st[4];
+        h->mr.n_stages = scheme_stages(run->scheme, st);
+        // the stage values, the last stage's and the sums start as the state
+        // (MultirateStepper::step, src/time/multirate.rs:1287-1293)
+        for (int b = 1; b <= h->mr.n_stages + 1; ++b) m.buf[b] = m.buf[DGSWE_STATE];
+    }
+    std::vector<double> element_dt(multirate ? (size_t)m.mesh.n_elements : 0);
+    std::vector<uint8_t> line_local;
     call(t);
     char msg[200];
     while (t < t_end) {
@@ -1408,7 +1775,21 @@ int oracle_run(oracle_handle* h, const dgswe_run_config* run, dgswe_callback cb,
             return finish(DGSWE_ERR_STOPPED, msg);
         }
         double target = has_interval ? fmin_(next_callback(callbacks_done), t_end) : t_end;
-        double dt = min_element_dt(m, run->cfl, run->scheme, nullptr);
+        double dt, fitted = INF;
+        if (multirate) {
+            // Simulation::run_with_callback with a multirate integrator
+            // (src/simulation/runner.rs:370-382)
+            min_element_dt(m, run->cfl, run->scheme, element_dt.data());
+            bool has_lines = false;
+            double bound = mr_flags(m, element_dt, line_local, has_lines);
+            double cap = run->dt_max > 0.0 ? fmin_(run->dt_max, bound) : bound;
+            if (!std::isfinite(cap)) cap = 0.0;
+            fitted = mr_assign(m, h->mr, element_dt, has_lines ? &line_local : nullptr, cap,
+                               target - t);
+            dt = h->mr.stable_step;
+        } else {
+            dt = min_element_dt(m, run->cfl, run->scheme, nullptr);
+        }
         if (run->dt_max > 0.0) dt = fmin_(dt, run->dt_max);
         if (run->dt_min > 0.0 && dt < run->dt_min) {
             std::snprintf(msg, sizeof msg, "Time step (%.2e) below minimum (%.2e)", dt, run->dt_min);
@@ -1416,9 +1797,13 @@ int oracle_run(oracle_handle* h, const dgswe_run_config* run, dgswe_callback cb,
         }
         dt_min_used = fmin_(dt_min_used, dt);
         dt_max_used = fmax_(dt_max_used, dt);
+        if (multirate) dt = fmin_(dt, fitted);
         bool landed = t + dt * (1.0 + LANDING_SLACK) >= target;
         if (landed) dt = target - t;
-        step_one_level(m, run->scheme, t, dt);
+        if (multirate)
+            mr_step(m, h->mr, run->scheme, t, dt);
+        else
+            step_one_level(m, run->scheme, t, dt);
         t = landed ? target : t + dt;
         n_steps += 1;
         if (!state_is_finite(m)) {
@@ -1435,6 +1820,20 @@ int oracle_run(oracle_handle* h, const dgswe_run_config* run, dgswe_callback cb,
         }
     }
     return finish(DGSWE_OK, "");
+}
+
+int oracle_multirate_stats_get(const oracle_handle* h, dgswe_multirate_stats* out) {
+    if (!h || !out) return DGSWE_ERR_INVALID;
+    const Multirate& mr = h->mr;
+    out->steps = mr.steps;
+    out->element_evaluations = mr.element_evaluations;
+    out->global_evaluations = mr.global_evaluations;
+    out->finest_level = mr.finest_used;
+    out->model_seconds = mr.model_seconds;
+    out->ideal_evaluations = mr.ideal_evaluations;
+    out->level_evaluations = mr.level_evaluations;
+    out->line_local_elements = mr.line_local_elements;
+    return DGSWE_OK;
 }
 
 // ---- pointwise entry points for the known-answer tests -------------------

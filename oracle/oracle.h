@@ -33,6 +33,8 @@ int oracle_step(oracle_handle* h, int32_t scheme, double t, double dt);
 int oracle_run(oracle_handle* h, const dgswe_run_config* run, dgswe_callback cb, void* user,
                dgswe_report* report);
 int64_t oracle_negative_depth_clips(const oracle_handle* h);
+/* MultirateStats of the last run with local time stepping (run->levels > 0) */
+int oracle_multirate_stats_get(const oracle_handle* h, dgswe_multirate_stats* out);
 
 /* pointwise functions for the known-answer tests */
 double oracle_manning_cbrt(double x);

@@ -36,6 +36,7 @@ POINTWISE = {
     "damp_nodes": (None, [C.c_int64, _dp, _dp, _dp, _dp, _dp, _dp, C.c_double, C.c_double,
                           C.c_double, C.c_double, C.c_double]),
     "tide_elevation": (C.c_double, [C.POINTER(abi.Boundary), C.c_double]),
+    "multirate_stats_get": (C.c_int, [C.c_void_p, C.POINTER(abi.MultirateStats)]),
 }
 
 _lib = None
