@@ -765,6 +765,8 @@ def run_multirate(args, rank: int, world: int, local: int):
                           "level_evaluations": s.level_evaluations,
                           "ideal_evaluations": s.ideal_evaluations,
                           "line_local_elements_per_step": s.line_local_elements / max(1, s.steps),
+                          "plans": int(s.plans), "plan_s": s.plan_seconds,
+                          "device_pass_s": s.device_seconds,
                           "coarse_dt_range": [m.dt_min, m.dt_max]},
             "evaluations_global_over_multirate":
                 (3.0 * form.mesh.n_elements * g.n_steps) / max(1, s.element_evaluations),

@@ -146,6 +146,9 @@ class MultirateStats(C.Structure):
         ("ideal_evaluations", C.c_double),
         ("level_evaluations", C.c_double),
         ("line_local_elements", C.c_int64),
+        ("plans", C.c_int64),
+        ("plan_seconds", C.c_double),
+        ("device_seconds", C.c_double),
     ]
 
 

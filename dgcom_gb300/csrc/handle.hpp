@@ -68,9 +68,12 @@ struct dgswe_handle {
     uint8_t *d_level = nullptr, *d_rate = nullptr, *d_flags = nullptr;
     int32_t *d_order = nullptr, *d_edges = nullptr, *d_bfaces = nullptr;
     dgswe_multirate_stats mr_stats{};
+    cudaEvent_t ev_lts[2] = {nullptr, nullptr};
 
     ~dgswe_handle() {
         delete planner;
+        for (cudaEvent_t e : ev_lts)
+            if (e) cudaEventDestroy(e);
         if (step_graph) cudaGraphExecDestroy(step_graph);
         for (void* p : allocations) cudaFree(p);
         if (h_ctl) cudaFreeHost(h_ctl);

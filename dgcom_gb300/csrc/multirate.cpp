@@ -8,6 +8,8 @@
 #include <limits>
 #include <utility>
 
+#include <omp.h>
+
 namespace dgswe {
 
 namespace {
@@ -17,19 +19,42 @@ const double kLandingSlack = 1e-9;  // LANDING_SLACK (src/time/multirate.rs:589)
 inline bool finite(double x) { return std::isfinite(x); }
 
 // items 0..n by key, largest first, index order within a key; at_least[d]
-// for d in 0..=finest
+// for d in 0..=finest. A counting sort: each thread counts its contiguous
+// chunk, the chunks' offsets follow from the counts, each thread scatters
+// its chunk in index order, so the order is the serial one.
 template <class Key>
 void order_by_key(int64_t n, int finest, Key key, std::vector<int32_t>& order,
                   std::vector<int64_t>& at_least) {
-    std::vector<int64_t> count(finest + 2, 0);
-    for (int64_t i = 0; i < n; ++i) count[key(i)] += 1;
-    at_least.assign(finest + 2, 0);
-    for (int d = finest; d >= 0; --d) at_least[d] = at_least[d + 1] + count[d];
-    std::vector<int64_t> next(finest + 1);
-    for (int v = 0; v <= finest; ++v) next[v] = at_least[v + 1];
+    const int V = finest + 1;
+    const int max_threads = omp_get_max_threads();
+    std::vector<int64_t> hist((size_t)max_threads * V, 0), off((size_t)max_threads * V, 0);
+    at_least.assign(V + 1, 0);
     order.assign(n, 0);
-    for (int64_t i = 0; i < n; ++i) order[next[key(i)]++] = (int32_t)i;
-    at_least.resize(finest + 1);
+#pragma omp parallel num_threads(max_threads)
+    {
+        const int t = omp_get_thread_num(), nt = omp_get_num_threads();
+        const int64_t lo = n * t / nt, hi = n * (t + 1) / nt;
+        int64_t* h = &hist[(size_t)t * V];
+        for (int64_t i = lo; i < hi; ++i) h[key(i)] += 1;
+#pragma omp barrier
+#pragma omp single
+        {
+            std::vector<int64_t> count(V, 0);
+            for (int u = 0; u < nt; ++u)
+                for (int v = 0; v < V; ++v) count[v] += hist[(size_t)u * V + v];
+            for (int d = V - 1; d >= 0; --d) at_least[d] = at_least[d + 1] + count[d];
+            for (int v = 0; v < V; ++v) {
+                int64_t o = at_least[v + 1];  // key v starts after the larger keys
+                for (int u = 0; u < nt; ++u) {
+                    off[(size_t)u * V + v] = o;
+                    o += hist[(size_t)u * V + v];
+                }
+            }
+        }
+        int64_t* o = &off[(size_t)t * V];
+        for (int64_t i = lo; i < hi; ++i) order[o[key(i)]++] = (int32_t)i;
+    }
+    at_least.resize(V);
 }
 
 }  // namespace
@@ -61,6 +86,7 @@ int MultiratePlanner::depth(int64_t p, int finest) {
 double MultiratePlanner::assign_levels(const double* element_dt, int64_t n, int max_levels,
                                        double dt_cap, std::vector<uint8_t>& level, int& finest) {
     double lo = std::numeric_limits<double>::infinity(), hi = 0.0;
+#pragma omp parallel for schedule(static) reduction(min : lo) reduction(max : hi)
     for (int64_t k = 0; k < n; ++k) {
         const double d = element_dt[k];
         if (!finite(d)) continue;

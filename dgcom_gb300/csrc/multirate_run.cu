@@ -51,6 +51,10 @@ int prepare(dgswe_handle* h, int levels, int n_stages) {
         h->planner_stages = n_stages;
         h->plan_uploaded = 0;
     }
+    if (!h->ev_lts[0]) {
+        CK(cudaEventCreate(&h->ev_lts[0]));
+        CK(cudaEventCreate(&h->ev_lts[1]));
+    }
     if (!h->d_level) {
         const size_t K = (size_t)h->K, E = h->h_edge_left.size(), B = h->h_bface.size();
         if (int s = dev_alloc(h, K, &h->d_level)) return s;
@@ -252,6 +256,7 @@ int run_multirate(dgswe_handle* h, const dgswe_run_config* run, dgswe_callback c
         if (bounded) {
             for (int bit : {2, 4}) {
                 double longest = 0.0;
+#pragma omp parallel for schedule(static) reduction(max : longest)
                 for (int64_t k = 0; k < K; ++k)
                     if (std::isfinite(dt_el[k]) && (flags[k] & bit)) longest = std::max(longest, dt_el[k]);
                 if (longest > 0.0) {
@@ -262,8 +267,12 @@ int run_multirate(dgswe_handle* h, const dgswe_run_config* run, dgswe_callback c
         }
         double cap = run->dt_max > 0.0 ? std::min(run->dt_max, bound) : bound;
         if (!std::isfinite(cap)) cap = 0.0;
-        if (lines)
+        if (lines) {
+#pragma omp parallel for schedule(static)
             for (int64_t k = 0; k < K; ++k) line_local[k] = flags[k] & 1;
+        }
+        const auto plan0 = std::chrono::steady_clock::now();
+        const uint64_t version0 = pl.version();
         const double fitted = pl.assign(dt_el.data(), lines ? line_local.data() : nullptr, cap,
                                         target - t);
         double dt = pl.stable_step();
@@ -279,7 +288,12 @@ int run_multirate(dgswe_handle* h, const dgswe_run_config* run, dgswe_callback c
         const bool landed = t + dt * (1.0 + kLandingSlack) >= target;
         if (landed) dt = target - t;
         if (int s = upload_plan(h, n)) return s;
+        stats.plans += pl.version() != version0 ? 1 : 0;
+        stats.plan_seconds +=
+            std::chrono::duration<double>(std::chrono::steady_clock::now() - plan0).count();
+        CK(cudaEventRecord(h->ev_lts[0], st));
         coarse_step(h, sc, n, t, dt);
+        CK(cudaEventRecord(h->ev_lts[1], st));
         // MultirateStepper::count_step (src/time/multirate.rs:1319-1331)
         stats.steps += 1;
         stats.element_evaluations += pl.evaluations_per_step();
@@ -295,6 +309,9 @@ int run_multirate(dgswe_handle* h, const dgswe_run_config* run, dgswe_callback c
         CK(cudaMemcpyAsync(&nonfinite, &h->ctl->nonfinite, sizeof nonfinite,
                            cudaMemcpyDeviceToHost, st));
         if (int s = sync(h)) return s;
+        float pass_ms = 0.0f;
+        CK(cudaEventElapsedTime(&pass_ms, h->ev_lts[0], h->ev_lts[1]));
+        stats.device_seconds += 1e-3 * pass_ms;
         if (nonfinite) {
             std::snprintf(msg, sizeof msg, "The state is not finite at t = %.1f s: it has blown up",
                           t);

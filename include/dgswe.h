@@ -354,6 +354,9 @@ typedef struct dgswe_multirate_stats {
     double ideal_evaluations;     /* every element at its own stable step */
     double level_evaluations;     /* every stage at the element's level */
     int64_t line_local_elements;  /* summed over the coarse steps */
+    int64_t plans;                /* coarse steps whose levels or rates changed */
+    double plan_seconds;          /* host time planning them (and copying the plans) */
+    double device_seconds;        /* device time of the coarse steps' passes */
 } dgswe_multirate_stats;
 
 int dgswe_multirate_stats_get(const dgswe_handle* handle, dgswe_multirate_stats* out);

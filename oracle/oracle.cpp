@@ -1833,6 +1833,9 @@ int oracle_multirate_stats_get(const oracle_handle* h, dgswe_multirate_stats* ou
     out->ideal_evaluations = mr.ideal_evaluations;
     out->level_evaluations = mr.level_evaluations;
     out->line_local_elements = mr.line_local_elements;
+    out->plans = 0;
+    out->plan_seconds = 0.0;
+    out->device_seconds = 0.0;
     return DGSWE_OK;
 }
 
