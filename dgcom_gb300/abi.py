@@ -21,7 +21,7 @@ OK, ERR_INVALID, ERR_CUDA, ERR_NONFINITE, ERR_DT_MIN, ERR_MAX_STEPS, ERR_STOPPED
 # dgswe_formulation
 WET_DRY, ENTROPY_STABLE, ENTROPY_CONSERVATIVE = range(3)
 # dgswe_boundary_kind
-BC_WALL, BC_CHARACTERISTIC = range(2)
+BC_WALL, BC_CHARACTERISTIC, BC_NODE_TIDES = range(3)
 # dgswe_elevation_only
 AT_REST, INCOMING_WAVE = range(2)
 # dgswe_friction
@@ -50,6 +50,24 @@ class TideConstituent(C.Structure):
     ]
 
 
+class NodeTides(C.Structure):
+    _fields_ = [
+        ("n_constituents", C.c_int32),
+        ("omega", _dp),
+        ("f_rate", _dp),
+        ("n_slots", C.c_int64),
+        ("positions", _dp),
+        ("coefficients", _dp),
+        ("mean", _dp),
+        ("source_depth", _dp),
+        ("slot_of_node", C.POINTER(C.c_uint32)),
+        ("velocity", C.c_int32),
+        ("use_mean", C.c_int32),
+        ("max_transport_ratio", C.c_double),
+        ("ramp_duration", C.c_double),
+    ]
+
+
 class Boundary(C.Structure):
     _fields_ = [
         ("tag", C.c_int32),
@@ -60,6 +78,7 @@ class Boundary(C.Structure):
         ("constituents", C.POINTER(TideConstituent)),
         ("mean_elevation", C.c_double),
         ("ramp_duration", C.c_double),
+        ("node_tides", C.POINTER(NodeTides)),
     ]
 
 

@@ -301,6 +301,96 @@ def adjoint_ensemble_members(n_members: int = 64, seed: int = 2029,
     return out
 
 
+def face_node_lists(n1: int) -> list[list[int]]:
+    """The volume nodes of faces 0..3 in face-node order (faces 2 and 3
+    reversed: compute_face_nodes, src/operators/operators_2d.rs:388-412)."""
+    return [[a for a in range(n1)],
+            [j * n1 + n1 - 1 for j in range(n1)],
+            [(n1 - 1) * n1 + a for a in reversed(range(n1))],
+            [j * n1 for j in reversed(range(n1))]]
+
+
+def boundary_face_nodes(form: SWEDeviceForm2D, tag: int) -> list[int]:
+    """The flat nodes of the boundary faces tagged ``tag``, each once, in
+    element and face order (as TidalAtlas::boundary_tides numbers its slots,
+    src/boundary/tidal_atlas.rs:598-630)."""
+    mesh = form.mesh
+    count: dict = {}
+    for k, quad in enumerate(mesh.elements):
+        for f in range(4):
+            key = tuple(sorted((int(quad[f]), int(quad[(f + 1) % 4]))))
+            count[key] = count.get(key, 0) + 1
+    periodic = {(int(p[0]), int(p[1])) for p in mesh.periodic} | \
+        {(int(p[2]), int(p[3])) for p in mesh.periodic}
+    n1 = form.order + 1
+    faces = face_node_lists(n1)
+    seen, out = set(), []
+    for k, quad in enumerate(mesh.elements):
+        for f in range(4):
+            key = tuple(sorted((int(quad[f]), int(quad[(f + 1) % 4]))))
+            if count[key] > 1 or (k, f) in periodic:
+                continue
+            if mesh.face_tags is not None and int(mesh.face_tags[k][f]) != tag:
+                continue
+            for node in faces[f]:
+                flat = k * n1 * n1 + node
+                if flat not in seen:
+                    seen.add(flat)
+                    out.append(flat)
+    return out
+
+
+def synthetic_node_tides(form: SWEDeviceForm2D, tag: int = TAG_OPEN,
+                         names=("M2", "S2", "N2", "K1", "O1"), seed: int = 2030,
+                         velocity: bool = True, use_mean: bool = True,
+                         max_transport_ratio: float | None = 2.5,
+                         ramp_duration: float | None = 3600.0, by_position: bool = False):
+    """BoundaryTides of a synthetic atlas on the boundary faces tagged
+    ``tag``: per forced node, each constituent's elevation amplitude and
+    phase vary smoothly along the boundary (amplitude 1 m for M2 scaled by
+    the canonical ratios, ±20 % and ±15° along it), velocity constants of
+    0.05–0.3 m/s, a mean level of a few cm and the source depth 0.8–1.2 times
+    the node's own, all smooth along the boundary. ``by_position``: no
+    slot_of_node (each face node takes the nearest slot)."""
+    from .physics import NodeTidesBoundary
+
+    ratio = {"M2": 1.0, "S2": 0.35, "N2": 0.2, "K2": 0.1, "K1": 0.1, "O1": 0.08, "P1": 0.03,
+             "Q1": 0.02}
+    rng = np.random.default_rng(seed)
+    flats = boundary_face_nodes(form, tag)
+    x, y = form.positions()
+    x, y = x.reshape(-1)[flats], y.reshape(-1)[flats]
+    length = max(float(np.ptp(x) + np.ptp(y)), 1.0)
+    along = ((x - x.min()) + (y - y.min())) / length
+    n, m = len(names), len(flats)
+    coef = np.zeros((m, n, 6))
+    for j, name in enumerate(names):
+        amp = ratio.get(name, 0.05) * (1.0 + 0.2 * np.sin(2 * math.pi * along + rng.uniform(0, 6)))
+        ph = math.radians(rng.uniform(0, 360)) + math.radians(15.0) * along
+        coef[:, j, 0] = amp * np.cos(ph)
+        coef[:, j, 1] = amp * np.sin(ph)
+        for q in (2, 4):
+            ua = rng.uniform(0.05, 0.3) * ratio.get(name, 0.05)
+            uph = math.radians(rng.uniform(0, 360)) + math.radians(10.0) * along
+            coef[:, j, q] = ua * np.cos(uph)
+            coef[:, j, q + 1] = ua * np.sin(uph)
+    omega = np.array([math.radians(tides.angular_speed(nm)) / 3600.0 for nm in names])
+    f_rate = rng.uniform(-2e-10, 2e-10, n)
+    bed = (form.bathymetry.reshape(-1)[flats] if form.bathymetry is not None else np.zeros(m))
+    # smooth along the boundary, so coincident nodes of two faces agree
+    depth = np.maximum(-bed, 0.5) * (1.0 + 0.2 * np.cos(2 * math.pi * along))
+    mean = 0.025 + 0.02 * np.sin(3 * math.pi * along)
+    slot_of_node = None
+    if not by_position:
+        slot_of_node = np.full(form.n_values, 0xFFFFFFFF, dtype=np.uint32)
+        slot_of_node[flats] = np.arange(m, dtype=np.uint32)
+    return NodeTidesBoundary(omega=omega, f_rate=f_rate, positions=np.column_stack([x, y]),
+                             coefficients=coef, mean=mean,
+                             source_depth=depth, slot_of_node=slot_of_node, velocity=velocity,
+                             use_mean=use_mean, max_transport_ratio=max_transport_ratio,
+                             ramp_duration=ramp_duration)
+
+
 # -- the reference's split-form test setups ------------------------------------
 
 L_TEST = 20_000.0

@@ -243,6 +243,82 @@ int64_t dgswe_negative_depth_clips(const dgswe_handle* h) {
 
 namespace {
 
+// Per-node tides (DGSWE_BC_NODE_TIDES): the conditions' constituents and
+// constants back to back, and every boundary face node's slot: the one
+// slot_of_node gives its flat node, else the nearest forced node
+// (BoundaryTides::slot_of, src/boundary/tidal_atlas.rs:1026-1045)
+int node_tide_tables(dgswe_handle* h, const dgswe_form& f, const Operators& ops,
+                     const Topology& topo, const Tables& t) {
+    bool any = false;
+    for (int b = 0; b < f.n_boundaries; ++b) any = any || f.boundaries[b].kind == DGSWE_BC_NODE_TIDES;
+    if (!any) return DGSWE_OK;
+    std::vector<double> omega, frate, coef, mean, depth;
+    std::vector<int64_t> slot0(f.n_boundaries, 0);
+    for (int b = 0; b < f.n_boundaries; ++b) {
+        if (f.boundaries[b].kind != DGSWE_BC_NODE_TIDES) continue;
+        const dgswe_node_tides& nt = *f.boundaries[b].node_tides;
+        Condition& c = h->P.cond[b];
+        c.nt_omega0 = (int)omega.size();
+        c.nt_slot0 = slot0[b] = (int64_t)mean.size();
+        c.nt_coef0 = (int64_t)coef.size();
+        omega.insert(omega.end(), nt.omega, nt.omega + nt.n_constituents);
+        frate.insert(frate.end(), nt.f_rate, nt.f_rate + nt.n_constituents);
+        coef.insert(coef.end(), nt.coefficients,
+                    nt.coefficients + (size_t)nt.n_slots * nt.n_constituents * 6);
+        for (int64_t q = 0; q < nt.n_slots; ++q) {
+            mean.push_back(nt.mean ? nt.mean[q] : 0.0);
+            depth.push_back(nt.source_depth ? nt.source_depth[q] : 0.0);
+        }
+    }
+    const int n1 = ops.n1, nn = ops.nn;
+    std::vector<int32_t> slot(t.bface.size() * n1, -1);
+    for (size_t bf = 0; bf < t.bface.size(); ++bf) {
+        const int ci = t.bface_cond[bf];
+        if (ci < 0 || ci >= f.n_boundaries || f.boundaries[ci].kind != DGSWE_BC_NODE_TIDES) continue;
+        const dgswe_node_tides& nt = *f.boundaries[ci].node_tides;
+        const int64_t k = t.bface[bf] >> 2;
+        const int face = (int)(t.bface[bf] & 3);
+        for (int fi = 0; fi < n1; ++fi) {
+            const int node = ops.face_node[face][fi];
+            int64_t q = -1;
+            if (nt.slot_of_node) {
+                const uint32_t v = nt.slot_of_node[k * nn + node];
+                if (v != 0xFFFFFFFFu) {
+                    if ((int64_t)v >= nt.n_slots)
+                        return fail(h, DGSWE_ERR_INVALID, "a tide slot beyond n_slots");
+                    q = v;
+                }
+            }
+            if (q < 0) {  // the nearest forced node (Mesh2D::reference_to_physical)
+                const std::array<double, 8>& c = topo.corners[k];
+                const double r = ops.r[node], sv = ops.s[node];
+                const double n0 = (1 - r) * (1 - sv) / 4, n1b = (1 + r) * (1 - sv) / 4,
+                             n2 = (1 + r) * (1 + sv) / 4, n3 = (1 - r) * (1 + sv) / 4;
+                const double x = n0 * c[0] + n1b * c[2] + n2 * c[4] + n3 * c[6];
+                const double y = n0 * c[1] + n1b * c[3] + n2 * c[5] + n3 * c[7];
+                double best = INFINITY;
+                for (int64_t p = 0; p < nt.n_slots; ++p) {
+                    const double d = std::hypot(nt.positions[2 * p] - x, nt.positions[2 * p + 1] - y);
+                    if (d < best) {
+                        best = d;
+                        q = p;
+                    }
+                }
+            }
+            slot[bf * n1 + fi] = (int32_t)(slot0[ci] + q);
+        }
+    }
+    DevTables& T = h->T;
+    int s = DGSWE_OK;
+    if ((s = upload_vec(h, slot, &T.bface_slot))) return s;
+    if ((s = upload_vec(h, omega, &T.nt_omega))) return s;
+    if ((s = upload_vec(h, frate, &T.nt_frate))) return s;
+    if ((s = upload_vec(h, coef, &T.nt_coef))) return s;
+    if ((s = upload_vec(h, mean, &T.nt_mean))) return s;
+    if ((s = upload_vec(h, depth, &T.nt_depth))) return s;
+    return DGSWE_OK;
+}
+
 int create_impl(dgswe_handle* h, const dgswe_form* f, int device) {
     auto bail = [](int s) { return s; };
     h->device = device;
@@ -334,6 +410,7 @@ int create_impl(dgswe_handle* h, const dgswe_form* f, int device) {
     fill_physics(*f, ops, !t.fcor.empty(), h->P, h->X);
     h->P.n_conditions = f->n_boundaries;
     for (int b = 0; b < f->n_boundaries; ++b) h->P.cond[b] = make_condition(f->boundaries[b]);
+    if ((s = node_tide_tables(h, *f, ops, topo, t))) return bail(s);
 
     // buffers, faces, control
     if ((s = ensure_buffer(h, DGSWE_STATE))) return bail(s);

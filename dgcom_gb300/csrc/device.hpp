@@ -44,6 +44,12 @@ struct DevTables {
     // direction and line position p, g·D[p][pos_c]·w (x and y) of the node i
     // at p, so that ∂(g∇B)_i/∂B_c is a table entry (adjoint handles only)
     const double* gdb_t = nullptr;  // [K·nn][2][n1][2]
+    // Per-node tides (BoundaryTides): each boundary face node's slot (−1:
+    // not a per-node tide), the conditions' constituents and their slots'
+    // constants, mean levels and source depths
+    const int32_t* bface_slot = nullptr;  // [B·n1]
+    const double *nt_omega = nullptr, *nt_frate = nullptr, *nt_coef = nullptr;
+    const double *nt_mean = nullptr, *nt_depth = nullptr;
 };
 
 struct Constituent {
@@ -57,6 +63,12 @@ struct Condition {
     double wall_h_min;
     double mean, ramp;
     Constituent c[kMaxConstituents];
+    // per-node tides (kind 2): the condition's constituents from nt_omega0
+    // in DevTables::nt_omega / nt_frate, its slots from nt_slot0, their
+    // constants from nt_coef0 in DevTables::nt_coef ([slot][n][6])
+    int nt_n, nt_velocity, nt_use_mean, nt_omega0;
+    int64_t nt_slot0, nt_coef0;
+    double nt_max_ratio;
 };
 
 struct Physics {

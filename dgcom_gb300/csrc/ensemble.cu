@@ -244,8 +244,12 @@ int create_impl(dgswe_ensemble* h, const dgswe_form* forms, int n, int device) {
     std::vector<Condition> conds;
     for (int m = 0; m < n; ++m) {
         cond_base[m] = (int)conds.size();
-        for (int b = 0; b < forms[m].n_boundaries; ++b)
+        for (int b = 0; b < forms[m].n_boundaries; ++b) {
+            if (forms[m].boundaries[b].kind == DGSWE_BC_NODE_TIDES)
+                return fail(h, DGSWE_ERR_UNSUPPORTED,
+                            "member %d: tides per boundary node run on a single mesh", m);
             conds.push_back(make_condition(forms[m].boundaries[b]));
+        }
     }
     h->cond_base = cond_base;
     // order groups, members in the caller's order within each

@@ -74,8 +74,20 @@ inline int check_form(const dgswe_form* f, std::string& why) {
         return why = "boundary conditions", DGSWE_ERR_INVALID;
     for (int b = 0; b < f->n_boundaries; ++b) {
         const dgswe_boundary& c = f->boundaries[b];
-        if (c.kind != DGSWE_BC_WALL && c.kind != DGSWE_BC_CHARACTERISTIC)
+        if (c.kind != DGSWE_BC_WALL && c.kind != DGSWE_BC_CHARACTERISTIC &&
+            c.kind != DGSWE_BC_NODE_TIDES)
             return why = "a boundary condition without a device form", DGSWE_ERR_UNSUPPORTED;
+        if (c.kind == DGSWE_BC_NODE_TIDES) {
+            const dgswe_node_tides* t = c.node_tides;
+            if (!t || t->n_constituents < 0 || t->n_constituents > 256 || t->n_slots <= 0 ||
+                !t->positions || !t->coefficients ||
+                (t->n_constituents > 0 && (!t->omega || !t->f_rate)))
+                return why = "per-node tides without their data", DGSWE_ERR_INVALID;
+            if (t->n_slots >= (1ll << 31)) return why = "too many tide slots", DGSWE_ERR_INVALID;
+            if (t->velocity && t->max_transport_ratio > 0.0 && t->max_transport_ratio < 1.0)
+                return why = "a transport ratio limit below 1", DGSWE_ERR_INVALID;
+            continue;
+        }
         if (c.n_constituents < 0 || c.n_constituents > kMaxConstituents ||
             (c.n_constituents > 0 && !c.constituents))
             return why = "tide constituents", DGSWE_ERR_INVALID;
@@ -93,10 +105,20 @@ inline Condition make_condition(const dgswe_boundary& in) {
     Condition c{};
     c.kind = in.kind;
     c.elevation_only = in.elevation_only;
-    c.n_constituents = in.n_constituents;
     c.wall_h_min = in.wall_h_min;
     c.mean = in.mean_elevation;
     c.ramp = in.ramp_duration;
+    if (in.kind == DGSWE_BC_NODE_TIDES) {
+        // the tables' offsets are the handle's (nt_omega0, nt_slot0, nt_coef0)
+        const dgswe_node_tides& t = *in.node_tides;
+        c.ramp = t.ramp_duration;
+        c.nt_n = t.n_constituents;
+        c.nt_velocity = t.velocity ? 1 : 0;
+        c.nt_use_mean = t.use_mean && t.mean ? 1 : 0;
+        c.nt_max_ratio = t.max_transport_ratio;
+        return c;
+    }
+    c.n_constituents = in.n_constituents;
     for (int i = 0; i < in.n_constituents; ++i) {
         const dgswe_tide_constituent& k = in.constituents[i];
         c.c[i] = {k.amplitude, 2.0 * M_PI / k.period, k.phase, k.f,

@@ -172,11 +172,35 @@ __global__ void __launch_bounds__(256) face_kernel(DevTables T, Physics P, DevBu
         else
             entropy_surface(qi, qe, nx, ny, P, fs, fdummy);
     } else {
-        // CharacteristicOBC with a uniform harmonic tide, flux F(q_b)·n
+        // CharacteristicOBC, flux F(q_b)·n: a uniform harmonic tide, or the
+        // tide per boundary node (characteristic_boundary_state,
+        // src/boundary/characteristic.rs:411-437)
         const int member = T.elem_member ? T.elem_member[k] : 0;
-        const double eta =
-            tide_elevation(c, LISTED ? lts_stage(lp, k).time : ctl[member].stage[slot].time);
-        const Q qb = characteristic_state(qi, u, v, eta, nx, ny, c.elevation_only, g, h_min);
+        const double t = LISTED ? lts_stage(lp, k).time : ctl[member].stage[slot].time;
+        Q qb;
+        if (c.kind == kBcNodeTides) {
+            const int64_t s = T.bface_slot[bfi * N1 + fi];
+            double eta, ue, ve;
+            bool has_uv;
+            node_tide_state(T.nt_omega + c.nt_omega0, T.nt_frate + c.nt_omega0,
+                            T.nt_coef + c.nt_coef0 + (s - c.nt_slot0) * c.nt_n * 6, c.nt_n, t,
+                            c.ramp, c.nt_use_mean ? T.nt_mean[s] : 0.0, c.nt_velocity,
+                            c.nt_max_ratio, T.nt_depth[s], qi.b, eta, ue, ve, has_uv);
+            const double h_e = fmax(eta - qi.b, 0.0);
+            double un_e = 0.0, ut_e;
+            if (has_uv) {
+                un_e = ue * nx + ve * ny;
+                ut_e = -ue * ny + ve * nx;
+            } else {
+                if (c.elevation_only == kIncomingWave)
+                    un_e = 2.0 * (sqrt(g * fmax(-qi.b, 0.0)) - sqrt(g * h_e));
+                ut_e = -u * ny + v * nx;
+            }
+            qb = characteristic_state_ext(qi, h_e, un_e, ut_e, nx, ny, g, h_min);
+        } else {
+            qb = characteristic_state(qi, u, v, tide_elevation(c, t), nx, ny, c.elevation_only, g,
+                                      h_min);
+        }
         fs = wflux(qb, qb, nx, ny, g);
     }
     const int64_t sl = B * N1 + fi;

@@ -30,7 +30,7 @@ namespace dgswe {
 namespace DGSWE_NS {
 
 constexpr int kWetDry = 0, kEntropyStable = 1, kEntropyConservative = 2;
-constexpr int kBcWall = 0;
+constexpr int kBcWall = 0, kBcNodeTides = 2;
 constexpr int kIncomingWave = 1;
 
 // ---------------------------------------------------------------------------
@@ -436,16 +436,11 @@ DG_PT Q wall_ghost(const Q& qi, double u, double v, double nx, double ny, double
     return qe;
 }
 
-// CharacteristicOBC's boundary state (src/boundary/characteristic.rs:411-437,
-// 481-520) from the interior node qi (velocity u, v) and the external
-// elevation eta, with its node velocity
-DG_PT Q characteristic_state(const Q& qi, double u, double v, double eta, double nx, double ny,
-                             int elevation_only, double g, double h_min) {
-    const double bathy = qi.b;
-    const double h_e = fmax(eta - bathy, 0.0);
-    double un_e = 0.0;
-    if (elevation_only == kIncomingWave) un_e = 2.0 * (sqrt(g * fmax(-bathy, 0.0)) - sqrt(g * h_e));
-    const double ut_e = -u * ny + v * nx;
+// characteristic_state (src/boundary/characteristic.rs:481-520): the
+// boundary state from the interior node qi and the external depth and
+// normal and tangential velocity, with its node velocity
+DG_PT Q characteristic_state_ext(const Q& qi, double h_e, double un_e, double ut_e, double nx,
+                                 double ny, double g, double h_min) {
     const double h_i = fmax(qi.h, 0.0);
     double un_i = 0.0, ut_i = 0.0;
     if (h_i > h_min) {
@@ -488,6 +483,61 @@ DG_PT Q characteristic_state(const Q& qi, double u, double v, double eta, double
     qb.b = qi.b;
     node_velocity(qb.h, qb.hu, qb.hv, h_min, qb.u, qb.v);
     return qb;
+}
+
+// CharacteristicOBC's boundary state (src/boundary/characteristic.rs:411-437)
+// for elevation-only external data: the interior node qi (velocity u, v)
+// and the external elevation eta
+DG_PT Q characteristic_state(const Q& qi, double u, double v, double eta, double nx, double ny,
+                             int elevation_only, double g, double h_min) {
+    const double bathy = qi.b;
+    const double h_e = fmax(eta - bathy, 0.0);
+    double un_e = 0.0;
+    if (elevation_only == kIncomingWave) un_e = 2.0 * (sqrt(g * fmax(-bathy, 0.0)) - sqrt(g * h_e));
+    const double ut_e = -u * ny + v * nx;
+    return characteristic_state_ext(qi, h_e, un_e, ut_e, nx, ny, g, h_min);
+}
+
+// tidal_ramp (src/boundary/harmonic_tide.rs:24-32): τ²(3 − 2τ), τ = t/duration in [0, 1]
+DG_PT double tidal_ramp(double t, double duration) {
+    if (!fp::gt0(duration)) return 1.0;
+    double tau = t / duration;
+    tau = fp::lt0(tau) ? 0.0 : (fp::gt(tau, 1.0) ? 1.0 : tau);
+    return tau * tau * (3.0 - 2.0 * tau);
+}
+
+// BoundaryTides' external state at a slot (tide_term, tide_level,
+// tide_state: src/boundary/tidal_atlas.rs:1078-1131) over the child bed
+// `bed`: η, and (u, v) if the tides carry velocity (has_uv)
+DG_PT void node_tide_state(const double* omega, const double* f_rate, const double* coef, int n,
+                           double t, double ramp_duration, double mean, int velocity,
+                           double max_ratio, double source_depth, double bed, double& eta,
+                           double& u, double& v, bool& has_uv) {
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    for (int j = 0; j < n; ++j) {
+        const double f = 1.0 + f_rate[j] * t;
+        const double x = omega[j] * t;
+        const double cs = cos(x), sn = sin(x);
+        const double* c = coef + 6 * j;
+        s0 += f * (c[0] * cs + c[1] * sn);
+        s1 += f * (c[2] * cs + c[3] * sn);
+        s2 += f * (c[4] * cs + c[5] * sn);
+    }
+    const double ramp = tidal_ramp(t, ramp_duration);
+    eta = mean + ramp * s0;
+    u = ramp * s1;
+    v = ramp * s2;
+    has_uv = velocity != 0;
+    if (has_uv && max_ratio > 0.0) {
+        const double d_source = source_depth + eta, d_child = eta - bed;
+        if (fp::gt0(source_depth) && fp::gt0(d_source) && fp::gt0(d_child)) {
+            double ratio = d_source / d_child;
+            const double lo = 1.0 / max_ratio;
+            ratio = fp::lt(ratio, lo) ? lo : (fp::gt(ratio, max_ratio) ? max_ratio : ratio);
+            u *= ratio;
+            v *= ratio;
+        }
+    }
 }
 
 }  // namespace DGSWE_NS

@@ -40,6 +40,30 @@ class TidalBoundary:
 
 
 @dataclass
+class NodeTidesBoundary:
+    """CharacteristicOBC with BoundaryTides: an atlas's harmonic constants
+    per forced boundary node (src/boundary/tidal_atlas.rs:855-1070, the
+    device form DeviceExternal2D::Tides). ``coefficients`` [n_slots][n][6]
+    are C, S of η, u and v per constituent at the epoch's nodal terms;
+    ``omega`` ω′ and ``f_rate`` ḟ/f₀ per constituent; ``slot_of_node`` the
+    slot of each flat mesh node (0xFFFFFFFF: none; None: by nearest
+    position)."""
+
+    omega: np.ndarray
+    f_rate: np.ndarray
+    positions: np.ndarray            # [n_slots][2]
+    coefficients: np.ndarray         # [n_slots][n][6]
+    mean: np.ndarray | None = None
+    source_depth: np.ndarray | None = None
+    slot_of_node: np.ndarray | None = None
+    velocity: bool = False
+    use_mean: bool = False
+    max_transport_ratio: float | None = None
+    ramp_duration: float | None = None
+    incoming_wave: bool = False
+
+
+@dataclass
 class SWEDeviceForm2D:
     mesh: QuadMesh
     order: int
@@ -151,6 +175,36 @@ class SWEDeviceForm2D:
             if isinstance(bc, WallBoundary):
                 bcs[i].kind = abi.BC_WALL
                 bcs[i].wall_h_min = bc.h_min
+            elif isinstance(bc, NodeTidesBoundary):
+                bcs[i].kind = abi.BC_NODE_TIDES
+                bcs[i].elevation_only = abi.INCOMING_WAVE if bc.incoming_wave else abi.AT_REST
+                nt = abi.NodeTides()
+                nt.n_constituents = len(bc.omega)
+                nt.omega = arr(bc.omega, np.float64).ctypes.data_as(C.POINTER(C.c_double))
+                nt.f_rate = arr(bc.f_rate, np.float64).ctypes.data_as(C.POINTER(C.c_double))
+                pos = arr(np.asarray(bc.positions).reshape(-1, 2), np.float64)
+                nt.n_slots = pos.shape[0]
+                nt.positions = pos.ctypes.data_as(C.POINTER(C.c_double))
+                coef = arr(np.asarray(bc.coefficients).reshape(-1), np.float64)
+                if coef.size != pos.shape[0] * len(bc.omega) * 6:
+                    raise ValueError("coefficients need [n_slots][n_constituents][6] values")
+                nt.coefficients = coef.ctypes.data_as(C.POINTER(C.c_double))
+                if bc.mean is not None:
+                    nt.mean = arr(bc.mean, np.float64).ctypes.data_as(C.POINTER(C.c_double))
+                if bc.source_depth is not None:
+                    nt.source_depth = arr(bc.source_depth, np.float64).ctypes.data_as(
+                        C.POINTER(C.c_double))
+                if bc.slot_of_node is not None:
+                    sl = arr(np.asarray(bc.slot_of_node).reshape(-1), np.uint32)
+                    if sl.size != self.n_values:
+                        raise ValueError("slot_of_node needs one slot per mesh node")
+                    nt.slot_of_node = sl.ctypes.data_as(C.POINTER(C.c_uint32))
+                nt.velocity = 1 if bc.velocity else 0
+                nt.use_mean = 1 if bc.use_mean else 0
+                nt.max_transport_ratio = bc.max_transport_ratio or 0.0
+                nt.ramp_duration = bc.ramp_duration or 0.0
+                keep.append(nt)
+                bcs[i].node_tides = C.pointer(nt)
             else:
                 bcs[i].kind = abi.BC_CHARACTERISTIC
                 bcs[i].elevation_only = abi.INCOMING_WAVE if bc.incoming_wave else abi.AT_REST

@@ -60,8 +60,10 @@ enum dgswe_formulation {
 
 /* DeviceBoundary2D (src/boundary/boundary_2d.rs:213-231). */
 enum dgswe_boundary_kind {
-    DGSWE_BC_WALL = 0,          /* Reflective2D: free-slip mirror ghost state */
-    DGSWE_BC_CHARACTERISTIC = 1 /* CharacteristicOBC with a uniform harmonic tide */
+    DGSWE_BC_WALL = 0,           /* Reflective2D: free-slip mirror ghost state */
+    DGSWE_BC_CHARACTERISTIC = 1, /* CharacteristicOBC with a uniform harmonic tide */
+    DGSWE_BC_NODE_TIDES = 2      /* CharacteristicOBC with harmonic constants per boundary
+                                    node (DeviceExternal2D::Tides, BoundaryTides) */
 };
 
 /* ElevationOnly (src/boundary/characteristic.rs:347-355). */
@@ -113,6 +115,31 @@ typedef struct dgswe_tide_constituent {
 } dgswe_tide_constituent;
 
 /* The condition of the boundary faces tagged `tag`. */
+/* BoundaryTides (src/boundary/tidal_atlas.rs:855-1070) as plain data: an
+ * atlas's tide at the forced boundary nodes, in the order of its slots. The
+ * external state of slot s at time t is, with f_j = 1 + f_rate_j·t and the
+ * constants c = coefficients[s][j] = (C_η, S_η, C_u, S_u, C_v, S_v),
+ *   (η, u, v) = (mean_s, 0, 0) + ramp(t)·Σ_j f_j (C cos ω′_j t + S sin ω′_j t)
+ * (tide_term, tide_level), with (u, v) only if velocity ≠ 0, scaled by
+ * D_source/D_child within [1/r, r] where max_transport_ratio r > 0
+ * (tide_state). A boundary face node takes the slot slot_of_node gives its
+ * flat mesh node, or else the slot nearest to it. */
+typedef struct dgswe_node_tides {
+    int32_t n_constituents;
+    const double* omega;          /* [n] ω′ = ω + u̇ (rad/s) */
+    const double* f_rate;         /* [n] ḟ/f₀ (1/s) */
+    int64_t n_slots;
+    const double* positions;      /* [n_slots][2] x, y of the forced nodes */
+    const double* coefficients;   /* [n_slots][n][6] */
+    const double* mean;           /* [n_slots] Z0 (use_mean), or NULL */
+    const double* source_depth;   /* [n_slots] the source's still-water depth, or NULL */
+    const uint32_t* slot_of_node; /* [n_elements·(N+1)²] or NULL; 0xFFFFFFFF: none */
+    int32_t velocity;             /* the tides carry (u, v) */
+    int32_t use_mean;             /* add mean (not ramped) */
+    double max_transport_ratio;   /* ≤ 0: no transport scaling */
+    double ramp_duration;         /* s; ≤ 0: no ramp */
+} dgswe_node_tides;
+
 typedef struct dgswe_boundary {
     int32_t tag;            /* the face tag this condition applies to */
     int32_t kind;           /* dgswe_boundary_kind */
@@ -122,6 +149,7 @@ typedef struct dgswe_boundary {
     const dgswe_tide_constituent* constituents;
     double mean_elevation;  /* η₀ (m), not ramped */
     double ramp_duration;   /* s; ≤ 0: no ramp (src/boundary/harmonic_tide.rs:24-32) */
+    const dgswe_node_tides* node_tides; /* DGSWE_BC_NODE_TIDES: the tide per node */
 } dgswe_boundary;
 
 /* SWEDeviceForm2D (src/physics/device.rs:27-62) as plain data, with the

@@ -414,6 +414,65 @@ struct Boundary {
     int elevation_only = DGSWE_AT_REST;
     std::vector<dgswe_tide_constituent> constituents;
     double mean_elevation = 0.0, ramp_duration = 0.0;
+    // BoundaryTides (src/boundary/tidal_atlas.rs:855-1070), a copy
+    struct NodeTides {
+        int n = 0;
+        std::vector<double> omega, f_rate, positions, coefficients, mean, source_depth;
+        std::vector<uint32_t> slot_of_node;
+        bool velocity = false, use_mean = false;
+        double max_ratio = 0.0, ramp = 0.0;
+        int64_t n_slots = 0;
+    } tides;
+
+    // BoundaryTides::slot_of (tidal_atlas.rs:1026-1045)
+    int64_t slot_of(int64_t node_index, double x, double y) const {
+        if (!tides.slot_of_node.empty() && tides.slot_of_node[node_index] != 0xFFFFFFFFu)
+            return tides.slot_of_node[node_index];
+        int64_t best = 0;
+        double dmin = INF;
+        for (int64_t p = 0; p < tides.n_slots; ++p) {
+            double d = std::hypot(tides.positions[2 * p] - x, tides.positions[2 * p + 1] - y);
+            if (d < dmin) {
+                dmin = d;
+                best = p;
+            }
+        }
+        return best;
+    }
+
+    // BoundaryTides::external_state (tidal_atlas.rs:1049-1065): η and, with
+    // velocity, (u, v) over the child bed `bed`
+    void node_external(int64_t slot, double t, double bed, double& eta, double& u, double& v,
+                       bool& has_uv) const {
+        const int n = tides.n;
+        double sum[3] = {0.0, 0.0, 0.0};
+        for (int j = 0; j < n; ++j) {
+            double f = 1.0 + tides.f_rate[j] * t;
+            double x = tides.omega[j] * t;
+            double sn = std::sin(x), cs = std::cos(x);
+            const double* c = &tides.coefficients[((size_t)slot * n + j) * 6];
+            sum[0] += f * (c[0] * cs + c[1] * sn);  // tide_term (tidal_atlas.rs:1078-1082)
+            sum[1] += f * (c[2] * cs + c[3] * sn);
+            sum[2] += f * (c[4] * cs + c[5] * sn);
+        }
+        double ramp = tidal_ramp(t, tides.ramp);
+        double mean = tides.use_mean ? tides.mean[slot] : 0.0;
+        eta = mean + ramp * sum[0];  // tide_level (tidal_atlas.rs:1088-1091)
+        u = ramp * sum[1];
+        v = ramp * sum[2];
+        has_uv = tides.velocity;
+        if (has_uv && tides.max_ratio > 0.0) {  // tide_state (tidal_atlas.rs:1100-1131)
+            double h_source = tides.source_depth[slot];
+            double d_source = h_source + eta, d_child = eta - bed;
+            if (h_source > 0.0 && d_source > 0.0 && d_child > 0.0) {
+                double ratio = d_source / d_child;
+                double lo = 1.0 / tides.max_ratio;
+                ratio = ratio < lo ? lo : (ratio > tides.max_ratio ? tides.max_ratio : ratio);
+                u *= ratio;
+                v *= ratio;
+            }
+        }
+    }
 
     // HarmonicTide::elevation (src/boundary/harmonic_tide.rs:124-136)
     double elevation(double t) const {
@@ -565,17 +624,36 @@ static State boundary_flux(const Model& m, int64_t k, int face, int node, const 
         surface_flux(m, q_int, q_ext, nx, ny, fa, fb);
         return fa;
     }
-    // CharacteristicOBC with a uniform tide: characteristic_boundary_state
-    // (src/boundary/characteristic.rs:411-437)
-    double eta = bc.elevation(time);
+    // CharacteristicOBC: characteristic_boundary_state
+    // (src/boundary/characteristic.rs:411-437) with a uniform tide or the
+    // tide per boundary node
     double bathy = q_int.b;
+    double eta, ue = 0.0, ve = 0.0;
+    bool has_uv = false;
+    if (bc.kind == DGSWE_BC_NODE_TIDES) {
+        auto c = m.mesh.corners(k);
+        double r = m.ops.nodes_r[node], sv = m.ops.nodes_s[node];
+        double n0 = (1 - r) * (1 - sv) / 4, n1b = (1 + r) * (1 - sv) / 4;
+        double n2 = (1 + r) * (1 + sv) / 4, n3 = (1 - r) * (1 + sv) / 4;
+        double x = n0 * c[0][0] + n1b * c[1][0] + n2 * c[2][0] + n3 * c[3][0];
+        double y = n0 * c[0][1] + n1b * c[1][1] + n2 * c[2][1] + n3 * c[3][1];
+        int64_t slot = bc.slot_of(k * m.ops.nn + node, x, y);
+        bc.node_external(slot, time, bathy, eta, ue, ve, has_uv);
+    } else {
+        eta = bc.elevation(time);
+    }
     double h_e = fmax_(eta - bathy, 0.0);
-    double un_e = 0.0;
-    if (bc.elevation_only == DGSWE_INCOMING_WAVE)
-        un_e = 2.0 * (std::sqrt(g * fmax_(-bathy, 0.0)) - std::sqrt(g * h_e));
-    double u, v;
-    velocity_simple(interior, h_min, u, v);
-    double ut_e = -u * ny + v * nx;
+    double un_e = 0.0, ut_e;
+    if (has_uv) {
+        un_e = ue * nx + ve * ny;
+        ut_e = -ue * ny + ve * nx;
+    } else {
+        if (bc.elevation_only == DGSWE_INCOMING_WAVE)
+            un_e = 2.0 * (std::sqrt(g * fmax_(-bathy, 0.0)) - std::sqrt(g * h_e));
+        double u, v;
+        velocity_simple(interior, h_min, u, v);
+        ut_e = -u * ny + v * nx;
+    }
     State qb = characteristic_state(interior, h_e, un_e, ut_e, nx, ny, g, h_min);
     Node nb = make_node(qb, q_int.b, h_min);
     (void)k;
@@ -1623,6 +1701,31 @@ int oracle_create(const dgswe_form* f, int device, oracle_handle** out) {
         bc.constituents.assign(in.constituents, in.constituents + in.n_constituents);
         bc.mean_elevation = in.mean_elevation;
         bc.ramp_duration = in.ramp_duration;
+        if (in.kind == DGSWE_BC_NODE_TIDES) {
+            const dgswe_node_tides* t = in.node_tides;
+            if (!t || t->n_slots <= 0 || !t->positions || !t->coefficients) {
+                delete m;
+                return DGSWE_ERR_INVALID;
+            }
+            Boundary::NodeTides& nt = bc.tides;
+            nt.n = t->n_constituents;
+            nt.n_slots = t->n_slots;
+            nt.omega.assign(t->omega, t->omega + nt.n);
+            nt.f_rate.assign(t->f_rate, t->f_rate + nt.n);
+            nt.positions.assign(t->positions, t->positions + 2 * t->n_slots);
+            nt.coefficients.assign(t->coefficients, t->coefficients + (size_t)t->n_slots * nt.n * 6);
+            nt.mean.assign(t->n_slots, 0.0);
+            nt.source_depth.assign(t->n_slots, 0.0);
+            if (t->mean) nt.mean.assign(t->mean, t->mean + t->n_slots);
+            if (t->source_depth) nt.source_depth.assign(t->source_depth, t->source_depth + t->n_slots);
+            if (t->slot_of_node)
+                nt.slot_of_node.assign(t->slot_of_node,
+                                       t->slot_of_node + (size_t)f->n_elements * m->ops.nn);
+            nt.velocity = t->velocity != 0;
+            nt.use_mean = t->use_mean != 0 && t->mean;
+            nt.max_ratio = t->max_transport_ratio;
+            nt.ramp = t->ramp_duration;
+        }
         m->boundaries[in.tag] = bc;
     }
     for (auto& e : m->mesh.edges)
