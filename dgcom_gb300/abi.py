@@ -21,7 +21,7 @@ OK, ERR_INVALID, ERR_CUDA, ERR_NONFINITE, ERR_DT_MIN, ERR_MAX_STEPS, ERR_STOPPED
 # dgswe_formulation
 WET_DRY, ENTROPY_STABLE, ENTROPY_CONSERVATIVE = range(3)
 # dgswe_boundary_kind
-BC_WALL, BC_CHARACTERISTIC, BC_NODE_TIDES = range(3)
+BC_WALL, BC_CHARACTERISTIC, BC_NODE_TIDES, BC_PARENT = range(4)
 # dgswe_elevation_only
 AT_REST, INCOMING_WAVE = range(2)
 # dgswe_friction
@@ -68,6 +68,24 @@ class NodeTides(C.Structure):
     ]
 
 
+class ParentSeries(C.Structure):
+    _fields_ = [
+        ("n_slots", C.c_int64),
+        ("positions", _dp),
+        ("on_boundary", C.POINTER(C.c_uint8)),
+        ("slot_of_node", C.POINTER(C.c_uint32)),
+        ("n_times", C.c_int64),
+        ("times", _dp),
+        ("values", C.POINTER(C.c_float)),
+        ("parent_depth", _dp),
+        ("cubic", C.c_int32),
+        ("velocity", C.c_int32),
+        ("reference_level", C.c_double),
+        ("max_transport_ratio", C.c_double),
+        ("ramp_duration", C.c_double),
+    ]
+
+
 class Boundary(C.Structure):
     _fields_ = [
         ("tag", C.c_int32),
@@ -79,6 +97,7 @@ class Boundary(C.Structure):
         ("mean_elevation", C.c_double),
         ("ramp_duration", C.c_double),
         ("node_tides", C.POINTER(NodeTides)),
+        ("parent", C.POINTER(ParentSeries)),
     ]
 
 

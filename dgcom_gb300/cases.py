@@ -391,6 +391,58 @@ def synthetic_node_tides(form: SWEDeviceForm2D, tag: int = TAG_OPEN,
                              ramp_duration=ramp_duration)
 
 
+def synthetic_parent(form: SWEDeviceForm2D, tag: int = TAG_OPEN, t0: float = 0.0,
+                     t1: float = 43_200.0, dt_snap: float = 3600.0, seed: int = 2031,
+                     cubic: bool = True, velocity: bool = True,
+                     max_transport_ratio: float | None = 2.5, reference_level: float = 0.1,
+                     ramp_duration: float | None = 3600.0, by_position: bool = False,
+                     band: int = 0):
+    """An OceanModelState of a synthetic parent on the boundary faces tagged
+    ``tag``: hourly snapshots (float32) from t0 to t1 of a parent whose ζ is
+    a semidiurnal and a diurnal wave travelling along the boundary plus a
+    slow surge, with depth-mean currents, and a parent depth 0.8–1.2 times
+    the node's own. ``band`` extra slots off the boundary (not on_boundary)
+    stand in for a relaxation band's nodes. ``by_position``: no
+    slot_of_node."""
+    from .physics import ParentBoundary
+
+    rng = np.random.default_rng(seed)
+    flats = boundary_face_nodes(form, tag)
+    x, y = form.positions()
+    x, y = x.reshape(-1)[flats], y.reshape(-1)[flats]
+    length = max(float(np.ptp(x) + np.ptp(y)), 1.0)
+    along = ((x - x.min()) + (y - y.min())) / length
+    times = np.arange(t0, t1 + 0.5 * dt_snap, dt_snap)
+    w1, w2 = 2 * math.pi / 44_714.0, 2 * math.pi / 86_164.0
+    p1, p2 = rng.uniform(0, 2 * math.pi, 2)
+    tt = times[None, :]
+    a = along[:, None]
+    zeta = (0.8 * np.cos(w1 * tt - 0.6 * a + p1) + 0.2 * np.cos(w2 * tt - 0.3 * a + p2)
+            + 0.05 * np.sin(2 * math.pi * tt / 172_800.0))
+    u = 0.3 * np.cos(w1 * tt - 0.6 * a + p1 + 0.7)
+    v = 0.1 * np.sin(w1 * tt - 0.6 * a + p1 + 0.2)
+    values = np.stack([zeta, u, v], axis=-1)
+    positions = np.column_stack([x, y])
+    bed = form.bathymetry.reshape(-1)[flats] if form.bathymetry is not None else np.zeros(len(x))
+    depth = np.maximum(-bed, 0.5) * (1.0 + 0.2 * np.cos(2 * math.pi * along))
+    on_boundary = np.ones(len(x), dtype=bool)
+    if band:
+        # band slots: inside the domain, far from the boundary's nodes
+        positions = np.vstack([positions, positions[:band] + 1e5])
+        values = np.concatenate([values, values[:band] * 0.5], axis=0)
+        depth = np.concatenate([depth, depth[:band]])
+        on_boundary = np.concatenate([on_boundary, np.zeros(band, dtype=bool)])
+    slot_of_node = None
+    if not by_position:
+        slot_of_node = np.full(form.n_values, 0xFFFFFFFF, dtype=np.uint32)
+        slot_of_node[flats] = np.arange(len(flats), dtype=np.uint32)
+    return ParentBoundary(positions=positions, times=times,
+                          values=values.astype(np.float32), parent_depth=depth,
+                          on_boundary=on_boundary, slot_of_node=slot_of_node, cubic=cubic,
+                          velocity=velocity, reference_level=reference_level,
+                          max_transport_ratio=max_transport_ratio, ramp_duration=ramp_duration)
+
+
 # -- the reference's split-form test setups ------------------------------------
 
 L_TEST = 20_000.0

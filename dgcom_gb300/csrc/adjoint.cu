@@ -413,9 +413,10 @@ int check_config(dgswe_adjoint* a, const dgswe_form* forms, int n, const dgswe_a
         if (forms[m].order != forms[0].order)
             return afail(a, DGSWE_ERR_UNSUPPORTED, "an adjoint ensemble has members of one order");
         for (int b = 0; b < forms[m].n_boundaries; ++b)
-            if (forms[m].boundaries[b].kind == DGSWE_BC_NODE_TIDES)
+            if (forms[m].boundaries[b].kind == DGSWE_BC_NODE_TIDES ||
+                forms[m].boundaries[b].kind == DGSWE_BC_PARENT)
                 return afail(a, DGSWE_ERR_UNSUPPORTED,
-                             "the adjoint covers walls and uniform tides, not tides per node");
+                             "the adjoint covers walls and uniform tides, not data per node");
     }
     if (cfg->scheme != DGSWE_SSP_RK3)
         return afail(a, DGSWE_ERR_UNSUPPORTED, "the adjoint covers SSP-RK3");

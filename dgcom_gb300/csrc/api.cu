@@ -247,14 +247,33 @@ namespace {
 // constants back to back, and every boundary face node's slot: the one
 // slot_of_node gives its flat node, else the nearest forced node
 // (BoundaryTides::slot_of, src/boundary/tidal_atlas.rs:1026-1045)
+bool per_node(const dgswe_boundary& b) {
+    return b.kind == DGSWE_BC_NODE_TIDES || b.kind == DGSWE_BC_PARENT;
+}
+
 int node_tide_tables(dgswe_handle* h, const dgswe_form& f, const Operators& ops,
                      const Topology& topo, const Tables& t) {
     bool any = false;
-    for (int b = 0; b < f.n_boundaries; ++b) any = any || f.boundaries[b].kind == DGSWE_BC_NODE_TIDES;
+    for (int b = 0; b < f.n_boundaries; ++b) any = any || per_node(f.boundaries[b]);
     if (!any) return DGSWE_OK;
-    std::vector<double> omega, frate, coef, mean, depth;
+    std::vector<double> omega, frate, coef, mean, depth, ptimes;
+    std::vector<float> pvalues;
     std::vector<int64_t> slot0(f.n_boundaries, 0);
     for (int b = 0; b < f.n_boundaries; ++b) {
+        if (f.boundaries[b].kind == DGSWE_BC_PARENT) {
+            const dgswe_parent_series& ps = *f.boundaries[b].parent;
+            Condition& c = h->P.cond[b];
+            c.nt_slot0 = slot0[b] = (int64_t)depth.size();
+            c.pt_time0 = (int64_t)ptimes.size();
+            c.pt_val0 = (int64_t)pvalues.size();
+            ptimes.insert(ptimes.end(), ps.times, ps.times + ps.n_times);
+            pvalues.insert(pvalues.end(), ps.values, ps.values + (size_t)ps.n_slots * ps.n_times * 3);
+            for (int64_t q = 0; q < ps.n_slots; ++q) {
+                mean.push_back(0.0);
+                depth.push_back(ps.parent_depth ? ps.parent_depth[q] : NAN);
+            }
+            continue;
+        }
         if (f.boundaries[b].kind != DGSWE_BC_NODE_TIDES) continue;
         const dgswe_node_tides& nt = *f.boundaries[b].node_tides;
         Condition& c = h->P.cond[b];
@@ -274,18 +293,23 @@ int node_tide_tables(dgswe_handle* h, const dgswe_form& f, const Operators& ops,
     std::vector<int32_t> slot(t.bface.size() * n1, -1);
     for (size_t bf = 0; bf < t.bface.size(); ++bf) {
         const int ci = t.bface_cond[bf];
-        if (ci < 0 || ci >= f.n_boundaries || f.boundaries[ci].kind != DGSWE_BC_NODE_TIDES) continue;
-        const dgswe_node_tides& nt = *f.boundaries[ci].node_tides;
+        if (ci < 0 || ci >= f.n_boundaries || !per_node(f.boundaries[ci])) continue;
+        const dgswe_boundary& bc = f.boundaries[ci];
+        const bool parent = bc.kind == DGSWE_BC_PARENT;
+        const int64_t n_slots = parent ? bc.parent->n_slots : bc.node_tides->n_slots;
+        const double* positions = parent ? bc.parent->positions : bc.node_tides->positions;
+        const uint32_t* slot_of_node = parent ? bc.parent->slot_of_node : bc.node_tides->slot_of_node;
+        const uint8_t* on_boundary = parent ? bc.parent->on_boundary : nullptr;
         const int64_t k = t.bface[bf] >> 2;
         const int face = (int)(t.bface[bf] & 3);
         for (int fi = 0; fi < n1; ++fi) {
             const int node = ops.face_node[face][fi];
             int64_t q = -1;
-            if (nt.slot_of_node) {
-                const uint32_t v = nt.slot_of_node[k * nn + node];
+            if (slot_of_node) {
+                const uint32_t v = slot_of_node[k * nn + node];
                 if (v != 0xFFFFFFFFu) {
-                    if ((int64_t)v >= nt.n_slots)
-                        return fail(h, DGSWE_ERR_INVALID, "a tide slot beyond n_slots");
+                    if ((int64_t)v >= n_slots)
+                        return fail(h, DGSWE_ERR_INVALID, "a boundary slot beyond n_slots");
                     q = v;
                 }
             }
@@ -297,8 +321,9 @@ int node_tide_tables(dgswe_handle* h, const dgswe_form& f, const Operators& ops,
                 const double x = n0 * c[0] + n1b * c[2] + n2 * c[4] + n3 * c[6];
                 const double y = n0 * c[1] + n1b * c[3] + n2 * c[5] + n3 * c[7];
                 double best = INFINITY;
-                for (int64_t p = 0; p < nt.n_slots; ++p) {
-                    const double d = std::hypot(nt.positions[2 * p] - x, nt.positions[2 * p + 1] - y);
+                for (int64_t p = 0; p < n_slots; ++p) {
+                    if (on_boundary && !on_boundary[p]) continue;
+                    const double d = std::hypot(positions[2 * p] - x, positions[2 * p + 1] - y);
                     if (d < best) {
                         best = d;
                         q = p;
@@ -316,6 +341,16 @@ int node_tide_tables(dgswe_handle* h, const dgswe_form& f, const Operators& ops,
     if ((s = upload_vec(h, coef, &T.nt_coef))) return s;
     if ((s = upload_vec(h, mean, &T.nt_mean))) return s;
     if ((s = upload_vec(h, depth, &T.nt_depth))) return s;
+    if ((s = upload_vec(h, ptimes, &T.pt_times))) return s;
+    if ((s = upload_vec(h, pvalues, &T.pt_values))) return s;
+    // the parents' time ranges, for the runs' checks
+    for (int b = 0; b < f.n_boundaries; ++b)
+        if (f.boundaries[b].kind == DGSWE_BC_PARENT) {
+            const dgswe_parent_series& ps = *f.boundaries[b].parent;
+            if (ps.n_times > 1)
+                h->parent_range = {std::max(h->parent_range.first, ps.times[0]),
+                                   std::min(h->parent_range.second, ps.times[ps.n_times - 1])};
+        }
     return DGSWE_OK;
 }
 
@@ -519,6 +554,8 @@ int dgswe_compute_rhs(dgswe_handle* h, int32_t input, double time, double* out_h
     if (!valid_buffer(input) || n != h->n_values || !out_h || !out_hu || !out_hv)
         return fail(h, DGSWE_ERR_INVALID, "compute_rhs: buffer %d, %lld values", input,
                     (long long)n);
+    if (!(time >= h->parent_range.first && time <= h->parent_range.second))
+        return fail(h, DGSWE_ERR_INVALID, "compute_rhs: t = %g leaves the parent's snapshots", time);
     CK(cudaSetDevice(h->device));
     if (int s = ensure_buffer(h, input)) return s;
     if (int s = ensure_buffer(h, kRhsBuffer)) return s;
@@ -540,6 +577,9 @@ int dgswe_stage(dgswe_handle* h, const dgswe_stage_plan* plan) {
         return fail(h, DGSWE_ERR_INVALID, "stage: invalid plan or buffer ids");
     if (plan->out == plan->input)
         return fail(h, DGSWE_ERR_INVALID, "stage: out must differ from input");
+    if (!(plan->time >= h->parent_range.first && plan->time <= h->parent_range.second))
+        return fail(h, DGSWE_ERR_INVALID, "stage: t = %g leaves the parent's snapshots",
+                    plan->time);
     CK(cudaSetDevice(h->device));
     for (int id : {plan->base, plan->input, plan->out})
         if (int s = ensure_buffer(h, id)) return s;
@@ -597,6 +637,8 @@ int dgswe_step(dgswe_handle* h, int32_t scheme, double t, double dt) {
     if (!h) return DGSWE_ERR_INVALID;
     if (scheme != DGSWE_SSP_RK3 && scheme != DGSWE_SSP_RK43)
         return fail(h, DGSWE_ERR_INVALID, "step: scheme %d", scheme);
+    if (!(t >= h->parent_range.first && t + dt <= h->parent_range.second))
+        return fail(h, DGSWE_ERR_INVALID, "step: (%g, %g) leaves the parent's snapshots", t, t + dt);
     CK(cudaSetDevice(h->device));
     double st[4][4];
     const int n = scheme_table(scheme, st);
@@ -627,6 +669,10 @@ int dgswe_run(dgswe_handle* h, const dgswe_run_config* run, dgswe_callback callb
     if (run->levels < 0 || run->levels > DGSWE_MAX_LEVELS)
         return fail(h, DGSWE_ERR_INVALID, "run: %d levels of local time stepping (0..%d)",
                     run->levels, DGSWE_MAX_LEVELS);
+    if (!(run->t_start >= h->parent_range.first && run->t_end <= h->parent_range.second))
+        return fail(h, DGSWE_ERR_INVALID,
+                    "run: the span (%g, %g) leaves the parent's snapshots (%g, %g)", run->t_start,
+                    run->t_end, h->parent_range.first, h->parent_range.second);
     if (run->levels > 0) return run_multirate(h, run, callback, user, report);
     std::memset(report, 0, sizeof(*report));
     std::snprintf(report->device, sizeof report->device, "%s", h->device_name.c_str());

@@ -50,6 +50,10 @@ struct DevTables {
     const int32_t* bface_slot = nullptr;  // [B·n1]
     const double *nt_omega = nullptr, *nt_frate = nullptr, *nt_coef = nullptr;
     const double *nt_mean = nullptr, *nt_depth = nullptr;
+    // parent series: snapshot times, values (f32) and each slot's parent
+    // depth (per-node tides and parents share bface_slot and nt_depth)
+    const double* pt_times = nullptr;
+    const float* pt_values = nullptr;
 };
 
 struct Constituent {
@@ -69,6 +73,13 @@ struct Condition {
     int nt_n, nt_velocity, nt_use_mean, nt_omega0;
     int64_t nt_slot0, nt_coef0;
     double nt_max_ratio;
+    // a parent model (kind 3): its snapshot times from pt_time0 in
+    // DevTables::pt_times, its slots from pt_slot0, their series from
+    // pt_val0 in DevTables::pt_values ([slot][time][3]); the nt_ fields'
+    // velocity, transport ratio and slot base serve it too
+    int pt_n_times, pt_cubic;
+    int64_t pt_time0, pt_val0;
+    double pt_reference_level;
 };
 
 struct Physics {

@@ -245,9 +245,10 @@ int create_impl(dgswe_ensemble* h, const dgswe_form* forms, int n, int device) {
     for (int m = 0; m < n; ++m) {
         cond_base[m] = (int)conds.size();
         for (int b = 0; b < forms[m].n_boundaries; ++b) {
-            if (forms[m].boundaries[b].kind == DGSWE_BC_NODE_TIDES)
+            if (forms[m].boundaries[b].kind == DGSWE_BC_NODE_TIDES ||
+                forms[m].boundaries[b].kind == DGSWE_BC_PARENT)
                 return fail(h, DGSWE_ERR_UNSUPPORTED,
-                            "member %d: tides per boundary node run on a single mesh", m);
+                            "member %d: boundary data per node runs on a single mesh", m);
             conds.push_back(make_condition(forms[m].boundaries[b]));
         }
     }

@@ -5,7 +5,9 @@
 
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/dgswe.h"
@@ -69,6 +71,8 @@ struct dgswe_handle {
     int32_t *d_order = nullptr, *d_edges = nullptr, *d_bfaces = nullptr;
     dgswe_multirate_stats mr_stats{};
     cudaEvent_t ev_lts[2] = {nullptr, nullptr};
+    // the times every parent series covers (a run must stay within them)
+    std::pair<double, double> parent_range{-INFINITY, INFINITY};
 
     ~dgswe_handle() {
         delete planner;

@@ -75,8 +75,25 @@ inline int check_form(const dgswe_form* f, std::string& why) {
     for (int b = 0; b < f->n_boundaries; ++b) {
         const dgswe_boundary& c = f->boundaries[b];
         if (c.kind != DGSWE_BC_WALL && c.kind != DGSWE_BC_CHARACTERISTIC &&
-            c.kind != DGSWE_BC_NODE_TIDES)
+            c.kind != DGSWE_BC_NODE_TIDES && c.kind != DGSWE_BC_PARENT)
             return why = "a boundary condition without a device form", DGSWE_ERR_UNSUPPORTED;
+        if (c.kind == DGSWE_BC_PARENT) {
+            const dgswe_parent_series* p = c.parent;
+            if (!p || p->n_slots <= 0 || p->n_times <= 0 || !p->positions || !p->times ||
+                !p->values)
+                return why = "a parent series without its data", DGSWE_ERR_INVALID;
+            if (p->n_slots >= (1ll << 31) || p->n_times >= (1ll << 31))
+                return why = "a parent series too large", DGSWE_ERR_INVALID;
+            for (int64_t i = 1; i < p->n_times; ++i)
+                if (!(p->times[i] > p->times[i - 1]))
+                    return why = "parent snapshot times must increase", DGSWE_ERR_INVALID;
+            if (p->velocity && p->max_transport_ratio > 0.0 && p->max_transport_ratio < 1.0)
+                return why = "a transport ratio limit below 1", DGSWE_ERR_INVALID;
+            bool any = p->on_boundary == nullptr;
+            for (int64_t q = 0; !any && q < p->n_slots; ++q) any = p->on_boundary[q] != 0;
+            if (!any) return why = "a parent series without boundary slots", DGSWE_ERR_INVALID;
+            continue;
+        }
         if (c.kind == DGSWE_BC_NODE_TIDES) {
             const dgswe_node_tides* t = c.node_tides;
             if (!t || t->n_constituents < 0 || t->n_constituents > 256 || t->n_slots <= 0 ||
@@ -116,6 +133,17 @@ inline Condition make_condition(const dgswe_boundary& in) {
         c.nt_velocity = t.velocity ? 1 : 0;
         c.nt_use_mean = t.use_mean && t.mean ? 1 : 0;
         c.nt_max_ratio = t.max_transport_ratio;
+        return c;
+    }
+    if (in.kind == DGSWE_BC_PARENT) {
+        // the tables' offsets are the handle's (nt_slot0, pt_time0, pt_val0)
+        const dgswe_parent_series& p = *in.parent;
+        c.ramp = p.ramp_duration;
+        c.nt_velocity = p.velocity ? 1 : 0;
+        c.nt_max_ratio = p.max_transport_ratio;
+        c.pt_n_times = (int)p.n_times;
+        c.pt_cubic = p.cubic ? 1 : 0;
+        c.pt_reference_level = p.reference_level;
         return c;
     }
     c.n_constituents = in.n_constituents;

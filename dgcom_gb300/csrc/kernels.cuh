@@ -178,14 +178,20 @@ __global__ void __launch_bounds__(256) face_kernel(DevTables T, Physics P, DevBu
         const int member = T.elem_member ? T.elem_member[k] : 0;
         const double t = LISTED ? lts_stage(lp, k).time : ctl[member].stage[slot].time;
         Q qb;
-        if (c.kind == kBcNodeTides) {
+        if (c.kind == kBcNodeTides || c.kind == kBcParent) {
             const int64_t s = T.bface_slot[bfi * N1 + fi];
             double eta, ue, ve;
             bool has_uv;
-            node_tide_state(T.nt_omega + c.nt_omega0, T.nt_frate + c.nt_omega0,
-                            T.nt_coef + c.nt_coef0 + (s - c.nt_slot0) * c.nt_n * 6, c.nt_n, t,
-                            c.ramp, c.nt_use_mean ? T.nt_mean[s] : 0.0, c.nt_velocity,
-                            c.nt_max_ratio, T.nt_depth[s], qi.b, eta, ue, ve, has_uv);
+            if (c.kind == kBcNodeTides)
+                node_tide_state(T.nt_omega + c.nt_omega0, T.nt_frate + c.nt_omega0,
+                                T.nt_coef + c.nt_coef0 + (s - c.nt_slot0) * c.nt_n * 6, c.nt_n, t,
+                                c.ramp, c.nt_use_mean ? T.nt_mean[s] : 0.0, c.nt_velocity,
+                                c.nt_max_ratio, T.nt_depth[s], qi.b, eta, ue, ve, has_uv);
+            else
+                parent_state_at(T.pt_times + c.pt_time0, c.pt_n_times, c.pt_cubic,
+                                T.pt_values + c.pt_val0 + (s - c.nt_slot0) * c.pt_n_times * 3, t,
+                                c.ramp, c.pt_reference_level, c.nt_velocity, c.nt_max_ratio,
+                                T.nt_depth[s], qi.b, eta, ue, ve, has_uv);
             const double h_e = fmax(eta - qi.b, 0.0);
             double un_e = 0.0, ut_e;
             if (has_uv) {

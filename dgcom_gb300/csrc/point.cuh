@@ -30,7 +30,7 @@ namespace dgswe {
 namespace DGSWE_NS {
 
 constexpr int kWetDry = 0, kEntropyStable = 1, kEntropyConservative = 2;
-constexpr int kBcWall = 0, kBcNodeTides = 2;
+constexpr int kBcWall = 0, kBcNodeTides = 2, kBcParent = 3;
 constexpr int kIncomingWave = 1;
 
 // ---------------------------------------------------------------------------
@@ -504,6 +504,84 @@ DG_PT double tidal_ramp(double t, double duration) {
     double tau = t / duration;
     tau = fp::lt0(tau) ? 0.0 : (fp::gt(tau, 1.0) ? 1.0 : tau);
     return tau * tau * (3.0 - 2.0 * tau);
+}
+
+// OceanModelState's external state at a slot over the child bed `bed`
+// (src/boundary/ocean_nesting.rs:565-600, 833-880): the snapshots'
+// Lagrange weights at t (TimeStencil::new, src/io/field_series.rs:41-81;
+// linear, or cubic through up to four), Σ w·values (parent_term), the ramp,
+// the datum shift and the transport scaling (parent_state). `series` is the
+// slot's [n_times][3] ζ, u, v. t outside the times takes the nearest end
+// (the host refuses such runs beforehand).
+DG_PT void parent_state_at(const double* times, int n, int cubic, const float* series, double t,
+                           double ramp_duration, double reference_level, int velocity,
+                           double max_ratio, double parent_depth, double bed, double& eta,
+                           double& u, double& v, bool& has_uv) {
+    int idx[4] = {0, 0, 0, 0};
+    double w[4] = {1.0, 0.0, 0.0, 0.0};
+    int len = 1;
+    if (n > 1) {
+        if (!fp::ge(t, times[0])) {
+            idx[0] = 0;
+        } else if (!fp::le(t, times[n - 1])) {
+            idx[0] = n - 1;
+        } else {
+            // the first index whose time is ≥ t, within [1, n − 1]
+            int lo = 0, hi = n;
+            while (lo < hi) {
+                const int mid = (lo + hi) / 2;
+                if (fp::lt(times[mid], t)) lo = mid + 1;
+                else hi = mid;
+            }
+            const int i1 = lo < 1 ? 1 : (lo > n - 1 ? n - 1 : lo);
+            const int i0 = i1 - 1;
+            if (t == times[i0]) {
+                idx[0] = i0;
+            } else if (t == times[i1]) {
+                idx[0] = i1;
+            } else {
+                const int a0 = cubic ? (i0 > 0 ? i0 - 1 : 0) : i0;
+                const int a1 = cubic ? (i1 + 1 < n - 1 ? i1 + 1 : n - 1) : i1;
+                len = a1 - a0 + 1;
+                for (int s = 0; s < len; ++s) {
+                    const int a = a0 + s;
+                    double p = 1.0;
+                    bool first = true;
+                    for (int b = a0; b <= a1; ++b) {
+                        if (b == a) continue;
+                        const double x = (t - times[b]) / (times[a] - times[b]);
+                        p = first ? x : p * x;
+                        first = false;
+                    }
+                    idx[s] = a;
+                    w[s] = p;
+                }
+            }
+        }
+    }
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    for (int k = 0; k < len; ++k) {
+        const float* q = series + 3 * idx[k];
+        s0 += w[k] * (double)q[0];
+        s1 += w[k] * (double)q[1];
+        s2 += w[k] * (double)q[2];
+    }
+    const double ramp = tidal_ramp(t, ramp_duration);
+    const double zeta = ramp * s0;
+    u = ramp * s1;
+    v = ramp * s2;
+    eta = zeta + ramp * reference_level;
+    has_uv = velocity != 0;
+    if (has_uv && max_ratio > 0.0 && fp::finite(parent_depth)) {
+        const double d_parent = zeta + parent_depth, d_child = eta - bed;
+        if (fp::gt0(d_parent) && fp::gt0(d_child)) {
+            double ratio = d_parent / d_child;
+            const double lo = 1.0 / max_ratio;
+            ratio = fp::lt(ratio, lo) ? lo : (fp::gt(ratio, max_ratio) ? max_ratio : ratio);
+            u *= ratio;
+            v *= ratio;
+        }
+    }
 }
 
 // BoundaryTides' external state at a slot (tide_term, tide_level,

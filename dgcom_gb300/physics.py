@@ -64,6 +64,29 @@ class NodeTidesBoundary:
 
 
 @dataclass
+class ParentBoundary:
+    """CharacteristicOBC driven by a parent model's state per boundary node
+    (OceanModelState, src/boundary/ocean_nesting.rs; the device form
+    DeviceExternal2D::Parent). ``values`` [n_slots][n_times][3] are ζ, u, v
+    (stored as float32, as the reference stores them) at the snapshot
+    ``times`` (simulation seconds); ``cubic`` Lagrange through up to four
+    snapshots, else linear."""
+
+    positions: np.ndarray            # [n_slots][2]
+    times: np.ndarray                # [n_times]
+    values: np.ndarray               # [n_slots][n_times][3]
+    parent_depth: np.ndarray | None = None
+    on_boundary: np.ndarray | None = None
+    slot_of_node: np.ndarray | None = None
+    cubic: bool = True
+    velocity: bool = True
+    reference_level: float = 0.0
+    max_transport_ratio: float | None = None
+    ramp_duration: float | None = None
+    incoming_wave: bool = False
+
+
+@dataclass
 class SWEDeviceForm2D:
     mesh: QuadMesh
     order: int
@@ -175,6 +198,38 @@ class SWEDeviceForm2D:
             if isinstance(bc, WallBoundary):
                 bcs[i].kind = abi.BC_WALL
                 bcs[i].wall_h_min = bc.h_min
+            elif isinstance(bc, ParentBoundary):
+                bcs[i].kind = abi.BC_PARENT
+                bcs[i].elevation_only = abi.INCOMING_WAVE if bc.incoming_wave else abi.AT_REST
+                ps = abi.ParentSeries()
+                pos = arr(np.asarray(bc.positions).reshape(-1, 2), np.float64)
+                ps.n_slots = pos.shape[0]
+                ps.positions = pos.ctypes.data_as(C.POINTER(C.c_double))
+                tt = arr(bc.times, np.float64)
+                ps.n_times = tt.size
+                ps.times = tt.ctypes.data_as(C.POINTER(C.c_double))
+                vals = arr(np.asarray(bc.values).reshape(-1), np.float32)
+                if vals.size != pos.shape[0] * tt.size * 3:
+                    raise ValueError("values need [n_slots][n_times][3] entries")
+                ps.values = vals.ctypes.data_as(C.POINTER(C.c_float))
+                if bc.parent_depth is not None:
+                    ps.parent_depth = arr(bc.parent_depth, np.float64).ctypes.data_as(
+                        C.POINTER(C.c_double))
+                if bc.on_boundary is not None:
+                    ps.on_boundary = arr(np.asarray(bc.on_boundary, dtype=bool),
+                                         np.uint8).ctypes.data_as(C.POINTER(C.c_uint8))
+                if bc.slot_of_node is not None:
+                    sl = arr(np.asarray(bc.slot_of_node).reshape(-1), np.uint32)
+                    if sl.size != self.n_values:
+                        raise ValueError("slot_of_node needs one slot per mesh node")
+                    ps.slot_of_node = sl.ctypes.data_as(C.POINTER(C.c_uint32))
+                ps.cubic = 1 if bc.cubic else 0
+                ps.velocity = 1 if bc.velocity else 0
+                ps.reference_level = bc.reference_level
+                ps.max_transport_ratio = bc.max_transport_ratio or 0.0
+                ps.ramp_duration = bc.ramp_duration or 0.0
+                keep.append(ps)
+                bcs[i].parent = C.pointer(ps)
             elif isinstance(bc, NodeTidesBoundary):
                 bcs[i].kind = abi.BC_NODE_TIDES
                 bcs[i].elevation_only = abi.INCOMING_WAVE if bc.incoming_wave else abi.AT_REST

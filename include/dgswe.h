@@ -62,8 +62,10 @@ enum dgswe_formulation {
 enum dgswe_boundary_kind {
     DGSWE_BC_WALL = 0,           /* Reflective2D: free-slip mirror ghost state */
     DGSWE_BC_CHARACTERISTIC = 1, /* CharacteristicOBC with a uniform harmonic tide */
-    DGSWE_BC_NODE_TIDES = 2      /* CharacteristicOBC with harmonic constants per boundary
+    DGSWE_BC_NODE_TIDES = 2,     /* CharacteristicOBC with harmonic constants per boundary
                                     node (DeviceExternal2D::Tides, BoundaryTides) */
+    DGSWE_BC_PARENT = 3          /* CharacteristicOBC with a parent model's series per
+                                    boundary node (DeviceExternal2D::Parent, OceanModelState) */
 };
 
 /* ElevationOnly (src/boundary/characteristic.rs:347-355). */
@@ -140,6 +142,33 @@ typedef struct dgswe_node_tides {
     double ramp_duration;         /* s; ≤ 0: no ramp */
 } dgswe_node_tides;
 
+/* OceanModelState's boundary data (src/boundary/ocean_nesting.rs:540-900)
+ * as plain data: a parent model's ζ, u, v (f32, as the reference stores
+ * them) per slot and snapshot, the snapshots' simulation times. At time t
+ * the snapshots' Lagrange weights w (linear between the bracketing two, or
+ * cubic through up to four: TimeStencil, src/io/field_series.rs:26-90) give
+ *   ζ, u, v = ramp(t)·Σ w_k values_k,  η = ζ + ramp(t)·reference_level
+ * (parent_term, parent_state), with (u, v) only if velocity ≠ 0, scaled by
+ * D_parent/D_child within [1/r, r] where max_transport_ratio r > 0 and the
+ * parent depth is finite. A boundary face node takes the slot slot_of_node
+ * gives its flat node, or else the nearest slot marked on_boundary. The
+ * run's times must lie within [times[0], times[n_times − 1]]. */
+typedef struct dgswe_parent_series {
+    int64_t n_slots;
+    const double* positions;      /* [n_slots][2] */
+    const uint8_t* on_boundary;   /* [n_slots] slots a face node may take by position; NULL: all */
+    const uint32_t* slot_of_node; /* [n_elements·(N+1)²] or NULL; 0xFFFFFFFF: none */
+    int64_t n_times;
+    const double* times;          /* [n_times] strictly increasing (simulation seconds) */
+    const float* values;          /* [n_slots][n_times][3] ζ, u, v */
+    const double* parent_depth;   /* [n_slots] (NaN: unknown), or NULL */
+    int32_t cubic;                /* TimeInterpolation::Cubic, else Linear */
+    int32_t velocity;             /* the parent carries (u, v) */
+    double reference_level;       /* the datum shift, ramped with ζ */
+    double max_transport_ratio;   /* ≤ 0: no transport scaling */
+    double ramp_duration;         /* s; ≤ 0: no ramp */
+} dgswe_parent_series;
+
 typedef struct dgswe_boundary {
     int32_t tag;            /* the face tag this condition applies to */
     int32_t kind;           /* dgswe_boundary_kind */
@@ -150,6 +179,7 @@ typedef struct dgswe_boundary {
     double mean_elevation;  /* η₀ (m), not ramped */
     double ramp_duration;   /* s; ≤ 0: no ramp (src/boundary/harmonic_tide.rs:24-32) */
     const dgswe_node_tides* node_tides; /* DGSWE_BC_NODE_TIDES: the tide per node */
+    const dgswe_parent_series* parent;  /* DGSWE_BC_PARENT: the parent per node */
 } dgswe_boundary;
 
 /* SWEDeviceForm2D (src/physics/device.rs:27-62) as plain data, with the

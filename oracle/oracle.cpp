@@ -408,6 +408,38 @@ static std::string build_geometry(const Mesh& mesh, const Ops& ops, Geometry& g)
 // ---------------------------------------------------------------------------
 // The model: the form, its boundary conditions and buffers
 
+// TimeStencil::new (src/io/field_series.rs:41-81): the snapshots' Lagrange
+// weights at `time`, linear between the bracketing two or cubic through up
+// to four; false outside [times[0], times[n − 1]]
+static bool time_stencil(const double* times, int64_t n, double time, bool cubic, int64_t idx[4],
+                         double w[4], int& len) {
+    auto single = [&](int64_t k) {
+        idx[0] = k;
+        w[0] = 1.0;
+        len = 1;
+        return true;
+    };
+    if (n == 0) return false;
+    if (n == 1) return single(0);
+    if (!(time >= times[0] && time <= times[n - 1])) return false;
+    int64_t i1 = std::partition_point(times, times + n, [&](double t) { return t < time; }) - times;
+    i1 = i1 < 1 ? 1 : (i1 > n - 1 ? n - 1 : i1);
+    int64_t i0 = i1 - 1;
+    if (time == times[i0]) return single(i0);
+    if (time == times[i1]) return single(i1);
+    int64_t lo = cubic ? (i0 > 0 ? i0 - 1 : 0) : i0;
+    int64_t hi = cubic ? std::min(i1 + 1, n - 1) : i1;
+    len = (int)(hi - lo + 1);
+    for (int64_t a = lo; a <= hi; ++a) {
+        double p = 1.0;
+        for (int64_t b = lo; b <= hi; ++b)
+            if (b != a) p *= (time - times[b]) / (times[a] - times[b]);
+        idx[a - lo] = a;
+        w[a - lo] = p;
+    }
+    return true;
+}
+
 struct Boundary {
     int kind = DGSWE_BC_WALL;
     double wall_h_min = 1e-6;
@@ -423,6 +455,70 @@ struct Boundary {
         double max_ratio = 0.0, ramp = 0.0;
         int64_t n_slots = 0;
     } tides;
+    // OceanModelState's boundary data (src/boundary/ocean_nesting.rs), a copy
+    struct Parent {
+        int64_t n_slots = 0, n_times = 0;
+        std::vector<double> positions, times, depth;
+        std::vector<float> values;  // [slot][time][3]
+        std::vector<uint8_t> on_boundary;
+        std::vector<uint32_t> slot_of_node;
+        bool cubic = false, velocity = false;
+        double reference_level = 0.0, max_ratio = 0.0, ramp = 0.0;
+    } parent;
+
+    // OceanModelState::slot_of (ocean_nesting.rs:543-562)
+    int64_t parent_slot_of(int64_t node_index, double x, double y) const {
+        if (!parent.slot_of_node.empty() && parent.slot_of_node[node_index] != 0xFFFFFFFFu)
+            return parent.slot_of_node[node_index];
+        int64_t best = -1;
+        double dmin = INF;
+        for (int64_t p = 0; p < parent.n_slots; ++p) {
+            if (!parent.on_boundary.empty() && !parent.on_boundary[p]) continue;
+            double d = std::hypot(parent.positions[2 * p] - x, parent.positions[2 * p + 1] - y);
+            if (best < 0 || d < dmin) {
+                dmin = d;
+                best = p;
+            }
+        }
+        return best;
+    }
+
+    // OceanModelState::external_state (ocean_nesting.rs:821-826): evaluate
+    // with parent_term and parent_state (ocean_nesting.rs:833-880)
+    void parent_external(int64_t slot, double t, double bed, double& eta, double& u, double& v,
+                         bool& has_uv) const {
+        int64_t idx[4];
+        double w[4];
+        int len = 0;
+        if (!time_stencil(parent.times.data(), parent.n_times, t, parent.cubic, idx, w, len)) {
+            eta = u = v = NAN;  // the reference panics: a configuration error
+            has_uv = parent.velocity;
+            return;
+        }
+        double sum[3] = {0.0, 0.0, 0.0};
+        for (int k = 0; k < len; ++k) {
+            const float* q = &parent.values[((size_t)slot * parent.n_times + idx[k]) * 3];
+            sum[0] += w[k] * (double)q[0];
+            sum[1] += w[k] * (double)q[1];
+            sum[2] += w[k] * (double)q[2];
+        }
+        double ramp = tidal_ramp(t, parent.ramp);
+        double zeta = ramp * sum[0];
+        u = ramp * sum[1];
+        v = ramp * sum[2];
+        eta = zeta + ramp * parent.reference_level;
+        has_uv = parent.velocity;
+        if (has_uv && parent.max_ratio > 0.0 && std::isfinite(parent.depth[slot])) {
+            double d_parent = zeta + parent.depth[slot], d_child = eta - bed;
+            if (d_parent > 0.0 && d_child > 0.0) {
+                double ratio = d_parent / d_child;
+                double lo = 1.0 / parent.max_ratio;
+                ratio = ratio < lo ? lo : (ratio > parent.max_ratio ? parent.max_ratio : ratio);
+                u *= ratio;
+                v *= ratio;
+            }
+        }
+    }
 
     // BoundaryTides::slot_of (tidal_atlas.rs:1026-1045)
     int64_t slot_of(int64_t node_index, double x, double y) const {
@@ -630,15 +726,20 @@ static State boundary_flux(const Model& m, int64_t k, int face, int node, const 
     double bathy = q_int.b;
     double eta, ue = 0.0, ve = 0.0;
     bool has_uv = false;
-    if (bc.kind == DGSWE_BC_NODE_TIDES) {
+    if (bc.kind == DGSWE_BC_NODE_TIDES || bc.kind == DGSWE_BC_PARENT) {
         auto c = m.mesh.corners(k);
         double r = m.ops.nodes_r[node], sv = m.ops.nodes_s[node];
         double n0 = (1 - r) * (1 - sv) / 4, n1b = (1 + r) * (1 - sv) / 4;
         double n2 = (1 + r) * (1 + sv) / 4, n3 = (1 - r) * (1 + sv) / 4;
         double x = n0 * c[0][0] + n1b * c[1][0] + n2 * c[2][0] + n3 * c[3][0];
         double y = n0 * c[0][1] + n1b * c[1][1] + n2 * c[2][1] + n3 * c[3][1];
-        int64_t slot = bc.slot_of(k * m.ops.nn + node, x, y);
-        bc.node_external(slot, time, bathy, eta, ue, ve, has_uv);
+        if (bc.kind == DGSWE_BC_PARENT) {
+            int64_t slot = bc.parent_slot_of(k * m.ops.nn + node, x, y);
+            bc.parent_external(slot, time, bathy, eta, ue, ve, has_uv);
+        } else {
+            int64_t slot = bc.slot_of(k * m.ops.nn + node, x, y);
+            bc.node_external(slot, time, bathy, eta, ue, ve, has_uv);
+        }
     } else {
         eta = bc.elevation(time);
     }
@@ -1726,6 +1827,31 @@ int oracle_create(const dgswe_form* f, int device, oracle_handle** out) {
             nt.max_ratio = t->max_transport_ratio;
             nt.ramp = t->ramp_duration;
         }
+        if (in.kind == DGSWE_BC_PARENT) {
+            const dgswe_parent_series* p = in.parent;
+            if (!p || p->n_slots <= 0 || p->n_times <= 0 || !p->positions || !p->times ||
+                !p->values) {
+                delete m;
+                return DGSWE_ERR_INVALID;
+            }
+            Boundary::Parent& pp = bc.parent;
+            pp.n_slots = p->n_slots;
+            pp.n_times = p->n_times;
+            pp.positions.assign(p->positions, p->positions + 2 * p->n_slots);
+            pp.times.assign(p->times, p->times + p->n_times);
+            pp.values.assign(p->values, p->values + (size_t)p->n_slots * p->n_times * 3);
+            pp.depth.assign(p->n_slots, NAN);
+            if (p->parent_depth) pp.depth.assign(p->parent_depth, p->parent_depth + p->n_slots);
+            if (p->on_boundary) pp.on_boundary.assign(p->on_boundary, p->on_boundary + p->n_slots);
+            if (p->slot_of_node)
+                pp.slot_of_node.assign(p->slot_of_node,
+                                       p->slot_of_node + (size_t)f->n_elements * m->ops.nn);
+            pp.cubic = p->cubic != 0;
+            pp.velocity = p->velocity != 0;
+            pp.reference_level = p->reference_level;
+            pp.max_ratio = p->max_transport_ratio;
+            pp.ramp = p->ramp_duration;
+        }
         m->boundaries[in.tag] = bc;
     }
     for (auto& e : m->mesh.edges)
@@ -1943,6 +2069,13 @@ int oracle_multirate_stats_get(const oracle_handle* h, dgswe_multirate_stats* ou
 }
 
 // ---- pointwise entry points for the known-answer tests -------------------
+
+int oracle_time_stencil(const double* times, int64_t n, double t, int cubic, int64_t* idx,
+                        double* w) {
+    int len = 0;
+    if (!time_stencil(times, n, t, cubic != 0, idx, w, len)) return 0;
+    return len;
+}
 
 double oracle_manning_cbrt(double x) { return manning_cbrt(x); }
 double oracle_tidal_ramp(double t, double duration) { return tidal_ramp(t, duration); }

@@ -34,6 +34,9 @@ int oracle_run(oracle_handle* h, const dgswe_run_config* run, dgswe_callback cb,
                dgswe_report* report);
 int64_t oracle_negative_depth_clips(const oracle_handle* h);
 /* MultirateStats of the last run with local time stepping (run->levels > 0) */
+/* TimeStencil::new: the snapshots and weights at t (returns how many; 0: outside) */
+int oracle_time_stencil(const double* times, int64_t n, double t, int cubic, int64_t* idx,
+                        double* w);
 int oracle_multirate_stats_get(const oracle_handle* h, dgswe_multirate_stats* out);
 
 /* pointwise functions for the known-answer tests */

@@ -37,6 +37,7 @@ POINTWISE = {
                           C.c_double, C.c_double, C.c_double]),
     "tide_elevation": (C.c_double, [C.POINTER(abi.Boundary), C.c_double]),
     "multirate_stats_get": (C.c_int, [C.c_void_p, C.POINTER(abi.MultirateStats)]),
+    "time_stencil": (C.c_int, [_dp, C.c_int64, C.c_double, C.c_int, C.POINTER(C.c_int64), _dp]),
 }
 
 _lib = None
