@@ -441,9 +441,9 @@ def run_adjoint(args, rank: int, world: int, local: int):
     """The discrete adjoint on the refined tidal channel: the gradient of a
     50-station misfit (observations from a forward run with a perturbed
     friction field) w.r.t. Manning's n per element, the bed, and the M2
-    amplitude and phase; its time against the forward's, at the memory
-    budget that checkpoints about every 45 steps and with every state
-    stored; central differences on random directions, by replaying the
+    amplitude and phase; its time against the forward's with checkpoints
+    every 45 steps (the replay keeping each step's full reverse data, or
+    only the step-start states) and with every state stored; central differences on random directions, by replaying the
     forward's steps. One GPU: replicas are independent runs."""
     import dataclasses
 
@@ -466,10 +466,16 @@ def run_adjoint(args, rank: int, world: int, local: int):
     results = {}
     g = None
     dts = None
-    stride_budget = (math.ceil(steps / 45.0) + 45 + 1) * state_bytes
-    for label, budget in [("stride~45", stride_budget), ("all stored", 0.0)]:
+    # checkpoints every 45 steps: with the segment's full reverse data (8
+    # states a step), or with its step-start states only; every state stored
+    every = 45
+    full_budget = (math.ceil(steps / every) + 8 * every + 1) * state_bytes
+    start_budget = (math.ceil(steps / every) + every + 1) * state_bytes
+    for label, budget, ck in [("every 45, full segments", full_budget, every),
+                              ("every 45, step-start segments", start_budget, every),
+                              ("all stored", 0.0, 0)]:
         with Adjoint(form, steps, stations, cfl=case.cfl, t_start=t0, memory_budget=budget,
-                     device=local) as a:
+                     device=local, checkpoint_every=ck) as a:
             a.forward(state, eta_obs=eta_obs)  # warm-up
             J, _, dts = a.forward(state, eta_obs=eta_obs)
             g = a.reverse()
@@ -477,7 +483,8 @@ def run_adjoint(args, rank: int, world: int, local: int):
         results[label] = {"J": J, "forward_ms": st.forward_ms, "reverse_ms": st.reverse_ms,
                           "reverse_over_forward": st.reverse_ms / st.forward_ms,
                           "gradient_over_forward": (st.forward_ms + st.reverse_ms) / st.forward_ms,
-                          "stride": int(st.stride), "stored_gb": st.stored_bytes / 1e9,
+                          "stride": int(st.stride), "full_segments": bool(st.full_segments),
+                          "stored_gb": st.stored_bytes / 1e9,
                           "recomputed_steps": int(st.recomputed_steps)}
     # central differences of the forward (the steps replayed) on random directions
     rng = np.random.default_rng(7)
@@ -534,7 +541,7 @@ def run_adjoint(args, rank: int, world: int, local: int):
         checks.append({"kind": kind, "adjoint": adj, "fd": fd,
                        "rel": abs(adj - fd) / max(abs(fd), abs(adj), 1e-300)})
     rels = [c["rel"] for c in checks]
-    headline = results["stride~45"]
+    headline = results["every 45, full segments"]
     if rank == 0:
         line = {
             "metric": "adjoint time / forward time (discrete adjoint of the FP64 DG SWE run)",

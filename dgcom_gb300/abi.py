@@ -257,6 +257,7 @@ class AdjointConfig(C.Structure):
         ("stations", _dp),
         ("memory_budget", C.c_double),
         ("station_member", C.POINTER(C.c_int32)),
+        ("checkpoint_every", C.c_int64),
     ]
 
 
@@ -268,6 +269,7 @@ class AdjointStats(C.Structure):
         ("forward_wall_s", C.c_double),
         ("reverse_wall_s", C.c_double),
         ("stride", C.c_int64),
+        ("full_segments", C.c_int32),
         ("recomputed_steps", C.c_int64),
         ("stored_states", C.c_int64),
         ("stored_bytes", C.c_double),

@@ -42,7 +42,8 @@ class Gradient:
 class Adjoint:
     def __init__(self, form: SWEDeviceForm2D, n_steps: int, stations, cfl: float = 0.5,
                  t_start: float = 0.0, memory_budget: float = 0.0, device: int = 0,
-                 library: abi.Library | None = None, *, _members=None, _station_member=None):
+                 library: abi.Library | None = None, *, checkpoint_every: int = 0,
+                 _members=None, _station_member=None):
         self.lib = library or abi.cuda_library()
         self.forms = list(_members) if _members is not None else [form]
         self.form = self.forms[0]
@@ -64,6 +65,7 @@ class Adjoint:
         cfg.stations = self.stations.ctypes.data_as(_dp) if self.stations.size else None
         cfg.memory_budget = memory_budget
         cfg.station_member = member.ctypes.data_as(C.POINTER(C.c_int32)) if n_st else None
+        cfg.checkpoint_every = int(checkpoint_every)
         handle = C.c_void_p()
         if _members is None:
             c_form, self._keep = form.to_c()
@@ -92,14 +94,15 @@ class Adjoint:
     @classmethod
     def ensemble(cls, forms, n_steps: int, stations, station_member, cfl: float = 0.5,
                  t_start: float = 0.0, memory_budget: float = 0.0, device: int = 0,
-                 library: abi.Library | None = None) -> "Adjoint":
+                 library: abi.Library | None = None, checkpoint_every: int = 0) -> "Adjoint":
         """One batched adjoint over ensemble members of one order: each member
         its own time steps and stations (``station_member``); arrays are the
         members' concatenated (``member_slice``)."""
         if not forms:
             raise ValueError("an ensemble needs at least one member")
         return cls(forms[0], n_steps, stations, cfl, t_start, memory_budget, device, library,
-                   _members=forms, _station_member=station_member)
+                   checkpoint_every=checkpoint_every, _members=forms,
+                   _station_member=station_member)
 
     def member_slice(self, member: int) -> slice:
         """Member ``member``'s values in the concatenated per-node arrays."""

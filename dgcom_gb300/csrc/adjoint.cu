@@ -12,13 +12,20 @@
 // stations and J): the same kernels, with each element reading its member's
 // step control.
 //
-// Storage: the state at the start of each step (h, hu, hv) is what the
-// reverse sweep needs; within a step the three stages are recomputed. When
-// all N states fit in the memory budget, the forward sweep keeps them all;
-// otherwise it keeps every s-th one, and the reverse sweep recomputes each
-// segment of s steps once from its checkpoint, into a segment buffer,
-// before reversing it (two-level checkpointing, s the smallest stride the
-// budget allows).
+// Storage: the reverse of a step needs its start state, its stage inputs
+// and what each stage's reverse keeps (the combination and the damped
+// momentum). When all N step-start states fit in the memory budget, the
+// forward sweep keeps them all and the reverse recomputes each step's
+// stages once. Otherwise the forward keeps every s-th state (checkpoints)
+// and the reverse replays each segment of s steps from its checkpoint
+// before reversing it:
+//  - full segments, when the budget holds them: the replay keeps every
+//    step's stage inputs and kept values (8 states a step), so each step is
+//    computed once in the reverse sweep;
+//  - else step-start segments: the replay keeps the s step-start states and
+//    each step's stages are computed again as it is reversed (twice in all).
+// s is the caller's checkpoint interval, or the one the budget allows with
+// the least memory.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -95,8 +102,9 @@ struct dgswe_adjoint {
     double* d_eta = nullptr;      // [n_steps][n_stations]
     double* d_obs = nullptr;      // [n_steps][n_stations]
     double* d_ckpt = nullptr;     // stored step-start states, 3·nv doubles each
-    double* d_seg = nullptr;      // a segment's step-start states (stride > 1)
+    double* d_seg = nullptr;      // a segment's step-start states, or full steps (stride > 1)
     int64_t stride = 1, n_ckpt = 0;
+    bool full = false;            // full segments: per step q, S1, S2 (3 fields), keep (3 × 5)
     DevBuf S[4]{};  // the step's stage inputs and last output
     DevBuf Kp[3]{}; // kept combination and damped momentum of each stage
     double *lam[3] = {}, *lam_t[3] = {}, *lam_b[3] = {};
@@ -260,6 +268,31 @@ void forward_step(dgswe_adjoint* a, const DevBuf& q) {
     }
 }
 
+// The three stages of a step reversed, the stage inputs in S[0..2] and what
+// they keep in Kp[0..2]: λ of each stage's input from λ of its output, then
+// λ of the step's start state (the first stage's input plus the three
+// stages' base terms) into lam
+int reverse_stages(dgswe_adjoint* a) {
+    const Target& t = a->tg;
+    const int64_t nv = t.nv;
+    cudaStream_t st = t.stream;
+    for (int s = 2; s >= 0; --s) {
+        AdjStage As = a->A;
+        double** lo = s == 2 ? a->lam : a->lam_t;
+        As.lo_h = lo[0];
+        As.lo_hu = lo[1];
+        As.lo_hv = lo[2];
+        t.ks->stage_adjoint(t.n1, *t.T, *t.P, *t.X, a->S[s], a->Kp[s], As, t.ctl, s, st);
+        t.ks->face_adjoint(t.n1, *t.T, *t.P, a->S[s], As, t.ctl, s, st);
+        t.ks->adjoint_combine(a->S[s], As, a->lam_t[0], a->lam_t[1], a->lam_t[2], nv, t.P->h_min,
+                              st);
+    }
+    for (int c = 0; c < 3; ++c)
+        sum_clear_kernel<<<(unsigned)((nv + 255) / 256), 256, 0, st>>>(a->lam[c], a->lam_t[c],
+                                                                       a->lam_b[c], nv);
+    return DGSWE_OK;
+}
+
 // Everything after the target exists: stations, the bed slope's transpose,
 // buffers, checkpoints
 int setup(dgswe_adjoint* a, const dgswe_form* forms, const dgswe_adjoint_config* cfg) {
@@ -380,25 +413,44 @@ int setup(dgswe_adjoint* a, const dgswe_form* forms, const dgswe_adjoint_config*
         ACK(cudaMemGetInfo(&free_b, &total));
         budget = std::max(0.0, (double)free_b - 2.0 * (1ull << 30));
     }
-    int64_t stride = 1;
-    if ((double)N * sb > budget) {
-        stride = 0;
-        for (int64_t st = 2; st <= N; ++st)
-            if ((double)((N + st - 1) / st + st) * sb <= budget) {
+    // states held: checkpoints, and the segment (8 states a step when full)
+    auto held = [&](int64_t st, bool full) {
+        return (double)((N + st - 1) / st + (st > 1 ? (full ? 8 : 1) * st : 0)) * sb;
+    };
+    int64_t stride = 0;
+    bool full = false;
+    if (cfg->checkpoint_every > 0) {
+        stride = std::min<int64_t>(cfg->checkpoint_every, N);
+        if (stride > 1 && held(stride, true) <= budget) full = true;
+        else if (held(stride, false) > budget)
+            return afail(a, DGSWE_ERR_INVALID,
+                         "checkpoints every %lld steps need %.3g B, over the budget of %.3g B",
+                         (long long)stride, held(stride, false), budget);
+    } else if (held(1, false) <= budget) {
+        stride = 1;
+    } else {
+        double least = INFINITY;
+        for (int64_t st = 2; st <= N; ++st)  // full segments with the least memory
+            if (held(st, true) <= budget && held(st, true) < least) {
+                least = held(st, true);
                 stride = st;
-                break;
+                full = true;
             }
+        for (int64_t st = 2; stride == 0 && st <= N; ++st)
+            if (held(st, false) <= budget) stride = st;
         if (stride == 0)
             return afail(a, DGSWE_ERR_INVALID,
                          "the memory budget (%.3g B) holds fewer than 2·√N states of %.3g B", budget,
                          sb);
     }
     a->stride = stride;
+    a->full = full;
     a->n_ckpt = (N + stride - 1) / stride;
     if ((s = dalloc(a, 3 * (size_t)nv * a->n_ckpt, &a->d_ckpt))) return s;
-    if (stride > 1 && (s = dalloc(a, 3 * (size_t)nv * stride, &a->d_seg))) return s;
+    if (stride > 1 && (s = dalloc(a, (full ? 24 : 3) * (size_t)nv * stride, &a->d_seg))) return s;
     a->stats.stride = stride;
-    a->stats.stored_states = a->n_ckpt + (stride > 1 ? stride : 0);
+    a->stats.full_segments = full ? 1 : 0;
+    a->stats.stored_states = a->n_ckpt + (stride > 1 ? (full ? 8 : 1) * stride : 0);
     a->stats.stored_bytes = (double)a->stats.stored_states * sb;
     return DGSWE_OK;
 }
@@ -694,9 +746,57 @@ int dgswe_adjoint_reverse(dgswe_adjoint* a, double* grad_h0, double* grad_hu0, d
     ACK(cudaEventRecord(a->e0, st));
     int64_t recomputed = 0;
     DevBuf& q = a->S[0];
+    const size_t slot = 24 * (size_t)nv;  // a full segment's step: q, S1, S2, keep 0..2
+    auto keep_copy = [&](double* dst, const DevBuf& src, bool to_slot) -> int {
+        // the five fields of a keep buffer are contiguous (devbuf)
+        if (to_slot)
+            ACK(cudaMemcpyAsync(dst, src.h, 5 * bv, cudaMemcpyDeviceToDevice, st));
+        else
+            ACK(cudaMemcpyAsync(src.h, dst, 5 * bv, cudaMemcpyDeviceToDevice, st));
+        return DGSWE_OK;
+    };
     for (int64_t c0 = (a->n_ckpt - 1) * a->stride; c0 >= 0; c0 -= a->stride) {
         const int64_t c1 = std::min(c0 + a->stride, N);
         const double* ck = a->d_ckpt + (c0 / a->stride) * 3 * nv;
+        if (a->full) {
+            // the segment replayed once, every step's reverse data kept
+            if (int s = unpack(a, q, ck, nv, st)) return s;
+            t.ks->velocity(q, nv, t.P->h_min, st);
+            for (int64_t n = c0; n < c1; ++n) {
+                double* sl = a->d_seg + (n - c0) * slot;
+                if (int s = args_to_ctl(a, n)) return s;
+                for (int s = 0; s < 3; ++s) {
+                    t.ks->face(t.n1, *t.T, *t.P, a->S[s], t.fb_h, t.fb_hu, t.fb_hv, t.ctl, s, on,
+                               st);
+                    t.ks->stage_keep(t.n1, *t.T, *t.P, *t.X, a->S[s], q, a->S[s + 1], t.fb_h,
+                                     t.fb_hu, t.fb_hv, t.ctl, s, 0, a->Kp[s], st);
+                }
+                for (int b = 0; b < 3; ++b)
+                    if (int s = pack(a, sl + b * 3 * nv, a->S[b], nv, st)) return s;
+                for (int s = 0; s < 3; ++s)
+                    if (int e = keep_copy(sl + (9 + 5 * s) * nv, a->Kp[s], true)) return e;
+                // the step's result (with its velocities) starts the next
+                ACK(cudaMemcpyAsync(q.h, a->S[3].h, 5 * bv, cudaMemcpyDeviceToDevice, st));
+                recomputed += 1;
+            }
+            for (int64_t n = c1 - 1; n >= c0; --n) {
+                t.ks->station_seed(a->d_eta + n * n_st, a->d_obs + n * n_st, a->d_node0, a->d_w,
+                                   n_st, nn, a->lam[0], t.P->has_bed ? A.lbed : nullptr, st);
+                const double* sl = a->d_seg + (n - c0) * slot;
+                for (int b = 0; b < 3; ++b) {
+                    if (int s = unpack(a, a->S[b], sl + b * 3 * nv, nv, st)) return s;
+                    t.ks->velocity(a->S[b], nv, t.P->h_min, st);
+                }
+                for (int s = 0; s < 3; ++s)
+                    if (int e = keep_copy(const_cast<double*>(sl) + (9 + 5 * s) * nv, a->Kp[s],
+                                          false))
+                        return e;
+                if (int s = args_to_ctl(a, n)) return s;
+                if (int s = reverse_stages(a)) return s;
+            }
+            if (c0 == 0) break;
+            continue;
+        }
         if (a->stride > 1) {  // the segment's step-start states, recomputed from its checkpoint
             if (int s = unpack(a, q, ck, nv, st)) return s;
             t.ks->velocity(q, nv, t.P->h_min, st);
@@ -722,22 +822,7 @@ int dgswe_adjoint_reverse(dgswe_adjoint* a, double* grad_h0, double* grad_hu0, d
                 t.ks->stage_keep(t.n1, *t.T, *t.P, *t.X, a->S[s], q, a->S[s + 1], t.fb_h, t.fb_hu,
                                  t.fb_hv, t.ctl, s, 0, a->Kp[s], st);
             }
-            // the stages reversed: λ of each stage's input from λ of its output
-            for (int s = 2; s >= 0; --s) {
-                AdjStage As = A;
-                double** lo = s == 2 ? a->lam : a->lam_t;
-                As.lo_h = lo[0];
-                As.lo_hu = lo[1];
-                As.lo_hv = lo[2];
-                t.ks->stage_adjoint(t.n1, *t.T, *t.P, *t.X, a->S[s], a->Kp[s], As, t.ctl, s, st);
-                t.ks->face_adjoint(t.n1, *t.T, *t.P, a->S[s], As, t.ctl, s, st);
-                t.ks->adjoint_combine(a->S[s], As, a->lam_t[0], a->lam_t[1], a->lam_t[2], nv,
-                                      t.P->h_min, st);
-            }
-            // λ of q_n: the first stage's input plus the three stages' base terms
-            for (int c = 0; c < 3; ++c)
-                sum_clear_kernel<<<(unsigned)((nv + 255) / 256), 256, 0, st>>>(a->lam[c], a->lam_t[c],
-                                                                               a->lam_b[c], nv);
+            if (int s = reverse_stages(a)) return s;
             recomputed += 1;
         }
         if (c0 == 0) break;

@@ -541,7 +541,9 @@ int dgswe_ensemble_run(dgswe_ensemble* ensemble, const dgswe_run_config* run, in
  * derivative given is exact for perturbations that keep coincident nodes
  * equal (a continuous bed). Step-start states are stored in HBM within
  * memory_budget; when all N do not fit, a two-level checkpointing stores
- * every s-th one and recomputes each segment once. */
+ * every s-th one and replays each segment from it: keeping each step's
+ * stage inputs and kept values when the budget holds 8 states a step of the
+ * segment (full segments), else its step-start states only. */
 #define DGSWE_MAX_CONSTITUENTS 8
 
 typedef struct dgswe_adjoint dgswe_adjoint;
@@ -556,6 +558,9 @@ typedef struct dgswe_adjoint_config {
     double memory_budget;     /* bytes of HBM for stored states; ≤ 0: free memory − 2 GiB */
     const int32_t* station_member; /* [n_stations] each station's member (an ensemble's
                                       adjoint); NULL: member 0 */
+    int64_t checkpoint_every;  /* checkpoint interval s (steps); ≤ 0: every step if the
+                                  budget holds them all, else the interval that needs
+                                  the least memory */
 } dgswe_adjoint_config;
 
 typedef struct dgswe_adjoint_stats {
@@ -563,7 +568,9 @@ typedef struct dgswe_adjoint_stats {
     double forward_ms;        /* device time of the forward sweep */
     double reverse_ms;        /* of the reverse sweep */
     double forward_wall_s, reverse_wall_s;
-    int64_t stride;           /* 1: every step-start state stored */
+    int64_t stride;           /* checkpoint interval; 1: every step-start state stored */
+    int32_t full_segments;    /* the replay keeps every step's reverse data: each step is
+                                 computed once in the reverse sweep, not twice */
     int64_t recomputed_steps; /* forward steps the reverse sweep recomputed */
     int64_t stored_states;
     double stored_bytes;

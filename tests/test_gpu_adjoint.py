@@ -235,13 +235,22 @@ def test_checkpoint_segments_give_the_same_gradient():
         g1 = full.reverse()
         assert full.stats().stride == 1
     state_bytes = 3 * 8 * state[0].size
+    # step-start segments: each step's stages computed twice in the reverse
     with Adjoint(form, STEPS, STATIONS, t_start=T_START, memory_budget=6.5 * state_bytes) as seg:
         seg.forward(state)
         g2 = seg.reverse()
         st = seg.stats()
-        assert st.stride > 1 and st.recomputed_steps > STEPS
-    for a, b in [(g1.h0, g2.h0), (g1.bed, g2.bed), (g1.manning, g2.manning)]:
-        assert np.abs(a - b).max() <= 1e-12 * max(np.abs(a).max(), 1e-300)
+        assert st.stride > 1 and not st.full_segments and st.recomputed_steps > STEPS
+    # full segments every 4 steps: each step computed once
+    with Adjoint(form, STEPS, STATIONS, t_start=T_START, memory_budget=40 * state_bytes,
+                 checkpoint_every=4) as seg:
+        seg.forward(state)
+        g3 = seg.reverse()
+        st = seg.stats()
+        assert st.stride == 4 and st.full_segments and st.recomputed_steps == STEPS
+    for g in (g2, g3):
+        for a, b in [(g1.h0, g.h0), (g1.bed, g.bed), (g1.manning, g.manning)]:
+            assert np.abs(a - b).max() <= 1e-12 * max(np.abs(a).max(), 1e-300)
 
 
 def test_replayed_steps_give_the_recorded_functional():
