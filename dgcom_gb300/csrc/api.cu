@@ -243,15 +243,17 @@ int64_t dgswe_negative_depth_clips(const dgswe_handle* h) {
 
 namespace {
 
-// Per-node tides (DGSWE_BC_NODE_TIDES): the conditions' constituents and
-// constants back to back, and every boundary face node's slot: the one
-// slot_of_node gives its flat node, else the nearest forced node
-// (BoundaryTides::slot_of, src/boundary/tidal_atlas.rs:1026-1045)
+// Boundary data per node (DGSWE_BC_NODE_TIDES, DGSWE_BC_PARENT): the
+// conditions' constituents and constants, or snapshot times and series,
+// back to back, and every boundary face node's slot: the one slot_of_node
+// gives its flat node, else the nearest forced node (BoundaryTides::slot_of,
+// src/boundary/tidal_atlas.rs:1026-1045; OceanModelState::slot_of,
+// src/boundary/ocean_nesting.rs:543-562)
 bool per_node(const dgswe_boundary& b) {
     return b.kind == DGSWE_BC_NODE_TIDES || b.kind == DGSWE_BC_PARENT;
 }
 
-int node_tide_tables(dgswe_handle* h, const dgswe_form& f, const Operators& ops,
+int boundary_node_tables(dgswe_handle* h, const dgswe_form& f, const Operators& ops,
                      const Topology& topo, const Tables& t) {
     bool any = false;
     for (int b = 0; b < f.n_boundaries; ++b) any = any || per_node(f.boundaries[b]);
@@ -445,7 +447,7 @@ int create_impl(dgswe_handle* h, const dgswe_form* f, int device) {
     fill_physics(*f, ops, !t.fcor.empty(), h->P, h->X);
     h->P.n_conditions = f->n_boundaries;
     for (int b = 0; b < f->n_boundaries; ++b) h->P.cond[b] = make_condition(f->boundaries[b]);
-    if ((s = node_tide_tables(h, *f, ops, topo, t))) return bail(s);
+    if ((s = boundary_node_tables(h, *f, ops, topo, t))) return bail(s);
 
     // buffers, faces, control
     if ((s = ensure_buffer(h, DGSWE_STATE))) return bail(s);
