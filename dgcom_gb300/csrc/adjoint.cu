@@ -268,11 +268,11 @@ void forward_step(dgswe_adjoint* a, const DevBuf& q) {
     }
 }
 
-// The three stages of a step reversed, the stage inputs in S[0..2] and what
-// they keep in Kp[0..2]: λ of each stage's input from λ of its output, then
+// The three stages of a step reversed, the stage inputs in[0..2] and what
+// they keep keep[0..2]: λ of each stage's input from λ of its output, then
 // λ of the step's start state (the first stage's input plus the three
 // stages' base terms) into lam
-int reverse_stages(dgswe_adjoint* a) {
+int reverse_stages(dgswe_adjoint* a, const DevBuf* in, const DevBuf* keep) {
     const Target& t = a->tg;
     const int64_t nv = t.nv;
     cudaStream_t st = t.stream;
@@ -282,9 +282,9 @@ int reverse_stages(dgswe_adjoint* a) {
         As.lo_h = lo[0];
         As.lo_hu = lo[1];
         As.lo_hv = lo[2];
-        t.ks->stage_adjoint(t.n1, *t.T, *t.P, *t.X, a->S[s], a->Kp[s], As, t.ctl, s, st);
-        t.ks->face_adjoint(t.n1, *t.T, *t.P, a->S[s], As, t.ctl, s, st);
-        t.ks->adjoint_combine(a->S[s], As, a->lam_t[0], a->lam_t[1], a->lam_t[2], nv, t.P->h_min,
+        t.ks->stage_adjoint(t.n1, *t.T, *t.P, *t.X, in[s], keep[s], As, t.ctl, s, st);
+        t.ks->face_adjoint(t.n1, *t.T, *t.P, in[s], As, t.ctl, s, st);
+        t.ks->adjoint_combine(in[s], As, a->lam_t[0], a->lam_t[1], a->lam_t[2], nv, t.P->h_min,
                               st);
     }
     for (int c = 0; c < 3; ++c)
@@ -746,53 +746,52 @@ int dgswe_adjoint_reverse(dgswe_adjoint* a, double* grad_h0, double* grad_hu0, d
     ACK(cudaEventRecord(a->e0, st));
     int64_t recomputed = 0;
     DevBuf& q = a->S[0];
-    const size_t slot = 24 * (size_t)nv;  // a full segment's step: q, S1, S2, keep 0..2
-    auto keep_copy = [&](double* dst, const DevBuf& src, bool to_slot) -> int {
-        // the five fields of a keep buffer are contiguous (devbuf)
-        if (to_slot)
-            ACK(cudaMemcpyAsync(dst, src.h, 5 * bv, cudaMemcpyDeviceToDevice, st));
-        else
-            ACK(cudaMemcpyAsync(src.h, dst, 5 * bv, cudaMemcpyDeviceToDevice, st));
-        return DGSWE_OK;
+    // a full segment's step n: its start state, the inputs of stages 1 and 2
+    // (h, hu, hv each; their velocities in S[b]'s, recomputed) and what the
+    // three stages keep (5 fields each), written there by the replay itself
+    const size_t slot = 24 * (size_t)nv;
+    auto view = [&](int64_t n, int64_t c0, int b) {
+        double* p = a->d_seg + (n - c0) * slot + 3 * (size_t)b * nv;
+        return DevBuf{p, p + nv, p + 2 * nv, a->S[b].u, a->S[b].v};
+    };
+    auto keep_view = [&](int64_t n, int64_t c0, int s) {
+        double* p = a->d_seg + (n - c0) * slot + (9 + 5 * (size_t)s) * nv;
+        return DevBuf{p, p + nv, p + 2 * nv, p + 3 * nv, p + 4 * nv};
     };
     for (int64_t c0 = (a->n_ckpt - 1) * a->stride; c0 >= 0; c0 -= a->stride) {
         const int64_t c1 = std::min(c0 + a->stride, N);
         const double* ck = a->d_ckpt + (c0 / a->stride) * 3 * nv;
         if (a->full) {
-            // the segment replayed once, every step's reverse data kept
-            if (int s = unpack(a, q, ck, nv, st)) return s;
-            t.ks->velocity(q, nv, t.P->h_min, st);
+            // the segment replayed once into its storage, every step's
+            // reverse data kept; the last step's result is not needed
+            {
+                const DevBuf q0 = view(c0, c0, 0);
+                if (int s = unpack(a, q0, ck, nv, st)) return s;
+                t.ks->velocity(q0, nv, t.P->h_min, st);
+            }
             for (int64_t n = c0; n < c1; ++n) {
-                double* sl = a->d_seg + (n - c0) * slot;
                 if (int s = args_to_ctl(a, n)) return s;
+                const DevBuf in[3] = {view(n, c0, 0), view(n, c0, 1), view(n, c0, 2)};
+                // stage 2 writes the next step's start (its velocities where
+                // this step's start had its own: stage 0 has read them)
+                const DevBuf out[3] = {in[1], in[2], n + 1 < c1 ? view(n + 1, c0, 0) : a->S[3]};
                 for (int s = 0; s < 3; ++s) {
-                    t.ks->face(t.n1, *t.T, *t.P, a->S[s], t.fb_h, t.fb_hu, t.fb_hv, t.ctl, s, on,
+                    t.ks->face(t.n1, *t.T, *t.P, in[s], t.fb_h, t.fb_hu, t.fb_hv, t.ctl, s, on,
                                st);
-                    t.ks->stage_keep(t.n1, *t.T, *t.P, *t.X, a->S[s], q, a->S[s + 1], t.fb_h,
-                                     t.fb_hu, t.fb_hv, t.ctl, s, 0, a->Kp[s], st);
+                    t.ks->stage_keep(t.n1, *t.T, *t.P, *t.X, in[s], in[0], out[s], t.fb_h, t.fb_hu,
+                                     t.fb_hv, t.ctl, s, 0, keep_view(n, c0, s), st);
                 }
-                for (int b = 0; b < 3; ++b)
-                    if (int s = pack(a, sl + b * 3 * nv, a->S[b], nv, st)) return s;
-                for (int s = 0; s < 3; ++s)
-                    if (int e = keep_copy(sl + (9 + 5 * s) * nv, a->Kp[s], true)) return e;
-                // the step's result (with its velocities) starts the next
-                ACK(cudaMemcpyAsync(q.h, a->S[3].h, 5 * bv, cudaMemcpyDeviceToDevice, st));
                 recomputed += 1;
             }
             for (int64_t n = c1 - 1; n >= c0; --n) {
                 t.ks->station_seed(a->d_eta + n * n_st, a->d_obs + n * n_st, a->d_node0, a->d_w,
                                    n_st, nn, a->lam[0], t.P->has_bed ? A.lbed : nullptr, st);
-                const double* sl = a->d_seg + (n - c0) * slot;
-                for (int b = 0; b < 3; ++b) {
-                    if (int s = unpack(a, a->S[b], sl + b * 3 * nv, nv, st)) return s;
-                    t.ks->velocity(a->S[b], nv, t.P->h_min, st);
-                }
-                for (int s = 0; s < 3; ++s)
-                    if (int e = keep_copy(const_cast<double*>(sl) + (9 + 5 * s) * nv, a->Kp[s],
-                                          false))
-                        return e;
+                const DevBuf in[3] = {view(n, c0, 0), view(n, c0, 1), view(n, c0, 2)};
+                const DevBuf keep[3] = {keep_view(n, c0, 0), keep_view(n, c0, 1),
+                                        keep_view(n, c0, 2)};
+                for (int b = 0; b < 3; ++b) t.ks->velocity(in[b], nv, t.P->h_min, st);
                 if (int s = args_to_ctl(a, n)) return s;
-                if (int s = reverse_stages(a)) return s;
+                if (int s = reverse_stages(a, in, keep)) return s;
             }
             if (c0 == 0) break;
             continue;
@@ -822,7 +821,7 @@ int dgswe_adjoint_reverse(dgswe_adjoint* a, double* grad_h0, double* grad_hu0, d
                 t.ks->stage_keep(t.n1, *t.T, *t.P, *t.X, a->S[s], q, a->S[s + 1], t.fb_h, t.fb_hu,
                                  t.fb_hv, t.ctl, s, 0, a->Kp[s], st);
             }
-            if (int s = reverse_stages(a)) return s;
+            if (int s = reverse_stages(a, a->S, a->Kp)) return s;
             recomputed += 1;
         }
         if (c0 == 0) break;
