@@ -86,6 +86,16 @@ class ParentSeries(C.Structure):
     ]
 
 
+class Relaxation(C.Structure):
+    _fields_ = [
+        ("parent", C.POINTER(ParentSeries)),
+        ("weight", _dp),
+        ("rate", C.c_double),
+        ("wet_depth", C.c_double),
+        ("momentum_only", C.c_int32),
+    ]
+
+
 class Boundary(C.Structure):
     _fields_ = [
         ("tag", C.c_int32),
@@ -137,6 +147,7 @@ class Form(C.Structure):
         ("numerics", C.c_int32),
         ("has_line_local", C.c_int32),
         ("line_local_depth", C.c_double),
+        ("relaxation", C.POINTER(Relaxation)),
     ]
 
 

@@ -19,6 +19,7 @@ No public dataset is involved: every input is generated here."""
 
 from __future__ import annotations
 
+import dataclasses
 import math
 from dataclasses import dataclass
 
@@ -441,6 +442,43 @@ def synthetic_parent(form: SWEDeviceForm2D, tag: int = TAG_OPEN, t0: float = 0.0
                           on_boundary=on_boundary, slot_of_node=slot_of_node, cubic=cubic,
                           velocity=velocity, reference_level=reference_level,
                           max_transport_ratio=max_transport_ratio, ramp_duration=ramp_duration)
+
+
+def synthetic_nesting(form: SWEDeviceForm2D, tag: int = TAG_OPEN, band_width: float = 4000.0,
+                      rate: float = 1.0 / 1800.0, momentum_only: bool = False, **parent_kw):
+    """A nesting of ``form`` in the synthetic parent (``synthetic_parent``):
+    one series for the open boundary's nodes (weight 1) and for every node
+    within ``band_width`` of them (weight (1 − d/W)², the relaxation band,
+    as OceanModelState::new lays them out, src/boundary/ocean_nesting.rs:
+    325-395). Returns the boundary condition and the relaxation band."""
+    from .physics import RelaxationBand
+
+    boundary = synthetic_parent(form, tag, by_position=False, **parent_kw)
+    flats = boundary_face_nodes(form, tag)
+    x, y = form.positions()
+    x, y = x.reshape(-1), y.reshape(-1)
+    bx, by = x[flats], y[flats]
+    d = np.sqrt((x[:, None] - bx[None, :]) ** 2 + (y[:, None] - by[None, :]) ** 2).min(axis=1)
+    on = np.zeros(form.n_values, dtype=bool)
+    on[flats] = True
+    band = np.flatnonzero(~on & (d < band_width))
+    m = len(flats)
+    # band slots take the nearest boundary node's series, scaled down inland
+    nearest = np.argmin((x[band, None] - bx[None, :]) ** 2 + (y[band, None] - by[None, :]) ** 2,
+                        axis=1)
+    fall = (1.0 - 0.3 * d[band] / band_width)[:, None, None]
+    values = np.concatenate([boundary.values, (boundary.values[nearest] * fall).astype(np.float32)])
+    depth = np.concatenate([boundary.parent_depth, boundary.parent_depth[nearest]])
+    positions = np.vstack([boundary.positions, np.column_stack([x[band], y[band]])])
+    slot_of_node = np.full(form.n_values, 0xFFFFFFFF, dtype=np.uint32)
+    slot_of_node[flats] = np.arange(m, dtype=np.uint32)
+    slot_of_node[band] = m + np.arange(len(band), dtype=np.uint32)
+    on_boundary = np.concatenate([np.ones(m, dtype=bool), np.zeros(len(band), dtype=bool)])
+    weight = np.concatenate([np.ones(m), (1.0 - d[band] / band_width) ** 2])
+    parent = dataclasses.replace(boundary, positions=positions, values=values, parent_depth=depth,
+                                 on_boundary=on_boundary, slot_of_node=slot_of_node)
+    return parent, RelaxationBand(parent=parent, weight=weight, rate=rate,
+                                  momentum_only=momentum_only)
 
 
 # -- the reference's split-form test setups ------------------------------------

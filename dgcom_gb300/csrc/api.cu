@@ -346,6 +346,11 @@ int boundary_node_tables(dgswe_handle* h, const dgswe_form& f, const Operators& 
     if ((s = upload_vec(h, ptimes, &T.pt_times))) return s;
     if ((s = upload_vec(h, pvalues, &T.pt_values))) return s;
     // the parents' time ranges, for the runs' checks
+    if (f.relaxation && f.relaxation->parent->n_times > 1) {
+        const dgswe_parent_series& ps = *f.relaxation->parent;
+        h->parent_range = {std::max(h->parent_range.first, ps.times[0]),
+                           std::min(h->parent_range.second, ps.times[ps.n_times - 1])};
+    }
     for (int b = 0; b < f.n_boundaries; ++b)
         if (f.boundaries[b].kind == DGSWE_BC_PARENT) {
             const dgswe_parent_series& ps = *f.boundaries[b].parent;
@@ -353,6 +358,55 @@ int boundary_node_tables(dgswe_handle* h, const dgswe_form& f, const Operators& 
                 h->parent_range = {std::max(h->parent_range.first, ps.times[0]),
                                    std::min(h->parent_range.second, ps.times[ps.n_times - 1])};
         }
+    return DGSWE_OK;
+}
+
+// The nesting relaxation band: the nodes whose slot has a positive weight,
+// the parent's series, and the per-node source buffer
+int relaxation_tables(dgswe_handle* h, const dgswe_form& f) {
+    if (!f.relaxation) return DGSWE_OK;
+    const dgswe_relaxation& r = *f.relaxation;
+    const dgswe_parent_series& ps = *r.parent;
+    std::vector<int64_t> node;
+    std::vector<int32_t> slot;
+    for (int64_t g = 0; g < h->n_values; ++g) {
+        const uint32_t q = ps.slot_of_node[g];
+        if (q == 0xFFFFFFFFu) continue;
+        if ((int64_t)q >= ps.n_slots)
+            return fail(h, DGSWE_ERR_INVALID, "a relaxation slot beyond n_slots");
+        if (!(r.weight[q] > 0.0)) continue;
+        node.push_back(g);
+        slot.push_back((int32_t)q);
+    }
+    DevTables& T = h->T;
+    T.rx_n = (int64_t)node.size();
+    if (T.rx_n == 0) return DGSWE_OK;
+    std::vector<double> weight(r.weight, r.weight + ps.n_slots);
+    std::vector<double> depth(ps.n_slots, NAN);
+    if (ps.parent_depth) depth.assign(ps.parent_depth, ps.parent_depth + ps.n_slots);
+    std::vector<double> times(ps.times, ps.times + ps.n_times);
+    std::vector<float> values(ps.values, ps.values + (size_t)ps.n_slots * ps.n_times * 3);
+    int s = DGSWE_OK;
+    if ((s = upload_vec(h, node, &T.rx_node))) return s;
+    if ((s = upload_vec(h, slot, &T.rx_slot))) return s;
+    if ((s = upload_vec(h, weight, &T.rx_weight))) return s;
+    if ((s = upload_vec(h, depth, &T.rx_depth))) return s;
+    if ((s = upload_vec(h, times, &T.rx_times))) return s;
+    if ((s = upload_vec(h, values, &T.rx_values))) return s;
+    T.rx_n_times = (int)ps.n_times;
+    T.rx_cubic = ps.cubic ? 1 : 0;
+    T.rx_velocity = ps.velocity ? 1 : 0;
+    T.rx_momentum_only = r.momentum_only ? 1 : 0;
+    T.rx_ref_level = ps.reference_level;
+    T.rx_max_ratio = ps.max_transport_ratio;
+    T.rx_ramp = ps.ramp_duration;
+    T.rx_rate = r.rate;
+    T.rx_wet = r.wet_depth;
+    void* p = nullptr;
+    CK(cudaMalloc(&p, 3 * (size_t)h->n_values * sizeof(double)));
+    h->allocations.push_back(p);
+    CK(cudaMemset(p, 0, 3 * (size_t)h->n_values * sizeof(double)));
+    T.rx_src = (double*)p;
     return DGSWE_OK;
 }
 
@@ -448,6 +502,7 @@ int create_impl(dgswe_handle* h, const dgswe_form* f, int device) {
     h->P.n_conditions = f->n_boundaries;
     for (int b = 0; b < f->n_boundaries; ++b) h->P.cond[b] = make_condition(f->boundaries[b]);
     if ((s = boundary_node_tables(h, *f, ops, topo, t))) return bail(s);
+    if ((s = relaxation_tables(h, *f))) return bail(s);
 
     // buffers, faces, control
     if ((s = ensure_buffer(h, DGSWE_STATE))) return bail(s);
@@ -478,6 +533,7 @@ int create_impl(dgswe_handle* h, const dgswe_form* f, int device) {
     h->form.bathymetry = nullptr;
     h->form.manning_n_nodes = nullptr;
     h->form.boundaries = nullptr;
+    h->form.relaxation = nullptr;
     return DGSWE_OK;
 }
 

@@ -54,6 +54,18 @@ struct DevTables {
     // depth (per-node tides and parents share bface_slot and nt_depth)
     const double* pt_times = nullptr;
     const float* pt_values = nullptr;
+    // the nesting relaxation band: its nodes (flat index) and their slots,
+    // the parent's series and each slot's weight and depth, the options,
+    // and the source of the current stage per node ([3][K·nn], 0 off the
+    // band) that the stage kernel adds after Coriolis
+    int64_t rx_n = 0;
+    const int64_t* rx_node = nullptr;
+    const int32_t* rx_slot = nullptr;
+    const double *rx_weight = nullptr, *rx_depth = nullptr, *rx_times = nullptr;
+    const float* rx_values = nullptr;
+    int rx_n_times = 0, rx_cubic = 0, rx_velocity = 0, rx_momentum_only = 0;
+    double rx_ref_level = 0.0, rx_max_ratio = 0.0, rx_ramp = 0.0, rx_rate = 0.0, rx_wet = 0.0;
+    double* rx_src = nullptr;
 };
 
 struct Constituent {

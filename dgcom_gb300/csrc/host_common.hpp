@@ -69,6 +69,18 @@ inline int check_form(const dgswe_form* f, std::string& why) {
         return why = "per-node Manning without data", DGSWE_ERR_INVALID;
     if (f->has_wet_dry && !(f->wet_dry_h_dry > 0.0 && f->wet_dry_relaxation_time > 0.0))
         return why = "the wet/dry depth and relaxation time must be positive", DGSWE_ERR_INVALID;
+    if (f->relaxation) {
+        const dgswe_relaxation& r = *f->relaxation;
+        const dgswe_parent_series* p = r.parent;
+        if (!p || p->n_slots <= 0 || p->n_times <= 0 || !p->times || !p->values ||
+            !p->slot_of_node || !r.weight || !(r.rate >= 0.0) || !(r.wet_depth >= 0.0))
+            return why = "a relaxation band without its data", DGSWE_ERR_INVALID;
+        if (p->n_slots >= (1ll << 31) || p->n_times >= (1ll << 31))
+            return why = "a relaxation band too large", DGSWE_ERR_INVALID;
+        for (int64_t i = 1; i < p->n_times; ++i)
+            if (!(p->times[i] > p->times[i - 1]))
+                return why = "parent snapshot times must increase", DGSWE_ERR_INVALID;
+    }
     if (f->n_boundaries < 0 || f->n_boundaries > kMaxConditions ||
         (f->n_boundaries > 0 && !f->boundaries))
         return why = "boundary conditions", DGSWE_ERR_INVALID;

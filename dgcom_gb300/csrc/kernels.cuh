@@ -109,6 +109,50 @@ __device__ void entropy_surface(const Q& qa, const Q& qb, double nx, double ny, 
     fb = {-s.h + 0.0, -s.hu + fb_b * (-nx), -s.hv + fb_b * (-ny)};
 }
 
+// The nesting relaxation band's source at the stage's input, per band node
+// (NestingRelaxation2D::add_element and relaxation_source,
+// src/boundary/ocean_nesting.rs:955-1030), into T.rx_src at its element's
+// stage time (in a multirate pass, the element's own)
+template <bool LISTED>
+__global__ void __launch_bounds__(256) relax_kernel(DevTables T, Physics P, DevBuf in,
+                                                    const StepCtl* ctl, int slot, LtsPass lp) {
+    const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= T.rx_n) return;
+    const int64_t g = T.rx_node[b];
+    const int64_t k = g / P.nn;
+    const int32_t s = T.rx_slot[b];
+    const int64_t nv = T.K * P.nn;
+    double sh = 0.0, shu = 0.0, shv = 0.0;
+    const double h = in.h[g], w = T.rx_weight[s];
+    if (fp::gt0(w) && !fp::lt(h, T.rx_wet)) {
+        const int member = T.elem_member ? T.elem_member[k] : 0;
+        const double t = LISTED ? lts_stage(lp, k).time : ctl[member].stage[slot].time;
+        const double bed = P.has_bed ? T.bed[g] : 0.0;
+        double eta, u, v;
+        bool has_uv;
+        parent_state_at(T.rx_times, T.rx_n_times, T.rx_cubic, T.rx_values + (int64_t)s * T.rx_n_times * 3,
+                        t, T.rx_ramp, T.rx_ref_level, T.rx_velocity, T.rx_max_ratio, T.rx_depth[s],
+                        bed, eta, u, v, has_uv);
+        const double hp = eta - bed;
+        if (!fp::lt(hp, T.rx_wet)) {
+            const double gamma = w * T.rx_rate;
+            const double hu = in.hu[g], hv = in.hv[g];
+            if (!has_uv) {
+                u = hu / h;
+                v = hv / h;
+            }
+            const double dh = T.rx_momentum_only ? 0.0 : hp - h;
+            const double depth = T.rx_momentum_only ? h : hp;
+            sh = gamma * dh;
+            shu = gamma * (depth * u - hu);
+            shv = gamma * (depth * v - hv);
+        }
+    }
+    T.rx_src[g] = sh;
+    T.rx_src[nv + g] = shu;
+    T.rx_src[2 * nv + g] = shv;
+}
+
 // LISTED: a multirate pass's faces (lp's edge and boundary-face lists),
 // each boundary face at its element's stage time
 template <int N1, bool LISTED>
@@ -569,6 +613,12 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS, Cfg<N1>::MIN_BLOCKS)
             const double f = P.coriolis_field ? T.fcor[gi] : P.f0;
             Fhu += f * hv;
             Fhv += -f * hu;
+        }
+        if (T.rx_src) {  // the nesting relaxation band (0 off the band)
+            const int64_t nv = T.K * NN;
+            Fh += T.rx_src[gi];
+            Fhu += T.rx_src[nv + gi];
+            Fhv += T.rx_src[2 * nv + gi];
         }
         if (mode == kRhsOnly) {
             out.h[gi] = Fh;

@@ -8,9 +8,18 @@
 namespace dgswe {
 namespace DGSWE_NS {
 
+// The relaxation band's source of a stage, before its stage kernel reads it
+template <bool LISTED>
+static void relax(const DevTables& T, const Physics& P, const DevBuf& in, const StepCtl* ctl,
+                  int slot, const LtsPass& lp, cudaStream_t s) {
+    if (T.rx_n == 0 || !T.rx_src) return;
+    relax_kernel<LISTED><<<(unsigned)((T.rx_n + 255) / 256), 256, 0, s>>>(T, P, in, ctl, slot, lp);
+}
+
 template <int N1>
 static void face_n(const DevTables& T, const Physics& P, const DevBuf& in, double* fh, double* fhu,
                    double* fhv, const StepCtl* ctl, int slot, const int* active, cudaStream_t s) {
+    relax<false>(T, P, in, ctl, slot, LtsPass{}, s);
     const int64_t items = (T.n_edges + T.n_bfaces) * N1;
     if (items == 0) return;
     const int threads = 256;
@@ -23,6 +32,7 @@ template <int N1>
 static void face_listed_n(const DevTables& T, const Physics& P, const DevBuf& in, double* fh,
                           double* fhu, double* fhv, StepCtl* ctl, const LtsPass& lp,
                           cudaStream_t s) {
+    relax<true>(T, P, in, ctl, 0, lp, s);
     const int64_t items = (lp.n_edges + lp.n_bfaces) * N1;
     if (items == 0) return;
     const int threads = 256;

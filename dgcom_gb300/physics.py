@@ -87,6 +87,20 @@ class ParentBoundary:
 
 
 @dataclass
+class RelaxationBand:
+    """NestingRelaxation2D (src/boundary/ocean_nesting.rs:900-1065; the
+    device source DeviceSource2D::NestingRelaxation): relax the band's nodes
+    towards ``parent`` (its slot_of_node covers them) at rate ``weight[slot]
+    · rate``."""
+
+    parent: "ParentBoundary"
+    weight: np.ndarray             # [n_slots]
+    rate: float                    # 1/τ (1/s)
+    wet_depth: float = 0.05
+    momentum_only: bool = False
+
+
+@dataclass
 class SWEDeviceForm2D:
     mesh: QuadMesh
     order: int
@@ -116,6 +130,7 @@ class SWEDeviceForm2D:
     # (src/physics/builder.rs:296-322), the WetDry subcells' depth and the
     # wet/dry correction's h_dry, whichever is deeper
     line_local_depth: float | None | str = "auto"
+    relaxation: RelaxationBand | None = None
 
     def local_depth(self) -> float | None:
         """The line-local depth the C form carries (None: none)."""
@@ -144,6 +159,37 @@ class SWEDeviceForm2D:
             a = np.ascontiguousarray(a, dtype=dtype)
             keep.append(a)
             return a
+
+        def parent_series(bc) -> abi.ParentSeries:
+            ps = abi.ParentSeries()
+            pos = arr(np.asarray(bc.positions).reshape(-1, 2), np.float64)
+            ps.n_slots = pos.shape[0]
+            ps.positions = pos.ctypes.data_as(C.POINTER(C.c_double))
+            tt = arr(bc.times, np.float64)
+            ps.n_times = tt.size
+            ps.times = tt.ctypes.data_as(C.POINTER(C.c_double))
+            vals = arr(np.asarray(bc.values).reshape(-1), np.float32)
+            if vals.size != pos.shape[0] * tt.size * 3:
+                raise ValueError("values need [n_slots][n_times][3] entries")
+            ps.values = vals.ctypes.data_as(C.POINTER(C.c_float))
+            if bc.parent_depth is not None:
+                ps.parent_depth = arr(bc.parent_depth, np.float64).ctypes.data_as(
+                    C.POINTER(C.c_double))
+            if bc.on_boundary is not None:
+                ps.on_boundary = arr(np.asarray(bc.on_boundary, dtype=bool),
+                                     np.uint8).ctypes.data_as(C.POINTER(C.c_uint8))
+            if bc.slot_of_node is not None:
+                sl = arr(np.asarray(bc.slot_of_node).reshape(-1), np.uint32)
+                if sl.size != self.n_values:
+                    raise ValueError("slot_of_node needs one slot per mesh node")
+                ps.slot_of_node = sl.ctypes.data_as(C.POINTER(C.c_uint32))
+            ps.cubic = 1 if bc.cubic else 0
+            ps.velocity = 1 if bc.velocity else 0
+            ps.reference_level = bc.reference_level
+            ps.max_transport_ratio = bc.max_transport_ratio or 0.0
+            ps.ramp_duration = bc.ramp_duration or 0.0
+            keep.append(ps)
+            return ps
 
         f = abi.Form()
         f.abi_version = abi.ABI_VERSION
@@ -201,35 +247,7 @@ class SWEDeviceForm2D:
             elif isinstance(bc, ParentBoundary):
                 bcs[i].kind = abi.BC_PARENT
                 bcs[i].elevation_only = abi.INCOMING_WAVE if bc.incoming_wave else abi.AT_REST
-                ps = abi.ParentSeries()
-                pos = arr(np.asarray(bc.positions).reshape(-1, 2), np.float64)
-                ps.n_slots = pos.shape[0]
-                ps.positions = pos.ctypes.data_as(C.POINTER(C.c_double))
-                tt = arr(bc.times, np.float64)
-                ps.n_times = tt.size
-                ps.times = tt.ctypes.data_as(C.POINTER(C.c_double))
-                vals = arr(np.asarray(bc.values).reshape(-1), np.float32)
-                if vals.size != pos.shape[0] * tt.size * 3:
-                    raise ValueError("values need [n_slots][n_times][3] entries")
-                ps.values = vals.ctypes.data_as(C.POINTER(C.c_float))
-                if bc.parent_depth is not None:
-                    ps.parent_depth = arr(bc.parent_depth, np.float64).ctypes.data_as(
-                        C.POINTER(C.c_double))
-                if bc.on_boundary is not None:
-                    ps.on_boundary = arr(np.asarray(bc.on_boundary, dtype=bool),
-                                         np.uint8).ctypes.data_as(C.POINTER(C.c_uint8))
-                if bc.slot_of_node is not None:
-                    sl = arr(np.asarray(bc.slot_of_node).reshape(-1), np.uint32)
-                    if sl.size != self.n_values:
-                        raise ValueError("slot_of_node needs one slot per mesh node")
-                    ps.slot_of_node = sl.ctypes.data_as(C.POINTER(C.c_uint32))
-                ps.cubic = 1 if bc.cubic else 0
-                ps.velocity = 1 if bc.velocity else 0
-                ps.reference_level = bc.reference_level
-                ps.max_transport_ratio = bc.max_transport_ratio or 0.0
-                ps.ramp_duration = bc.ramp_duration or 0.0
-                keep.append(ps)
-                bcs[i].parent = C.pointer(ps)
+                bcs[i].parent = C.pointer(parent_series(bc))
             elif isinstance(bc, NodeTidesBoundary):
                 bcs[i].kind = abi.BC_NODE_TIDES
                 bcs[i].elevation_only = abi.INCOMING_WAVE if bc.incoming_wave else abi.AT_REST
@@ -276,6 +294,16 @@ class SWEDeviceForm2D:
         depth = self.local_depth()
         f.has_line_local = 0 if depth is None else 1
         f.line_local_depth = 0.0 if depth is None else float(depth)
+        if self.relaxation is not None:
+            r = abi.Relaxation()
+            r.parent = C.pointer(parent_series(self.relaxation.parent))
+            w = arr(self.relaxation.weight, np.float64)
+            r.weight = w.ctypes.data_as(C.POINTER(C.c_double))
+            r.rate = self.relaxation.rate
+            r.wet_depth = self.relaxation.wet_depth
+            r.momentum_only = 1 if self.relaxation.momentum_only else 0
+            keep.append(r)
+            f.relaxation = C.pointer(r)
         return f, keep
 
 

@@ -169,6 +169,23 @@ typedef struct dgswe_parent_series {
     double ramp_duration;         /* s; ≤ 0: no ramp */
 } dgswe_parent_series;
 
+/* NestingRelaxation2D (src/boundary/ocean_nesting.rs:900-1065; the device
+ * source DeviceSource2D::NestingRelaxation) as plain data: at every node
+ * whose slot (parent->slot_of_node, required) has weight w > 0, the source
+ *   γ (q_parent − q),  γ = w·rate
+ * with the parent's η, u, v there (as the parent boundary evaluates them;
+ * without currents the node's own velocity), zero where the node or the
+ * parent is shallower than wet_depth; with momentum_only the depth is kept
+ * and the momentum relaxed at the node's depth (relaxation_source). It is
+ * added to the RHS after Coriolis. */
+typedef struct dgswe_relaxation {
+    const dgswe_parent_series* parent;
+    const double* weight;   /* [parent->n_slots] band weight; 1 on the boundary */
+    double rate;            /* 1/τ (1/s) */
+    double wet_depth;       /* m */
+    int32_t momentum_only;
+} dgswe_relaxation;
+
 typedef struct dgswe_boundary {
     int32_t tag;            /* the face tag this condition applies to */
     int32_t kind;           /* dgswe_boundary_kind */
@@ -233,6 +250,9 @@ typedef struct dgswe_form {
      * (the rates spread one face per stage). */
     int32_t has_line_local;
     double line_local_depth;
+
+    /* A nesting relaxation band towards a parent model, or NULL */
+    const dgswe_relaxation* relaxation;
 } dgswe_form;
 
 /* ---- stages and runs ---------------------------------------------------- */

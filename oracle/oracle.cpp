@@ -594,6 +594,16 @@ struct Buffer {
     State get(size_t i) const { return {h[i], hu[i], hv[i]}; }
 };
 
+// NestingRelaxation2D (src/boundary/ocean_nesting.rs:900-1065): the parent
+// (a Boundary holding its series) and each slot's weight
+struct Relaxation {
+    bool on = false;
+    Boundary parent;
+    std::vector<double> weight;
+    double rate = 0.0, wet_depth = 0.0;
+    bool momentum_only = false;
+};
+
 struct Model {
     dgswe_form form;
     Ops ops;
@@ -608,6 +618,7 @@ struct Model {
     std::string error;
     WetDry wd;
     bool has_bed = false;
+    Relaxation relax;
 
     explicit Model(int order) : ops(order) {}
     size_t n_values() const { return (size_t)mesh.n_elements * ops.nn; }
@@ -1042,6 +1053,35 @@ static void element_rhs(const Model& m, const Buffer& q, int64_t k, double time,
             State st = q.get((size_t)k * nn + i);
             out_hu[i] += f * st.hv;
             out_hv[i] += -f * st.hu;
+        }
+    }
+    // NestingRelaxation2D::add_element with relaxation_source
+    // (src/boundary/ocean_nesting.rs:955-1030), after Coriolis
+    if (m.relax.on) {
+        const Relaxation& r = m.relax;
+        for (int i = 0; i < nn; ++i) {
+            size_t flat = (size_t)k * nn + i;
+            uint32_t slot = r.parent.parent.slot_of_node[flat];
+            if (slot == 0xFFFFFFFFu) continue;
+            State st = q.get(flat);
+            double w = r.weight[slot];
+            if (w <= 0.0 || st.h < r.wet_depth) continue;
+            double bed = m.bed_at(k, i);
+            double eta, u, v;
+            bool has_uv;
+            r.parent.parent_external(slot, time, bed, eta, u, v, has_uv);
+            double h = eta - bed;
+            if (h < r.wet_depth) continue;
+            double gamma = w * r.rate;
+            if (!has_uv) {
+                u = st.hu / st.h;
+                v = st.hv / st.h;
+            }
+            double dh = r.momentum_only ? 0.0 : h - st.h;
+            double depth = r.momentum_only ? st.h : h;
+            out_h[i] += gamma * dh;
+            out_hu[i] += gamma * (depth * u - st.hu);
+            out_hv[i] += gamma * (depth * v - st.hv);
         }
     }
 }
@@ -1854,12 +1894,39 @@ int oracle_create(const dgswe_form* f, int device, oracle_handle** out) {
         }
         m->boundaries[in.tag] = bc;
     }
+    if (f->relaxation) {
+        const dgswe_relaxation& r = *f->relaxation;
+        const dgswe_parent_series* p = r.parent;
+        if (!p || !p->slot_of_node || !r.weight || p->n_slots <= 0 || p->n_times <= 0) {
+            delete m;
+            return DGSWE_ERR_INVALID;
+        }
+        Boundary::Parent& pp = m->relax.parent.parent;
+        pp.n_slots = p->n_slots;
+        pp.n_times = p->n_times;
+        pp.times.assign(p->times, p->times + p->n_times);
+        pp.values.assign(p->values, p->values + (size_t)p->n_slots * p->n_times * 3);
+        pp.depth.assign(p->n_slots, NAN);
+        if (p->parent_depth) pp.depth.assign(p->parent_depth, p->parent_depth + p->n_slots);
+        pp.slot_of_node.assign(p->slot_of_node, p->slot_of_node + (size_t)f->n_elements * m->ops.nn);
+        pp.cubic = p->cubic != 0;
+        pp.velocity = p->velocity != 0;
+        pp.reference_level = p->reference_level;
+        pp.max_ratio = p->max_transport_ratio;
+        pp.ramp = p->ramp_duration;
+        m->relax.weight.assign(r.weight, r.weight + p->n_slots);
+        m->relax.rate = r.rate;
+        m->relax.wet_depth = r.wet_depth;
+        m->relax.momentum_only = r.momentum_only != 0;
+        m->relax.on = true;
+    }
     for (auto& e : m->mesh.edges)
         if (e.right.element < 0 && !m->boundaries.count(e.tag)) {
             delete m;
             return DGSWE_ERR_INVALID;
         }
     m->form.boundaries = nullptr;
+    m->form.relaxation = nullptr;
     m->form.bathymetry = nullptr;
     m->form.manning_n_nodes = nullptr;
     m->form.vertices = nullptr;

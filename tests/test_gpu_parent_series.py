@@ -78,3 +78,52 @@ def test_run_matches_oracle_and_the_span_is_checked():
             dev.run_with_callback(DeviceRun(span=(40_000.0, 50_000.0), cfl=0.5))
     finally:
         dev.close()
+
+
+def nested(numerics, momentum_only=False, cubic=True):
+    case = cases.tidal_channel(nx=24, ny=3, order=2, numerics=numerics)
+    form = case.form
+    parent, band = cases.synthetic_nesting(form, band_width=6000.0, cubic=cubic,
+                                           momentum_only=momentum_only)
+    form = dataclasses.replace(form, boundaries={**form.boundaries, TAG_OPEN: parent},
+                               relaxation=band)
+    return case, form, cases.with_flow(case, eta_amp=0.3, u=0.3, v=0.05)
+
+
+@pytest.mark.parametrize("numerics", [abi.NUMERICS_FAST, abi.NUMERICS_EXACT])
+@pytest.mark.parametrize("momentum_only", [False, True])
+@pytest.mark.parametrize("cubic", [False, True])
+def test_relaxation_band_matches_oracle(numerics, momentum_only, cubic):
+    case, form, q = nested(numerics, momentum_only, cubic)
+    dev, ref = SWEPhysics2D(form, 0), oracle(form)
+    try:
+        for s in (dev, ref):
+            s.upload(*q)
+        for t in (1800.0, 9000.5):
+            err = rel_err(dev.compute_rhs_into(t), ref.compute_rhs_into(t))
+            assert err <= TOL_RHS, f"t {t}: RHS {err:.3e}"
+        dt = ref.compute_dt_ssp(0.5)
+        for s in (dev, ref):
+            s.stage_where(base=0, input=0, out=1, time=9000.5, a=1.0, b=0.0, c=dt)
+        err = rel_err(dev.download(1), ref.download(1))
+        assert err <= TOL, f"stage {err:.3e}"
+    finally:
+        dev.close()
+        ref.close()
+
+
+@pytest.mark.parametrize("levels", [0, 3])
+def test_nested_run_matches_oracle(levels):
+    case, form, q = nested(abi.NUMERICS_EXACT)
+    out = []
+    for sim in (SWEPhysics2D(form, 0), oracle(form)):
+        try:
+            sim.upload(*q)
+            rep = sim.run_with_callback(DeviceRun(span=(4000.0, 4200.0), cfl=0.5, levels=levels))
+            assert rep.success, rep.message
+            out.append((sim.download(), rep.n_steps))
+        finally:
+            sim.close()
+    (a, na), (b, nb) = out
+    assert na == nb
+    assert rel_err(a, b) <= 1e-10

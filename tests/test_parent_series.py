@@ -76,3 +76,41 @@ def test_a_still_parent_is_the_still_boundary(cubic):
             ref.close()
     for a, b in zip(*out):
         assert np.array_equal(a, b)
+
+
+def nested(momentum_only=False, cubic=True):
+    case = cases.tidal_channel(nx=24, ny=3, order=2)
+    form = case.form
+    form.bathymetry = form.bathymetry - 5.0
+    q = cases.with_flow(case, eta_amp=0.3, u=0.3, v=0.05)
+    parent, band = cases.synthetic_nesting(form, band_width=6000.0, cubic=cubic,
+                                           momentum_only=momentum_only)
+    form = dataclasses.replace(form, boundaries={**form.boundaries, TAG_OPEN: parent})
+    return form, band, q
+
+
+def rhs(form, q, t=9000.5):
+    ref = oracle(form)
+    try:
+        ref.upload(*q)
+        return ref.compute_rhs_into(t)
+    finally:
+        ref.close()
+
+
+def test_a_band_of_zero_weight_changes_nothing():
+    form, band, q = nested()
+    base = rhs(form, q)
+    zero = dataclasses.replace(band, weight=np.zeros_like(band.weight))
+    for a, b in zip(base, rhs(dataclasses.replace(form, relaxation=zero), q)):
+        assert np.array_equal(a, b)
+    relaxed = rhs(dataclasses.replace(form, relaxation=band), q)
+    assert np.abs(relaxed[1] - base[1]).max() > 0.0
+
+
+def test_momentum_only_keeps_the_mass():
+    form, band, q = nested(momentum_only=True)
+    base = rhs(form, q)
+    relaxed = rhs(dataclasses.replace(form, relaxation=band), q)
+    assert np.array_equal(base[0], relaxed[0])
+    assert np.abs(relaxed[1] - base[1]).max() > 0.0
