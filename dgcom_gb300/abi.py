@@ -185,6 +185,27 @@ class RunConfig(C.Structure):
 MAX_LEVELS = 8  # DGSWE_MAX_LEVELS
 
 
+class MultirateStage(C.Structure):
+    """dgswe_multirate_stage: one stage pass of a multirate coarse step."""
+    _fields_ = [
+        ("t", C.c_double),
+        ("dt", C.c_double),
+        ("finest", C.c_int32),
+        ("substep", C.c_int32),
+        ("depth", C.c_int32),
+        ("stage", C.c_int32),
+        ("last", C.c_int32),
+        ("start", C.c_double),
+        ("input", C.c_double),
+        ("beta", C.c_double),
+        ("c", C.c_double),
+        ("base", C.c_int32),
+        ("input_buffer", C.c_int32),
+        ("out", C.c_int32),
+        ("acc", C.c_int32),
+    ]
+
+
 class MultirateStats(C.Structure):
     _fields_ = [
         ("steps", C.c_int64),
@@ -313,6 +334,13 @@ CUDA_ONLY = {
     "profile_steps": (C.c_int, [C.c_void_p, C.POINTER(RunConfig), C.c_int64, C.POINTER(Profile)]),
     # local time stepping: the last run's work counts; the level planner (host only)
     "multirate_stats_get": (C.c_int, [C.c_void_p, C.POINTER(MultirateStats)]),
+    # the LocalTimeStepping passes of a host-planned coarse step
+    "begin_coarse_step": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_uint8),
+                                    C.POINTER(C.c_uint8)]),
+    "stage_where": (C.c_int, [C.c_void_p, C.POINTER(MultirateStage)]),
+    "finish_where": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "depth_flags": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_double,
+                              C.POINTER(C.c_uint8)]),
     "planner_create": (C.c_int, [C.POINTER(Form), C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "planner_destroy": (None, [C.c_void_p]),
     "planner_assign": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_uint8), C.c_double, C.c_double,

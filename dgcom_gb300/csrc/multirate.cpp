@@ -275,6 +275,21 @@ void MultiratePlanner::edge_lists(const std::vector<int64_t>& edge_left,
     }
 }
 
+void MultiratePlanner::set_plan(const uint8_t* levels, const uint8_t* rates) {
+    memo_ = false;
+    level_.assign(levels, levels + K_);
+    int finest = 0;
+    for (int64_t k = 0; k < K_; ++k) finest = std::max(finest, (int)level_[k]);
+    for (int s = 0; s < n_stages_; ++s) rate_[s].assign(rates + s * K_, rates + (s + 1) * K_);
+    finest_ = finest;
+    int64_t lev = 0;
+    for (int64_t k = 0; k < K_; ++k) lev += (int64_t)1 << level_[k];
+    level_evaluations_ = (int64_t)n_stages_ * lev;
+    inverse_dt_sum_ = 0.0;
+    n_line_local_ = 0;
+    make_lists();
+}
+
 void MultiratePlanner::assign_one_level() {
     memo_ = false;
     finest_ = 0;

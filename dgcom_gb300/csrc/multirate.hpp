@@ -50,6 +50,10 @@ public:
                   double landing);
     // Every element on level 0 (global steps)
     void assign_one_level();
+    // Given levels and rates (rates[s] for each stage, each between the
+    // element's level and the finest): a host that plans itself
+    // (LocalTimeStepping::begin_coarse_step)
+    void set_plan(const uint8_t* levels, const uint8_t* rates);
 
     int finest() const { return finest_; }
     int nn() const { return nn_; }

@@ -332,6 +332,121 @@ int run_multirate(dgswe_handle* h, const dgswe_run_config* run, dgswe_callback c
 }  // namespace host
 }  // namespace dgswe
 
+extern "C" {
+
+int dgswe_begin_coarse_step(dgswe_handle* h, int32_t n_stages, const uint8_t* levels,
+                            const uint8_t* rates) {
+    if (!h) return DGSWE_ERR_INVALID;
+    if ((n_stages != 3 && n_stages != 4) || !levels || !rates)
+        return fail(h, DGSWE_ERR_INVALID, "begin_coarse_step: %d stages", n_stages);
+    int finest = 0;
+    for (int64_t k = 0; k < h->K; ++k) finest = std::max(finest, (int)levels[k]);
+    if (finest > kMaxLevels)
+        return fail(h, DGSWE_ERR_INVALID, "begin_coarse_step: level %d above %d", finest,
+                    kMaxLevels);
+    // a stage's rate lies between the element's level and the finest
+    // (MultirateStepper::rates)
+    for (int64_t k = 0; k < h->K; ++k) {
+        for (int s = 0; s < n_stages; ++s)
+            if (rates[s * h->K + k] < levels[k] || rates[s * h->K + k] > finest)
+                return fail(h, DGSWE_ERR_INVALID,
+                            "begin_coarse_step: element %lld's stage %d rate %d (level %d)",
+                            (long long)k, s, rates[s * h->K + k], levels[k]);
+    }
+    CK(cudaSetDevice(h->device));
+    if (int s = prepare(h, kMaxLevels, n_stages)) return s;
+    h->planner->set_plan(levels, rates);
+    return upload_plan(h, n_stages);
+}
+
+int dgswe_stage_where(dgswe_handle* h, const dgswe_multirate_stage* p) {
+    if (!h) return DGSWE_ERR_INVALID;
+    if (!h->planner || h->plan_uploaded != h->planner->version())
+        return fail(h, DGSWE_ERR_INVALID, "stage_where: no coarse step begun");
+    const MultiratePlanner& pl = *h->planner;
+    const int n = h->planner_stages;
+    if (!p || p->stage < 0 || p->stage >= n || p->finest != pl.finest() || p->depth < 0 ||
+        p->depth > p->finest || p->substep < 0 || p->substep >= (1 << p->finest))
+        return fail(h, DGSWE_ERR_INVALID, "stage_where: stage %d, finest %d, depth %d",
+                    p ? p->stage : -1, p ? p->finest : -1, p ? p->depth : -1);
+    for (int id : {p->base, p->input_buffer, p->out})
+        if (id < 0 || id >= DGSWE_N_BUFFERS)
+            return fail(h, DGSWE_ERR_INVALID, "stage_where: buffer %d", id);
+    if (p->last && (p->acc < 0 || p->acc >= DGSWE_N_BUFFERS))
+        return fail(h, DGSWE_ERR_INVALID, "stage_where: accumulation buffer %d", p->acc);
+    if (p->out == p->input_buffer)
+        return fail(h, DGSWE_ERR_INVALID, "stage_where: out must differ from input");
+    CK(cudaSetDevice(h->device));
+    for (int id : {p->base, p->input_buffer, p->out, p->last ? p->acc : p->out})
+        if (int s = ensure_buffer(h, id)) return s;
+    const size_t K = (size_t)h->K, E = h->h_edge_left.size(), B = h->h_bface.size();
+    LtsPass lp;
+    lp.n = pl.count(p->stage, p->depth);
+    lp.list = h->d_order + p->stage * K;
+    lp.edges = h->d_edges + p->stage * E;
+    lp.n_edges = pl.edge_count(p->stage, p->depth);
+    lp.bfaces = h->d_bfaces + p->stage * B;
+    lp.n_bfaces = pl.bface_count(p->stage, p->depth);
+    lp.level = h->d_level;
+    lp.rate = h->d_rate + p->stage * K;
+    lp.t = p->t;
+    lp.dt = p->dt;
+    lp.finest = p->finest;
+    lp.substep = p->substep;
+    lp.depth = p->depth;
+    lp.last = p->last ? 1 : 0;
+    lp.start = p->start;
+    lp.input = p->input;
+    lp.beta = p->beta;
+    lp.c = p->c;
+    if (lp.n > 0) {
+        const DevBuf& in = h->buf[p->input_buffer].view;
+        h->ks->face_listed(h->n1, h->T, h->P, in, h->fb_h, h->fb_hu, h->fb_hv, h->ctl, lp,
+                           h->stream);
+        h->ks->stage_listed(h->n1, h->T, h->P, h->X, in, h->buf[p->base].view,
+                            h->buf[p->out].view, h->buf[p->last ? p->acc : p->out].view, h->fb_h,
+                            h->fb_hu, h->fb_hv, h->ctl, lp.last ? kModeAccumulate : kModePost, lp,
+                            h->stream);
+    }
+    CK(cudaGetLastError());
+    return sync(h);
+}
+
+int dgswe_finish_where(dgswe_handle* h, int32_t acc, int32_t depth) {
+    if (!h) return DGSWE_ERR_INVALID;
+    if (!h->planner || h->plan_uploaded != h->planner->version())
+        return fail(h, DGSWE_ERR_INVALID, "finish_where: no coarse step begun");
+    const MultiratePlanner& pl = *h->planner;
+    if (acc <= DGSWE_STATE || acc >= DGSWE_N_BUFFERS || depth < 0 || depth > pl.finest())
+        return fail(h, DGSWE_ERR_INVALID, "finish_where: buffer %d, depth %d", acc, depth);
+    CK(cudaSetDevice(h->device));
+    if (int s = ensure_buffer(h, acc)) return s;
+    LtsPass fin;
+    fin.list = h->d_order + h->planner_stages * (size_t)h->K;
+    fin.n = pl.count(h->planner_stages, depth);
+    h->ks->finish_listed(h->n1, h->T, h->P, h->buf[acc].view, h->buf[DGSWE_STATE].view, h->ctl,
+                         fin, h->stream);
+    CK(cudaGetLastError());
+    return sync(h);
+}
+
+int dgswe_depth_flags(dgswe_handle* h, int32_t buffer, double d0, double d1, double d2,
+                      uint8_t* flags) {
+    if (!h) return DGSWE_ERR_INVALID;
+    if (buffer < 0 || buffer >= DGSWE_N_BUFFERS || !flags)
+        return fail(h, DGSWE_ERR_INVALID, "depth_flags: buffer %d", buffer);
+    CK(cudaSetDevice(h->device));
+    if (int s = ensure_buffer(h, buffer)) return s;
+    if (int s = prepare(h, h->planner ? h->planner_levels : kMaxLevels,
+                        h->planner ? h->planner_stages : 3))
+        return s;
+    h->ks->depth_flags(h->buf[buffer].view.h, h->K, h->nn, d0, d1, d2, h->d_flags, h->stream);
+    CK(cudaMemcpyAsync(flags, h->d_flags, (size_t)h->K, cudaMemcpyDeviceToHost, h->stream));
+    return sync(h);
+}
+
+}  // extern "C"
+
 extern "C" int dgswe_multirate_stats_get(const dgswe_handle* h, dgswe_multirate_stats* out) {
     if (!h || !out) return DGSWE_ERR_INVALID;
     *out = h->mr_stats;

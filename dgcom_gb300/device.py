@@ -152,6 +152,36 @@ class SWEPhysics2D:
         """state ← acc, post-processed."""
         self._check(self.lib.finish(self.handle, acc), "finish")
 
+    # -- LocalTimeStepping passes (a host-planned multirate coarse step) ----------
+    def begin_coarse_step(self, levels, rates):
+        """LocalTimeStepping::begin_coarse_step: the coarse step's levels
+        [n_elements] and stage rates [n_stages][n_elements]."""
+        lv = np.ascontiguousarray(levels, dtype=np.uint8)
+        rt = np.ascontiguousarray(rates, dtype=np.uint8)
+        if lv.shape != (self.form.mesh.n_elements,) or rt.shape[1:] != lv.shape:
+            raise ValueError("one level per element and one rate per stage and element")
+        u8 = C.POINTER(C.c_uint8)
+        self._check(self.lib.begin_coarse_step(self.handle, rt.shape[0], lv.ctypes.data_as(u8),
+                                               rt.ctypes.data_as(u8)), "begin_coarse_step")
+
+    def multirate_stage(self, plan: abi.MultirateStage):
+        """LocalTimeStepping::stage_where: the stage pass over the elements
+        whose rate of ``plan.stage`` is at least ``plan.depth``."""
+        self._check(self.lib.stage_where(self.handle, C.byref(plan)), "stage_where")
+
+    def multirate_finish(self, acc: int, depth: int):
+        """LocalTimeStepping::finish_where: state ← acc on the elements whose
+        level is at least ``depth``."""
+        self._check(self.lib.finish_where(self.handle, acc, depth), "finish_where")
+
+    def depth_flags(self, d0: float, d1: float, d2: float, buffer: int = abi.STATE) -> np.ndarray:
+        """Per element, bit i set when every node of ``buffer`` is deeper
+        than d_i (the line-local and coarse-step-bound tests)."""
+        out = np.zeros(self.form.mesh.n_elements, dtype=np.uint8)
+        self._check(self.lib.depth_flags(self.handle, buffer, d0, d1, d2,
+                                         out.ctypes.data_as(C.POINTER(C.c_uint8))), "depth_flags")
+        return out
+
     def step(self, t: float, dt: float, scheme: int = abi.SSP_RK3):
         """One fused one-level SSP step of the state."""
         self._check(self.lib.step(self.handle, scheme, t, dt), "step")

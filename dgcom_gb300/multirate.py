@@ -1,7 +1,14 @@
 """The multirate level planner through the C ABI (``dgswe_planner_*`` in
 include/dgswe.h; host only, no device): MultirateStepper's level assignment
 (src/time/multirate.rs:527-752, 993-1157) on a form's mesh. A run with
-local time stepping (``DeviceRun(levels=…)``) plans with the same code."""
+local time stepping (``DeviceRun(levels=…)``) plans with the same code.
+
+``HostStepper`` takes multirate coarse steps with the planning on the host
+and every pass through the LocalTimeStepping entry points
+(``dgswe_begin_coarse_step``, ``dgswe_stage_where``, ``dgswe_finish_where``,
+``dgswe_depth_flags``): the way the reference's own MultirateStepper drives
+its device backend (src/time/multirate.rs:1160-1331, gpu/src/swe2d.rs:4403-4660),
+and the sequence a binding that keeps that stepper follows."""
 
 from __future__ import annotations
 
@@ -100,3 +107,102 @@ class Planner:
 
     def __exit__(self, *exc):
         self.close()
+
+
+LINE_LOCAL_HEADROOM = 1.0         # src/physics/builder.rs:148
+SUBCELL_CAP_DEPTH_FACTOR = 100.0  # src/solver/rhs/swe_2d.rs:2185
+LANDING_SLACK = 1e-9              # src/time/multirate.rs:589
+
+# Shu–Osher weights per stage (start, input, beta, c): SspScheme::stages
+SHU_OSHER = {
+    abi.SSP_RK3: ((1.0, 0.0, 1.0, 0.0), (0.75, 0.25, 0.25, 1.0),
+                  (1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0, 0.5)),
+    abi.SSP_RK43: ((1.0, 0.0, 0.5, 0.0), (0.0, 1.0, 0.5, 0.5),
+                   (2.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0, 1.0), (0.0, 1.0, 0.5, 0.5)),
+}
+
+
+def substep_depth(p: int, finest: int) -> int:
+    """The depth of finest substep p of 2^finest: the coarsest level whose
+    substep starts there (MultirateStepper::schedule)."""
+    if p == 0 or p == 1 << finest:
+        return 0
+    return finest - ((p & -p).bit_length() - 1)
+
+
+class HostStepper:
+    """MultirateStepper::step on a device handle, planned on the host.
+
+    Buffers: the state (0), the stage values 1..n-1, the last stage n and
+    the substep sums n+1, as in a device-driven run."""
+
+    def __init__(self, dev, max_levels: int, scheme: int = abi.SSP_RK3):
+        self.dev = dev
+        self.scheme = scheme
+        self.stages = SHU_OSHER[scheme]
+        self.planner = Planner(dev.form, max_levels, scheme)
+        c_form, _keep = dev.form.to_c()
+        lines = bool(c_form.has_line_local) and dev.form.order >= 1
+        depth = c_form.line_local_depth
+        self.d0 = (np.inf if not lines else
+                   (-np.inf if depth == -np.inf else depth + LINE_LOCAL_HEADROOM))
+        self.lines = lines
+        h_dry = c_form.positivity_h_dry
+        self.bounded = h_dry > 0.0
+        self.d1 = SUBCELL_CAP_DEPTH_FACTOR * h_dry if self.bounded else np.inf
+        self.d2 = h_dry if self.bounded else np.inf
+        self.plans = 0
+
+    def start(self):
+        """The stage values, the last stage's and the sums start as the
+        state (src/time/multirate.rs:1287-1293)."""
+        q = self.dev.download()
+        for b in range(1, len(self.stages) + 2):
+            self.dev.upload(*q, buffer=b)
+
+    def coarse_step_bound(self, element_dt, flags) -> float:
+        """SWEPhysics2D::coarse_step_bound (src/physics/builder.rs:610-632)."""
+        if not self.bounded:
+            return np.inf
+        finite = np.isfinite(element_dt)
+        for bit in (2, 4):
+            sel = finite & ((flags & bit) != 0)
+            longest = float(element_dt[sel].max()) if sel.any() else 0.0
+            if longest > 0.0:
+                return longest
+        return np.inf
+
+    def step(self, t: float, target: float, cfl: float, dt_max: float | None = None):
+        """One coarse step from t toward target: (the new time, the plan)."""
+        dev = self.dev
+        dts = dev.element_dt(cfl, self.scheme)
+        flags = dev.depth_flags(self.d0, self.d1, self.d2)
+        bound = self.coarse_step_bound(dts, flags)
+        cap = min(dt_max, bound) if dt_max else bound
+        if not np.isfinite(cap):
+            cap = 0.0
+        plan = self.planner.assign(dts, (flags & 1) != 0 if self.lines else None, cap,
+                                   target - t)
+        dt = plan.stable_step
+        if dt_max:
+            dt = min(dt, dt_max)
+        dt = min(dt, plan.dt)
+        landed = t + dt * (1.0 + LANDING_SLACK) >= target
+        if landed:
+            dt = target - t
+        dev.begin_coarse_step(plan.levels, plan.rates)
+        n, L = len(self.stages), plan.finest
+        for p in range(1 << L):
+            d = substep_depth(p, L)
+            for s, (start, inp, beta, c) in enumerate(self.stages):
+                last = s + 1 == n
+                dev.multirate_stage(abi.MultirateStage(
+                    t, dt, L, p, d, s, int(last), start, inp, beta, c,
+                    abi.STATE, abi.STATE if s == 0 else s, s + 1 if not last else n,
+                    n + 1 if last else 0))
+            dev.multirate_finish(n + 1, substep_depth(p + 1, L))
+        self.plans += 1
+        return (target if landed else t + dt), plan
+
+    def close(self):
+        self.planner.close()

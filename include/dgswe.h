@@ -422,6 +422,40 @@ int64_t dgswe_negative_depth_clips(const dgswe_handle* handle);
  * finest substep's stage passes over prefixes of level-sorted element and
  * face lists). One level is the global scheme, bit for bit. */
 
+/* The LocalTimeStepping passes, for a host that runs its own multirate
+ * stepper (the reference's Simulation with Multirate drives its device
+ * backend this way, gpu/src/swe2d.rs:4403-4660):
+ *   begin_coarse_step  LocalTimeStepping::begin_coarse_step: the coarse
+ *                      step's levels [n_elements] and every stage's rates
+ *                      [n_stages][n_elements], each between its element's
+ *                      level and the finest level; the library orders the
+ *                      passes' elements and faces by them;
+ *   stage_where        LocalTimeStepping::stage_where with its StagePlan
+ *                      (src/time/multirate.rs:207-260): the elements whose
+ *                      rate of `stage` is at least `depth`, each with its
+ *                      element_stage;
+ *   finish_where       LocalTimeStepping::finish_where: state ← acc and the
+ *                      post-processing on the elements whose level is at
+ *                      least `depth`;
+ *   depth_flags        per element, whether every node of `buffer` is
+ *                      deeper than d0, d1, d2 (bits 0, 1, 2): line_local's
+ *                      and coarse_step_bound's tests. */
+typedef struct dgswe_multirate_stage {
+    double t, dt;                    /* the coarse step (StagePlan::step) */
+    int32_t finest, substep, depth;  /* 2^finest finest substeps; this one and its depth */
+    int32_t stage, last;             /* the stage (0-based); whether it is the scheme's last */
+    double start, input, beta, c;    /* its Shu–Osher weights (ShuOsherStage) */
+    int32_t base, input_buffer, out, acc; /* buffer ids: the substep start, the RHS argument,
+                                             the stage value, the substep sum (last stage) */
+} dgswe_multirate_stage;
+
+int dgswe_begin_coarse_step(dgswe_handle* handle, int32_t n_stages, const uint8_t* levels,
+                            const uint8_t* rates);
+int dgswe_stage_where(dgswe_handle* handle, const dgswe_multirate_stage* plan);
+int dgswe_finish_where(dgswe_handle* handle, int32_t acc, int32_t depth);
+int dgswe_depth_flags(dgswe_handle* handle, int32_t buffer, double d0, double d1, double d2,
+                      uint8_t* flags);
+
 /* MultirateStats (src/time/multirate.rs:785-860) of the handle's last run */
 typedef struct dgswe_multirate_stats {
     int64_t steps;                /* coarse steps */

@@ -218,3 +218,20 @@ def test_plan_invariants_on_a_jittered_mesh(cuda_lib, seed):
         values = plan.levels if key == 3 else plan.rates[key]
         ordered = values[plan.order[key]]
         assert np.all(np.diff(ordered.astype(int)) <= 0)
+
+
+def test_substep_depths_are_the_schedule():
+    """The passes of a coarse step of finest level L: substep p's stages
+    run on the elements rated at least depth(p), and the substeps of the
+    elements of level at least depth(p + 1) end after it
+    (MultirateStepper::schedule, src/time/multirate.rs:1160-1210)."""
+    from dgcom_gb300.multirate import substep_depth
+
+    assert [substep_depth(p, 0) for p in range(2)] == [0, 0]
+    assert [substep_depth(p, 2) for p in range(5)] == [0, 2, 1, 2, 0]
+    assert [substep_depth(p, 3) for p in range(9)] == [0, 3, 2, 3, 1, 3, 2, 3, 0]
+    # an element of level l starts a substep every 2^(L-l) finest substeps
+    L = 4
+    for level in range(L + 1):
+        starts = [p for p in range(1 << L) if substep_depth(p, L) <= level]
+        assert starts == list(range(0, 1 << L, 1 << (L - level)))
