@@ -17,8 +17,16 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-# BoundaryTag (src/mesh/data/boundary_tags.rs:8-34) as the ABI's face tags
-TAG_WALL, TAG_OPEN, TAG_TIDAL, TAG_RIVER = 0, 1, 2, 4
+# BoundaryTag (src/mesh/data/boundary_tags.rs:8-34) as the ABI's face tags:
+# the variants in declaration order (Periodic, 3, is a face pairing here,
+# not a tag), and Custom(n) as CUSTOM_TAG_BASE + n
+TAG_WALL, TAG_OPEN, TAG_TIDAL, TAG_RIVER, TAG_DIRICHLET, TAG_NEUMANN = 0, 1, 2, 4, 5, 6
+CUSTOM_TAG_BASE = 1000
+
+
+def custom_tag(n: int) -> int:
+    """The face tag of BoundaryTag::Custom(n)."""
+    return CUSTOM_TAG_BASE + int(n)
 
 
 @dataclass
@@ -175,12 +183,18 @@ def hilbert_index(x: np.ndarray, y: np.ndarray, bits: int) -> np.ndarray:
 
 def in_hilbert_order(mesh: QuadMesh) -> tuple[QuadMesh, np.ndarray]:
     """The mesh with its elements along a Hilbert curve through their
-    centroids (Mesh2D::in_hilbert_order, src/mesh/core/mesh2d.rs:711-760),
-    and for each new element its old index. Periodic pairs are renumbered."""
-    c = mesh.corners().mean(axis=1)
+    centroids and its vertices numbered by first use in that order
+    (Mesh2D::in_hilbert_order and select_elements,
+    src/mesh/core/mesh2d.rs:711-790), and for each new element its old
+    index. One scale for both directions (square cells of a 2^16 grid over
+    the centroids' larger extent); equal keys keep the old order. Periodic
+    pairs are renumbered."""
+    p = mesh.corners()
+    c = 0.25 * (((p[:, 0] + p[:, 1]) + p[:, 2]) + p[:, 3])
     lo, hi = c.min(axis=0), c.max(axis=0)
-    span = np.where(hi > lo, hi - lo, 1.0)
-    cells = np.minimum(((c - lo) / span * 65535.0).astype(np.int64), 65535)
+    extent = float((hi - lo).max()) if c.size else 0.0
+    scale = 65535.0 / extent if extent > 0.0 else 0.0
+    cells = ((c - lo) * scale).astype(np.int64)  # truncation toward zero, as `as u32`
     order = np.argsort(hilbert_index(cells[:, 0], cells[:, 1], 16), kind="stable")
     new_of_old = np.empty_like(order)
     new_of_old[order] = np.arange(order.size)
@@ -189,7 +203,12 @@ def in_hilbert_order(mesh: QuadMesh) -> tuple[QuadMesh, np.ndarray]:
         periodic[:, 0] = new_of_old[periodic[:, 0]]
         periodic[:, 2] = new_of_old[periodic[:, 2]]
     tags = None if mesh.face_tags is None else mesh.face_tags[order]
-    return QuadMesh(mesh.vertices, mesh.elements[order], periodic, tags), order
+    elements = mesh.elements[order]
+    used, first = np.unique(elements.reshape(-1), return_index=True)
+    by_use = used[np.argsort(first, kind="stable")]
+    new_vertex = np.full(mesh.vertices.shape[0], -1, np.int64)
+    new_vertex[by_use] = np.arange(by_use.size)
+    return (QuadMesh(mesh.vertices[by_use], new_vertex[elements], periodic, tags), order)
 
 
 def graded_jittered_box(lx: float, ly: float, nx: int, ny: int, size_range=(100.0, 400.0),

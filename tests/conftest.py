@@ -19,3 +19,20 @@ def cuda_lib():
 
     _build.build()
     return abi.cuda_library()
+
+
+@pytest.fixture(scope="session")
+def reference_data():
+    """A data file of the reference repository (read-only, CPU tests only),
+    or a skip where the repository is not present."""
+    import os
+
+    root = Path(os.environ.get("DGCOM_REFERENCE", "/root/reference"))
+
+    def get(relative: str) -> Path:
+        path = root / relative
+        if not path.is_file():
+            pytest.skip(f"reference data {relative} not present")
+        return path
+
+    return get
