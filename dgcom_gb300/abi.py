@@ -13,7 +13,7 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 LIBRARY_PATH = HERE / "libdgswe.so"
 
-ABI_VERSION = 2
+ABI_VERSION = 3
 
 # dgswe_status
 OK, ERR_INVALID, ERR_CUDA, ERR_NONFINITE, ERR_DT_MIN, ERR_MAX_STEPS, ERR_STOPPED, \
@@ -26,6 +26,8 @@ BC_WALL, BC_CHARACTERISTIC, BC_NODE_TIDES, BC_PARENT = range(4)
 AT_REST, INCOMING_WAVE = range(2)
 # dgswe_friction
 FRICTION_NONE, FRICTION_MANNING, FRICTION_MANNING_NODES = range(3)
+# dgswe_drag
+DRAG_CONSTANT, DRAG_LARGE_POND, DRAG_WU, DRAG_SMITH, DRAG_YELLAND_TAYLOR = range(5)
 # dgswe_scheme
 SSP_RK3, SSP_RK43 = range(2)
 # dgswe_numerics
@@ -96,6 +98,25 @@ class Relaxation(C.Structure):
     ]
 
 
+class Atmosphere(C.Structure):
+    _fields_ = [
+        ("n_times", C.c_int64),
+        ("times", _dp),
+        ("epoch_unix", C.c_double),
+        ("values", C.POINTER(C.c_float)),
+        ("source", C.c_int32),
+        ("wind", C.c_int32),
+        ("pressure", C.c_int32),
+        ("level", C.c_int32),
+        ("drag", C.c_int32),
+        ("drag_cd", C.c_double),
+        ("rho_air", C.c_double),
+        ("rho_water", C.c_double),
+        ("h_min", C.c_double),
+        ("ramp_duration", C.c_double),
+    ]
+
+
 class Boundary(C.Structure):
     _fields_ = [
         ("tag", C.c_int32),
@@ -108,6 +129,8 @@ class Boundary(C.Structure):
         ("ramp_duration", C.c_double),
         ("node_tides", C.POINTER(NodeTides)),
         ("parent", C.POINTER(ParentSeries)),
+        ("raise_", C.c_int32),
+        ("raise_factor", C.c_double),
     ]
 
 
@@ -148,6 +171,7 @@ class Form(C.Structure):
         ("has_line_local", C.c_int32),
         ("line_local_depth", C.c_double),
         ("relaxation", C.POINTER(Relaxation)),
+        ("atmosphere", C.POINTER(Atmosphere)),
     ]
 
 

@@ -481,6 +481,47 @@ def synthetic_nesting(form: SWEDeviceForm2D, tag: int = TAG_OPEN, band_width: fl
                                   momentum_only=momentum_only)
 
 
+def synthetic_atmosphere(form: SWEDeviceForm2D, t0: float = 0.0, t1: float = 43_200.0,
+                         dt_snap: float = 3600.0, epoch_unix: float = 1_750_000_000.0,
+                         seed: int = 2033, depth_hpa: float = 25.0, radius: float | None = None,
+                         max_wind: float = 22.0, background: tuple = (4.0, -2.0), **kw):
+    """A GriddedAtmosphere of a synthetic storm over ``form``'s mesh,
+    regridded onto its nodes as the reference's device holds one: a
+    Gaussian low p − p_ref = −Δp·exp(−r²/R²) (its exact gradient), a
+    cyclonic wind v_t = V·(r/R)·exp((1 − r²/R²)/2) around it plus a uniform
+    background wind, the centre crossing the mesh's box diagonally between
+    t0 and t1, snapshots every ``dt_snap`` (float32, Unix times from
+    ``epoch_unix``). ``kw`` sets the GriddedAtmosphere's other fields."""
+    from .physics import GriddedAtmosphere
+
+    rng = np.random.default_rng(seed)
+    x, y = form.positions()
+    x, y = x.reshape(-1), y.reshape(-1)
+    x0, x1, y0, y1 = x.min(), x.max(), y.min(), y.max()
+    span = max(x1 - x0, y1 - y0, 1.0)
+    R = radius if radius is not None else 0.35 * span
+    times = np.arange(t0, t1 + 0.5 * dt_snap, dt_snap)
+    frac = (times - t0) / max(t1 - t0, 1.0)
+    jitter = rng.uniform(-0.1, 0.1, 2) * span
+    cx = x0 - 0.2 * span + 1.4 * (x1 - x0 + 0.2 * span) * frac + jitter[0]
+    cy = y0 + 0.3 * (y1 - y0) + 0.4 * (y1 - y0) * frac + jitter[1]
+    dp = depth_hpa * 100.0
+    values = np.empty((len(times), x.size, 5), dtype=np.float32)
+    for n, (xc, yc) in enumerate(zip(cx, cy)):
+        dx, dy = x - xc, y - yc
+        r2 = (dx * dx + dy * dy) / (R * R)
+        e = np.exp(-r2)
+        p = -dp * e
+        px, py = 2.0 * dp * e * dx / (R * R), 2.0 * dp * e * dy / (R * R)
+        r = np.sqrt(dx * dx + dy * dy)
+        vt = max_wind * np.sqrt(r2) * np.exp(0.5 * (1.0 - r2))
+        inv = np.where(r > 0, 1.0 / np.maximum(r, 1e-12), 0.0)
+        u = background[0] - vt * dy * inv
+        v = background[1] + vt * dx * inv
+        values[n] = np.stack([u, v, px, py, p], axis=-1)
+    return GriddedAtmosphere(times=times + epoch_unix, values=values, epoch_unix=epoch_unix, **kw)
+
+
 # -- the reference's split-form test setups ------------------------------------
 
 L_TEST = 20_000.0

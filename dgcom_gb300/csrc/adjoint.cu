@@ -466,6 +466,8 @@ int check_config(dgswe_adjoint* a, const dgswe_form* forms, int n, const dgswe_a
             return afail(a, DGSWE_ERR_UNSUPPORTED, "an adjoint ensemble has members of one order");
         if (forms[m].relaxation)
             return afail(a, DGSWE_ERR_UNSUPPORTED, "the adjoint covers no relaxation band");
+        if (forms[m].atmosphere)
+            return afail(a, DGSWE_ERR_UNSUPPORTED, "the adjoint covers no weather forcing");
         for (int b = 0; b < forms[m].n_boundaries; ++b)
             if (forms[m].boundaries[b].kind == DGSWE_BC_NODE_TIDES ||
                 forms[m].boundaries[b].kind == DGSWE_BC_PARENT)

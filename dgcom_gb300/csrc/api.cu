@@ -410,6 +410,51 @@ int relaxation_tables(dgswe_handle* h, const dgswe_form& f) {
     return DGSWE_OK;
 }
 
+// The weather: its snapshots regridded onto the nodes, in SoA per time
+// ([time][5][K·nn]) so that a warp's nodes read each field contiguously,
+// and the per-node source buffer it writes (shared with the relaxation
+// band's)
+int atmosphere_tables(dgswe_handle* h, const dgswe_form& f) {
+    if (!f.atmosphere) return DGSWE_OK;
+    const dgswe_atmosphere& a = *f.atmosphere;
+    DevTables& T = h->T;
+    const int64_t n = h->n_values;
+    std::vector<float> values((size_t)a.n_times * 5 * n);
+    for (int64_t t = 0; t < a.n_times; ++t)
+        for (int64_t g = 0; g < n; ++g)
+            for (int q = 0; q < 5; ++q)
+                values[((size_t)t * 5 + q) * n + g] = a.values[((size_t)t * n + g) * 5 + q];
+    std::vector<double> times(a.times, a.times + a.n_times);
+    int s = DGSWE_OK;
+    if ((s = upload_vec(h, times, &T.at_times))) return s;
+    if ((s = upload_vec(h, values, &T.at_values))) return s;
+    T.at_n_times = (int)a.n_times;
+    T.at_source = a.source ? 1 : 0;
+    T.at_wind = a.wind ? 1 : 0;
+    T.at_pressure = a.pressure ? 1 : 0;
+    T.at_level = a.level ? 1 : 0;
+    T.at_drag = a.drag;
+    T.at_cd = a.drag_cd;
+    T.at_rho_air = a.rho_air;
+    T.at_rho_water = a.rho_water;
+    T.at_h_min = a.h_min;
+    T.at_ramp = a.ramp_duration;
+    T.at_epoch = a.epoch_unix;
+    // the runs' times must lie within the snapshots' (the reference panics
+    // outside them)
+    if (a.n_times > 1)
+        h->parent_range = {std::max(h->parent_range.first, a.times[0] - a.epoch_unix),
+                           std::min(h->parent_range.second, a.times[a.n_times - 1] - a.epoch_unix)};
+    if (T.at_source && !T.rx_src) {
+        void* p = nullptr;
+        CK(cudaMalloc(&p, 3 * (size_t)n * sizeof(double)));
+        h->allocations.push_back(p);
+        CK(cudaMemset(p, 0, 3 * (size_t)n * sizeof(double)));
+        T.rx_src = (double*)p;
+    }
+    return DGSWE_OK;
+}
+
 int create_impl(dgswe_handle* h, const dgswe_form* f, int device) {
     auto bail = [](int s) { return s; };
     h->device = device;
@@ -503,6 +548,7 @@ int create_impl(dgswe_handle* h, const dgswe_form* f, int device) {
     for (int b = 0; b < f->n_boundaries; ++b) h->P.cond[b] = make_condition(f->boundaries[b]);
     if ((s = boundary_node_tables(h, *f, ops, topo, t))) return bail(s);
     if ((s = relaxation_tables(h, *f))) return bail(s);
+    if ((s = atmosphere_tables(h, *f))) return bail(s);
 
     // buffers, faces, control
     if ((s = ensure_buffer(h, DGSWE_STATE))) return bail(s);
@@ -534,6 +580,7 @@ int create_impl(dgswe_handle* h, const dgswe_form* f, int device) {
     h->form.manning_n_nodes = nullptr;
     h->form.boundaries = nullptr;
     h->form.relaxation = nullptr;
+    h->form.atmosphere = nullptr;
     return DGSWE_OK;
 }
 
@@ -613,7 +660,7 @@ int dgswe_compute_rhs(dgswe_handle* h, int32_t input, double time, double* out_h
         return fail(h, DGSWE_ERR_INVALID, "compute_rhs: buffer %d, %lld values", input,
                     (long long)n);
     if (!(time >= h->parent_range.first && time <= h->parent_range.second))
-        return fail(h, DGSWE_ERR_INVALID, "compute_rhs: t = %g leaves the parent's snapshots", time);
+        return fail(h, DGSWE_ERR_INVALID, "compute_rhs: t = %g leaves the forcing's snapshots", time);
     CK(cudaSetDevice(h->device));
     if (int s = ensure_buffer(h, input)) return s;
     if (int s = ensure_buffer(h, kRhsBuffer)) return s;
@@ -636,7 +683,7 @@ int dgswe_stage(dgswe_handle* h, const dgswe_stage_plan* plan) {
     if (plan->out == plan->input)
         return fail(h, DGSWE_ERR_INVALID, "stage: out must differ from input");
     if (!(plan->time >= h->parent_range.first && plan->time <= h->parent_range.second))
-        return fail(h, DGSWE_ERR_INVALID, "stage: t = %g leaves the parent's snapshots",
+        return fail(h, DGSWE_ERR_INVALID, "stage: t = %g leaves the forcing's snapshots",
                     plan->time);
     CK(cudaSetDevice(h->device));
     for (int id : {plan->base, plan->input, plan->out})
@@ -696,7 +743,7 @@ int dgswe_step(dgswe_handle* h, int32_t scheme, double t, double dt) {
     if (scheme != DGSWE_SSP_RK3 && scheme != DGSWE_SSP_RK43)
         return fail(h, DGSWE_ERR_INVALID, "step: scheme %d", scheme);
     if (!(t >= h->parent_range.first && t + dt <= h->parent_range.second))
-        return fail(h, DGSWE_ERR_INVALID, "step: (%g, %g) leaves the parent's snapshots", t, t + dt);
+        return fail(h, DGSWE_ERR_INVALID, "step: (%g, %g) leaves the forcing's snapshots", t, t + dt);
     CK(cudaSetDevice(h->device));
     double st[4][4];
     const int n = scheme_table(scheme, st);
@@ -729,7 +776,7 @@ int dgswe_run(dgswe_handle* h, const dgswe_run_config* run, dgswe_callback callb
                     run->levels, DGSWE_MAX_LEVELS);
     if (!(run->t_start >= h->parent_range.first && run->t_end <= h->parent_range.second))
         return fail(h, DGSWE_ERR_INVALID,
-                    "run: the span (%g, %g) leaves the parent's snapshots (%g, %g)", run->t_start,
+                    "run: the span (%g, %g) leaves the forcing's snapshots (%g, %g)", run->t_start,
                     run->t_end, h->parent_range.first, h->parent_range.second);
     if (run->levels > 0) return run_multirate(h, run, callback, user, report);
     std::memset(report, 0, sizeof(*report));

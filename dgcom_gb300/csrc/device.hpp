@@ -66,6 +66,15 @@ struct DevTables {
     int rx_n_times = 0, rx_cubic = 0, rx_velocity = 0, rx_momentum_only = 0;
     double rx_ref_level = 0.0, rx_max_ratio = 0.0, rx_ramp = 0.0, rx_rate = 0.0, rx_wet = 0.0;
     double* rx_src = nullptr;
+    // the weather (GriddedAtmosphere2D): its snapshot times (Unix s) and
+    // values ([time][5][K·nn] f32: u, v, ∂p/∂x, ∂p/∂y, p − p_ref), the Unix
+    // time of simulation time 0 and the options. With at_source its momentum
+    // source goes into rx_src, which the band's kernel then adds to.
+    int at_n_times = 0, at_source = 0, at_wind = 0, at_pressure = 0, at_level = 0, at_drag = 0;
+    const double* at_times = nullptr;
+    const float* at_values = nullptr;
+    double at_epoch = 0.0, at_cd = 0.0, at_rho_air = 0.0, at_rho_water = 0.0, at_h_min = 0.0;
+    double at_ramp = 0.0;
 };
 
 struct Constituent {
@@ -92,6 +101,10 @@ struct Condition {
     int pt_n_times, pt_cubic;
     int64_t pt_time0, pt_val0;
     double pt_reference_level;
+    // InverseBarometer: the external η raised by raise_factor times the
+    // weather's level at the face node (characteristic kinds)
+    int raise;
+    double raise_factor;
 };
 
 struct Physics {

@@ -246,6 +246,9 @@ int create_impl(dgswe_ensemble* h, const dgswe_form* forms, int n, int device) {
         if (forms[m].relaxation)
             return fail(h, DGSWE_ERR_UNSUPPORTED,
                         "member %d: a nesting relaxation band runs on a single mesh", m);
+        if (forms[m].atmosphere)
+            return fail(h, DGSWE_ERR_UNSUPPORTED, "member %d: the weather runs on a single mesh",
+                        m);
         cond_base[m] = (int)conds.size();
         for (int b = 0; b < forms[m].n_boundaries; ++b) {
             if (forms[m].boundaries[b].kind == DGSWE_BC_NODE_TIDES ||

@@ -81,6 +81,19 @@ inline int check_form(const dgswe_form* f, std::string& why) {
             if (!(p->times[i] > p->times[i - 1]))
                 return why = "parent snapshot times must increase", DGSWE_ERR_INVALID;
     }
+    if (f->atmosphere) {
+        const dgswe_atmosphere& a = *f->atmosphere;
+        if (a.n_times <= 0 || !a.times || !a.values)
+            return why = "an atmosphere without its snapshots", DGSWE_ERR_INVALID;
+        if (a.n_times >= (1ll << 31)) return why = "too many weather snapshots", DGSWE_ERR_INVALID;
+        for (int64_t i = 1; i < a.n_times; ++i)
+            if (!(a.times[i] > a.times[i - 1]))
+                return why = "weather snapshot times must increase", DGSWE_ERR_INVALID;
+        if (a.drag < DGSWE_DRAG_CONSTANT || a.drag > DGSWE_DRAG_YELLAND_TAYLOR)
+            return why = "unknown drag coefficient", DGSWE_ERR_UNSUPPORTED;
+        if (!(a.rho_water > 0.0) || !(a.rho_air >= 0.0) || !std::isfinite(a.epoch_unix))
+            return why = "the atmosphere's densities and epoch", DGSWE_ERR_INVALID;
+    }
     if (f->n_boundaries < 0 || f->n_boundaries > kMaxConditions ||
         (f->n_boundaries > 0 && !f->boundaries))
         return why = "boundary conditions", DGSWE_ERR_INVALID;
@@ -89,6 +102,12 @@ inline int check_form(const dgswe_form* f, std::string& why) {
         if (c.kind != DGSWE_BC_WALL && c.kind != DGSWE_BC_CHARACTERISTIC &&
             c.kind != DGSWE_BC_NODE_TIDES && c.kind != DGSWE_BC_PARENT)
             return why = "a boundary condition without a device form", DGSWE_ERR_UNSUPPORTED;
+        if (c.raise && c.kind == DGSWE_BC_WALL)
+            return why = "a wall raised by the inverse barometer", DGSWE_ERR_INVALID;
+        if (c.raise && !f->atmosphere)
+            return why = "an inverse-barometer raise without an atmosphere", DGSWE_ERR_INVALID;
+        if (c.raise && !std::isfinite(c.raise_factor))
+            return why = "the raise factor", DGSWE_ERR_INVALID;
         if (c.kind == DGSWE_BC_PARENT) {
             const dgswe_parent_series* p = c.parent;
             if (!p || p->n_slots <= 0 || p->n_times <= 0 || !p->positions || !p->times ||
@@ -137,6 +156,8 @@ inline Condition make_condition(const dgswe_boundary& in) {
     c.wall_h_min = in.wall_h_min;
     c.mean = in.mean_elevation;
     c.ramp = in.ramp_duration;
+    c.raise = in.kind != DGSWE_BC_WALL && in.raise ? 1 : 0;
+    c.raise_factor = c.raise ? in.raise_factor : 0.0;
     if (in.kind == DGSWE_BC_NODE_TIDES) {
         // the tables' offsets are the handle's (nt_omega0, nt_slot0, nt_coef0)
         const dgswe_node_tides& t = *in.node_tides;

@@ -148,9 +148,63 @@ __global__ void __launch_bounds__(256) relax_kernel(DevTables T, Physics P, DevB
             shv = gamma * (depth * v - hv);
         }
     }
-    T.rx_src[g] = sh;
-    T.rx_src[nv + g] = shu;
-    T.rx_src[2 * nv + g] = shv;
+    if (T.at_source) {  // added to the weather's source of this pass
+        T.rx_src[g] += sh;
+        T.rx_src[nv + g] += shu;
+        T.rx_src[2 * nv + g] += shv;
+    } else {
+        T.rx_src[g] = sh;
+        T.rx_src[nv + g] = shu;
+        T.rx_src[2 * nv + g] = shv;
+    }
+}
+
+// The weather's momentum source at the stage's input
+// (GriddedAtmosphere2D::add_element, src/source/swe_2d/gridded_atmosphere.rs:698-729),
+// per node of every element (LISTED: of the pass's elements) at its
+// element's stage time, into T.rx_src; the relaxation band's kernel,
+// launched after it, adds the band's
+template <bool LISTED>
+__global__ void __launch_bounds__(256) atmos_kernel(DevTables T, Physics P, DevBuf in,
+                                                    const StepCtl* ctl, int slot, LtsPass lp) {
+    const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (item >= (LISTED ? lp.n : T.K) * P.nn) return;
+    const int64_t e = item / P.nn;
+    const int64_t k = LISTED ? (int64_t)lp.list[e] : e;
+    const int64_t g = k * P.nn + item % P.nn;
+    const int64_t nv = T.K * P.nn;
+    double su = 0.0, sv = 0.0;
+    const double h = in.h[g];
+    if (!fp::lt(h, T.at_h_min)) {
+        const double t = LISTED ? lts_stage(lp, k).time : ctl[0].stage[slot].time;
+        int idx[2];
+        double w[2];
+        const int len = weather_weights(T.at_times, T.at_n_times, T.at_epoch + t, idx, w);
+        const double ramp = tidal_ramp(t, T.at_ramp);
+        const double rw = T.at_wind ? ramp : 0.0, rp = T.at_pressure ? ramp : 0.0;
+        const double u = weather_field(T.at_values, nv, 0, g, idx, w, len);
+        const double v = weather_field(T.at_values, nv, 1, g, idx, w, len);
+        const double px = weather_field(T.at_values, nv, 2, g, idx, w, len);
+        const double py = weather_field(T.at_values, nv, 3, g, idx, w, len);
+        atmosphere_source(h, rw * u, rw * v, rp * px, rp * py, T.at_drag, T.at_cd, T.at_rho_air,
+                          T.at_rho_water, T.at_h_min, su, sv);
+    }
+    if (T.rx_n > 0) T.rx_src[g] = 0.0;
+    T.rx_src[nv + g] = su;
+    T.rx_src[2 * nv + g] = sv;
+}
+
+// The weather's inverse-barometer level at flat node g and simulation time
+// t (GriddedAtmosphere2D's BoundaryLevel by node index,
+// gridded_atmosphere.rs:873-895), 0 unless the level is the pressure's
+__device__ __forceinline__ double weather_level(const DevTables& T, const Physics& P, int64_t g,
+                                                double t) {
+    if (!T.at_level) return 0.0;
+    int idx[2];
+    double w[2];
+    const int len = weather_weights(T.at_times, T.at_n_times, T.at_epoch + t, idx, w);
+    const double p = weather_field(T.at_values, T.K * P.nn, 4, g, idx, w, len);
+    return inverse_barometer_level(p, tidal_ramp(t, T.at_ramp), T.at_rho_water);
 }
 
 // LISTED: a multirate pass's faces (lp's edge and boundary-face lists),
@@ -236,6 +290,7 @@ __global__ void __launch_bounds__(256) face_kernel(DevTables T, Physics P, DevBu
                                 T.pt_values + c.pt_val0 + (s - c.nt_slot0) * c.pt_n_times * 3, t,
                                 c.ramp, c.pt_reference_level, c.nt_velocity, c.nt_max_ratio,
                                 T.nt_depth[s], qi.b, eta, ue, ve, has_uv);
+            if (c.raise) eta += c.raise_factor * weather_level(T, P, k * NN + node, t);
             const double h_e = fmax(eta - qi.b, 0.0);
             double un_e = 0.0, ut_e;
             if (has_uv) {
@@ -248,8 +303,9 @@ __global__ void __launch_bounds__(256) face_kernel(DevTables T, Physics P, DevBu
             }
             qb = characteristic_state_ext(qi, h_e, un_e, ut_e, nx, ny, g, h_min);
         } else {
-            qb = characteristic_state(qi, u, v, tide_elevation(c, t), nx, ny, c.elevation_only, g,
-                                      h_min);
+            double eta = tide_elevation(c, t);
+            if (c.raise) eta += c.raise_factor * weather_level(T, P, k * NN + node, t);
+            qb = characteristic_state(qi, u, v, eta, nx, ny, c.elevation_only, g, h_min);
         }
         fs = wflux(qb, qb, nx, ny, g);
     }

@@ -8,10 +8,17 @@
 namespace dgswe {
 namespace DGSWE_NS {
 
-// The relaxation band's source of a stage, before its stage kernel reads it
+// The node sources of a stage, before its stage kernel reads them: the
+// weather's, then the relaxation band's
 template <bool LISTED>
 static void relax(const DevTables& T, const Physics& P, const DevBuf& in, const StepCtl* ctl,
                   int slot, const LtsPass& lp, cudaStream_t s) {
+    if (T.at_source && T.rx_src) {
+        const int64_t n = (LISTED ? lp.n : T.K) * P.nn;
+        if (n > 0)
+            atmos_kernel<LISTED><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(T, P, in, ctl, slot,
+                                                                            lp);
+    }
     if (T.rx_n == 0 || !T.rx_src) return;
     relax_kernel<LISTED><<<(unsigned)((T.rx_n + 255) / 256), 256, 0, s>>>(T, P, in, ctl, slot, lp);
 }

@@ -618,5 +618,130 @@ DG_PT void node_tide_state(const double* omega, const double* f_rate, const doub
     }
 }
 
+// ---------------------------------------------------------------------------
+// the weather (GriddedAtmosphere2D, src/source/swe_2d/gridded_atmosphere.rs)
+
+// The linear TimeStencil (src/io/field_series.rs:41-81,
+// TimeInterpolation::Linear) of the weather's snapshot times at Unix time
+// tu: one snapshot at a snapshot's own time, else the bracketing two with
+// their Lagrange weights. A time outside the snapshots takes the nearest
+// end (the host refuses runs there, where the reference panics).
+DG_PT int weather_weights(const double* times, int n, double tu, int idx[2], double w[2]) {
+    idx[0] = 0;
+    idx[1] = 0;
+    w[0] = 1.0;
+    w[1] = 0.0;
+    if (n <= 1) return 1;
+    if (!fp::ge(tu, times[0])) return 1;
+    if (!fp::le(tu, times[n - 1])) {
+        idx[0] = n - 1;
+        return 1;
+    }
+    // the first index whose time is ≥ tu, within [1, n − 1]
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) / 2;
+        if (fp::lt(times[mid], tu)) lo = mid + 1;
+        else hi = mid;
+    }
+    const int i1 = lo < 1 ? 1 : (lo > n - 1 ? n - 1 : lo);
+    const int i0 = i1 - 1;
+    if (tu == times[i0]) {
+        idx[0] = i0;
+        return 1;
+    }
+    if (tu == times[i1]) {
+        idx[0] = i1;
+        return 1;
+    }
+    idx[0] = i0;
+    idx[1] = i1;
+    w[0] = (tu - times[i1]) / (times[i0] - times[i1]);
+    w[1] = (tu - times[i0]) / (times[i1] - times[i0]);
+    return 2;
+}
+
+// One field of the weather at flat node g, its snapshots summed in turn
+// from zero (add_snapshot); values are [time][5][n_values] f32
+DG_PT double weather_field(const float* values, int64_t n_values, int q, int64_t g,
+                           const int idx[2], const double w[2], int len) {
+    double s = 0.0;
+    for (int j = 0; j < len; ++j)
+        s += w[j] * (double)values[((int64_t)idx[j] * 5 + q) * n_values + g];
+    return s;
+}
+
+// crate::math::hypot (src/math.rs:202-245, musl's): √(x² + y²) from the
+// squares split in two parts each (Dekker), so that the sum is exact enough
+// for the square root; scaled by 2^±700 away from overflow and underflow
+DG_PT double ref_hypot(double x, double y) {
+    int64_t ux = fp::bits(x) & INT64_MAX, uy = fp::bits(y) & INT64_MAX;
+    if (ux < uy) {
+        const int64_t t = ux;
+        ux = uy;
+        uy = t;
+    }
+    const int64_t ex = ux >> 52, ey = uy >> 52;
+    x = fp::from_bits(ux);
+    y = fp::from_bits(uy);
+    if (ey == 0x7ff) return y;
+    if (ex == 0x7ff || uy == 0) return x;
+    if (ex - ey > 64) return x + y;
+    double z = 1.0;
+    const double up = fp::from_bits(0x6bb0000000000000ll), down = fp::from_bits(0x1430000000000000ll);
+    if (ex > 0x3ff + 510) {
+        z = up;
+        x *= down;
+        y *= down;
+    } else if (ey < 0x3ff - 450) {
+        z = down;
+        x *= up;
+        y *= up;
+    }
+    const double split = 134217728.0 + 1.0;
+    const double xc = x * split, yc = y * split;
+    const double xh = x - xc + xc, yh = y - yc + yc;
+    const double xl = x - xh, yl = y - yh;
+    const double hx = x * x, hy = y * y;
+    const double lx = xh * xh - hx + 2.0 * xh * xl + xl * xl;
+    const double ly = yh * yh - hy + 2.0 * yh * yl + yl * yl;
+    return z * sqrt(ly + lx + hy + hx);
+}
+
+// DragCoefficient::compute (src/source/swe_2d/wind.rs:134-158) by its
+// device code
+DG_PT double drag_coefficient(int kind, double cd, double speed) {
+    switch (kind) {
+        case 0: return cd;
+        case 1:
+            return fp::le(speed, 11.0) ? 1.2e-3
+                                       : (0.49 + 0.065 * (fp::lt(25.0, speed) ? 25.0 : speed)) * 1e-3;
+        case 2: return (0.8 + 0.065 * speed) * 1e-3;
+        case 3: return (0.61 + 0.063 * speed) * 1e-3;
+        default: return fp::le(speed, 6.0) ? 1.1e-3 : (0.50 + 0.071 * speed) * 1e-3;
+    }
+}
+
+// atmosphere_source (gridded_atmosphere.rs:161-196): (τ − h∇p)/ρ_water with
+// τ = ρ_air C_d(|U|) |U| U from the ramped wind (u, v) and pressure gradient
+// (px, py); nothing below h_min
+DG_PT void atmosphere_source(double h, double u, double v, double px, double py, int drag,
+                             double cd, double rho_air, double rho_water, double h_min,
+                             double& su, double& sv) {
+    su = 0.0;
+    sv = 0.0;
+    if (fp::lt(h, h_min)) return;
+    const double speed = ref_hypot(u, v);
+    const double stress = rho_air * drag_coefficient(drag, cd, speed) * speed;
+    su = (stress * u - h * px) / rho_water;
+    sv = (stress * v - h * py) / rho_water;
+}
+
+// inverse_barometer_level (gridded_atmosphere.rs:198-202): −ramp·p/(ρ g),
+// g = 9.81 (the module's constant)
+DG_PT double inverse_barometer_level(double p, double ramp, double rho_water) {
+    return -ramp * p / (rho_water * 9.81);
+}
+
 }  // namespace DGSWE_NS
 }  // namespace dgswe

@@ -37,6 +37,9 @@ class TidalBoundary:
     mean_elevation: float = 0.0
     ramp_duration: float | None = 3600.0
     incoming_wave: bool = False
+    # InverseBarometer (src/boundary/characteristic.rs:273-340): the external
+    # η raised by this factor times the form's atmosphere's level; None: not
+    raise_factor: float | None = None
 
 
 @dataclass
@@ -61,6 +64,7 @@ class NodeTidesBoundary:
     max_transport_ratio: float | None = None
     ramp_duration: float | None = None
     incoming_wave: bool = False
+    raise_factor: float | None = None
 
 
 @dataclass
@@ -84,6 +88,7 @@ class ParentBoundary:
     max_transport_ratio: float | None = None
     ramp_duration: float | None = None
     incoming_wave: bool = False
+    raise_factor: float | None = None
 
 
 @dataclass
@@ -98,6 +103,40 @@ class RelaxationBand:
     rate: float                    # 1/τ (1/s)
     wet_depth: float = 0.05
     momentum_only: bool = False
+
+
+@dataclass
+class GriddedAtmosphere:
+    """GriddedAtmosphere2D (src/source/swe_2d/gridded_atmosphere.rs) as a
+    device holds it: a weather model's snapshots regridded onto the mesh
+    nodes (``values`` [n_times][n_values][5] f32: u, v, ∂p/∂x, ∂p/∂y,
+    p − p_ref, the wind in the mesh axes, unramped) at the Unix ``times``,
+    with ``epoch_unix`` the Unix time of simulation time 0 (ModelClock).
+    With ``source`` it is the device source DeviceSource2D::Atmosphere (the
+    wind stress where ``wind``, the pressure gradient where ``pressure``);
+    boundaries with a ``raise_factor`` read its inverse-barometer level,
+    which is the pressure's when ``pressure`` and the weather has a pressure
+    field (``has_pressure``; GriddedAtmosphere2D::has_level), else 0. The
+    defaults are the reference's: Large & Pond drag, ρ_air 1.225 kg/m³,
+    ρ 1025 kg/m³, nodes shallower than 1 cm not forced, no ramp."""
+
+    times: np.ndarray
+    values: np.ndarray
+    epoch_unix: float = 0.0
+    source: bool = True
+    wind: bool = True
+    pressure: bool = True
+    has_pressure: bool = True
+    drag: int = abi.DRAG_LARGE_POND
+    drag_cd: float = 0.0
+    rho_air: float = 1.225
+    rho_water: float = 1025.0
+    h_min: float = 0.01
+    ramp_duration: float | None = None
+
+    def model_times(self) -> np.ndarray:
+        """The snapshots' simulation times."""
+        return np.asarray(self.times, dtype=np.float64) - self.epoch_unix
 
 
 @dataclass
@@ -131,6 +170,7 @@ class SWEDeviceForm2D:
     # wet/dry correction's h_dry, whichever is deeper
     line_local_depth: float | None | str = "auto"
     relaxation: RelaxationBand | None = None
+    atmosphere: GriddedAtmosphere | None = None
 
     def local_depth(self) -> float | None:
         """The line-local depth the C form carries (None: none)."""
@@ -287,6 +327,10 @@ class SWEDeviceForm2D:
                 bcs[i].constituents = cons
                 bcs[i].mean_elevation = bc.mean_elevation
                 bcs[i].ramp_duration = bc.ramp_duration or 0.0
+            factor = getattr(bc, "raise_factor", None)
+            if factor is not None:
+                bcs[i].raise_ = 1
+                bcs[i].raise_factor = float(factor)
         keep.append(bcs)
         f.n_boundaries = len(self.boundaries)
         f.boundaries = bcs
@@ -304,6 +348,29 @@ class SWEDeviceForm2D:
             r.momentum_only = 1 if self.relaxation.momentum_only else 0
             keep.append(r)
             f.relaxation = C.pointer(r)
+        if self.atmosphere is not None:
+            at = self.atmosphere
+            a = abi.Atmosphere()
+            tt = arr(at.times, np.float64)
+            vals = arr(np.asarray(at.values).reshape(-1), np.float32)
+            if vals.size != tt.size * self.n_values * 5:
+                raise ValueError("the atmosphere needs [n_times][n_values][5] values")
+            a.n_times = tt.size
+            a.times = tt.ctypes.data_as(C.POINTER(C.c_double))
+            a.epoch_unix = float(at.epoch_unix)
+            a.values = vals.ctypes.data_as(C.POINTER(C.c_float))
+            a.source = 1 if at.source else 0
+            a.wind = 1 if at.wind else 0
+            a.pressure = 1 if at.pressure else 0
+            a.level = 1 if (at.pressure and at.has_pressure) else 0
+            a.drag = int(at.drag)
+            a.drag_cd = float(at.drag_cd)
+            a.rho_air = float(at.rho_air)
+            a.rho_water = float(at.rho_water)
+            a.h_min = float(at.h_min)
+            a.ramp_duration = at.ramp_duration or 0.0
+            keep.append(a)
+            f.atmosphere = C.pointer(a)
         return f, keep
 
 

@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define DGSWE_ABI_VERSION 2u
+#define DGSWE_ABI_VERSION 3u
 
 /* ---- status codes ------------------------------------------------------ */
 enum dgswe_status {
@@ -80,6 +80,16 @@ enum dgswe_friction {
     DGSWE_FRICTION_NONE = 0,
     DGSWE_FRICTION_MANNING = 1,      /* uniform n */
     DGSWE_FRICTION_MANNING_NODES = 2 /* n per node (manning_n_nodes) */
+};
+
+/* DragCoefficient (src/source/swe_2d/wind.rs:64-158), by its device code
+ * (DragCoefficient::device_code, wind.rs:108-128). */
+enum dgswe_drag {
+    DGSWE_DRAG_CONSTANT = 0,      /* drag_cd */
+    DGSWE_DRAG_LARGE_POND = 1,    /* 1.2e-3 to 11 m/s, then (0.49 + 0.065 min(|U|, 25))·1e-3 */
+    DGSWE_DRAG_WU = 2,            /* (0.8 + 0.065 |U|)·1e-3 */
+    DGSWE_DRAG_SMITH = 3,         /* (0.61 + 0.063 |U|)·1e-3 */
+    DGSWE_DRAG_YELLAND_TAYLOR = 4 /* 1.1e-3 to 6 m/s, then (0.50 + 0.071 |U|)·1e-3 */
 };
 
 /* SspScheme (src/time/integrator.rs:226-298). */
@@ -186,6 +196,40 @@ typedef struct dgswe_relaxation {
     int32_t momentum_only;
 } dgswe_relaxation;
 
+/* GriddedAtmosphere2D (src/source/swe_2d/gridded_atmosphere.rs:60-900) as a
+ * device holds it: a weather model's snapshots regridded onto the mesh
+ * nodes (GriddedAtmosphere2D::regridded), each node's
+ *   (u, v, ∂p/∂x, ∂p/∂y, p − p_ref)
+ * in f32, the wind in the mesh axes, unramped. At simulation time t the
+ * snapshots' linear time weights at epoch_unix + t (TimeStencil,
+ * TimeInterpolation::Linear) sum them in turn from zero (add_snapshot), and
+ * the ramp is tidal_ramp(t, ramp_duration). As a source term
+ * (DeviceSource2D::Atmosphere, when `source` ≠ 0) every node at least h_min
+ * deep gets
+ *   (S_hu, S_hv) = (τ − h ∇p)/ρ_water,  τ = ρ_air C_d(|U|) |U| U,
+ * with U = ramp·(u, v) if `wind` and ∇p = ramp·(∂p/∂x, ∂p/∂y) if `pressure`
+ * (atmosphere_source), added to the RHS after Coriolis and the relaxation
+ * band. A characteristic boundary with `raise` reads its inverse-barometer
+ * level −ramp·(p − p_ref)/(ρ_water g), g = 9.81, at each face node
+ * (DeviceLevel::Atmosphere, inverse_barometer_level), 0 unless `level`.
+ * The run's times must lie within the snapshots'. */
+typedef struct dgswe_atmosphere {
+    int64_t n_times;
+    const double* times;      /* [n_times] strictly increasing Unix seconds */
+    double epoch_unix;        /* Unix time of simulation time 0 (ModelClock) */
+    const float* values;      /* [n_times][n_elements·(N+1)²][5] */
+    int32_t source;           /* add the momentum source (else only boundaries read it) */
+    int32_t wind;             /* the source applies the wind stress */
+    int32_t pressure;         /* the source applies the pressure gradient */
+    int32_t level;            /* the level is the pressure's (has_level); else 0 */
+    int32_t drag;             /* dgswe_drag */
+    double drag_cd;           /* DGSWE_DRAG_CONSTANT's C_d */
+    double rho_air;           /* kg/m³ */
+    double rho_water;         /* kg/m³ */
+    double h_min;             /* nodes shallower than this are not forced */
+    double ramp_duration;     /* s; ≤ 0: no ramp */
+} dgswe_atmosphere;
+
 typedef struct dgswe_boundary {
     int32_t tag;            /* the face tag this condition applies to */
     int32_t kind;           /* dgswe_boundary_kind */
@@ -197,6 +241,12 @@ typedef struct dgswe_boundary {
     double ramp_duration;   /* s; ≤ 0: no ramp (src/boundary/harmonic_tide.rs:24-32) */
     const dgswe_node_tides* node_tides; /* DGSWE_BC_NODE_TIDES: the tide per node */
     const dgswe_parent_series* parent;  /* DGSWE_BC_PARENT: the parent per node */
+    /* InverseBarometer (src/boundary/characteristic.rs:273-340): a
+     * characteristic boundary's external η raised by raise_factor times the
+     * form's atmosphere's level at each face node (DeviceBoundary2D's
+     * `raise`); 0: not raised */
+    int32_t raise;
+    double raise_factor;
 } dgswe_boundary;
 
 /* SWEDeviceForm2D (src/physics/device.rs:27-62) as plain data, with the
@@ -253,6 +303,10 @@ typedef struct dgswe_form {
 
     /* A nesting relaxation band towards a parent model, or NULL */
     const dgswe_relaxation* relaxation;
+
+    /* A weather model's wind and air pressure (the source term and the
+     * boundaries' inverse-barometer level), or NULL */
+    const dgswe_atmosphere* atmosphere;
 } dgswe_form;
 
 /* ---- stages and runs ---------------------------------------------------- */

@@ -443,6 +443,9 @@ static bool time_stencil(const double* times, int64_t n, double time, bool cubic
 struct Boundary {
     int kind = DGSWE_BC_WALL;
     double wall_h_min = 1e-6;
+    // InverseBarometer (src/boundary/characteristic.rs:273-340)
+    bool raise = false;
+    double raise_factor = 0.0;
     int elevation_only = DGSWE_AT_REST;
     std::vector<dgswe_tide_constituent> constituents;
     double mean_elevation = 0.0, ramp_duration = 0.0;
@@ -604,6 +607,46 @@ struct Relaxation {
     bool momentum_only = false;
 };
 
+// GriddedAtmosphere2D (src/source/swe_2d/gridded_atmosphere.rs:60-900) as
+// the device form holds it: the snapshots regridded onto the nodes
+// ([time][node][5]: u, v, ∂p/∂x, ∂p/∂y, p − p_ref, f32) and the options
+struct Atmosphere {
+    bool on = false, source = false, wind = false, pressure = false, level = false;
+    int drag = 1;
+    double cd = 0.0, rho_air = 1.225, rho_water = 1025.0, h_min = 0.01, ramp = 0.0, epoch = 0.0;
+    std::vector<double> times;
+    std::vector<float> values;
+    size_t n_nodes = 0;
+
+    // The weather at flat node g and simulation time t: the linear time
+    // stencil at epoch + t (time_stencil), the snapshots summed in turn from
+    // zero (add_snapshot, :143-150; cached, :680-688). Outside the snapshots
+    // the nearest end (the reference panics there; the runs refuse it).
+    void at(size_t g, double t, double out[5]) const {
+        int64_t idx[4] = {0, 0, 0, 0};
+        double w[4] = {1.0, 0.0, 0.0, 0.0};
+        int len = 1;
+        const int64_t n = (int64_t)times.size();
+        if (!time_stencil(times.data(), n, epoch + t, false, idx, w, len)) {
+            idx[0] = epoch + t < times[0] ? 0 : n - 1;
+            w[0] = 1.0;
+            len = 1;
+        }
+        for (int q = 0; q < 5; ++q) out[q] = 0.0;
+        for (int j = 0; j < len; ++j) {
+            const float* v = &values[((size_t)idx[j] * n_nodes + g) * 5];
+            for (int q = 0; q < 5; ++q) out[q] += w[j] * (double)v[q];
+        }
+    }
+    // BoundaryLevel::level by node index (:873-895)
+    double level_at(size_t g, double t) const {
+        if (!level) return 0.0;
+        double s[5];
+        at(g, t, s);
+        return inverse_barometer_level(s[4], tidal_ramp(t, ramp), rho_water);
+    }
+};
+
 struct Model {
     dgswe_form form;
     Ops ops;
@@ -619,6 +662,7 @@ struct Model {
     WetDry wd;
     bool has_bed = false;
     Relaxation relax;
+    Atmosphere atm;
 
     explicit Model(int order) : ops(order) {}
     size_t n_values() const { return (size_t)mesh.n_elements * ops.nn; }
@@ -754,6 +798,9 @@ static State boundary_flux(const Model& m, int64_t k, int face, int node, const 
     } else {
         eta = bc.elevation(time);
     }
+    // InverseBarometer::external_state: raised by the weather's level at the
+    // face node (GriddedAtmosphere2D's level by node index)
+    if (bc.raise) eta += bc.raise_factor * m.atm.level_at((size_t)k * m.ops.nn + node, time);
     double h_e = fmax_(eta - bathy, 0.0);
     double un_e = 0.0, ut_e;
     if (has_uv) {
@@ -1082,6 +1129,25 @@ static void element_rhs(const Model& m, const Buffer& q, int64_t k, double time,
             out_h[i] += gamma * dh;
             out_hu[i] += gamma * (depth * u - st.hu);
             out_hv[i] += gamma * (depth * v - st.hv);
+        }
+    }
+    // GriddedAtmosphere2D::add_element (src/source/swe_2d/gridded_atmosphere.rs:698-729),
+    // after the band
+    if (m.atm.on && m.atm.source && (m.atm.wind || m.atm.pressure)) {
+        const Atmosphere& a = m.atm;
+        double ramp = tidal_ramp(time, a.ramp);
+        double rw = a.wind ? ramp : 0.0, rp = a.pressure ? ramp : 0.0;
+        for (int i = 0; i < nn; ++i) {
+            size_t flat = (size_t)k * nn + i;
+            double h = q.get(flat).h;
+            if (h < a.h_min) continue;
+            double wx[5];
+            a.at(flat, time, wx);
+            double su, sv;
+            atmosphere_source(h, rw * wx[0], rw * wx[1], rp * wx[2], rp * wx[3], a.drag, a.cd,
+                              a.rho_air, a.rho_water, a.h_min, su, sv);
+            out_hu[i] += su;
+            out_hv[i] += sv;
         }
     }
 }
@@ -1842,6 +1908,12 @@ int oracle_create(const dgswe_form* f, int device, oracle_handle** out) {
         bc.constituents.assign(in.constituents, in.constituents + in.n_constituents);
         bc.mean_elevation = in.mean_elevation;
         bc.ramp_duration = in.ramp_duration;
+        bc.raise = in.kind != DGSWE_BC_WALL && in.raise != 0;
+        bc.raise_factor = in.raise_factor;
+        if (bc.raise && !f->atmosphere) {
+            delete m;
+            return DGSWE_ERR_INVALID;
+        }
         if (in.kind == DGSWE_BC_NODE_TIDES) {
             const dgswe_node_tides* t = in.node_tides;
             if (!t || t->n_slots <= 0 || !t->positions || !t->coefficients) {
@@ -1920,6 +1992,29 @@ int oracle_create(const dgswe_form* f, int device, oracle_handle** out) {
         m->relax.momentum_only = r.momentum_only != 0;
         m->relax.on = true;
     }
+    if (f->atmosphere) {
+        const dgswe_atmosphere& a = *f->atmosphere;
+        if (a.n_times <= 0 || !a.times || !a.values || !(a.rho_water > 0.0)) {
+            delete m;
+            return DGSWE_ERR_INVALID;
+        }
+        Atmosphere& at = m->atm;
+        at.on = true;
+        at.source = a.source != 0;
+        at.wind = a.wind != 0;
+        at.pressure = a.pressure != 0;
+        at.level = a.level != 0;
+        at.drag = a.drag;
+        at.cd = a.drag_cd;
+        at.rho_air = a.rho_air;
+        at.rho_water = a.rho_water;
+        at.h_min = a.h_min;
+        at.ramp = a.ramp_duration;
+        at.epoch = a.epoch_unix;
+        at.n_nodes = (size_t)f->n_elements * m->ops.nn;
+        at.times.assign(a.times, a.times + a.n_times);
+        at.values.assign(a.values, a.values + (size_t)a.n_times * at.n_nodes * 5);
+    }
     for (auto& e : m->mesh.edges)
         if (e.right.element < 0 && !m->boundaries.count(e.tag)) {
             delete m;
@@ -1927,6 +2022,7 @@ int oracle_create(const dgswe_form* f, int device, oracle_handle** out) {
         }
     m->form.boundaries = nullptr;
     m->form.relaxation = nullptr;
+    m->form.atmosphere = nullptr;
     m->form.bathymetry = nullptr;
     m->form.manning_n_nodes = nullptr;
     m->form.vertices = nullptr;
@@ -2146,6 +2242,18 @@ int oracle_time_stencil(const double* times, int64_t n, double t, int cubic, int
 
 double oracle_manning_cbrt(double x) { return manning_cbrt(x); }
 double oracle_tidal_ramp(double t, double duration) { return tidal_ramp(t, duration); }
+double oracle_hypot(double x, double y) { return ref_hypot(x, y); }
+double oracle_drag_coefficient(int kind, double cd, double speed) {
+    return drag_coefficient(kind, cd, speed);
+}
+void oracle_atmosphere_source(double h, double u, double v, double px, double py, int drag,
+                              double cd, double rho_air, double rho_water, double h_min,
+                              double out[2]) {
+    atmosphere_source(h, u, v, px, py, drag, cd, rho_air, rho_water, h_min, out[0], out[1]);
+}
+double oracle_inverse_barometer_level(double p, double ramp, double rho_water) {
+    return inverse_barometer_level(p, ramp, rho_water);
+}
 
 void oracle_characteristic_state(const double interior[3], double h_e, double un_e, double ut_e,
                                  double nx, double ny, double g, double h_min, double out[3]) {

@@ -42,6 +42,12 @@ int oracle_multirate_stats_get(const oracle_handle* h, dgswe_multirate_stats* ou
 /* pointwise functions for the known-answer tests */
 double oracle_manning_cbrt(double x);
 double oracle_tidal_ramp(double t, double duration);
+double oracle_hypot(double x, double y);
+double oracle_drag_coefficient(int kind, double cd, double speed);
+void oracle_atmosphere_source(double h, double u, double v, double px, double py, int drag,
+                              double cd, double rho_air, double rho_water, double h_min,
+                              double out[2]);
+double oracle_inverse_barometer_level(double p, double ramp, double rho_water);
 void oracle_characteristic_state(const double interior[3], double h_e, double un_e, double ut_e,
                                  double nx, double ny, double g, double h_min, double out[3]);
 void oracle_desingularized_velocity(double h_dry, double h, double hu, double hv, double out[2]);

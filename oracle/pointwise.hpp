@@ -16,6 +16,7 @@
 #include <cstdint>
 #include <cstring>
 #include <limits>
+#include <utility>
 
 namespace oracle {
 
@@ -394,6 +395,85 @@ inline double tidal_ramp(double t, double duration) {
     double tau = t / duration;
     tau = tau < 0.0 ? 0.0 : (tau > 1.0 ? 1.0 : tau);
     return tau * tau * (3.0 - 2.0 * tau);
+}
+
+// crate::math::hypot (src/math.rs:202-245): musl's hypot, the squares split
+// in two parts each (Dekker) so that their sum is exact enough for the
+// correctly rounded square root, scaled by 2^±700 near overflow/underflow
+inline double ref_hypot(double x, double y) {
+    auto square = [](double v, double& hi, double& lo) {
+        const double split = 134217728.0 + 1.0;  // 2^27 + 1
+        double vc = v * split;
+        double vh = v - vc + vc;
+        double vl = v - vh;
+        hi = v * v;
+        lo = vh * vh - hi + 2.0 * vh * vl + vl * vl;
+    };
+    auto from = [](uint64_t b) {
+        double d;
+        std::memcpy(&d, &b, sizeof d);
+        return d;
+    };
+    auto to = [](double d) {
+        uint64_t b;
+        std::memcpy(&b, &d, sizeof b);
+        return b;
+    };
+    uint64_t ux = to(x) & (UINT64_MAX >> 1), uy = to(y) & (UINT64_MAX >> 1);
+    if (ux < uy) std::swap(ux, uy);
+    int64_t ex = (int64_t)(ux >> 52), ey = (int64_t)(uy >> 52);
+    x = from(ux);
+    y = from(uy);
+    if (ey == 0x7ff) return y;
+    if (ex == 0x7ff || uy == 0) return x;
+    if (ex - ey > 64) return x + y;
+    double z = 1.0;
+    if (ex > 0x3ff + 510) {
+        z = from(0x6bb0000000000000ull);
+        x *= from(0x1430000000000000ull);
+        y *= from(0x1430000000000000ull);
+    } else if (ey < 0x3ff - 450) {
+        z = from(0x1430000000000000ull);
+        x *= from(0x6bb0000000000000ull);
+        y *= from(0x6bb0000000000000ull);
+    }
+    double hx, lx, hy, ly;
+    square(x, hx, lx);
+    square(y, hy, ly);
+    return z * std::sqrt(ly + lx + hy + hx);
+}
+
+// DragCoefficient::compute (src/source/swe_2d/wind.rs:134-158), by its
+// device code (DragCoefficient::from_device_code, wind.rs:118-128)
+inline double drag_coefficient(int kind, double cd, double speed) {
+    switch (kind) {
+        case 0: return cd;
+        case 1: return speed <= 11.0 ? 1.2e-3 : (0.49 + 0.065 * fmin_(speed, 25.0)) * 1e-3;
+        case 2: return (0.8 + 0.065 * speed) * 1e-3;
+        case 3: return (0.61 + 0.063 * speed) * 1e-3;
+        default: return speed <= 6.0 ? 1.1e-3 : (0.50 + 0.071 * speed) * 1e-3;
+    }
+}
+
+// atmosphere_source and wind_stress
+// (src/source/swe_2d/gridded_atmosphere.rs:161-196): (τ − h ∇p)/ρ_water,
+// τ = ρ_air C_d(|U|) |U| U, nothing below h_min
+inline void atmosphere_source(double h, double u, double v, double px, double py, int drag,
+                              double cd, double rho_air, double rho_water, double h_min,
+                              double& su, double& sv) {
+    su = 0.0;
+    sv = 0.0;
+    if (h < h_min) return;
+    double speed = ref_hypot(u, v);
+    double stress = rho_air * drag_coefficient(drag, cd, speed) * speed;
+    double tau_x = stress * u, tau_y = stress * v;
+    su = (tau_x - h * px) / rho_water;
+    sv = (tau_y - h * py) / rho_water;
+}
+
+// inverse_barometer_level (gridded_atmosphere.rs:198-202), g = 9.81
+inline double inverse_barometer_level(double p, double ramp, double rho_water) {
+    return -ramp * p / (rho_water * 9.81);
 }
 
 }  // namespace oracle

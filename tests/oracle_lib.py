@@ -21,6 +21,11 @@ POINTWISE = {
     "set_threads": (C.c_int, [C.c_int]),
     "manning_cbrt": (C.c_double, [C.c_double]),
     "tidal_ramp": (C.c_double, [C.c_double, C.c_double]),
+    "hypot": (C.c_double, [C.c_double, C.c_double]),
+    "drag_coefficient": (C.c_double, [C.c_int, C.c_double, C.c_double]),
+    "atmosphere_source": (None, [C.c_double] * 5 + [C.c_int] + [C.c_double] * 4
+                          + [C.POINTER(C.c_double)]),
+    "inverse_barometer_level": (C.c_double, [C.c_double, C.c_double, C.c_double]),
     "characteristic_state": (None, [_dp, C.c_double, C.c_double, C.c_double, C.c_double,
                                     C.c_double, C.c_double, C.c_double, _dp]),
     "desingularized_velocity": (None, [C.c_double, C.c_double, C.c_double, C.c_double, _dp]),
