@@ -395,7 +395,7 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS, Cfg<N1>::MIN_BLOCKS)
     constexpr int NN = C::NN, NP = C::NP, NA = C::NA, EPB = C::EPB;
     __shared__ double s_q[EPB][6][NN];
     __shared__ double s_x[EPB][C::X];
-    __shared__ int s_flag[EPB][2];
+    __shared__ int s_flag[EPB][3];
     __shared__ double s_red[EPB][5];
 
     if (!*active) return;
@@ -414,6 +414,7 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS, Cfg<N1>::MIN_BLOCKS)
     if (i == 0) {
         s_flag[e][0] = 0;
         s_flag[e][1] = 0;
+        s_flag[e][2] = 0;
     }
     double h = 0, hu = 0, hv = 0, u = 0, v = 0, b = 0;
     if (valid) {
@@ -431,10 +432,17 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS, Cfg<N1>::MIN_BLOCKS)
     s_q[e][4][i] = v;
     s_q[e][5][i] = b;
     __syncthreads();
-    if (valid && P.formulation == kWetDry && fp::lt(h, P.subcell_depth))
+    if (valid && P.formulation == kWetDry && fp::lt(h, P.subcell_depth)) {
         atomicOr(&s_flag[e][0], 1);
+        if (!fp::nz(h)) atomicAdd(&s_flag[e][2], 1);
+    }
     __syncthreads();
     const bool sub = s_flag[e][0] != 0;
+    // A subcell element without water at any node (every h = ±0, so every
+    // u = v = 0): its reconstructed subcell faces are dry, so the interface
+    // fluxes, pressure and bed terms are all ±0, and it skips the subcell
+    // phases (they read only h, u, v and the bed)
+    const bool dry = s_flag[e][2] == NN;
     double rh = 0.0, rhu = 0.0, rhv = 0.0;
     const bool affine = valid ? T.affine[k] != 0 : true;
 
@@ -465,7 +473,7 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS, Cfg<N1>::MIN_BLOCKS)
             slot_f[1] = g_hu;
             slot_f[2] = g_hv;
         }
-    } else if (valid && sub) {
+    } else if (valid && sub && !dry) {
         // subcell faces of this node's subcell on its r-line and s-line
 #pragma unroll
         for (int dir = 0; dir < 2; ++dir) {
@@ -537,7 +545,7 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS, Cfg<N1>::MIN_BLOCKS)
             rhu -= h * T.gdb[gi * 2];
             rhv -= h * T.gdb[gi * 2 + 1];
         }
-    } else if (valid && sub) {
+    } else if (valid && sub && !dry) {
 #pragma unroll
         for (int dir = 0; dir < 2; ++dir) {
             const int line = dir == 0 ? j : a;
@@ -566,7 +574,7 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS, Cfg<N1>::MIN_BLOCKS)
     __syncthreads();
 
     // ---- phase C: the subcells' fluxes and bed terms at this node ----
-    if (valid && sub) {
+    if (valid && sub && !dry) {
 #pragma unroll
         for (int dir = 0; dir < 2; ++dir) {
             const int line = dir == 0 ? j : a;
