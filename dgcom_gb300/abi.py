@@ -342,6 +342,8 @@ ENTRY_POINTS = {
     "upload": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp, _dp, C.c_int64]),
     "download": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp, _dp, C.c_int64]),
     "compute_rhs": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, _dp, _dp, _dp, C.c_int64]),
+    "compute_rhs_mass_fluxes": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, _dp, _dp, _dp,
+                                          C.c_int64, _dp, C.c_int64, _dp, C.c_int64]),
     "stage": (C.c_int, [C.c_void_p, C.POINTER(StagePlan)]),
     "finish": (C.c_int, [C.c_void_p, C.c_int32]),
     "element_dt": (C.c_int, [C.c_void_p, C.c_double, C.c_int32, _dp, _dp]),

@@ -675,6 +675,55 @@ int dgswe_compute_rhs(dgswe_handle* h, int32_t input, double time, double* out_h
     return sync(h);
 }
 
+int dgswe_compute_rhs_mass_fluxes(dgswe_handle* h, int32_t input, double time, double* out_h,
+                                  double* out_hu, double* out_hv, int64_t n, double* face_mass,
+                                  int64_t n_face, double* subcell_mass, int64_t n_sub) {
+    if (!h) return DGSWE_ERR_INVALID;
+    const int64_t face_len = h->K * 4 * h->n1, sub_len = h->K * 2 * h->n1 * (h->n1 - 1);
+    if (!valid_buffer(input) || n != h->n_values || !out_h || !out_hu || !out_hv ||
+        (face_mass && n_face != face_len) || (subcell_mass && n_sub != sub_len))
+        return fail(h, DGSWE_ERR_INVALID,
+                    "compute_rhs_mass_fluxes: buffer %d, %lld values, %lld face and %lld subcell "
+                    "fluxes (expected %lld, %lld, %lld)",
+                    input, (long long)n, (long long)n_face, (long long)n_sub,
+                    (long long)h->n_values, (long long)face_len, (long long)sub_len);
+    if (!(time >= h->parent_range.first && time <= h->parent_range.second))
+        return fail(h, DGSWE_ERR_INVALID,
+                    "compute_rhs_mass_fluxes: t = %g leaves the forcing's snapshots", time);
+    CK(cudaSetDevice(h->device));
+    if (int s = ensure_buffer(h, input)) return s;
+    if (int s = ensure_buffer(h, kRhsBuffer)) return s;
+    if (subcell_mass && !h->sub_mass) {
+        void* p = nullptr;
+        CK(cudaMalloc(&p, (size_t)sub_len * sizeof(double)));
+        h->allocations.push_back(p);
+        h->sub_mass = (double*)p;
+    }
+    if (int s = write_host_args(h, StageArgs{time, 0.0, 0.0, 1.0, 1.0, 0.0})) return s;
+    StageExtra X = h->X;
+    X.subcell_mass = subcell_mass ? h->sub_mass : nullptr;
+    const DevBuf& in = h->buf[input].view;
+    const DevBuf& rhs = h->buf[kRhsBuffer].view;
+    h->ks->face(h->n1, h->T, h->P, in, h->fb_h, h->fb_hu, h->fb_hv, h->ctl, kHostSlot, always(h),
+                h->stream);
+    h->ks->stage(h->n1, h->T, h->P, X, in, in, rhs, rhs, h->fb_h, h->fb_hu, h->fb_hv, h->ctl,
+                 kHostSlot, kModeRhsOnly, 0, always(h), h->stream);
+    CK(cudaGetLastError());
+    const size_t bytes = (size_t)n * sizeof(double);
+    CK(cudaMemcpyAsync(out_h, rhs.h, bytes, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(out_hu, rhs.hu, bytes, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(out_hv, rhs.hv, bytes, cudaMemcpyDeviceToHost, h->stream));
+    // the face-flux buffer is the reference's face_mass layout already:
+    // [(k·4 + face)·n1 + fi], F*_h along the element's outward unit normal
+    if (face_mass)
+        CK(cudaMemcpyAsync(face_mass, h->fb_h, (size_t)face_len * sizeof(double),
+                           cudaMemcpyDeviceToHost, h->stream));
+    if (subcell_mass)
+        CK(cudaMemcpyAsync(subcell_mass, h->sub_mass, (size_t)sub_len * sizeof(double),
+                           cudaMemcpyDeviceToHost, h->stream));
+    return sync(h);
+}
+
 int dgswe_stage(dgswe_handle* h, const dgswe_stage_plan* plan) {
     if (!h) return DGSWE_ERR_INVALID;
     if (!plan || !valid_buffer(plan->base) || !valid_buffer(plan->input) ||

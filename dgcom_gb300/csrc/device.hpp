@@ -130,6 +130,9 @@ struct Physics {
 // −1, in order) and the reciprocal weights
 struct StageExtra {
     double xl[5], xr[5], inv_w[5];
+    // a RHS that keeps its subcell mass fluxes: [K][2·n1·(n1 − 1)], NaN in
+    // the elements without subcells (null: not kept)
+    double* subcell_mass = nullptr;
 };
 
 // The element step's parameters: the CFL and the positivity bound of a

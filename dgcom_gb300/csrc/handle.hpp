@@ -52,6 +52,7 @@ struct dgswe_handle {
     dgswe::host::DeviceBuffer buf[DGSWE_N_BUFFERS + 1];
     double *fb_h = nullptr, *fb_hu = nullptr, *fb_hv = nullptr;
     double* dt_el = nullptr;
+    double* sub_mass = nullptr;  // subcell mass fluxes (dgswe_compute_rhs_mass_fluxes), lazily
     StepCtl* ctl = nullptr;    // device
     StepCtl* h_ctl = nullptr;  // pinned host mirror
     std::string device_name;

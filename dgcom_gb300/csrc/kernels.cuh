@@ -332,7 +332,8 @@ struct Cfg {
     static constexpr int MIN_BLOCKS = 5;
     static constexpr int PAIR_DOUBLES = NN * NP * 3;
     static constexpr int FACE_DOUBLES = 2 * NN * 8;           // reconstructed faces
-    static constexpr int IFL_DOUBLES = 2 * N1 * (N1 - 1) * 6;  // subcell interface fluxes
+    static constexpr int NSUB = 2 * N1 * (N1 - 1);            // subcell interfaces
+    static constexpr int IFL_DOUBLES = NSUB * 6;               // their fluxes
     static constexpr int X = PAIR_DOUBLES > FACE_DOUBLES + IFL_DOUBLES ? PAIR_DOUBLES
                                                                        : FACE_DOUBLES + IFL_DOUBLES;
 };
@@ -545,6 +546,12 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS, Cfg<N1>::MIN_BLOCKS)
             rhu -= h * T.gdb[gi * 2];
             rhv -= h * T.gdb[gi * 2 + 1];
         }
+        if (X.subcell_mass)  // no subcells: NaN (compute_rhs_swe_2d_mass_fluxes_into)
+            for (int q = i; q < C::NSUB; q += NN)
+                X.subcell_mass[k * C::NSUB + q] = fp::from_bits(0x7FF8000000000000ll);
+    } else if (valid && sub && dry) {
+        if (X.subcell_mass)  // the dry element's interface fluxes are ±0
+            for (int q = i; q < C::NSUB; q += NN) X.subcell_mass[k * C::NSUB + q] = 0.0;
     } else if (valid && sub && !dry) {
 #pragma unroll
         for (int dir = 0; dir < 2; ++dir) {
@@ -563,6 +570,8 @@ __global__ void __launch_bounds__(Cfg<N1>::THREADS, Cfg<N1>::MIN_BLOCKS)
             hydro_hll(Sd{fa_[0], fa_[1], fa_[2], fa_[3]}, Sd{fb_[0], fb_[1], fb_[2], fb_[3]}, mx, my,
                       norm, mx * inv, my * inv, g, sqrt_g, half_g, h_min, fa, fb);
             double* o = &ifl[((dir * N1 + line) * (N1 - 1) + pos) * 6];
+            if (X.subcell_mass)  // subcell_slot (src/solver/rhs/subcells.rs:37-42)
+                X.subcell_mass[k * C::NSUB + (dir * N1 + line) * (N1 - 1) + pos] = fa.h;
             o[0] = fa.h;
             o[1] = fa.hu;
             o[2] = fa.hv;

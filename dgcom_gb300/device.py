@@ -122,6 +122,22 @@ class SWEPhysics2D:
                                          self.n_values), "compute_rhs")
         return tuple(out)
 
+    def compute_rhs_mass_fluxes_into(self, time: float, input: int = abi.STATE):
+        """The RHS of buffer ``input`` at ``time`` with its mass fluxes
+        (compute_rhs_swe_2d_mass_fluxes_into, src/solver/rhs/swe_2d.rs:
+        1042-1075): F*_h of every element face node, ``[K][4][N+1]``, and
+        the mass flux through every subcell interface, ``[K][2(N+1)N]``, NaN
+        in the elements without subcells."""
+        n1 = self.form.order + 1
+        k = self.form.mesh.n_elements
+        out = [np.empty(self.n_values) for _ in range(3)]
+        face = np.empty(k * 4 * n1)
+        sub = np.empty(k * 2 * n1 * (n1 - 1))
+        self._check(self.lib.compute_rhs_mass_fluxes(
+            self.handle, input, time, *map(_ptr, out), self.n_values, _ptr(face), face.size,
+            _ptr(sub), sub.size), "compute_rhs_mass_fluxes")
+        return tuple(out), face.reshape(k, 4, n1), sub.reshape(k, -1)
+
     def element_dt(self, cfl: float, scheme: int = abi.SSP_RK3) -> np.ndarray:
         """LocalTimeStepping::element_dt: every element's stable step."""
         out = np.empty(self.form.mesh.n_elements)

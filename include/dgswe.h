@@ -435,6 +435,20 @@ int dgswe_download(dgswe_handle* handle, int32_t buffer, double* h, double* hu,
 int dgswe_compute_rhs(dgswe_handle* handle, int32_t input, double time,
                       double* out_h, double* out_hu, double* out_hv, int64_t n);
 
+/* compute_rhs_swe_2d_mass_fluxes_into (src/solver/rhs/swe_2d.rs:1042-1075;
+ * BarotropicPhysics::compute_rhs_mass_fluxes_into, src/physics/builder.rs:
+ * 785-817): dgswe_compute_rhs that also writes the numerical mass flux of
+ * every element face node, face_mass[(k·4 + face)·(N+1) + fi] = F*_h along
+ * the element's outward unit normal (n_face = n_elements·4·(N+1)), and of
+ * every subcell interface of the elements that take the subcells,
+ * subcell_mass[k·2(N+1)N + (dir·(N+1) + line)·N + a] (the interface between
+ * nodes a and a + 1 of the line, metric-scaled; n_sub = n_elements·2(N+1)N),
+ * NaN in every other element. Either output may be NULL. */
+int dgswe_compute_rhs_mass_fluxes(dgswe_handle* handle, int32_t input, double time,
+                                  double* out_h, double* out_hu, double* out_hv, int64_t n,
+                                  double* face_mass, int64_t n_face, double* subcell_mass,
+                                  int64_t n_sub);
+
 /* One stage pass over every element: LocalTimeStepping::stage_where
  * (src/physics/builder.rs:652-737). */
 int dgswe_stage(dgswe_handle* handle, const dgswe_stage_plan* plan);

@@ -683,6 +683,12 @@ struct Workspace {
         double distance = 0.0;
     };
     std::vector<Outer> outer;
+    // compute_rhs_swe_2d_mass_fluxes_into's outputs of the element being
+    // computed (src/solver/rhs/swe_2d.rs:1017-1075), or null: the mass
+    // component of F* at its 4·n1 face nodes and the mass flux through its
+    // 2·n1·(n1 − 1) subcell interfaces
+    double* face_mass = nullptr;
+    double* subcell_mass = nullptr;
     explicit Workspace(const Ops& ops)
         : nodes(ops.nn), rhs(ops.nn), metric(ops.n1), interfaces(ops.n1 + 1), faces(ops.n1),
           outer(4 * ops.n1) {}
@@ -897,7 +903,7 @@ static void line_volume(const Model& m, Workspace& ws, Idx idx, bool affine,
 // SplitFormSWE2D::line_subcells (src/solver/rhs/swe_2d_split_form.rs:938-1035)
 template <class Idx>
 static void line_subcells(const Model& m, Workspace& ws, Idx idx, const Workspace::Outer& end0,
-                          const Workspace::Outer& end1, bool affine) {
+                          const Workspace::Outer& end1, bool affine, double* mass) {
     const Ops& ops = m.ops;
     int n1 = ops.n1;
     const std::vector<double>& w = ops.w1;
@@ -955,6 +961,7 @@ static void line_subcells(const Model& m, Workspace& ws, Idx idx, const Workspac
         auto mm = ws.interfaces[a + 1];
         State f_a, f_b;
         hydrostatic_hll(ws.faces[a].second, ws.faces[a + 1].first, mm.first, mm.second, g, h_min, f_a, f_b);
+        if (mass) mass[a] = f_a.h;
         ws.rhs[ia] = ws.rhs[ia] - (1.0 / w[a]) * f_a;
         ws.rhs[ib] = ws.rhs[ib] + (1.0 / w[a + 1]) * f_b;
     }
@@ -1027,6 +1034,12 @@ static void element_rhs(const Model& m, const Buffer& q, int64_t k, double time,
     if (subcells)
         for (int face = 0; face < 4; ++face)
             for (int fi = 0; fi < n1; ++fi) ws.outer[face * n1 + fi] = outer_node(m, q, k, face, fi);
+    else if (ws.subcell_mass)
+        for (int slot = 0; slot < 2 * n1 * (n1 - 1); ++slot) ws.subcell_mass[slot] = NAN;
+    // subcell_slot (src/solver/rhs/subcells.rs:37-42): (dir·n1 + line)·(n1 − 1) + a
+    auto line_mass = [&](int dir, int line) {
+        return ws.subcell_mass ? ws.subcell_mass + (dir * n1 + line) * (n1 - 1) : nullptr;
+    };
     bool affine = g.affine[k] != 0;
     double ar0, ar1, as0, as1;
     g.contravariant(k, 0, ar0, ar1, as0, as1);
@@ -1044,7 +1057,8 @@ static void element_rhs(const Model& m, const Buffer& q, int64_t k, double time,
             }
         }
         if (subcells)
-            line_subcells(m, ws, r_line, ws.outer[3 * n1 + rev], ws.outer[n1 + fwd], affine);
+            line_subcells(m, ws, r_line, ws.outer[3 * n1 + rev], ws.outer[n1 + fwd], affine,
+                          line_mass(0, line));
         else
             line_volume(m, ws, r_line, affine, {ar0, ar1});
         for (int j = 0; j < n1; ++j) {
@@ -1057,7 +1071,8 @@ static void element_rhs(const Model& m, const Buffer& q, int64_t k, double time,
             }
         }
         if (subcells)
-            line_subcells(m, ws, s_line, ws.outer[fwd], ws.outer[2 * n1 + rev], affine);
+            line_subcells(m, ws, s_line, ws.outer[fwd], ws.outer[2 * n1 + rev], affine,
+                          line_mass(1, line));
         else
             line_volume(m, ws, s_line, affine, {as0, as1});
     }
@@ -1074,6 +1089,7 @@ static void element_rhs(const Model& m, const Buffer& q, int64_t k, double time,
             const Node& q_int = ws.nodes[node];
             State f_star = interior ? m.faces[(2 * e + side) * n1 + fi]
                                     : boundary_flux(m, k, face, node, q_int, nx, ny, time, edge.tag);
+            if (ws.face_mass) ws.face_mass[face * n1 + fi] = f_star.h;
             State flux_diff = wintermeyer_flux(q_int, q_int, nx, ny, m.form.g) - f_star;
             ws.rhs[node] = ws.rhs[node] + (scale * ops.lift_at(face, node, fi)) * flux_diff;
         }
@@ -2077,6 +2093,79 @@ int oracle_compute_rhs(oracle_handle* h, int32_t input, double time, double* oh,
             element_rhs(m, q, k, time, ws, oh + o, ohu + o, ohv + o);
         }
     }
+    return DGSWE_OK;
+}
+
+// compute_rhs_swe_2d_mass_fluxes_into (src/solver/rhs/swe_2d.rs:1042-1075):
+// the RHS with each element face node's F*_h and each subcell interface's
+// mass flux (NaN in elements without subcells); either may be null
+int oracle_compute_rhs_mass_fluxes(oracle_handle* h, int32_t input, double time, double* oh,
+                                   double* ohu, double* ohv, int64_t n, double* face_mass,
+                                   int64_t n_face, double* subcell_mass, int64_t n_sub) {
+    Model& m = *h->m;
+    const int n1 = m.ops.n1, nn = m.ops.nn;
+    const int64_t K = m.mesh.n_elements;
+    if (!check_buffer(m, input).empty() || n != (int64_t)m.n_values()) return DGSWE_ERR_INVALID;
+    if ((face_mass && n_face != K * 4 * n1) || (subcell_mass && n_sub != K * 2 * n1 * (n1 - 1)))
+        return DGSWE_ERR_INVALID;
+    const Buffer& q = m.buf[input];
+    face_pass(m, q);
+#pragma omp parallel
+    {
+        Workspace ws(m.ops);
+#pragma omp for schedule(static)
+        for (int64_t k = 0; k < K; ++k) {
+            size_t o = (size_t)k * nn;
+            ws.face_mass = face_mass ? face_mass + k * 4 * n1 : nullptr;
+            ws.subcell_mass = subcell_mass ? subcell_mass + k * 2 * n1 * (n1 - 1) : nullptr;
+            element_rhs(m, q, k, time, ws, oh + o, ohu + o, ohv + o);
+        }
+    }
+    return DGSWE_OK;
+}
+
+// subcell_divergence_element (src/solver/rhs/transport_3d.rs:253-330): the
+// divergence of a transport (hu, hv) on element k's GLL subcells from its
+// interface fluxes (subcell_slot order) and its faces' F*, with the line
+// ends' own m·(hu, hv) replaced by F* through the lift; with the RHS's mass
+// fluxes it is −dh/dt node by node in a subcell element. Test helper.
+int oracle_subcell_divergence(oracle_handle* h, int64_t k, const double* hu, const double* hv,
+                              const double* interfaces, const double* face, double* div) {
+    const Model& m = *h->m;
+    const Ops& ops = m.ops;
+    const Geometry& g = m.geom;
+    const int n1 = ops.n1, nn = ops.nn;
+    if (k < 0 || k >= m.mesh.n_elements) return DGSWE_ERR_INVALID;
+    const bool affine = g.affine[k] != 0;
+    auto node_of = [&](int dir, int line, int a) { return dir == 0 ? line * n1 + a : a * n1 + line; };
+    for (int i = 0; i < nn; ++i) div[i] = 0.0;
+    for (int dir = 0; dir < 2; ++dir)
+        for (int line = 0; line < n1; ++line) {
+            std::vector<std::pair<double, double>> metric(n1);
+            for (int a = 0; a < n1; ++a) {  // line_metric (src/solver/rhs/subcells.rs:94-114)
+                double r0, r1, s0, s1;
+                g.contravariant(k, affine ? 0 : node_of(dir, line, a), r0, r1, s0, s1);
+                metric[a] = dir == 0 ? std::make_pair(r0, r1) : std::make_pair(s0, s1);
+            }
+            auto end_flux = [&](int a) {
+                int node = node_of(dir, line, a);
+                return metric[a].first * hu[node] + metric[a].second * hv[node];
+            };
+            for (int a = 0; a < n1; ++a) {
+                double right = a + 1 < n1 ? interfaces[(dir * n1 + line) * (n1 - 1) + a] : end_flux(a);
+                double left = a > 0 ? interfaces[(dir * n1 + line) * (n1 - 1) + a - 1] : end_flux(a);
+                div[node_of(dir, line, a)] += (right - left) / ops.w1[a];
+            }
+        }
+    for (int i = 0; i < nn; ++i) div[i] *= g.det_j_inv[g.nidx(k, i)];
+    for (int f = 0; f < 4; ++f)  // subtract_face_lift
+        for (int fi = 0; fi < n1; ++fi) {
+            int node = ops.face_nodes[f][fi];
+            size_t fn = g.fidx(k, f, fi);
+            double scale = g.surface_j[fn] * g.det_j_inv[g.nidx(k, node)];
+            double jump = g.nxv[fn] * hu[node] + g.nyv[fn] * hv[node] - face[f * n1 + fi];
+            for (int i = 0; i < nn; ++i) div[i] -= scale * ops.lift_at(f, i, fi) * jump;
+        }
     return DGSWE_OK;
 }
 

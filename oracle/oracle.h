@@ -25,6 +25,11 @@ int oracle_upload(oracle_handle* h, int32_t buffer, const double* hh, const doub
 int oracle_download(oracle_handle* h, int32_t buffer, double* hh, double* hu, double* hv, int64_t n);
 int oracle_compute_rhs(oracle_handle* h, int32_t input, double time, double* out_h, double* out_hu,
                        double* out_hv, int64_t n);
+int oracle_compute_rhs_mass_fluxes(oracle_handle* h, int32_t input, double time, double* oh,
+                                   double* ohu, double* ohv, int64_t n, double* face_mass,
+                                   int64_t n_face, double* subcell_mass, int64_t n_sub);
+int oracle_subcell_divergence(oracle_handle* h, int64_t k, const double* hu, const double* hv,
+                              const double* interfaces, const double* face, double* div);
 int oracle_stage(oracle_handle* h, const dgswe_stage_plan* plan);
 int oracle_finish(oracle_handle* h, int32_t acc);
 int oracle_element_dt(oracle_handle* h, double cfl, int32_t scheme, double* dt_elements,

@@ -22,6 +22,7 @@ POINTWISE = {
     "manning_cbrt": (C.c_double, [C.c_double]),
     "tidal_ramp": (C.c_double, [C.c_double, C.c_double]),
     "hypot": (C.c_double, [C.c_double, C.c_double]),
+    "subcell_divergence": (C.c_int, [C.c_void_p, C.c_int64, _dp, _dp, _dp, _dp, _dp]),
     "drag_coefficient": (C.c_double, [C.c_int, C.c_double, C.c_double]),
     "atmosphere_source": (None, [C.c_double] * 5 + [C.c_int] + [C.c_double] * 4
                           + [C.POINTER(C.c_double)]),
