@@ -44,7 +44,7 @@ UNIT = "DOF-updates/s"
 BYTES_PER_NODE_STAGE = {2: 81.8, 3: 77.5}  # algorithmic bytes (state, bed, mesh), N=2 / N=3
 # stage_kernel<4>'s DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per
 # node-stage in one ncu capture of the 200k-quad coastal box, for scaling by nodes
-STAGE_TRAFFIC_PER_NODE_STAGE = {3: 192.1}
+STAGE_TRAFFIC_PER_NODE_STAGE = {3: 190.4}
 
 
 def peaks():
@@ -321,7 +321,7 @@ def run_ours(args, rank: int, world: int, local: int):
                          "traffic": (STAGE_TRAFFIC_PER_NODE_STAGE[args.order] * nodes
                                      if args.order in STAGE_TRAFFIC_PER_NODE_STAGE else None),
                          "peak_kind": peak_kind, "kernel": f"stage_kernel<{args.order + 1}>",
-                         "note": "bound by the FP64 pipe (86.5 % of it in ncu), not HBM; traffic "
+                         "note": "bound by the FP64 pipe (86.4 % of it in ncu), not HBM; traffic "
                                  "from an ncu capture at 200k quads scaled by nodes"},
             "kernel_ms": {"stage": timed.stage_ms / args.steps, "face": timed.face_ms / args.steps,
                           "dt": timed.dt_ms / args.steps, "control": timed.control_ms / args.steps},
