@@ -72,11 +72,26 @@ struct dgswe_handle {
     int32_t *d_order = nullptr, *d_edges = nullptr, *d_bfaces = nullptr;
     dgswe_multirate_stats mr_stats{};
     cudaEvent_t ev_lts[2] = {nullptr, nullptr};
+    // the level planner on the device (multirate_plan.cu): the face
+    // neighbours, scratch, the kept plan's inputs and limited levels, the
+    // pinned host copy of its scalars and counts
+    struct {
+        int64_t* nb = nullptr;
+        int8_t* nb_face = nullptr;
+        uint8_t *level_tmp = nullptr, *memo_level = nullptr, *memo_line = nullptr;
+        uint8_t *memo_limited = nullptr, *node_a = nullptr, *node_b = nullptr;
+        int64_t *sort_counts = nullptr, *at_least = nullptr;
+        void* scalars = nullptr;
+        void* host = nullptr;
+        bool memo_valid = false, memo_lines = false;
+        int memo_finest = -1;
+    } dplan;
     // the times every parent series covers (a run must stay within them)
     std::pair<double, double> parent_range{-INFINITY, INFINITY};
 
     ~dgswe_handle() {
         delete planner;
+        if (dplan.host) cudaFreeHost(dplan.host);
         for (cudaEvent_t e : ev_lts)
             if (e) cudaEventDestroy(e);
         if (step_graph) cudaGraphExecDestroy(step_graph);
@@ -105,6 +120,12 @@ int begin_run(dgswe_handle* h, const dgswe_run_config* run, double target);
 // dgswe_run with local time stepping (run->levels > 0; multirate_run.cu)
 int run_multirate(dgswe_handle* h, const dgswe_run_config* run, dgswe_callback callback,
                   void* user, dgswe_report* report);
+// A coarse step's plan made on the device (multirate_plan.cu) from the
+// element steps in h->dt_el and the depth flags in h->d_flags, into the
+// handle's plan arrays and the planner's counts: the fitted coarse step and
+// the stable step before the fit
+int device_plan(dgswe_handle* h, int n_stages, bool lines, bool bounded, double dt_max,
+                double landing, double& fitted_dt, double& stable_dt);
 
 }  // namespace host
 }  // namespace dgswe

@@ -290,6 +290,29 @@ void MultiratePlanner::set_plan(const uint8_t* levels, const uint8_t* rates) {
     make_lists();
 }
 
+void MultiratePlanner::set_device_plan(int finest, int n_stages, int V, const int64_t* counts,
+                                       const int64_t* edge_counts, const int64_t* bface_counts,
+                                       int stride, int64_t evaluations,
+                                       int64_t level_evaluations) {
+    memo_ = false;
+    finest_ = finest;
+    for (int j = 0; j <= n_stages; ++j) {
+        count_[j].assign(counts + j * stride, counts + j * stride + V);
+        order_[j].clear();
+    }
+    for (int s = 0; s < n_stages; ++s) {
+        edge_count_[s].assign(edge_counts + s * stride, edge_counts + s * stride + V);
+        bface_count_[s].assign(bface_counts + s * stride, bface_counts + s * stride + V);
+        edge_order_[s].clear();
+        bface_order_[s].clear();
+        rate_[s].clear();
+    }
+    level_.clear();
+    evaluations_ = evaluations;
+    level_evaluations_ = level_evaluations;
+    version_ += 1;
+}
+
 void MultiratePlanner::assign_one_level() {
     memo_ = false;
     finest_ = 0;

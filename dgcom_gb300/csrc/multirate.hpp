@@ -54,6 +54,19 @@ public:
     // element's level and the finest): a host that plans itself
     // (LocalTimeStepping::begin_coarse_step)
     void set_plan(const uint8_t* levels, const uint8_t* rates);
+    // A plan the device made (multirate_plan.cu): its finest level and the
+    // counts of its passes (counts[j·stride + d], edge and boundary-face
+    // counts alike, d < V = finest + 1), and the evaluations; the device
+    // holds its levels, rates and orders, which this object does not keep
+    void set_device_plan(int finest, int n_stages, int V, const int64_t* counts,
+                         const int64_t* edge_counts, const int64_t* bface_counts, int stride,
+                         int64_t evaluations, int64_t level_evaluations);
+    // The step's figures of a device plan, kept plan or not
+    void set_step_figures(double stable_step, double inverse_dt_sum, int64_t n_line_local) {
+        stable_step_ = stable_step;
+        inverse_dt_sum_ = inverse_dt_sum;
+        n_line_local_ = n_line_local;
+    }
 
     int finest() const { return finest_; }
     int nn() const { return nn_; }

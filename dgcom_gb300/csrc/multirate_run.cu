@@ -50,6 +50,7 @@ int prepare(dgswe_handle* h, int levels, int n_stages) {
         h->planner_levels = levels;
         h->planner_stages = n_stages;
         h->plan_uploaded = 0;
+        h->dplan.memo_valid = false;
     }
     if (!h->ev_lts[0]) {
         CK(cudaEventCreate(&h->ev_lts[0]));
@@ -71,6 +72,7 @@ int prepare(dgswe_handle* h, int levels, int n_stages) {
 int upload_plan(dgswe_handle* h, int n_stages) {
     MultiratePlanner& pl = *h->planner;
     if (h->plan_uploaded == pl.version()) return DGSWE_OK;
+    h->dplan.memo_valid = false;  // the device planner's kept plan is overwritten
     pl.edge_lists(h->h_edge_left, h->h_edge_right, h->h_bface);
     const size_t K = (size_t)h->K, E = h->h_edge_left.size(), B = h->h_bface.size();
     cudaStream_t st = h->stream;
@@ -189,8 +191,6 @@ int run_multirate(dgswe_handle* h, const dgswe_run_config* run, dgswe_callback c
     const bool bounded = f.positivity_h_dry > 0.0;
     const double d1 = bounded ? kSubcellCapDepthFactor * f.positivity_h_dry : INFINITY;
     const double d2 = bounded ? f.positivity_h_dry : INFINITY;
-    std::vector<double> dt_el((size_t)K);
-    std::vector<uint8_t> flags((size_t)K), line_local((size_t)K);
     std::vector<double> hh, hu, hv;
 
     double t = run->t_start;
@@ -246,36 +246,14 @@ int run_multirate(dgswe_handle* h, const dgswe_run_config* run, dgswe_callback c
         const DevBuf& q = h->buf[DGSWE_STATE].view;
         h->ks->dt(h->n1, h->T, h->P, q, D, h->dt_el, h->ctl, &h->ctl->always, st);
         h->ks->depth_flags(q.h, K, h->nn, d0, d1, d2, h->d_flags, st);
-        CK(cudaMemcpyAsync(dt_el.data(), h->dt_el, (size_t)K * sizeof(double),
-                           cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(flags.data(), h->d_flags, (size_t)K, cudaMemcpyDeviceToHost, st));
-        if (int s = sync(h)) return s;
-        // coarse_step_bound (src/physics/builder.rs:611-632): the largest step
-        // of an element in water, not in a film
-        double bound = INFINITY;
-        if (bounded) {
-            for (int bit : {2, 4}) {
-                double longest = 0.0;
-#pragma omp parallel for schedule(static) reduction(max : longest)
-                for (int64_t k = 0; k < K; ++k)
-                    if (std::isfinite(dt_el[k]) && (flags[k] & bit)) longest = std::max(longest, dt_el[k]);
-                if (longest > 0.0) {
-                    bound = longest;
-                    break;
-                }
-            }
-        }
-        double cap = run->dt_max > 0.0 ? std::min(run->dt_max, bound) : bound;
-        if (!std::isfinite(cap)) cap = 0.0;
-        if (lines) {
-#pragma omp parallel for schedule(static)
-            for (int64_t k = 0; k < K; ++k) line_local[k] = flags[k] & 1;
-        }
+        // the plan, made on the device from the element steps and flags
+        // (multirate_plan.cu): the coarse step's levels, rates and pass
+        // orders stay there, its counts come to the host
         const auto plan0 = std::chrono::steady_clock::now();
         const uint64_t version0 = pl.version();
-        const double fitted = pl.assign(dt_el.data(), lines ? line_local.data() : nullptr, cap,
-                                        target - t);
-        double dt = pl.stable_step();
+        double fitted = 0.0, dt = 0.0;
+        if (int s = device_plan(h, n, lines, bounded, run->dt_max, target - t, fitted, dt))
+            return s;
         if (run->dt_max > 0.0) dt = std::fmin(dt, run->dt_max);
         if (run->dt_min > 0.0 && dt < run->dt_min) {
             std::snprintf(msg, sizeof msg, "Time step (%.2e) below minimum (%.2e)", dt,
@@ -287,7 +265,6 @@ int run_multirate(dgswe_handle* h, const dgswe_run_config* run, dgswe_callback c
         dt = std::fmin(dt, fitted);
         const bool landed = t + dt * (1.0 + kLandingSlack) >= target;
         if (landed) dt = target - t;
-        if (int s = upload_plan(h, n)) return s;
         stats.plans += pl.version() != version0 ? 1 : 0;
         stats.plan_seconds +=
             std::chrono::duration<double>(std::chrono::steady_clock::now() - plan0).count();

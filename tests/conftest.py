@@ -1,7 +1,14 @@
+import os
 import sys
 from pathlib import Path
 
 import pytest
+
+# Under pytest-xdist every worker would start an OpenMP team as wide as the
+# machine for the oracle; one thread per worker keeps them from starving
+# each other (a team's threads spin while they wait)
+if os.environ.get("PYTEST_XDIST_WORKER"):
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
 
 ROOT = Path(__file__).resolve().parents[1]
 for p in (ROOT, ROOT / "tests"):
