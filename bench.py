@@ -244,6 +244,8 @@ def run_ours(args, rank: int, world: int, local: int):
     dev = SWEPhysics2D(form, local)
     dev.upload(*case.state)
     lib = dev.lib
+    # the kernels' launch shapes, timed on this mesh and state (dgswe_autotune)
+    tuning = dev.autotune(5)
 
     def profile(steps: int, t_start: float) -> abi.Profile:
         cfg = abi.RunConfig()
@@ -322,6 +324,9 @@ def run_ours(args, rank: int, world: int, local: int):
                        "elements": form.mesh.n_elements, "order": args.order,
                        "nodes": nodes, "parallelism": f"replicas x{world}",
                        "l2": "inputs larger than L2 (state and tables ≫ 129 MB)"},
+            "launch": {"face_threads": tuning["face_threads"],
+                       "stage_threads": tuning["stage_threads"],
+                       "face_ms": tuning["face_ms"], "stage_ms": tuning["stage_ms"]},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak,
                          "traffic": (STAGE_TRAFFIC_PER_NODE_STAGE[args.order] * nodes

@@ -117,6 +117,15 @@ class Atmosphere(C.Structure):
     ]
 
 
+class Tuning(C.Structure):
+    _fields_ = [
+        ("face_threads", C.c_int32),
+        ("stage_threads", C.c_int32),
+        ("face_ms", C.c_double * 3),
+        ("stage_ms", C.c_double * 2),
+    ]
+
+
 class Boundary(C.Structure):
     _fields_ = [
         ("tag", C.c_int32),
@@ -375,6 +384,7 @@ CUDA_ONLY = {
     "planner_spread": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint8), C.c_int32,
                                  C.POINTER(C.c_uint8), C.POINTER(C.c_uint8)]),
     # device pointers in and out; working memory in the library's own array
+    "autotune": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.POINTER(Tuning)]),
     "compute_rhs_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]),
     # ensembles of independent members

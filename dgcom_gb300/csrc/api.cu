@@ -724,6 +724,80 @@ int dgswe_compute_rhs_mass_fluxes(dgswe_handle* h, int32_t input, double time, d
     return sync(h);
 }
 
+int dgswe_autotune(dgswe_handle* h, int32_t repeats, int32_t force_face, int32_t force_stage,
+                   dgswe_tuning* out) {
+    if (!h) return DGSWE_ERR_INVALID;
+    if (!out || repeats < 1 || force_stage > 1 ||
+        (force_face >= 0 && force_face != 64 && force_face != 128 && force_face != 256))
+        return fail(h, DGSWE_ERR_INVALID, "autotune: repeats %d, face %d, stage %d", repeats,
+                    force_face, force_stage);
+    CK(cudaSetDevice(h->device));
+    if (int s = ensure_buffer(h, DGSWE_STATE)) return s;
+    if (int s = ensure_buffer(h, kRhsBuffer)) return s;
+    if (int s = write_host_args(h, StageArgs{0.0, 0.0, 0.0, 1.0, 1.0, 0.0})) return s;
+    std::memset(out, 0, sizeof *out);
+    const DevBuf& in = h->buf[DGSWE_STATE].view;
+    const DevBuf& rhs = h->buf[kRhsBuffer].view;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    auto timed = [&](auto&& launch, double& ms) -> int {
+        launch();  // warm
+        CK(cudaEventRecord(e0, h->stream));
+        for (int r = 0; r < repeats; ++r) launch();
+        CK(cudaEventRecord(e1, h->stream));
+        CK(cudaEventSynchronize(e1));
+        float t = 0.0f;
+        CK(cudaEventElapsedTime(&t, e0, e1));
+        ms = (double)t / repeats;
+        return DGSWE_OK;
+    };
+    auto face = [&]() {
+        h->ks->face(h->n1, h->T, h->P, in, h->fb_h, h->fb_hu, h->fb_hv, h->ctl, kHostSlot,
+                    always(h), h->stream);
+    };
+    auto stage = [&]() {
+        h->ks->stage(h->n1, h->T, h->P, h->X, in, in, rhs, rhs, h->fb_h, h->fb_hu, h->fb_hv,
+                     h->ctl, kHostSlot, kModeRhsOnly, 0, always(h), h->stream);
+    };
+    int status = DGSWE_OK;
+    static const int kFace[3] = {64, 128, 256};
+    if (force_face >= 0) {
+        h->P.face_threads = force_face;
+    } else {
+        int best = 2;
+        for (int c = 0; c < 3 && status == DGSWE_OK; ++c) {
+            h->P.face_threads = kFace[c];
+            status = timed(face, out->face_ms[c]);
+            if (out->face_ms[c] < out->face_ms[best]) best = c;
+        }
+        h->P.face_threads = kFace[best];
+    }
+    if (status == DGSWE_OK) face();  // the stage reads its fluxes
+    if (force_stage >= 0) {
+        h->P.stage_shape = force_stage;
+    } else {
+        for (int c = 0; c < 2 && status == DGSWE_OK; ++c) {
+            h->P.stage_shape = c;
+            status = timed(stage, out->stage_ms[c]);
+        }
+        h->P.stage_shape = out->stage_ms[1] < out->stage_ms[0] ? 1 : 0;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (status != DGSWE_OK) return status;
+    CK(cudaGetLastError());
+    out->face_threads = h->P.face_threads;
+    const int per = h->P.stage_shape == 0 ? 128 : 64;
+    out->stage_threads = std::max(1, per / h->nn) * h->nn;
+    // the step graph holds the old shapes in its launches
+    if (h->step_graph) {
+        cudaGraphExecDestroy(h->step_graph);
+        h->step_graph = nullptr;
+    }
+    return sync(h);
+}
+
 int dgswe_stage(dgswe_handle* h, const dgswe_stage_plan* plan) {
     if (!h) return DGSWE_ERR_INVALID;
     if (!plan || !valid_buffer(plan->base) || !valid_buffer(plan->input) ||

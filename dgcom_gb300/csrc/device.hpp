@@ -124,6 +124,11 @@ struct Physics {
     Condition cond[kMaxConditions];
     double x[5], w[5], d[25];  // GLL nodes, weights, D
     int face_node[4][5];
+    // launch shapes (dgswe_autotune): the face kernel's threads per block
+    // and the stage kernel's shape (0: ⌊128/nn⌋ elements a block, 5 blocks
+    // per SM; 1: ⌊64/nn⌋ elements a block, 10 blocks per SM)
+    int face_threads = 256;
+    int stage_shape = 0;
 };
 
 // Subcell bounds x_l, x_r of each GLL subcell (sums of the weights from

@@ -318,18 +318,22 @@ __global__ void __launch_bounds__(256) face_kernel(DevTables T, Physics P, DevBu
 // ---------------------------------------------------------------------------
 // the stage kernel
 
-template <int N1>
+// SHAPE 0: ⌊128/NN⌋ elements a block; SHAPE 1: ⌊64/NN⌋ elements a block
+// at twice the blocks per SM (the same registers and warps per SM), one of
+// the launch shapes dgswe_autotune chooses between
+template <int N1, int SHAPE = 0>
 struct Cfg {
     static constexpr int NN = N1 * N1;
     static constexpr int NP = N1 - 1;      // pairs a node owns
     static constexpr int NA = 2 * (N1 - 1);  // pairs a node is in
-    static constexpr int EPB = (128 / NN) > 0 ? (128 / NN) : 1;
+    static constexpr int PER = SHAPE == 0 ? 128 : 64;
+    static constexpr int EPB = (PER / NN) > 0 ? (PER / NN) : 1;
     static constexpr int THREADS = EPB * NN;
     // stage_kernel blocks per SM: 5 caps it at ≤ 102 registers (96 at
     // N1 = 4, no spills) for 20 warps per SM; it is bound by the FP64 pipe
     // and waits on it, so more warps keep it busier (measured 5 % faster
     // on the 1 M-quad N = 3 case than 4 blocks)
-    static constexpr int MIN_BLOCKS = 5;
+    static constexpr int MIN_BLOCKS = SHAPE == 0 ? 5 : 10;
     static constexpr int PAIR_DOUBLES = NN * NP * 3;
     static constexpr int FACE_DOUBLES = 2 * NN * 8;           // reconstructed faces
     static constexpr int NSUB = 2 * N1 * (N1 - 1);            // subcell interfaces
@@ -386,13 +390,13 @@ __device__ __forceinline__ void line_metric(const DevTables& T, int64_t k, int d
 }
 
 // LISTED: a multirate pass over lp's elements, each with its own stage
-template <int N1, bool LISTED>
-__global__ void __launch_bounds__(Cfg<N1>::THREADS, Cfg<N1>::MIN_BLOCKS)
+template <int N1, bool LISTED, int SHAPE = 0>
+__global__ void __launch_bounds__(Cfg<N1, SHAPE>::THREADS, Cfg<N1, SHAPE>::MIN_BLOCKS)
     stage_kernel(DevTables T, Physics P, StageExtra X, DevBuf in, DevBuf base, DevBuf out,
                  DevBuf acc, const double* __restrict__ fb_h, const double* __restrict__ fb_hu,
                  const double* __restrict__ fb_hv, StepCtl* ctl, int slot, int mode,
                  int check_finite, const int* active, DevBuf keep, LtsPass lp) {
-    using C = Cfg<N1>;
+    using C = Cfg<N1, SHAPE>;
     constexpr int NN = C::NN, NP = C::NP, NA = C::NA, EPB = C::EPB;
     __shared__ double s_q[EPB][6][NN];
     __shared__ double s_x[EPB][C::X];

@@ -29,7 +29,7 @@ static void face_n(const DevTables& T, const Physics& P, const DevBuf& in, doubl
     relax<false>(T, P, in, ctl, slot, LtsPass{}, s);
     const int64_t items = (T.n_edges + T.n_bfaces) * N1;
     if (items == 0) return;
-    const int threads = 256;
+    const int threads = P.face_threads > 0 && P.face_threads <= 256 ? P.face_threads : 256;
     const unsigned blocks = (unsigned)((items + threads - 1) / threads);
     face_kernel<N1, false><<<blocks, threads, 0, s>>>(T, P, in, fh, fhu, fhv, ctl, slot, active,
                                                       LtsPass{});
@@ -42,7 +42,7 @@ static void face_listed_n(const DevTables& T, const Physics& P, const DevBuf& in
     relax<true>(T, P, in, ctl, 0, lp, s);
     const int64_t items = (lp.n_edges + lp.n_bfaces) * N1;
     if (items == 0) return;
-    const int threads = 256;
+    const int threads = P.face_threads > 0 && P.face_threads <= 256 ? P.face_threads : 256;
     const unsigned blocks = (unsigned)((items + threads - 1) / threads);
     face_kernel<N1, true><<<blocks, threads, 0, s>>>(T, P, in, fh, fhu, fhv, ctl, 0, &ctl->always,
                                                      lp);
@@ -53,6 +53,14 @@ static void stage_n(const DevTables& T, const Physics& P, const StageExtra& X, c
                     const DevBuf& base, const DevBuf& out, const DevBuf& acc, const double* fh,
                     const double* fhu, const double* fhv, StepCtl* ctl, int slot, int mode,
                     int check_finite, const int* active, const DevBuf& keep, cudaStream_t s) {
+    if (P.stage_shape == 1) {
+        using C1 = Cfg<N1, 1>;
+        const unsigned blocks = (unsigned)((T.K + C1::EPB - 1) / C1::EPB);
+        stage_kernel<N1, false, 1><<<blocks, C1::THREADS, 0, s>>>(
+            T, P, X, in, base, out, acc, fh, fhu, fhv, ctl, slot, mode, check_finite, active, keep,
+            LtsPass{});
+        return;
+    }
     using C = Cfg<N1>;
     const unsigned blocks = (unsigned)((T.K + C::EPB - 1) / C::EPB);
     stage_kernel<N1, false><<<blocks, C::THREADS, 0, s>>>(T, P, X, in, base, out, acc, fh, fhu, fhv,

@@ -138,6 +138,15 @@ class SWEPhysics2D:
             _ptr(sub), sub.size), "compute_rhs_mass_fluxes")
         return tuple(out), face.reshape(k, 4, n1), sub.reshape(k, -1)
 
+    def autotune(self, repeats: int = 5, face_threads: int = -1, stage_shape: int = -1) -> dict:
+        """dgswe_autotune: time the kernels' launch shapes on this mesh and
+        state and keep the fastest (or set them, where given)."""
+        t = abi.Tuning()
+        self._check(self.lib.autotune(self.handle, repeats, face_threads, stage_shape,
+                                      C.byref(t)), "autotune")
+        return {"face_threads": t.face_threads, "stage_threads": t.stage_threads,
+                "face_ms": list(t.face_ms), "stage_ms": list(t.stage_ms)}
+
     def element_dt(self, cfl: float, scheme: int = abi.SSP_RK3) -> np.ndarray:
         """LocalTimeStepping::element_dt: every element's stable step."""
         out = np.empty(self.form.mesh.n_elements)
