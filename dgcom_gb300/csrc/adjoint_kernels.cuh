@@ -75,6 +75,7 @@ __global__ void __launch_bounds__(AdjCfg<N1>::THREADS, AdjCfg<N1>::MIN_BLOCKS)
     __shared__ int s_flag[EPB][2];
     __shared__ double s_red[EPB][12];
     __shared__ int s_arg[EPB];
+    __shared__ int s_live[EPB];
 
     const int tid = threadIdx.x;
     const int e = tid / NN, i = tid % NN;
@@ -87,6 +88,7 @@ __global__ void __launch_bounds__(AdjCfg<N1>::THREADS, AdjCfg<N1>::MIN_BLOCKS)
     if (i == 0) {
         s_flag[e][0] = 0;
         s_flag[e][1] = 0;
+        s_live[e] = 0;
     }
     double h = 0, hu = 0, hv = 0, u = 0, v = 0, b = 0;
     if (valid) {
@@ -128,6 +130,7 @@ __global__ void __launch_bounds__(AdjCfg<N1>::THREADS, AdjCfg<N1>::MIN_BLOCKS)
         lo_h = A.lo_h[gi];
         lo_hu = A.lo_hu[gi];
         lo_hv = A.lo_hv[gi];
+        if (fp::nz(lo_h) || fp::nz(lo_hu) || fp::nz(lo_hv)) s_live[e] = 1;
     }
     double ldh = lo_h, ldhu = lo_hu, ldhv = lo_hv;  // λ of (vh, dhu, dhv)
     if (P.has_wet_dry) {
@@ -310,8 +313,14 @@ __global__ void __launch_bounds__(AdjCfg<N1>::THREADS, AdjCfg<N1>::MIN_BLOCKS)
     auto node_side = [&](int n) {
         return Sd{s_q[e][0][n], s_q[e][3][n], s_q[e][4][n], s_q[e][5][n]};
     };
+    // An element whose output λ is zero at every node sends zero back
+    // through its volume term (the reverse is linear in λ, its partials
+    // finite): it skips the volume phases, whose outputs are sums into
+    // shared λ and atomics
+    __syncthreads();
+    const bool work = valid && s_live[e] != 0;
     // step 1: pair slots' λ, or the subcell faces (forward)
-    if (valid && !sub) {
+    if (work && !sub) {
         if (P.has_bed) {
             Lh -= T.gdb[gi * 2] * lrhu + T.gdb[gi * 2 + 1] * lrhv;
         }
@@ -326,7 +335,7 @@ __global__ void __launch_bounds__(AdjCfg<N1>::THREADS, AdjCfg<N1>::MIN_BLOCKS)
             o[1] = -T.sched_hcoef[i * NA + q] * lrhu;
             o[2] = -T.sched_hcoef[i * NA + q] * lrhv;
         }
-    } else if (valid && sub) {
+    } else if (work && sub) {
 #pragma unroll
         for (int dir = 0; dir < 2; ++dir) {
             const int line = dir == 0 ? j : a;
@@ -380,7 +389,7 @@ __global__ void __launch_bounds__(AdjCfg<N1>::THREADS, AdjCfg<N1>::MIN_BLOCKS)
     }
     __syncthreads();
     // step 2: each owned pair's reverse; or the subcells' sums and bed terms
-    if (valid && !sub) {
+    if (work && !sub) {
         const double two_g = P.two_g;
 #pragma unroll
         for (int q = 0; q < NP; ++q) {
@@ -406,7 +415,7 @@ __global__ void __launch_bounds__(AdjCfg<N1>::THREADS, AdjCfg<N1>::MIN_BLOCKS)
             o[4] = f1 * mass;
             o[5] = f2 * mass;
         }
-    } else if (valid && sub) {
+    } else if (work && sub) {
 #pragma unroll
         for (int dir = 0; dir < 2; ++dir) {
             const int line = dir == 0 ? j : a;
@@ -475,7 +484,7 @@ __global__ void __launch_bounds__(AdjCfg<N1>::THREADS, AdjCfg<N1>::MIN_BLOCKS)
     }
     __syncthreads();
     // step 3: gather the pairs' λ and the bed slope's; or the interface HLLs
-    if (valid && !sub) {
+    if (work && !sub) {
 #pragma unroll
         for (int q = 0; q < NA; ++q) {
             const int sl = T.sched_slot[i * NA + q];
@@ -502,7 +511,7 @@ __global__ void __launch_bounds__(AdjCfg<N1>::THREADS, AdjCfg<N1>::MIN_BLOCKS)
                 }
             }
         }
-    } else if (valid && sub) {
+    } else if (work && sub) {
 #pragma unroll
         for (int dir = 0; dir < 2; ++dir) {
             const int line = dir == 0 ? j : a;
@@ -535,7 +544,7 @@ __global__ void __launch_bounds__(AdjCfg<N1>::THREADS, AdjCfg<N1>::MIN_BLOCKS)
     }
     __syncthreads();
     // step 4: the subcell reconstructions, reversed
-    if (valid && sub) {
+    if (work && sub) {
 #pragma unroll
         for (int dir = 0; dir < 2; ++dir) {
             const int line = dir == 0 ? j : a;
