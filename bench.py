@@ -240,6 +240,18 @@ def run_ours(args, rank: int, world: int, local: int):
     dist = Dist(world, "nccl")
     case = build_workload(args.elements, args.order)
     form = case.form
+    if args.weather:
+        # a synthetic storm over the box: the wind-stress and pressure source
+        # and the open boundary raised by its inverse-barometer level
+        import dataclasses
+
+        from dgcom_gb300 import cases
+        from dgcom_gb300.mesh import TAG_OPEN
+
+        weather = cases.synthetic_atmosphere(form, t0=0.0, t1=3600.0, dt_snap=3600.0)
+        open_bc = dataclasses.replace(form.boundaries[TAG_OPEN], raise_factor=1.0)
+        form = dataclasses.replace(form, atmosphere=weather,
+                                   boundaries={**form.boundaries, TAG_OPEN: open_bc})
     nodes = form.n_values
     dev = SWEPhysics2D(form, local)
     dev.upload(*case.state)
@@ -320,7 +332,9 @@ def run_ours(args, rank: int, world: int, local: int):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
             "config": {"workload": f"coastal box {form.mesh.n_elements} quads N={args.order} "
-                                   "SSP-RK3 (wet/dry, Manning, Coriolis, 4-constituent tide)",
+                                   "SSP-RK3 (wet/dry, Manning, Coriolis, 4-constituent tide"
+                                   + (", synthetic storm: wind, pressure, raised open boundary)"
+                                      if args.weather else ")"),
                        "elements": form.mesh.n_elements, "order": args.order,
                        "nodes": nodes, "parallelism": f"replicas x{world}",
                        "l2": "inputs larger than L2 (state and tables ≫ 129 MB)"},
@@ -804,6 +818,8 @@ def main():
     ap.add_argument("--elements", type=int, default=1_000_000)
     ap.add_argument("--order", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--weather", action="store_true",
+                    help="coastal: add a synthetic storm (GriddedAtmosphere2D's device form)")
     ap.add_argument("--workload", default="coastal",
                     choices=["coastal", "ensemble", "adjoint", "adjoint_ensemble", "multirate"],
                     help="coastal: the 1 M-quad coastal box (the headline); ensemble: batched "

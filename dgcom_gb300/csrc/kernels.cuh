@@ -167,6 +167,24 @@ __global__ void __launch_bounds__(256) relax_kernel(DevTables T, Physics P, DevB
 template <bool LISTED>
 __global__ void __launch_bounds__(256) atmos_kernel(DevTables T, Physics P, DevBuf in,
                                                     const StepCtl* ctl, int slot, LtsPass lp) {
+    // one stage time for every node of a global stage: its time weights and
+    // ramp once per block, in shared memory
+    __shared__ int s_idx[2], s_len;
+    __shared__ double s_w[2], s_ramp;
+    if (!LISTED) {
+        if (threadIdx.x == 0) {
+            const double t = ctl[0].stage[slot].time;
+            int idx[2];
+            double w[2];
+            s_len = weather_weights(T.at_times, T.at_n_times, T.at_epoch + t, idx, w);
+            s_idx[0] = idx[0];
+            s_idx[1] = idx[1];
+            s_w[0] = w[0];
+            s_w[1] = w[1];
+            s_ramp = tidal_ramp(t, T.at_ramp);
+        }
+        __syncthreads();
+    }
     const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (item >= (LISTED ? lp.n : T.K) * P.nn) return;
     const int64_t e = item / P.nn;
@@ -176,11 +194,22 @@ __global__ void __launch_bounds__(256) atmos_kernel(DevTables T, Physics P, DevB
     double su = 0.0, sv = 0.0;
     const double h = in.h[g];
     if (!fp::lt(h, T.at_h_min)) {
-        const double t = LISTED ? lts_stage(lp, k).time : ctl[0].stage[slot].time;
         int idx[2];
         double w[2];
-        const int len = weather_weights(T.at_times, T.at_n_times, T.at_epoch + t, idx, w);
-        const double ramp = tidal_ramp(t, T.at_ramp);
+        int len;
+        double ramp;
+        if (LISTED) {
+            const double t = lts_stage(lp, k).time;
+            len = weather_weights(T.at_times, T.at_n_times, T.at_epoch + t, idx, w);
+            ramp = tidal_ramp(t, T.at_ramp);
+        } else {
+            len = s_len;
+            idx[0] = s_idx[0];
+            idx[1] = s_idx[1];
+            w[0] = s_w[0];
+            w[1] = s_w[1];
+            ramp = s_ramp;
+        }
         const double rw = T.at_wind ? ramp : 0.0, rp = T.at_pressure ? ramp : 0.0;
         const double u = weather_field(T.at_values, nv, 0, g, idx, w, len);
         const double v = weather_field(T.at_values, nv, 1, g, idx, w, len);

@@ -661,13 +661,29 @@ DG_PT int weather_weights(const double* times, int n, double tu, int idx[2], dou
     return 2;
 }
 
+// The double of a float, exactly: on the device the normal floats are
+// widened on the integer pipes (sign, exponent rebiased, mantissa shifted;
+// the conversion instruction runs on the FP64 pipe), the rest converted
+DG_PT double widen(float f) {
+#if defined(__CUDA_ARCH__)
+    const unsigned int b = __float_as_uint(f);
+    const unsigned int e = (b >> 23) & 0xFFu;
+    if (e == 0u || e == 0xFFu) return (double)f;
+    const unsigned long long sign = (unsigned long long)(b & 0x80000000u) << 32;
+    return __longlong_as_double((long long)(sign | ((unsigned long long)(e + 896u) << 52) |
+                                            ((unsigned long long)(b & 0x7FFFFFu) << 29)));
+#else
+    return (double)f;
+#endif
+}
+
 // One field of the weather at flat node g, its snapshots summed in turn
 // from zero (add_snapshot); values are [time][5][n_values] f32
 DG_PT double weather_field(const float* values, int64_t n_values, int q, int64_t g,
                            const int idx[2], const double w[2], int len) {
     double s = 0.0;
     for (int j = 0; j < len; ++j)
-        s += w[j] * (double)values[((int64_t)idx[j] * 5 + q) * n_values + g];
+        s += w[j] * widen(values[((int64_t)idx[j] * 5 + q) * n_values + g]);
     return s;
 }
 
@@ -698,14 +714,12 @@ DG_PT double ref_hypot(double x, double y) {
         x *= up;
         y *= up;
     }
-    const double split = 134217728.0 + 1.0;
-    const double xc = x * split, yc = y * split;
-    const double xh = x - xc + xc, yh = y - yc + yc;
-    const double xl = x - xh, yl = y - yh;
+    // x² = hx + lx exactly: the reference splits x in two halves (Dekker's
+    // product); a fused multiply-add gives the same exact low part in one
+    // operation (the scaling above keeps the split's products in range)
     const double hx = x * x, hy = y * y;
-    const double lx = xh * xh - hx + 2.0 * xh * xl + xl * xl;
-    const double ly = yh * yh - hy + 2.0 * yh * yl + yl * yl;
-    return z * sqrt(ly + lx + hy + hx);
+    const double lx = fma(x, x, -hx), ly = fma(y, y, -hy);
+    return z * vsqrt(ly + lx + hy + hx);
 }
 
 // DragCoefficient::compute (src/source/swe_2d/wind.rs:134-158) by its
@@ -733,14 +747,14 @@ DG_PT void atmosphere_source(double h, double u, double v, double px, double py,
     if (fp::lt(h, h_min)) return;
     const double speed = ref_hypot(u, v);
     const double stress = rho_air * drag_coefficient(drag, cd, speed) * speed;
-    su = (stress * u - h * px) / rho_water;
-    sv = (stress * v - h * py) / rho_water;
+    su = vdiv(stress * u - h * px, rho_water);
+    sv = vdiv(stress * v - h * py, rho_water);
 }
 
 // inverse_barometer_level (gridded_atmosphere.rs:198-202): −ramp·p/(ρ g),
 // g = 9.81 (the module's constant)
 DG_PT double inverse_barometer_level(double p, double ramp, double rho_water) {
-    return -ramp * p / (rho_water * 9.81);
+    return vdiv(-ramp * p, rho_water * 9.81);
 }
 
 }  // namespace DGSWE_NS
