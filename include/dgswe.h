@@ -578,7 +578,7 @@ int dgswe_planner_spread(dgswe_planner* planner, uint8_t* levels, int32_t limit,
                          const uint8_t* line_local, uint8_t* rates);
 
 /* Launch shapes of a handle's kernels, chosen by timing them on its own
- * mesh and state (the benchmark spec's autotuner): the face kernel's threads per
+ * mesh and state (an autotuner): the face kernel's threads per
  * block (64, 128 or 256) and the stage kernel's elements per block
  * (⌊128/(N+1)²⌋ at 5 blocks per SM, or ⌊64/(N+1)²⌋ at 10). The shapes change
  * no result (tests compare them bit for bit). No reference counterpart. */
