@@ -122,13 +122,93 @@ def coastal_bed(x: np.ndarray, y: np.ndarray, lx: float, ly: float, seed: int,
     radius = rng.uniform(island_radius[0], island_radius[1], n_islands)
     crest = rng.uniform(2.0, 20.0, n_islands)
     centre_depth = _bilinear_grid(depth_grid, spacing, cx, cy)
+    # an island adds nothing representable beyond 6.5 radii (e^-42.25 · 320 m
+    # < 1e-16 m), so each one visits only the points of the 2 km buckets
+    # within that reach
+    shape = np.shape(bed)
+    bed = np.array(bed, dtype=np.float64).reshape(-1)
+    px, py = np.asarray(x, np.float64).reshape(-1), np.asarray(y, np.float64).reshape(-1)
+    cell = 2000.0
+    ncx = int(lx / cell) + 2
+    ncy = int(ly / cell) + 2
+    bx = np.clip((px / cell).astype(np.int64), 0, ncx - 1)
+    by = np.clip((py / cell).astype(np.int64), 0, ncy - 1)
+    order = np.argsort(by * ncx + bx, kind="stable")
+    start = np.searchsorted((by * ncx + bx)[order], np.arange(ncx * ncy + 1))
     for i in range(n_islands):
-        r2 = (x - cx[i]) ** 2 + (y - cy[i]) ** 2
-        bed = bed + (centre_depth[i] + crest[i]) * np.exp(-r2 / radius[i] ** 2)
-    return bed
+        reach = 6.5 * radius[i]
+        i0 = max(0, int((cx[i] - reach) / cell))
+        i1 = min(ncx - 1, int((cx[i] + reach) / cell))
+        j0 = max(0, int((cy[i] - reach) / cell))
+        j1 = min(ncy - 1, int((cy[i] + reach) / cell))
+        if i0 > i1 or j0 > j1:
+            continue
+        idx = np.concatenate([order[start[j * ncx + i0]:start[j * ncx + i1 + 1]]
+                              for j in range(j0, j1 + 1)])
+        r2 = (px[idx] - cx[i]) ** 2 + (py[idx] - cy[i]) ** 2
+        bed[idx] = bed[idx] + (centre_depth[i] + crest[i]) * np.exp(-r2 / radius[i] ** 2)
+    return bed.reshape(shape)
 
 
 COASTAL_TIDE = (("M2", 1.0), ("S2", 0.35), ("N2", 0.2), ("K1", 0.1))
+
+# √area of the quads of an unrefined quadtree leaf is its side / (2√3); the
+# three levels of the coastal paving hold quads of 400, 200 and 100 m at the
+# default mean size (√(200 km · 150 km / 1 M) = 173.2 m)
+PAVING_MEAN = 173.2
+PAVING_COARSEST = 400.0
+
+
+def _paving_count(level: np.ndarray, max_level: int) -> int:
+    """Quads of :func:`mesh.quadtree_paving` on a balanced level field, without
+    building it: three per triangle, four triangles per leaf plus one per
+    leaf edge with a finer neighbour."""
+    leaves = float((0.25 ** (max_level - level)).sum())
+    splits = 0.0
+    for a, b in ((level[:, :-1], level[:, 1:]), (level[:-1, :], level[1:, :])):
+        coarse = np.minimum(a, b)
+        splits += float((0.5 ** (max_level - coarse))[a != b].sum())
+    return int(round(3.0 * (4.0 * leaves + splits)))
+
+
+def coastal_paving(n_elements: int, seed: int, lx: float, ly: float, n_islands: int = 30,
+                   island_radius: tuple[float, float] = (1000.0, 5000.0)):
+    """A depth-graded unstructured quad paving of lx × ly with about
+    ``n_elements`` quads: a three-level quadtree (quads of 400, 200 and
+    100 m × mean/173.2 m, mean = √(lx·ly/n_elements)) whose leaves are
+    finest over shallow water and land and coarsest over deep water — the
+    level of a cell follows u^γ (u = (depth − 2 m)/298 m clipped to [0, 1],
+    levels at u^γ < ¼ and < ¾), with γ found by bisection so that the count
+    comes closest to ``n_elements``. Walls on the south, east and north
+    sides, open to the west."""
+    from .mesh import quadtree_levels, quadtree_paving
+
+    max_level = 2
+    scale = math.sqrt(lx * ly / n_elements) / PAVING_MEAN
+    root = PAVING_COARSEST * 2.0 * math.sqrt(3.0) * scale
+    nx, ny = (max(1, int(round(lx / root))) << max_level, max(1, int(round(ly / root))) << max_level)
+    xc = (np.arange(nx) + 0.5) * (lx / nx)
+    yc = (np.arange(ny) + 0.5) * (ly / ny)
+    gx, gy = np.meshgrid(xc, yc)
+    depth = -coastal_bed(gx, gy, lx, ly, seed, n_islands, island_radius)
+    u = np.clip((depth - 2.0) / 298.0, 0.0, 1.0)
+
+    def desired(log_gamma):
+        w = u ** math.exp(log_gamma)
+        return np.where(w < 0.25, 2, np.where(w < 0.75, 1, 0))
+
+    lo, hi = -8.0, 8.0  # the count grows with γ
+    for _ in range(40):
+        mid = 0.5 * (lo + hi)
+        if _paving_count(quadtree_levels(desired(mid), max_level), max_level) < n_elements:
+            lo = mid
+        else:
+            hi = mid
+    best = min((lo, hi), key=lambda g: abs(
+        _paving_count(quadtree_levels(desired(g), max_level), max_level) - n_elements))
+    return quadtree_paving(lx, ly, desired(best), max_level,
+                           sides=(TAG_WALL, TAG_WALL, TAG_WALL, TAG_OPEN), jitter=0.1,
+                           seed=seed, smoothing=1)
 
 
 def coastal_box(n_elements: int = 1_000_000, order: int = 3, seed: int = 2026,
@@ -136,17 +216,12 @@ def coastal_box(n_elements: int = 1_000_000, order: int = 3, seed: int = 2026,
                 ly: float = 150_000.0, n_islands: int = 30,
                 island_radius: tuple[float, float] = (1000.0, 5000.0),
                 tide: tuple = COASTAL_TIDE, manning_n: float = 0.02) -> Case:
-    """The 1 M-quad coastal box: a graded, jittered quad paving of lx × ly
-    (element size 100–400 m at the default size), Hilbert-ordered, with the
-    seeded coastal bed, walls on three sides and a tide on the open western
-    side, Manning's n and Coriolis at 63° N, from rest."""
-    nx = max(2, int(round(math.sqrt(n_elements * lx / ly))))
-    ny = max(2, int(round(n_elements / nx)))
-    mean = lx / nx
-    mesh = graded_jittered_box(lx, ly, nx, ny, size_range=(100.0 * mean / 173.0,
-                                                           250.0 * mean / 173.0),
-                               jitter=0.15, seed=seed,
-                               sides=(TAG_WALL, TAG_WALL, TAG_WALL, TAG_OPEN))
+    """The 1 M-quad coastal box: an unstructured quad paving of lx × ly
+    (:func:`coastal_paving`, element size 100–400 m at the default size),
+    Hilbert-ordered, with the seeded coastal bed, walls on three sides and a
+    tide on the open western side, Manning's n and Coriolis at 63° N, from
+    rest."""
+    mesh = coastal_paving(n_elements, seed, lx, ly, n_islands, island_radius)
     mesh, _ = in_hilbert_order(mesh)
     form = SWEDeviceForm2D(mesh=mesh, order=order, numerics=numerics)
     x, y = node_positions(mesh, order)

@@ -255,6 +255,164 @@ def graded_jittered_box(lx: float, ly: float, nx: int, ny: int, size_range=(100.
     return QuadMesh(verts, elems, np.zeros((0, 4), np.int64), tags)
 
 
+# -- quadtree paving -------------------------------------------------------
+#
+# An unstructured all-quad mesh of a box with a graded element size: a
+# 2:1-balanced quadtree of square-ish cells whose leaf level follows a
+# requested level field, each leaf fanned into triangles from its centre
+# (one triangle per leaf edge, or two where a finer neighbour puts a hanging
+# vertex at the edge's midpoint), and every triangle split into three quads
+# through its centroid and edge midpoints. The mesh is conforming (every
+# triangle edge's midpoint is shared by both sides), its vertices have
+# valence 3 (centroids), 4 (edge midpoints) or 4–8 (cell corners and
+# centres), and the quads of one triangle have equal areas. Leaves of
+# level l hold quads of √area ≈ 0.289·C_l (0.204·C_l beside a finer
+# neighbour), C_l the leaf's side.
+
+
+def quadtree_levels(desired: np.ndarray, max_level: int) -> np.ndarray:
+    """Leaf level of every finest cell of a quadtree over ``desired`` (an
+    (ny, nx) field of requested levels 0..max_level on the finest grid,
+    both sides multiples of 2^max_level): a block is split while any cell
+    in it asks for a finer level, and then leaves are refined until edge
+    neighbours differ by at most one level (2:1 balance)."""
+    want = np.asarray(desired, np.int64)
+    ny, nx = want.shape
+    step = 1 << max_level
+    if ny % step or nx % step:
+        raise ValueError("the finest grid must hold whole root cells")
+
+    def quantised(d):
+        level = np.zeros_like(d)
+        for lv in range(max_level):
+            b = 1 << (max_level - lv)
+            split = d.reshape(ny // b, b, nx // b, b).max(axis=(1, 3)) > lv
+            level = np.where(np.repeat(np.repeat(split, b, axis=0), b, axis=1),
+                             np.maximum(level, lv + 1), level)
+        return level
+
+    level = quantised(want)
+    for _ in range(4 * max_level + 4):
+        around = level.copy()
+        around[1:, :] = np.maximum(around[1:, :], level[:-1, :])
+        around[:-1, :] = np.maximum(around[:-1, :], level[1:, :])
+        around[:, 1:] = np.maximum(around[:, 1:], level[:, :-1])
+        around[:, :-1] = np.maximum(around[:, :-1], level[:, 1:])
+        coarse = level < around - 1
+        if not coarse.any():
+            return level
+        want = np.maximum(np.where(coarse, around - 1, want), level)
+        level = quantised(want)
+    raise RuntimeError("quadtree balance did not settle")
+
+
+def _leaf_triangles(level: np.ndarray, max_level: int) -> np.ndarray:
+    """(n, 6) integer triangles (centre, then two boundary points, counter-
+    clockwise) of every leaf's fan, in half-finest-cell units."""
+    ny, nx = level.shape
+    out = []
+    for lv in range(max_level + 1):
+        b = 1 << (max_level - lv)
+        jj, ii = np.nonzero(level[::b, ::b] == lv)
+        i0, j0 = ii * b, jj * b
+
+        def finer(i, j, inside):
+            hit = np.zeros(i.size, bool)
+            hit[inside] = level[j[inside], i[inside]] > lv
+            return hit
+
+        # a finer leaf across an edge puts a vertex at the edge's midpoint
+        split = (finer(i0, j0 - 1, j0 > 0), finer(i0 + b, j0, i0 + b < nx),
+                 finer(i0, j0 + b, j0 + b < ny), finer(i0 - 1, j0, i0 > 0))
+        x0, y0, h = 2 * i0, 2 * j0, b
+        ring = ((x0, y0), (x0 + h, y0), (x0 + 2 * h, y0), (x0 + 2 * h, y0 + h),
+                (x0 + 2 * h, y0 + 2 * h), (x0 + h, y0 + 2 * h), (x0, y0 + 2 * h), (x0, y0 + h))
+        code = split[0] * 1 + split[1] * 2 + split[2] * 4 + split[3] * 8
+        for c in np.unique(code):
+            sel = code == c
+            seq = [k for k in range(8) if k % 2 == 0 or (c >> (k // 2)) & 1]
+            for a, z in zip(seq, seq[1:] + seq[:1]):
+                out.append(np.stack([x0[sel] + h, y0[sel] + h, ring[a][0][sel], ring[a][1][sel],
+                                     ring[z][0][sel], ring[z][1][sel]], axis=1))
+    return np.concatenate(out).astype(np.int64)
+
+
+def quadtree_paving(lx: float, ly: float, desired: np.ndarray, max_level: int,
+                    sides=(TAG_WALL, TAG_WALL, TAG_WALL, TAG_OPEN), jitter: float = 0.1,
+                    seed: int = 0, smoothing: int = 1) -> QuadMesh:
+    """The quadtree paving of [0, lx]×[0, ly] for the requested level field
+    ``desired`` ((ny, nx) on the finest grid; see :func:`quadtree_levels`).
+    Interior vertices get ``smoothing`` Laplacian passes, then a seeded
+    jitter of up to ``jitter`` × their shortest edge in each coordinate;
+    boundary vertices stay on the sides. ``sides`` tag the [south, east,
+    north, west] boundary faces. Raises if a Jacobian is not positive."""
+    level = quadtree_levels(desired, max_level)
+    ny, nx = level.shape
+    tri = _leaf_triangles(level, max_level) * 6  # 1/12 of a finest cell
+    a, b, c = tri[:, 0:2], tri[:, 2:4], tri[:, 4:6]
+    ab, bc, ca = (a + b) // 2, (b + c) // 2, (c + a) // 2
+    g = (a + b + c) // 3
+    quads = np.stack([np.stack([a, ab, g, ca], 1), np.stack([b, bc, g, ab], 1),
+                      np.stack([c, ca, g, bc], 1)], 1).reshape(-1, 4, 2)
+    top_x, top_y = 12 * nx, 12 * ny
+    key = quads[..., 0] * (top_y + 1) + quads[..., 1]
+    unique, inverse = np.unique(key, return_inverse=True)
+    elements = inverse.reshape(-1, 4).astype(np.int64)
+    ix, iy = unique // (top_y + 1), unique % (top_y + 1)
+    on_side = (iy == 0, ix == top_x, iy == top_y, ix == 0)
+    boundary = on_side[0] | on_side[1] | on_side[2] | on_side[3]
+    tags = np.zeros(elements.shape, np.int32)
+    for f in range(4):
+        p, q = elements[:, f], elements[:, (f + 1) % 4]
+        for side in range(4):
+            tags[on_side[side][p] & on_side[side][q], f] = sides[side]
+    verts = np.stack([ix * (lx / top_x), iy * (ly / top_y)], axis=1)
+    e0 = elements.reshape(-1)
+    e1 = np.roll(elements, -1, axis=1).reshape(-1)
+    for _ in range(smoothing):
+        total = np.zeros_like(verts)
+        count = np.zeros(verts.shape[0])
+        np.add.at(total, e0, verts[e1])
+        np.add.at(total, e1, verts[e0])
+        np.add.at(count, e0, 1.0)
+        np.add.at(count, e1, 1.0)
+        verts = np.where(boundary[:, None], verts, total / count[:, None])
+    if jitter > 0.0:
+        rng = np.random.default_rng(seed)
+        shortest = np.full(verts.shape[0], np.inf)
+        edge = np.linalg.norm(verts[e1] - verts[e0], axis=1)
+        np.minimum.at(shortest, e0, edge)
+        np.minimum.at(shortest, e1, edge)
+        moved = verts + rng.uniform(-jitter, jitter, verts.shape) * shortest[:, None]
+        verts = np.where(boundary[:, None], verts, moved)
+    mesh = QuadMesh(verts, elements, np.zeros((0, 4), np.int64), tags)
+    if corner_jacobians(mesh).min() <= 0.0:
+        raise RuntimeError("quadtree paving: a Jacobian is not positive")
+    return mesh
+
+
+def corner_jacobians(mesh: QuadMesh) -> np.ndarray:
+    """(n_elements, 4) cross products of the two edges at each corner; a
+    bilinear quad's Jacobian is positive everywhere when these are."""
+    p = mesh.corners()
+    nxt = np.roll(p, -1, axis=1) - p
+    prv = np.roll(p, 1, axis=1) - p
+    return nxt[..., 0] * prv[..., 1] - nxt[..., 1] * prv[..., 0]
+
+
+def element_shape(mesh: QuadMesh) -> tuple[np.ndarray, np.ndarray]:
+    """(√area, stretch) of every element: the stretch is the ratio of the
+    singular values of the bilinear map's Jacobian at the element centre
+    (1 for a square, the side ratio for a rectangle)."""
+    p = mesh.corners()
+    xr = 0.5 * ((p[:, 1] - p[:, 0]) + (p[:, 2] - p[:, 3]))
+    xs = 0.5 * ((p[:, 3] - p[:, 0]) + (p[:, 2] - p[:, 1]))
+    sv = np.linalg.svd(np.stack([xr, xs], axis=2), compute_uv=False)
+    nxt = np.roll(p, -1, axis=1)
+    area = 0.5 * np.abs((p[..., 0] * nxt[..., 1] - nxt[..., 0] * p[..., 1]).sum(axis=1))
+    return np.sqrt(area), sv[:, 0] / sv[:, 1]
+
+
 def node_mass(mesh: QuadMesh, order: int) -> np.ndarray:
     """GLL weight × J at every node, (n_elements, (N+1)²): the diagonal mass
     matrix of GeometricFactors2D::compute (src/operators/geometric.rs:160-176)."""

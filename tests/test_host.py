@@ -122,3 +122,42 @@ def test_reverse_point_functions_match_finite_differences(tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True)
     assert out.returncode == 0, out.stdout + out.stderr
     assert out.stdout.strip().endswith("all ok")
+
+
+def test_coastal_paving_is_an_unstructured_conforming_quad_mesh():
+    """The coastal box's mesh: about the requested count, every interior
+    edge shared by exactly two elements in opposite directions, positive
+    Jacobians, the stretch below 3, element sizes over the three levels,
+    vertex valences other than 4 (not a tensor grid), and the sides
+    tagged (walls south, east and north, open to the west)."""
+    from dgcom_gb300.mesh import TAG_OPEN, TAG_WALL, corner_jacobians, element_shape
+
+    lx, ly = 200_000.0, 150_000.0
+    mesh = cases.coastal_paving(40_000, 2026, lx, ly)
+    assert abs(mesh.n_elements - 40_000) <= 400
+    e = mesh.elements
+    a, b = e.reshape(-1), np.roll(e, -1, axis=1).reshape(-1)
+    fwd = {(int(p), int(q)) for p, q in zip(a, b)}
+    assert len(fwd) == a.size  # no directed edge twice (orientation is consistent)
+    interior = [(p, q) for p, q in fwd if (q, p) in fwd]
+    boundary = [(p, q) for p, q in fwd if (q, p) not in fwd]
+    assert len(interior) + len(boundary) == a.size
+    v = mesh.vertices
+    on_box = lambda i: (v[i, 0] in (0.0, lx)) or (v[i, 1] in (0.0, ly))  # noqa: E731
+    assert all(on_box(p) and on_box(q) for p, q in boundary)
+    # boundary faces tagged by side; the west side open
+    tag_of = {}
+    for k in range(mesh.n_elements):
+        for f in range(4):
+            tag_of[(int(e[k, f]), int(e[k, (f + 1) % 4]))] = int(mesh.face_tags[k, f])
+    for p, q in boundary:
+        west = v[p, 0] == 0.0 and v[q, 0] == 0.0
+        assert tag_of[(p, q)] == (TAG_OPEN if west else TAG_WALL)
+    assert corner_jacobians(mesh).min() > 0.0
+    size, stretch = element_shape(mesh)
+    assert stretch.max() < 3.0
+    mean = np.sqrt(lx * ly / 40_000)
+    lo, hi = np.percentile(size, [1, 99]) / mean * 173.2
+    assert 70.0 < lo < 130.0 and 330.0 < hi < 470.0, (lo, hi)
+    valence = np.bincount(a, minlength=v.shape[0])
+    assert (valence == 3).any() and (valence > 4).any()
