@@ -1,38 +1,45 @@
-"""Gmsh mesh files: how real coastline-fitted domains reach the device path.
+"""Gmsh meshes for the device path: how coastline-fitted domains made in
+Gmsh reach the C ABI.
 
-Reads MSH 4.1 (ASCII and binary, either byte order) and MSH 2.2 (ASCII);
-writes MSH 2.2 (ASCII). The behaviour is the reference reader's
-(src/mesh/io/gmsh.rs):
+The reader takes the MSH 4.1 format (text, or binary in either byte order
+with 4- or 8-byte sizes) and the MSH 2.2 text format, following Gmsh's
+published file-format description; the writer writes MSH 2.2 text. What it
+accepts and refuses is what the reference's reader does
+(src/mesh/io/gmsh.rs), as the reference's tests pin it:
 
-- the mesh is first-order quadrilaterals (Gmsh type 3). Any other element
-  type is an error that counts them by type, with the Gmsh options that
-  give an all-quad first-order 2D mesh; points (type 15) are ignored and
-  2-node lines (type 1) carry boundary tags;
-- node tags may be sparse and in any order; the vertices are the nodes the
-  quadrilaterals use, in file order; clockwise quadrilaterals are turned
-  counter-clockwise; a degenerate or non-convex one (a non-positive
-  bilinear Jacobian at a corner), an edge of more than two elements and
-  two elements traversing their shared edge the same way are errors;
-- a boundary edge takes the tag of the physical groups of the line on it
-  (MSH 4.1: the groups of the line's curve entity; MSH 2.2: the line's
-  first tag): a named group by its name (``group_boundary_tag``), an
-  unnamed one by its number (1 wall, 2 open, 3 tidal, 4 river,
-  5 Dirichlet, 6 Neumann, other n custom). Untagged boundary edges are
-  walls; groups of one line that map to different tags, an edge with two
-  different tags, and a line that is not an edge of the mesh are errors;
-  lines on interior edges are ignored;
-- MSH 4.0, binary MSH 2, ``$Periodic`` and ``$PartitionedEntities`` are
-  errors; other sections are skipped; CRLF line ends are read;
-- the mesh comes back in Hilbert order (``mesh.in_hilbert_order``).
+- the domain is first-order quadrilaterals (Gmsh type 3); points (type 15)
+  are ignored, 2-node lines (type 1) carry boundary tags, and any other
+  element type is refused with a count per type and the Gmsh settings that
+  give an all-quad first-order mesh;
+- node tags may be sparse and unordered; the vertices are the nodes the
+  quadrilaterals use, in the order the file gives them; a clockwise
+  quadrilateral is turned round; a corner with a non-positive bilinear
+  Jacobian, an edge of three or more elements and two elements running the
+  same way along their common edge are refused;
+- a boundary edge takes the tag of the physical groups of the line element
+  on it (MSH 4.1: the groups of the line's curve entity; MSH 2.2: the
+  line's first integer tag), by group name where the group has one, else by
+  number (1 wall, 2 open, 3 tidal, 4 river, 5 Dirichlet, 6 Neumann, n
+  custom); untagged boundary edges are walls; lines on interior edges are
+  ignored; a line that is no edge of the mesh, a curve whose groups give two
+  tags and an edge given two tags are refused;
+- MSH 4.0, binary MSH 2, periodic and partitioned meshes are refused; other
+  sections are skipped; CRLF line ends are read;
+- the mesh is returned in Hilbert order (``mesh.in_hilbert_order``).
 
-Errors are ``GmshError`` subclasses named after the reference's variants.
-Tags are the ABI's face tags (``mesh.TAG_*``, ``mesh.custom_tag``)."""
+How it reads. The file is cut into its ``$Name … $EndName`` sections
+first. Each section that matters is decoded from one stream of numbers: a
+text section is split into tokens once and converted in bulk, a binary
+section is read through a byte cursor with ``numpy.frombuffer``; node and
+element blocks come out as arrays, never one number at a time. Mesh checks
+then run on whole arrays. Tags are the ABI's face tags (``mesh.TAG_*``,
+``mesh.custom_tag``)."""
 
 from __future__ import annotations
 
-import itertools
 import re
 import struct
+from dataclasses import dataclass, field
 from pathlib import Path
 
 import numpy as np
@@ -41,700 +48,806 @@ from .mesh import (CUSTOM_TAG_BASE, TAG_DIRICHLET, TAG_NEUMANN, TAG_OPEN, TAG_RI
                    TAG_WALL, QuadMesh, custom_tag, in_hilbert_order)
 
 
+# -- errors -------------------------------------------------------------------
+
 class GmshError(ValueError):
-    """A Gmsh file the device path cannot take (GmshError, gmsh.rs:82-111)."""
+    """Any Gmsh file the device path cannot take."""
 
 
 class GmshParseError(GmshError):
-    """Malformed file: a bad number, a truncated section, a missing end marker."""
+    """The bytes do not follow the format (a bad number, a short section)."""
 
 
 class UnsupportedVersion(GmshError):
-    pass
-
-
-class UnsupportedElements(GmshError):
-    """Element types the solver cannot use; ``counts`` = [(type, count)]."""
-
-    def __init__(self, counts):
-        self.counts = [(int(t), int(n)) for t, n in counts]
-        parts = []
-        for t, n in self.counts:
-            name = ELEMENT_TYPES.get(t, (0, "unknown element"))[1]
-            parts.append(f"{n} × {name} (type {t})")
-        super().__init__(
-            f"unsupported Gmsh elements: {', '.join(parts)}. The device path takes 2D meshes of "
-            "first-order quadrilaterals; in Gmsh, mesh in 2D with Mesh.ElementOrder = 1 and "
-            "recombine and subdivide to all quads (Mesh.RecombineAll = 1; "
-            "Mesh.SubdivisionAlgorithm = 1)")
-
-
-class GmshUnsupported(GmshError):
-    """A file feature the reader does not take (periodic, partitioned)."""
+    """A format version other than MSH 4.1 and MSH 2.x text."""
 
 
 class MissingSection(GmshError):
-    pass
+    """A section the mesh needs is absent."""
+
+
+class GmshUnsupported(GmshError):
+    """A feature of the format the device path has no use for."""
 
 
 class InvalidMesh(GmshError):
-    """The file parses but is not a valid quadrilateral mesh."""
+    """The file reads, but its elements do not form a usable quad mesh."""
 
 
-# Gmsh's fixed-order element types: node count and name
-ELEMENT_TYPES = {
-    1: (2, "2-node line"), 2: (3, "3-node triangle"), 3: (4, "4-node quadrangle"),
-    4: (4, "4-node tetrahedron"), 5: (8, "8-node hexahedron"), 6: (6, "6-node prism"),
-    7: (5, "5-node pyramid"), 8: (3, "3-node line"), 9: (6, "6-node triangle"),
-    10: (9, "9-node quadrangle"), 11: (10, "10-node tetrahedron"),
-    12: (27, "27-node hexahedron"), 13: (18, "18-node prism"), 14: (14, "14-node pyramid"),
-    15: (1, "1-node point"), 16: (8, "8-node quadrangle"), 17: (20, "20-node hexahedron"),
-    18: (15, "15-node prism"), 19: (13, "13-node pyramid"), 20: (9, "9-node triangle"),
-    21: (10, "10-node triangle"), 22: (12, "12-node triangle"), 23: (15, "15-node triangle"),
-    24: (15, "15-node incomplete triangle"), 25: (21, "21-node triangle"),
-    26: (4, "4-node line"), 27: (5, "5-node line"), 28: (6, "6-node line"),
-    29: (20, "20-node tetrahedron"), 30: (35, "35-node tetrahedron"),
-    31: (56, "56-node tetrahedron"), 36: (16, "16-node quadrangle"),
-    37: (25, "25-node quadrangle"), 38: (36, "36-node quadrangle"),
+class UnsupportedElements(GmshError):
+    """Elements other than quadrilaterals, lines and points; ``counts``
+    holds (Gmsh type, how many) in type order."""
+
+    def __init__(self, counts):
+        self.counts = sorted((int(t), int(n)) for t, n in counts)
+        listed = ", ".join(f"{n} × {_type_name(t)} (type {t})" for t, n in self.counts)
+        super().__init__(
+            f"the mesh holds {listed}, and the device path takes first-order "
+            "quadrilaterals only. In Gmsh: Mesh.ElementOrder = 1, Mesh.RecombineAll = 1 "
+            "and Mesh.SubdivisionAlgorithm = 1 give an all-quad 2D mesh")
+
+
+# -- element types and physical groups -------------------------------------------
+
+# Nodes per element of Gmsh's fixed-order element types (the format's table)
+NODES_PER_TYPE = {
+    1: 2, 2: 3, 3: 4, 4: 4, 5: 8, 6: 6, 7: 5, 8: 3, 9: 6, 10: 9, 11: 10, 12: 27, 13: 18,
+    14: 14, 15: 1, 16: 8, 17: 20, 18: 15, 19: 13, 20: 9, 21: 10, 22: 12, 23: 15, 24: 15,
+    25: 21, 26: 4, 27: 5, 28: 6, 29: 20, 30: 35, 31: 56, 36: 16, 37: 25, 38: 36,
 }
-LINE, QUAD, POINT = 1, 3, 15
+_SHAPES = {1: "line", 8: "line", 26: "line", 27: "line", 28: "line", 15: "point",
+           2: "triangle", 9: "triangle", 20: "triangle", 21: "triangle", 22: "triangle",
+           23: "triangle", 24: "incomplete triangle", 25: "triangle",
+           3: "quadrangle", 10: "quadrangle", 16: "quadrangle", 36: "quadrangle",
+           37: "quadrangle", 38: "quadrangle", 4: "tetrahedron", 11: "tetrahedron",
+           29: "tetrahedron", 30: "tetrahedron", 31: "tetrahedron", 5: "hexahedron",
+           12: "hexahedron", 17: "hexahedron", 6: "prism", 13: "prism", 18: "prism",
+           7: "pyramid", 14: "pyramid", 19: "pyramid"}
+T_LINE, T_QUAD, T_POINT = 1, 3, 15
 
-_NAMED = {}
-for _tag, _names in ((TAG_WALL, "wall walls land coast coastline shore shoreline closed"),
-                     (TAG_OPEN, "open ocean sea open_boundary"),
-                     (TAG_TIDAL, "tidal tide tides tidal_forcing"),
-                     (TAG_RIVER, "river rivers")):
-    for _n in _names.split():
-        _NAMED[_n] = _tag
-_NUMBERED = {1: TAG_WALL, 2: TAG_OPEN, 3: TAG_TIDAL, 4: TAG_RIVER, 5: TAG_DIRICHLET,
-             6: TAG_NEUMANN}
+
+def _type_name(t: int) -> str:
+    if t not in NODES_PER_TYPE:
+        return "element of an unknown type"
+    return f"{NODES_PER_TYPE[t]}-node {_SHAPES[t]}"
+
+
+# group names, compared lower-case with spaces and dashes read as "_"
+_BY_NAME = {
+    **dict.fromkeys(("wall", "walls", "land", "coast", "coastline", "shore", "shoreline",
+                     "closed"), TAG_WALL),
+    **dict.fromkeys(("open", "ocean", "sea", "open_boundary"), TAG_OPEN),
+    **dict.fromkeys(("tidal", "tide", "tides", "tidal_forcing"), TAG_TIDAL),
+    **dict.fromkeys(("river", "rivers"), TAG_RIVER),
+}
+_BY_NUMBER = (TAG_WALL, TAG_OPEN, TAG_TIDAL, TAG_RIVER, TAG_DIRICHLET, TAG_NEUMANN)  # 1..6
+_TAG_NAMES = {TAG_WALL: "Wall", TAG_OPEN: "Open", TAG_TIDAL: "TidalForcing", TAG_RIVER: "River",
+              TAG_DIRICHLET: "Dirichlet", TAG_NEUMANN: "Neumann"}
 
 
 def group_boundary_tag(number: int, name: str | None) -> int:
-    """The face tag of a physical group: by its name (case-insensitive,
-    spaces and dashes read as ``_``) if it has one, else by its number."""
+    """The face tag a physical group stands for: by its name where it has
+    one that means something, else by its number."""
     if number < 0:
-        raise InvalidMesh(f"negative physical group tag {number}")
-    if name is None:
-        return _NUMBERED.get(number, custom_tag(number))
-    key = name.lower().replace(" ", "_").replace("-", "_")
-    return _NAMED.get(key, custom_tag(number))
+        raise InvalidMesh(f"physical group {number}: group numbers are not negative")
+    if name is not None:
+        key = re.sub(r"[ \-]", "_", name.lower())
+        if key in _BY_NAME:
+            return _BY_NAME[key]
+    if 1 <= number <= len(_BY_NUMBER):
+        return _BY_NUMBER[number - 1]
+    return custom_tag(number)
 
 
 def tag_to_physical(tag: int) -> int:
-    """The physical group number a face tag is written with."""
-    for number, t in _NUMBERED.items():
-        if t == tag:
-            return number
+    """The physical group number a face tag is written under (the inverse of
+    :func:`group_boundary_tag` for unnamed groups)."""
+    if tag in _BY_NUMBER:
+        return _BY_NUMBER.index(tag) + 1
     if tag >= CUSTOM_TAG_BASE:
         return tag - CUSTOM_TAG_BASE
-    raise ValueError(f"face tag {tag} has no Gmsh physical group")
+    raise ValueError(f"face tag {tag} has no physical group number")
 
 
 def tag_name(tag: int) -> str:
-    names = {TAG_WALL: "Wall", TAG_OPEN: "Open", TAG_TIDAL: "TidalForcing", TAG_RIVER: "River",
-             TAG_DIRICHLET: "Dirichlet", TAG_NEUMANN: "Neumann"}
-    return names.get(tag, f"Custom({tag - CUSTOM_TAG_BASE})")
+    return _TAG_NAMES.get(tag, f"Custom({tag - CUSTOM_TAG_BASE})")
 
 
-# ---------------------------------------------------------------------------
-# Reading tokens and binary values
-# ---------------------------------------------------------------------------
+# -- cutting the file into sections ---------------------------------------------------
 
-_TOKEN = re.compile(rb"\S+")
-_INT_OK = re.compile(rb"[+-]?[0-9]+\Z")
-_FLOAT_OK = re.compile(rb"[+-]?(?:[0-9]+\.?[0-9]*(?:[eE][+-]?[0-9]+)?|\.[0-9]+(?:[eE][+-]?[0-9]+)?"
-                       rb"|inf|infinity|nan)\Z", re.IGNORECASE)
+@dataclass
+class _Section:
+    name: str
+    start: int   # first byte of the payload (after the header line)
+    stop: int    # first byte of "$End<name>"
 
 
-class _Reader:
-    def __init__(self, buf: bytes):
-        self.buf = buf
-        self.pos = 0
+_BINARY_SECTIONS = ("Entities", "Nodes", "Elements")
+
+
+def _line_of(data: bytes, pos: int) -> int:
+    return 1 + data.count(b"\n", 0, pos)
+
+
+def _header_at(data: bytes, pos: int) -> tuple[str, int]:
+    """The section name of the header line at ``pos`` and where its payload
+    starts."""
+    end = data.find(b"\n", pos)
+    end = len(data) if end < 0 else end
+    text = data[pos:end].strip()
+    if not text.startswith(b"$") or len(text) < 2:
+        shown = text[:40].decode("ascii", "replace")
+        raise GmshParseError(f"line {_line_of(data, pos)}: a section header ($Name) was due, "
+                             f'not "{shown}"')
+    return text[1:].decode("ascii", "replace"), min(end + 1, len(data))
+
+
+def _skip_space(data: bytes, pos: int) -> int:
+    while pos < len(data) and data[pos] in b" \t\r\n":
+        pos += 1
+    return pos
+
+
+class _Layout:
+    """What the format line said: text or binary, byte order, size width."""
+
+    def __init__(self):
+        self.version: str | None = None  # "4.1" or "2"
         self.binary = False
-        self.big_endian = False
+        self.order = "<"
         self.size_bytes = 8
 
-    def error(self, msg: str) -> GmshParseError:
-        line = 1 + self.buf.count(b"\n", 0, self.pos)
-        return GmshParseError(f"{msg} (line {line}, byte {self.pos})")
 
-    def at_end(self) -> bool:
-        m = _TOKEN.search(self.buf, self.pos)
-        if m is None:
-            self.pos = len(self.buf)
-            return True
-        self.pos = m.start()
-        return False
+def _cut(data: bytes, layout: _Layout, decode) -> None:
+    """Walk the sections in file order, handing each to ``decode(section,
+    stream)``. A text section ends at its ``$End`` line; a binary 4.1
+    section ends where its decoder stops reading."""
+    pos = _skip_space(data, 0)
+    while pos < len(data):
+        name, start = _header_at(data, pos)
+        marker = f"$End{name}".encode()
+        if layout.binary and name in _BINARY_SECTIONS:
+            stream = _BinaryStream(data, start, layout)
+            decode(_Section(name, start, -1), stream)
+            stop = _skip_space(data, stream.pos)
+        else:
+            if name == "MeshFormat":  # the version decides before anything else
+                _read_format(data, start, layout)
+            stop = _find_marker(data, start, marker)
+            if stop < 0:
+                raise GmshParseError(f"line {_line_of(data, start)}: ${name} has no {marker.decode()}")
+            if name != "MeshFormat":
+                decode(_Section(name, start, stop), _TextStream(data, start, stop))
+        if not data.startswith(marker, stop) or (len(data) > stop + len(marker)
+                                                 and data[stop + len(marker)] not in b" \t\r\n"):
+            raise GmshParseError(f"line {_line_of(data, stop)}: {marker.decode()} was due")
+        pos = _skip_space(data, stop + len(marker))
 
-    def token(self, what: str) -> bytes:
-        m = _TOKEN.search(self.buf, self.pos)
-        if m is None:
-            self.pos = len(self.buf)
-            raise self.error(f"unexpected end of file, expected {what}")
-        self.pos = m.end()
-        return m.group()
 
-    def _bad(self, what: str, tok: bytes) -> GmshParseError:
-        return self.error(f'invalid {what}: "{tok.decode("ascii", "replace")}"')
-
-    def ascii_int(self, what: str, unsigned: bool = False) -> int:
-        tok = self.token(what)
-        if not _INT_OK.match(tok) or (unsigned and tok.startswith(b"-")):
-            raise self._bad(what, tok)
-        return int(tok)
-
-    def ascii_float(self, what: str) -> float:
-        tok = self.token(what)
-        if not _FLOAT_OK.match(tok):
-            raise self._bad(what, tok)
-        return float(tok)
-
-    def line(self) -> str:
-        end = self.buf.find(b"\n", self.pos)
-        if end < 0:
-            end = len(self.buf)
-        text = self.buf[self.pos:end]
-        self.pos = min(end + 1, len(self.buf))
-        try:
-            return text.decode("utf-8").rstrip("\r")
-        except UnicodeDecodeError:
-            raise self.error("invalid text: not UTF-8") from None
-
-    def expect(self, expected: str):
-        tok = self.token(expected)
-        if tok != expected.encode():
-            raise self.error(f'expected {expected}, found "{tok.decode("ascii", "replace")}"')
-
-    def skip_section(self, name: str):
-        end = f"$End{name}".encode()
-        at = self.buf.find(end, self.pos)
+def _find_marker(data: bytes, start: int, marker: bytes) -> int:
+    """The first line holding ``marker`` alone at or after ``start``."""
+    at = start
+    while True:
+        at = data.find(marker, at)
         if at < 0:
-            raise self.error(f"missing $End{name}")
-        self.pos = at + len(end)
+            return -1
+        before_ok = at == 0 or data[at - 1] in b"\r\n"
+        end = at + len(marker)
+        after_ok = end == len(data) or data[end] in b" \t\r\n"
+        if before_ok and after_ok:
+            return at
+        at += 1
 
-    def raw(self, n: int, what: str) -> bytes:
-        if self.pos + n > len(self.buf):
-            raise self.error(f"unexpected end of file, expected {what}")
-        out = self.buf[self.pos:self.pos + n]
-        self.pos += n
+
+def _read_format(data: bytes, start: int, layout: _Layout) -> None:
+    eol = data.find(b"\n", start)
+    words = data[start:len(data) if eol < 0 else eol].split()
+    if len(words) < 3:
+        raise GmshParseError(f"line {_line_of(data, start)}: the format line needs a version, "
+                             "a file type and a data size")
+    version = words[0].decode("ascii", "replace")
+    try:
+        file_type, size = int(words[1]), int(words[2])
+    except ValueError:
+        raise GmshParseError(f"line {_line_of(data, start)}: the format line's file type and "
+                             "data size are integers") from None
+    if version == "4.1":
+        layout.version = "4.1"
+    elif version.startswith("2."):
+        layout.version = "2"
+    elif version.startswith("4"):
+        raise UnsupportedVersion(f"MSH {version} is not read: save the mesh as MSH 4.1 "
+                                 "(Mesh.MshFileVersion = 4.1) or MSH 2.2")
+    else:
+        raise UnsupportedVersion(f"MSH {version} is not read (MSH 4.1 and 2.2 are)")
+    if file_type == 0:
+        return
+    if file_type != 1:
+        raise GmshParseError(f"line {_line_of(data, start)}: file type {file_type} is neither "
+                             "text (0) nor binary (1)")
+    if layout.version != "4.1":
+        raise UnsupportedVersion("binary MSH 2 is not read: save the mesh as text or as MSH 4.1")
+    if size not in (4, 8):
+        raise GmshParseError(f"line {_line_of(data, start)}: sizes of {size} bytes (4 or 8 are "
+                             "written by Gmsh)")
+    # the binary marker: the integer 1 in the file's byte order, after the line
+    eol = data.find(b"\n", start)
+    mark = data[eol + 1:eol + 5] if eol >= 0 else b""
+    if mark == struct.pack("<i", 1):
+        layout.order = "<"
+    elif mark == struct.pack(">i", 1):
+        layout.order = ">"
+    else:
+        raise GmshParseError(f"line {_line_of(data, start)}: the binary marker (the integer 1) "
+                             "is missing")
+    layout.binary = True
+    layout.size_bytes = size
+
+
+# -- number streams ----------------------------------------------------------------------
+
+_INT = re.compile(rb"[+-]?\d+\Z")
+
+
+class _TextStream:
+    """The numbers of one text section, split into tokens once; ``ints``,
+    ``sizes`` and ``reals`` convert the next n in bulk and name the first
+    bad one (with its line) when a conversion fails."""
+
+    def __init__(self, data: bytes, start: int, stop: int):
+        self.data, self.start = data, start
+        self.tokens = data[start:stop].split()
+        self.at = 0
+
+    def _take(self, n: int, what) -> list:
+        if n < 0 or self.at + n > len(self.tokens):
+            name = what if isinstance(what, str) else what[0]
+            raise GmshParseError(f"line {_line_of(self.data, self.start)}: the section ends "
+                                 f"before its {name} values")
+        toks = self.tokens[self.at:self.at + n]
+        self.at += n
+        return toks
+
+    def _bad(self, index: int, what) -> GmshParseError:
+        names = (what,) if isinstance(what, str) else what
+        k = 0
+        for k, m in enumerate(re.finditer(rb"\S+", self.data[self.start:])):
+            if k == index:
+                line = _line_of(self.data, self.start + m.start())
+                name = names[(index - self._first) % len(names)]
+                return GmshParseError(f'invalid {name}: "{m.group().decode("ascii", "replace")}" '
+                                      f"(line {line}, token {index + 1} of the section)")
+        return GmshParseError(f"invalid {names[0]}")
+
+    def ints(self, n: int, what, nonnegative: bool = False) -> np.ndarray:
+        self._first = self.at
+        toks = self._take(n, what)
+        try:
+            out = np.array(toks, dtype=object).astype(np.int64) if n else np.zeros(0, np.int64)
+        except (ValueError, OverflowError):
+            out = None
+        if out is None or not all(_INT.match(t) for t in toks) or (nonnegative and (out < 0).any()):
+            for i, t in enumerate(toks):
+                if not _INT.match(t) or (nonnegative and t.startswith(b"-")):
+                    raise self._bad(self._first + i, what)
         return out
 
-    def _array(self, n: int, code: str, what: str) -> np.ndarray:
-        dtype = np.dtype(code).newbyteorder(">" if self.big_endian else "<")
-        data = self.raw(n * dtype.itemsize, what)
-        return np.frombuffer(data, dtype=dtype).astype(np.dtype(code).newbyteorder("="))
+    sizes = ints
 
-    # int: 4-byte binary or a token; size: size_t (4 or 8 bytes) or a token
-    def int(self, what: str) -> int:
-        if self.binary:
-            return int(self._array(1, "i4", what)[0])
-        return self.ascii_int(what)
-
-    def size(self, what: str) -> int:
-        if self.binary:
-            return int(self._array(1, "u4" if self.size_bytes == 4 else "u8", what)[0])
-        return self.ascii_int(what, unsigned=True)
-
-    def count(self, what: str, min_bytes: int) -> int:
-        """A count bounded by what the rest of the file can hold, so that a
-        corrupt count cannot ask for a huge allocation."""
-        n = self.size(what)
-        room = (len(self.buf) - self.pos) // max(min_bytes, 1) + 1
-        if n > room:
-            raise self.error(f"{what} {n} exceeds the file size")
-        return n
-
-    def double(self, what: str) -> float:
-        if self.binary:
-            return float(self._array(1, "f8", what)[0])
-        return self.ascii_float(what)
-
-    def sizes(self, n: int, what: str) -> np.ndarray:
-        if self.binary:
-            return self._array(n, "u4" if self.size_bytes == 4 else "u8", what).astype(np.int64)
-        return self._ascii_many(n, (what,), True)
-
-    def doubles(self, n: int, whats: tuple[str, ...]) -> np.ndarray:
-        if self.binary:
-            return self._array(n, "f8", whats[0])
-        return self._ascii_many(n, whats, False)
-
-    def _ascii_many(self, n: int, whats: tuple[str, ...], integer: bool) -> np.ndarray:
-        """n tokens, the k-th named whats[k % len(whats)] in messages."""
-        matches = list(itertools.islice(_TOKEN.finditer(self.buf, self.pos), n))
-        if len(matches) < n:
-            self.pos = len(self.buf)
-            raise self.error(f"unexpected end of file, expected {whats[len(matches) % len(whats)]}")
-        toks = [m.group() for m in matches]
-        ok = _INT_OK if integer else _FLOAT_OK
+    def reals(self, n: int, what) -> np.ndarray:
+        self._first = self.at
+        toks = self._take(n, what)
         try:
-            arr = np.array(toks).astype(np.int64 if integer else np.float64)
-            bad = (not all(ok.match(t) for t in toks)) or (integer and bool((arr < 0).any()))
-        except (ValueError, OverflowError):
-            bad = True
-        if bad:
-            for k, (m, t) in enumerate(zip(matches, toks)):
-                if not ok.match(t) or (integer and t.startswith(b"-")):
-                    self.pos = m.end()
-                    raise self._bad(whats[k % len(whats)], t)
-        self.pos = matches[-1].end() if matches else self.pos
-        return arr if n else np.zeros(0, np.int64 if integer else np.float64)
+            return np.array(toks, dtype=np.bytes_).astype(np.float64) if n else np.zeros(0)
+        except ValueError:
+            for i, t in enumerate(toks):
+                try:
+                    float(t)
+                except ValueError:
+                    raise self._bad(self._first + i, what) from None
+            raise GmshParseError(f"invalid {what}") from None
+
+    def rest_text(self) -> str:
+        return self.data[self.start:].decode("utf-8", "replace")
 
 
-# ---------------------------------------------------------------------------
-# Sections
-# ---------------------------------------------------------------------------
+class _BinaryStream:
+    """A byte cursor over a binary MSH 4.1 section: int32 values, size_t
+    values of the file's width, float64 values, all in its byte order."""
 
-class _Raw:
-    def __init__(self):
-        self.node_tags: list[np.ndarray] = []
-        self.node_xy: list[np.ndarray] = []
-        self.quads: list[tuple[int, list[int]]] = []        # (element tag, node tags)
-        self.lines: list[tuple[int, list[int], tuple]] = []  # (tag, nodes, groups)
-        self.names: dict[tuple[int, int], str] = {}
-        self.curve_groups: dict[int, list[int]] = {}
-        self.unsupported: dict[int, int] = {}
+    def __init__(self, data: bytes, start: int, layout: _Layout):
+        self.data, self.pos = data, start
+        self.order = layout.order
+        self.size_code = "u4" if layout.size_bytes == 4 else "u8"
 
-    def add_block(self, etype: int, tags: np.ndarray, nodes: np.ndarray, groups):
-        if etype == QUAD:
-            self.quads.extend(zip(tags.tolist(), nodes.tolist()))
-        elif etype == LINE:
-            self.lines.extend((t, n, groups) for t, n in zip(tags.tolist(), nodes.tolist()))
-        elif etype != POINT:
-            self.unsupported[etype] = self.unsupported.get(etype, 0) + len(tags)
+    def _array(self, n: int, code: str, what) -> np.ndarray:
+        dtype = np.dtype(self.order + code)
+        need = n * dtype.itemsize
+        if n < 0 or self.pos + need > len(self.data):
+            name = what if isinstance(what, str) else what[0]
+            raise GmshParseError(f"byte {self.pos}: the file ends before its {name} values")
+        out = np.frombuffer(self.data, dtype=dtype, count=n, offset=self.pos)
+        self.pos += need
+        return out.astype(dtype.newbyteorder("="))
 
-    def push_nodes(self, r: _Reader, tags: np.ndarray, xy: np.ndarray):
-        finite = np.isfinite(xy).all(axis=1)
-        if not finite.all():
-            k = int(np.argmin(finite))
-            raise r.error(f"node {int(tags[k])} has non-finite coordinates "
-                          f"({xy[k, 0]}, {xy[k, 1]})")
-        self.node_tags.append(tags)
-        self.node_xy.append(xy)
+    def ints(self, n: int, what, nonnegative: bool = False) -> np.ndarray:
+        return self._array(n, "i4", what).astype(np.int64)
 
+    def sizes(self, n: int, what, nonnegative: bool = False) -> np.ndarray:
+        out = self._array(n, self.size_code, what)
+        if (out > np.iinfo(np.int64).max).any():
+            raise GmshParseError(f"byte {self.pos}: a {what} beyond any file's reach")
+        return out.astype(np.int64)
 
-def _parse_msh(buf: bytes) -> _Raw:
-    r = _Reader(buf)
-    raw = _Raw()
-    version = None
-    while not r.at_end():
-        header = r.line().strip()
-        if not header.startswith("$"):
-            raise r.error(f'expected a section header, found "{header}"')
-        name = header[1:]
-
-        def need_format():
-            if version is None:
-                raise MissingSection(f"MeshFormat (before ${name})")
-            return version
-
-        if name == "MeshFormat":
-            version = _mesh_format(r)
-        elif name == "PhysicalNames":
-            _physical_names(r, raw)
-        elif name == "Entities":
-            if need_format() != "4.1":
-                raise r.error("$Entities in an MSH 2 file")
-            _entities(r, raw)
-        elif name == "Nodes":
-            (_nodes_v41 if need_format() == "4.1" else _nodes_v2)(r, raw)
-        elif name == "Elements":
-            (_elements_v41 if need_format() == "4.1" else _elements_v2)(r, raw)
-        elif name == "Periodic":
-            raise GmshUnsupported("periodic meshes ($Periodic)")
-        elif name == "PartitionedEntities":
-            raise GmshUnsupported("partitioned meshes ($PartitionedEntities): save the mesh "
-                                  "unpartitioned")
-        else:
-            r.skip_section(name)
-            continue
-        r.expect(f"$End{name}")
-    if version is None:
-        raise MissingSection("MeshFormat")
-    return raw
+    def reals(self, n: int, what) -> np.ndarray:
+        return self._array(n, "f8", what)
 
 
-def _mesh_format(r: _Reader) -> str:
-    v = r.token("format version").decode("ascii", "replace")
-    file_type = r.ascii_int("file type")
-    data_size = r.ascii_int("data size", unsigned=True)
-    if v == "4.1":
-        version = "4.1"
-    elif v.startswith("2."):
-        version = "2"
-    elif v.startswith("4"):
-        raise UnsupportedVersion(f"{v}: save as MSH 4.1 (Mesh.MshFileVersion = 4.1) or 2.2")
+def _count(stream, what: str, per_item_tokens: int = 1) -> int:
+    """A count that the rest of the section can hold (so a corrupt count
+    cannot ask for a huge array)."""
+    n = int(stream.sizes(1, what)[0])
+    if isinstance(stream, _TextStream):
+        room = len(stream.tokens) - stream.at
     else:
-        raise UnsupportedVersion(v)
-    if file_type == 0:
-        return version
-    if file_type == 1 and version == "4.1":
-        if data_size not in (4, 8):
-            raise r.error(f"unsupported data size {data_size}")
-        r.line()  # the rest of the header line
-        r.binary = True
-        r.size_bytes = data_size
-        mark = r.raw(4, "byte-order mark")
-        if mark == b"\x01\x00\x00\x00":
-            r.big_endian = False
-        elif mark == b"\x00\x00\x00\x01":
-            r.big_endian = True
-        else:
-            raise r.error(f"invalid byte-order mark {list(mark)}")
-        return version
-    if file_type == 1:
-        raise UnsupportedVersion("binary MSH 2: save as ASCII or as MSH 4.1")
-    raise r.error(f"invalid file type {file_type}")
+        room = len(stream.data) - stream.pos
+    if n * max(per_item_tokens, 1) > room + 1:
+        raise GmshParseError(f"a {what} of {n} is more than the rest of the file holds")
+    return n
 
 
-def _physical_names(r: _Reader, raw: _Raw):
-    binary, r.binary = r.binary, False  # always ASCII
-    n = r.ascii_int("physical name count", unsigned=True)
-    for _ in range(n):
-        dim = r.ascii_int("physical group dimension")
-        tag = r.ascii_int("physical group tag")
-        name = r.line().strip()
-        if len(name) >= 2 and name.startswith('"') and name.endswith('"'):
-            name = name[1:-1]
-        raw.names[(dim, tag)] = name
-    r.binary = binary
+# -- the file's tables ----------------------------------------------------------------------
+
+@dataclass
+class _Tables:
+    node_tags: list = field(default_factory=list)     # arrays of node tags
+    node_xy: list = field(default_factory=list)       # arrays (n, 2)
+    quad_tags: list = field(default_factory=list)
+    quad_nodes: list = field(default_factory=list)    # arrays (n, 4)
+    line_tags: list = field(default_factory=list)
+    line_nodes: list = field(default_factory=list)    # arrays (n, 2)
+    line_groups: list = field(default_factory=list)   # per line block: tuple of physical groups
+    other: dict = field(default_factory=dict)         # element type → count
+    names: dict = field(default_factory=dict)         # (dim, number) → name
+    curve_groups: dict = field(default_factory=dict)  # curve entity → physical groups
 
 
-def _entities(r: _Reader, raw: _Raw):
-    counts = [r.count("entity count", 1) for _ in range(4)]
+def _decoder(tables: _Tables, layout: _Layout):
+    def decode(section: _Section, stream):
+        name = section.name
+        if name in ("Nodes", "Elements", "Entities") and layout.version is None:
+            raise MissingSection(f"the file has no $MeshFormat before its ${name}")
+        if name == "PhysicalNames":
+            _physical_names(stream, tables)
+        elif name == "Entities":
+            if layout.version != "4.1":
+                raise GmshParseError("$Entities belongs to MSH 4 files, not to an MSH 2 file")
+            _entities(stream, tables)
+        elif name == "Nodes":
+            (_nodes_41 if layout.version == "4.1" else _nodes_22)(stream, tables)
+        elif name == "Elements":
+            (_elements_41 if layout.version == "4.1" else _elements_22)(stream, tables)
+        elif name == "Periodic":
+            raise GmshUnsupported("the mesh is periodic; periodic Gmsh meshes are not read")
+        elif name == "PartitionedEntities":
+            raise GmshUnsupported("the mesh is partitioned: save it whole "
+                                  "(Mesh.PartitionSplitMeshFiles = 0, no partitions)")
+        # any other section is skipped
+    return decode
+
+
+def _physical_names(stream: _TextStream, t: _Tables) -> None:
+    n = _count(stream, "physical name count", 3)
+    # names may hold spaces: read them from the lines, not from the tokens
+    lines = stream.rest_text().splitlines()[1:1 + n]
+    if len(lines) < n:
+        raise GmshParseError("$PhysicalNames ends before its names")
+    for row in lines:
+        parts = row.strip().split(None, 2)
+        if len(parts) < 3 or not _INT.match(parts[0].encode()) or not _INT.match(parts[1].encode()):
+            raise GmshParseError(f'a physical name row reads "dim number name", not "{row.strip()}"')
+        label = parts[2].strip()
+        if len(label) >= 2 and label[0] == label[-1] == '"':
+            label = label[1:-1]
+        t.names[(int(parts[0]), int(parts[1]))] = label
+
+
+def _entities(stream, t: _Tables) -> None:
+    counts = [_count(stream, "entity count") for _ in range(4)]
     for dim, n in enumerate(counts):
         for _ in range(n):
-            tag = r.int("entity tag")
-            for _ in range(3 if dim == 0 else 6):  # a point's coordinates, else a box
-                r.double("entity coordinate")
-            groups = [r.int("physical tag") for _ in range(r.count("physical tag count", 1))]
+            tag = int(stream.ints(1, "entity tag")[0])
+            stream.reals(3 if dim == 0 else 6, "entity coordinate")
+            groups = stream.ints(_count(stream, "physical tag count"), "physical tag")
             if dim > 0:
-                for _ in range(r.count("bounding entity count", 1)):
-                    r.int("bounding entity tag")
+                stream.ints(_count(stream, "bounding entity count"), "bounding entity tag")
             if dim == 1:
-                raw.curve_groups[tag] = groups
+                t.curve_groups[tag] = tuple(int(g) for g in groups)
 
 
-def _nodes_v41(r: _Reader, raw: _Raw):
-    n_blocks = r.count("node block count", 4)
-    n_nodes = r.count("node count", 4)
-    r.size("minimum node tag")
-    r.size("maximum node tag")
-    read = 0
+def _add_nodes(t: _Tables, tags: np.ndarray, xy: np.ndarray) -> None:
+    bad = ~np.isfinite(xy).all(axis=1)
+    if bad.any():
+        k = int(np.argmax(bad))
+        raise GmshParseError(f"node {int(tags[k])} sits at ({xy[k, 0]}, {xy[k, 1]}), not a "
+                             "finite point")
+    t.node_tags.append(tags)
+    t.node_xy.append(xy)
+
+
+def _nodes_41(stream, t: _Tables) -> None:
+    n_blocks = _count(stream, "node block count", 4)
+    n_total = _count(stream, "node count")
+    stream.sizes(2, "node tag range")
+    seen = 0
     for _ in range(n_blocks):
-        dim = r.int("entity dimension")
-        r.int("entity tag")
-        parametric = r.int("parametric flag")
-        n = r.count("nodes in block", 4)
-        if parametric == 0:
-            n_param = 0
-        elif parametric == 1 and 0 <= dim <= 3:
-            n_param = dim
-        else:
-            raise r.error(f"invalid node block ({dim}, {parametric})")
-        tags = r.sizes(n, "node tag")
-        per = 3 + n_param
-        names = ("node x", "node y") + ("node coordinate",) * (1 + n_param)
-        coords = r.doubles(n * per, names).reshape(n, per)
-        raw.push_nodes(r, tags, coords[:, :2].copy())
-        read += n
-    if read != n_nodes:
-        raise r.error(f"$Nodes declares {n_nodes} nodes, found {read}")
+        dim, _entity, parametric = (int(v) for v in stream.ints(3, "node block header"))
+        n = _count(stream, "node count of a block")
+        if parametric not in (0, 1) or not 0 <= dim <= 3:
+            raise GmshParseError(f"a node block of dimension {dim} with parametric flag "
+                                 f"{parametric}")
+        per = 3 + (dim if parametric else 0)
+        tags = stream.sizes(n, "node tag", nonnegative=True)
+        coords = stream.reals(n * per, ("node x", "node y", "node z") + ("node parameter",) * (per - 3))
+        coords = coords.reshape(n, per)
+        _add_nodes(t, tags, np.ascontiguousarray(coords[:, :2]))
+        seen += n
+    if seen != n_total:
+        raise GmshParseError(f"$Nodes announces {n_total} nodes and holds {seen}")
 
 
-def _nodes_v2(r: _Reader, raw: _Raw):
-    n = r.count("node count", 4)
-    vals = r.doubles(4 * n, ("node tag", "node x", "node y", "node z")).reshape(n, 4)
-    tags = vals[:, 0]
-    if not (np.all(tags == np.floor(tags)) and np.all(tags >= 0)):
-        k = int(np.argmax((tags != np.floor(tags)) | (tags < 0)))
-        raise r.error(f'invalid node tag: "{tags[k]}"')
-    raw.push_nodes(r, tags.astype(np.int64), vals[:, 1:3].copy())
+def _nodes_22(stream: _TextStream, t: _Tables) -> None:
+    n = _count(stream, "node count", 4)
+    rows = stream.reals(4 * n, ("node tag", "node x", "node y", "node z")).reshape(n, 4)
+    tags = rows[:, 0]
+    whole = (tags == np.floor(tags)) & (tags >= 0)
+    if not whole.all():
+        k = int(np.argmin(whole))
+        raise GmshParseError(f'invalid node tag: "{tags[k]}" (node {k + 1} of $Nodes)')
+    _add_nodes(t, tags.astype(np.int64), np.ascontiguousarray(rows[:, 1:3]))
 
 
-def _elements_v41(r: _Reader, raw: _Raw):
-    n_blocks = r.count("element block count", 4)
-    n_elements = r.count("element count", 4)
-    r.size("minimum element tag")
-    r.size("maximum element tag")
-    read = 0
+def _keep(t: _Tables, etype: int, tags: np.ndarray, nodes: np.ndarray, groups: tuple) -> None:
+    if etype == T_QUAD:
+        t.quad_tags.append(tags)
+        t.quad_nodes.append(nodes)
+    elif etype == T_LINE:
+        t.line_tags.append(tags)
+        t.line_nodes.append(nodes)
+        t.line_groups.extend([groups] * len(tags))
+    elif etype != T_POINT:
+        t.other[etype] = t.other.get(etype, 0) + len(tags)
+
+
+def _elements_41(stream, t: _Tables) -> None:
+    n_blocks = _count(stream, "element block count", 4)
+    n_total = _count(stream, "element count")
+    stream.sizes(2, "element tag range")
+    seen = 0
     for _ in range(n_blocks):
-        r.int("entity dimension")
-        entity = r.int("entity tag")
-        etype = r.int("element type")
-        n = r.count("elements in block", 4)
-        if etype not in ELEMENT_TYPES:
+        _dim, entity, etype = (int(v) for v in stream.ints(3, "element block header"))
+        n = _count(stream, "element count of a block")
+        if etype not in NODES_PER_TYPE:
             raise UnsupportedElements([(etype, n)])
-        nn = ELEMENT_TYPES[etype][0]
-        vals = r.sizes(n * (1 + nn), "element node tag").reshape(n, 1 + nn)
-        raw.add_block(etype, vals[:, 0], vals[:, 1:], ("curve", entity))
-        read += n
-    if read != n_elements:
-        raise r.error(f"$Elements declares {n_elements} elements, found {read}")
+        width = 1 + NODES_PER_TYPE[etype]
+        rows = stream.sizes(n * width, "element node tag", nonnegative=True).reshape(n, width)
+        groups = t.curve_groups.get(entity, ()) if etype == T_LINE else ()
+        _keep(t, etype, rows[:, 0], rows[:, 1:], groups)
+        seen += n
+    if seen != n_total:
+        raise GmshParseError(f"$Elements announces {n_total} elements and holds {seen}")
 
 
-def _elements_v2(r: _Reader, raw: _Raw):
-    n = r.count("element count", 4)
+def _elements_22(stream: _TextStream, t: _Tables) -> None:
+    n = _count(stream, "element count", 4)
+    # every value of an MSH 2.2 element row is an integer: convert the
+    # section once, then walk the rows (their lengths vary with the type)
+    values = stream.ints(len(stream.tokens) - stream.at, "element value")
+    stream.at -= len(values)
+    by_type: dict = {}
+    at = 0
     for _ in range(n):
-        tag = r.ascii_int("element tag", unsigned=True)
-        etype = r.ascii_int("element type")
-        n_tags = r.ascii_int("element tag count", unsigned=True)
-        physical = 0
-        for i in range(n_tags):
-            t = r.ascii_int("element tag")
-            if i == 0:
-                physical = t
-        if etype not in ELEMENT_TYPES:
+        if at + 3 > len(values):
+            raise GmshParseError("$Elements ends inside an element row")
+        tag, etype, n_tags = (int(v) for v in values[at:at + 3])
+        if etype not in NODES_PER_TYPE:
             raise UnsupportedElements([(etype, 1)])
-        nodes = [r.ascii_int("element node tag", unsigned=True)
-                 for _ in range(ELEMENT_TYPES[etype][0])]
-        raw.add_block(etype, np.array([tag]), np.array([nodes]), ("physical", physical))
+        if n_tags < 0 or tag < 0:
+            raise GmshParseError(f"element {tag}: a negative count or tag")
+        first = int(values[at + 3]) if n_tags > 0 and at + 3 < len(values) else 0
+        nodes_at = at + 3 + n_tags
+        nodes_to = nodes_at + NODES_PER_TYPE[etype]
+        if nodes_to > len(values):
+            raise GmshParseError("$Elements ends inside an element row")
+        by_type.setdefault(etype, []).append((tag, first, values[nodes_at:nodes_to]))
+        at = nodes_to
+    stream.at += at
+    for etype, rows in by_type.items():
+        tags = np.array([r[0] for r in rows], np.int64)
+        nodes = np.array([r[2] for r in rows], np.int64).reshape(len(rows), -1)
+        if etype == T_LINE:
+            for tag, first, nd in rows:
+                _keep(t, etype, np.array([tag]), nd.reshape(1, -1), (first,) if first else ())
+        else:
+            _keep(t, etype, tags, nodes, ())
 
 
-# ---------------------------------------------------------------------------
-# The mesh
-# ---------------------------------------------------------------------------
+# -- from the tables to the mesh ----------------------------------------------------------
 
-def _line_tag(raw: _Raw, groups) -> int | None:
-    kind, value = groups
-    if kind == "curve":
-        physical = raw.curve_groups.get(value, [])
-    else:
-        physical = [] if value == 0 else [value]
+def _xy(x: float, y: float) -> str:
+    return f"({float(x)!r}, {float(y)!r})"
+
+
+class _NodeIndex:
+    """Node tag → row of the concatenated node table, by binary search."""
+
+    def __init__(self, tags: np.ndarray):
+        self.order = np.argsort(tags, kind="stable")
+        self.sorted = tags[self.order]
+        twice = np.nonzero(self.sorted[1:] == self.sorted[:-1])[0]
+        if twice.size:
+            raise InvalidMesh(f"node {int(self.sorted[twice[0]])} is defined twice")
+
+    def rows(self, tags: np.ndarray) -> np.ndarray:
+        """Rows of ``tags``, −1 where a tag is not defined."""
+        if self.sorted.size == 0:
+            return np.full(tags.shape, -1, np.int64)
+        at = np.clip(np.searchsorted(self.sorted, tags), 0, self.sorted.size - 1)
+        return np.where(self.sorted[at] == tags, self.order[at], -1)
+
+
+def _quads(t: _Tables, index: _NodeIndex, xy: np.ndarray):
+    """Vertices (the used nodes, in file order), the quads on them turned
+    counter-clockwise, the quads' file tags and file node tags."""
+    tags = np.concatenate(t.quad_tags)
+    nodes = np.concatenate(t.quad_nodes).astype(np.int64)
+    rows = index.rows(nodes)
+    missing = np.argwhere(rows < 0)
+    if missing.size:
+        k, c = missing[0]
+        raise InvalidMesh(f"element {int(tags[k])} uses undefined node {int(nodes[k, c])}")
+    used = np.zeros(xy.shape[0], bool)
+    used[rows.reshape(-1)] = True
+    renumber = np.cumsum(used) - 1
+    vertices = xy[used]
+    quads = renumber[rows]
+    p = vertices[quads]
+    shoelace = (p[:, :, 0] * np.roll(p[:, :, 1], -1, axis=1)
+                - np.roll(p[:, :, 0], -1, axis=1) * p[:, :, 1]).sum(axis=1)
+    # a clockwise quad is read backwards from its first corner
+    clockwise = shoelace < 0.0
+    quads[clockwise] = np.roll(quads[clockwise][:, ::-1], 1, axis=1)
+    nodes = nodes.copy()
+    nodes[clockwise] = np.roll(nodes[clockwise][:, ::-1], 1, axis=1)
+    return vertices, quads, tags, nodes, np.where(used, renumber, -1)
+
+
+def _check_corners(vertices, quads, tags, nodes) -> None:
+    """Every corner turns left by more than round-off: the bilinear map's
+    Jacobian is positive there (and so everywhere)."""
+    p = vertices[quads]
+    into = p - np.roll(p, 1, axis=1)      # edge arriving at each corner
+    out = np.roll(p, -1, axis=1) - p      # edge leaving it
+    turn = into[..., 0] * out[..., 1] - into[..., 1] * out[..., 0]
+    size = np.hypot(into[..., 0], into[..., 1]) * np.hypot(out[..., 0], out[..., 1])
+    bad = ~(turn > 1e-12 * size)
+    if bad.any():
+        k, c = np.argwhere(bad)[0]
+        raise InvalidMesh(f"element {int(tags[k])} is degenerate or non-convex at node "
+                          f"{int(nodes[k, c])} {_xy(*p[k, c])}: the Jacobian of its bilinear "
+                          "map is not positive there")
+
+
+def _edges(vertices, quads, tags):
+    """The mesh's edges: for every face (4·k + f) its edge number, and per
+    edge how many faces it has; refuses an edge of three or more faces and
+    two faces running the same way along one."""
+    nv = vertices.shape[0]
+    a = quads.reshape(-1)
+    b = np.roll(quads, -1, axis=1).reshape(-1)
+    key = np.minimum(a, b) * nv + np.maximum(a, b)
+    keys, edge_of_face, faces = np.unique(key, return_inverse=True, return_counts=True)
+    by_edge = np.argsort(edge_of_face, kind="stable")
+    first = np.concatenate([[0], np.cumsum(faces)[:-1]])
+
+    def where(f):
+        return f"{_xy(*vertices[a[f]])}–{_xy(*vertices[b[f]])}"
+
+    crowded = np.nonzero(faces > 2)[0]
+    if crowded.size:
+        f = by_edge[first[crowded[0]]:first[crowded[0]] + faces[crowded[0]]]
+        owners = ", ".join(str(int(tags[i // 4])) for i in f)
+        raise InvalidMesh(f"the edge {where(f[0])} is shared by more than two elements "
+                          f"({owners})")
+    pairs = np.nonzero(faces == 2)[0]
+    f0, f1 = by_edge[first[pairs]], by_edge[first[pairs] + 1]
+    same_way = a[f0] == a[f1]
+    if same_way.any():
+        i = int(np.argmax(same_way))
+        raise InvalidMesh(f"elements {int(tags[f0[i] // 4])} and {int(tags[f1[i] // 4])} overlap "
+                          f"along {where(f0[i])}: both run along it the same way")
+    return keys, edge_of_face, faces, by_edge, first, where
+
+
+def _line_tag(t: _Tables, groups: tuple) -> int | None:
     tag = None
-    for p in physical:
-        t = group_boundary_tag(p, raw.names.get((1, p)))
-        if tag is not None and tag != t:
-            raise InvalidMesh("a curve is in physical groups that map to different boundary "
-                              f"tags ({tag_name(tag)} and {tag_name(t)})")
-        tag = t
+    for g in groups:
+        this = group_boundary_tag(int(g), t.names.get((1, int(g))))
+        if tag is not None and this != tag:
+            raise InvalidMesh(f"a boundary curve lies in physical groups that give it different "
+                              f"boundary tags, {tag_name(tag)} and {tag_name(this)}")
+        tag = this
     return tag
 
 
-def _fmt(x: float) -> str:
-    return repr(float(x))
-
-
-def _build(raw: _Raw) -> QuadMesh:
-    if raw.unsupported:
-        raise UnsupportedElements(sorted(raw.unsupported.items()))
-    if not raw.node_tags:
-        raise MissingSection("Nodes")
-    if not raw.quads:
-        raise InvalidMesh("no quadrilateral elements: once a model has physical groups, Gmsh "
-                          "saves only the elements in them, so give the domain a physical "
-                          "surface (or set Mesh.SaveAll = 1)")
-    node_tags = np.concatenate(raw.node_tags)
-    node_xy = np.concatenate(raw.node_xy)
-    order = np.argsort(node_tags, kind="stable")
-    sorted_tags = node_tags[order]
-    dup = np.nonzero(sorted_tags[1:] == sorted_tags[:-1])[0]
-    if dup.size:
-        raise InvalidMesh(f"node {int(sorted_tags[dup[0] + 1])} is defined twice")
-
-    def lookup(tags: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
-        at = np.clip(np.searchsorted(sorted_tags, tags), 0, sorted_tags.size - 1)
-        found = sorted_tags[at] == tags
-        return np.where(found, order[at], -1), found
-
-    qtags = np.array([t for t, _ in raw.quads], dtype=np.int64)
-    qnodes = np.array([n for _, n in raw.quads], dtype=np.int64).reshape(-1, 4)
-    qidx, found = lookup(qnodes)
-    if not found.all():
-        k, c = divmod(int(np.argmin(found.reshape(-1))), 4)
-        raise InvalidMesh(f"element {int(qtags[k])} uses undefined node {int(qnodes[k, c])}")
-    # vertices: the nodes the quadrilaterals use, in file order
-    used = np.zeros(node_tags.size, bool)
-    used[qidx.reshape(-1)] = True
-    vertex_of_node = np.full(node_tags.size, -1, np.int64)
-    vertex_of_node[used] = np.arange(int(used.sum()))
-    vertices = node_xy[used]
-    quads = vertex_of_node[qidx]
-
-    # counter-clockwise, then a positive Jacobian at every corner
-    p = vertices[quads]
-    twice_area = np.zeros(len(quads))
-    for i in range(4):
-        j = (i + 1) % 4
-        twice_area = twice_area + (p[:, i, 0] * p[:, j, 1] - p[:, j, 0] * p[:, i, 1])
-    flip = twice_area < 0.0
-    quads[flip] = quads[flip][:, [0, 3, 2, 1]]
-    p = vertices[quads]
-    bad = np.zeros((len(quads), 4), bool)
-    for i in range(4):
-        a, b, c = p[:, (i + 3) % 4], p[:, i], p[:, (i + 1) % 4]
-        e0, e1 = b - a, c - b
-        cross = e0[:, 0] * e1[:, 1] - e0[:, 1] * e1[:, 0]
-        scale = np.hypot(e0[:, 0], e0[:, 1]) * np.hypot(e1[:, 0], e1[:, 1])
-        bad[:, i] = np.isnan(cross) | (cross <= 1e-12 * scale)
-    if bad.any():
-        k, i = divmod(int(np.argmax(bad.reshape(-1))), 4)
-        corner = (4 - i) % 4 if flip[k] else i
-        x, y = p[k, i]
-        raise InvalidMesh(f"element {int(qtags[k])} is degenerate or non-convex at node "
-                          f"{int(qnodes[k, corner])} ({_fmt(x)}, {_fmt(y)}): its bilinear map "
-                          "has a non-positive Jacobian")
-
-    # edges: at most two faces each, traversed in opposite directions
-    K = len(quads)
-    a = quads.reshape(-1)
-    b = quads[:, [1, 2, 3, 0]].reshape(-1)
-    lo, hi = np.minimum(a, b), np.maximum(a, b)
-    key = lo * vertices.shape[0] + hi
-    ek, inverse, counts = np.unique(key, return_inverse=True, return_counts=True)
-
-    def segment(e: int) -> str:
-        (x0, y0), (x1, y1) = vertices[lo[e]], vertices[hi[e]]
-        return f"({_fmt(x0)}, {_fmt(y0)})–({_fmt(x1)}, {_fmt(y1)})"
-
-    faces_of = np.argsort(inverse, kind="stable")
-    starts = np.concatenate([[0], np.cumsum(counts)])
-    many = np.nonzero(counts > 2)[0]
-    if many.size:
-        e = int(many[0])
-        f = faces_of[starts[e]:starts[e] + 3]
-        raise InvalidMesh(f"the edge {segment(int(f[0]))} is shared by more than two elements "
-                          f"(elements {int(qtags[f[0] // 4])}, {int(qtags[f[1] // 4])} and "
-                          f"{int(qtags[f[2] // 4])})")
-    pairs = np.nonzero(counts == 2)[0]
-    f0 = faces_of[starts[pairs]]
-    f1 = faces_of[starts[pairs] + 1]
-    same = a[f0] == a[f1]
-    if same.any():
-        i = int(np.argmax(same))
-        raise InvalidMesh(f"elements {int(qtags[f0[i] // 4])} and {int(qtags[f1[i] // 4])} "
-                          f"overlap: they traverse their shared edge {segment(int(f0[i]))} in "
-                          "the same direction")
-
-    # boundary tags from the line elements; untagged boundary edges are walls
-    boundary = counts[inverse] == 1
-    edge_tag: dict[int, int] = {}
-    for etag, nodes, groups in raw.lines:
-        idx, ok = lookup(np.array(nodes, dtype=np.int64))
-        v = np.where(ok, vertex_of_node[np.maximum(idx, 0)], -1)
-        e = -1
-        if (v >= 0).all():
-            k = min(v) * vertices.shape[0] + max(v)
-            at = int(np.searchsorted(ek, k))
-            e = at if at < ek.size and ek[at] == k else -1
-        if e < 0:
-            raise InvalidMesh(f"line element {etag} (nodes {nodes[0]} and {nodes[1]}) is not an "
-                              "edge of the quadrilateral mesh")
-        if counts[e] != 1:
+def _face_tags(t: _Tables, index: _NodeIndex, used_row_to_vertex, nv, quads, edges):
+    keys, edge_of_face, faces, by_edge, first, where = edges
+    K = quads.shape[0]
+    tags = np.full(4 * K, TAG_WALL, np.int32)
+    if not t.line_tags:
+        return tags.reshape(K, 4)
+    line_tags = np.concatenate(t.line_tags)
+    line_nodes = np.concatenate(t.line_nodes).astype(np.int64)
+    rows = index.rows(line_nodes)
+    verts = np.where(rows >= 0, used_row_to_vertex[np.maximum(rows, 0)], -1)
+    key = np.minimum(verts[:, 0], verts[:, 1]) * nv + np.maximum(verts[:, 0], verts[:, 1])
+    at = np.clip(np.searchsorted(keys, key), 0, keys.size - 1)
+    on_mesh = (verts >= 0).all(axis=1) & (keys[at] == key)
+    if not on_mesh.all():
+        i = int(np.argmin(on_mesh))
+        raise InvalidMesh(f"line element {int(line_tags[i])} (nodes {int(line_nodes[i, 0])} and "
+                          f"{int(line_nodes[i, 1])}) is not an edge of the quadrilateral mesh")
+    given: dict = {}
+    for i in np.nonzero(faces[at] == 1)[0]:  # lines on interior edges carry nothing
+        tag = _line_tag(t, t.line_groups[i])
+        if tag is None:
             continue
-        t = _line_tag(raw, groups)
-        if t is None:
-            continue
-        if e in edge_tag and edge_tag[e] != t:
-            f = int(faces_of[starts[e]])
-            raise InvalidMesh(f"the boundary edge {segment(f)} has two boundary tags, "
-                              f"{tag_name(edge_tag[e])} and {tag_name(t)}")
-        edge_tag[e] = t
-    face_tags = np.full(K * 4, TAG_WALL, np.int32)
-    for e, t in edge_tag.items():
-        face_tags[faces_of[starts[e]]] = t
-    face_tags[~boundary] = TAG_WALL
-    mesh = QuadMesh(vertices, quads, np.zeros((0, 4), np.int64), face_tags.reshape(K, 4))
+        e = int(at[i])
+        if given.setdefault(e, tag) != tag:
+            raise InvalidMesh(f"the boundary edge {where(by_edge[first[e]])} has two boundary "
+                              f"tags, {tag_name(given[e])} and {tag_name(tag)}")
+    for e, tag in given.items():
+        tags[by_edge[first[e]]] = tag
+    return tags.reshape(K, 4)
+
+
+def _assemble(t: _Tables) -> QuadMesh:
+    if t.other:
+        raise UnsupportedElements(t.other.items())
+    if not t.node_tags:
+        raise MissingSection("the file has no $Nodes")
+    if not t.quad_tags or sum(len(x) for x in t.quad_tags) == 0:
+        raise InvalidMesh("the file holds no quadrilaterals. Gmsh saves only the elements of "
+                          "physical groups once there are any: put the domain in a physical "
+                          "surface, or set Mesh.SaveAll = 1")
+    node_tags = np.concatenate(t.node_tags)
+    xy = np.concatenate(t.node_xy)
+    index = _NodeIndex(node_tags)
+    vertices, quads, qtags, qnodes, row_to_vertex = _quads(t, index, xy)
+    _check_corners(vertices, quads, qtags, qnodes)
+    edges = _edges(vertices, quads, qtags)
+    face_tags = _face_tags(t, index, row_to_vertex, vertices.shape[0], quads, edges)
+    mesh = QuadMesh(vertices, quads, np.zeros((0, 4), np.int64), face_tags)
     return in_hilbert_order(mesh)[0]
 
 
+# -- public entry points ----------------------------------------------------------------------
+
 def parse_gmsh_mesh(data: bytes) -> QuadMesh:
-    """The quadrilateral mesh of a Gmsh file's contents (MSH 4.1 ASCII or
-    binary, MSH 2.2 ASCII)."""
-    return _build(_parse_msh(bytes(data)))
+    """The quadrilateral mesh in the bytes of a Gmsh file (MSH 4.1 text or
+    binary, MSH 2.2 text)."""
+    data = bytes(data)
+    layout = _Layout()
+    tables = _Tables()
+    try:
+        _cut(data, layout, _decoder(tables, layout))
+    except (IndexError, struct.error, OverflowError) as err:  # a cut file, whatever byte it ends on
+        raise GmshParseError(f"the file ends or breaks off inside a section ({err})") from None
+    if layout.version is None:
+        raise MissingSection("the file has no $MeshFormat")
+    return _assemble(tables)
 
 
 def read_gmsh_mesh(path) -> QuadMesh:
     return parse_gmsh_mesh(Path(path).read_bytes())
 
 
-def boundary_edges(mesh: QuadMesh):
-    """The boundary faces of a mesh as (element, face, vertex a, vertex b,
-    tag) rows, element by element (periodic pairs are interior)."""
-    K = mesh.n_elements
+def boundary_edges(mesh: QuadMesh) -> np.ndarray:
+    """The mesh's boundary faces, one row each in element order: (element,
+    face, first vertex, second vertex, tag). Periodic pairs are not
+    boundary."""
     a = mesh.elements.reshape(-1)
-    b = mesh.elements[:, [1, 2, 3, 0]].reshape(-1)
+    b = np.roll(mesh.elements, -1, axis=1).reshape(-1)
     key = np.minimum(a, b) * mesh.vertices.shape[0] + np.maximum(a, b)
-    _, inverse, counts = np.unique(key, return_inverse=True, return_counts=True)
-    on = counts[inverse] == 1
-    if mesh.periodic.size:
-        for k0, f0, k1, f1 in mesh.periodic:
-            on[4 * k0 + f0] = on[4 * k1 + f1] = False
-    tags = (mesh.face_tags.reshape(-1) if mesh.face_tags is not None
-            else np.zeros(4 * K, np.int32))
-    faces = np.nonzero(on)[0]
-    return np.stack([faces // 4, faces % 4, a[faces], b[faces], tags[faces]], axis=1)
+    _, edge_of_face, faces = np.unique(key, return_inverse=True, return_counts=True)
+    alone = faces[edge_of_face] == 1
+    for k0, f0, k1, f1 in mesh.periodic:
+        alone[4 * k0 + f0] = alone[4 * k1 + f1] = False
+    tags = (np.zeros(a.size, np.int32) if mesh.face_tags is None
+            else mesh.face_tags.reshape(-1))
+    f = np.nonzero(alone)[0]
+    return np.stack([f // 4, f % 4, a[f], b[f], tags[f]], axis=1)
 
 
 def write_gmsh_mesh(mesh: QuadMesh, path) -> None:
-    """MSH 2.2 ASCII: the vertices, each boundary face as a line in the
-    physical group of its tag (so the tags survive a round trip), then the
-    quadrilaterals (write_gmsh_mesh, gmsh.rs:950-1015)."""
+    """The mesh as MSH 2.2 text: its vertices (shortest round-trip
+    decimals), every boundary face as a line element whose physical and
+    elementary tags are its tag's group number (so the tags read back), then
+    the quadrilaterals."""
     if mesh.periodic.size:
-        raise GmshUnsupported("periodic meshes cannot be written to MSH 2.2")
-    out = ["$MeshFormat", "2.2 0 8", "$EndMeshFormat", "$Nodes", str(mesh.vertices.shape[0])]
-    out += [f"{i + 1} {_fmt(x)} {_fmt(y)} 0" for i, (x, y) in enumerate(mesh.vertices)]
-    out += ["$EndNodes", "$Elements"]
-    edges = boundary_edges(mesh)
-    out.append(str(len(edges) + mesh.n_elements))
-    eid = 1
-    for _, _, va, vb, tag in edges:
-        phys = tag_to_physical(int(tag))
-        lo, hi = min(va, vb), max(va, vb)
-        out.append(f"{eid} 1 2 {phys} {phys} {lo + 1} {hi + 1}")
-        eid += 1
-    for q in mesh.elements:
-        out.append(f"{eid} 3 2 0 0 {q[0] + 1} {q[1] + 1} {q[2] + 1} {q[3] + 1}")
-        eid += 1
-    out.append("$EndElements")
-    Path(path).write_text("\n".join(out) + "\n")
+        raise GmshUnsupported("a periodic mesh has no MSH 2.2 form here")
+    rows = boundary_edges(mesh)
+    nv = mesh.vertices.shape[0]
+    text = ["$MeshFormat", "2.2 0 8", "$EndMeshFormat", "$Nodes", str(nv)]
+    text += [f"{i} {x!r} {y!r} 0" for i, (x, y) in enumerate(mesh.vertices.tolist(), start=1)]
+    text += ["$EndNodes", "$Elements", str(len(rows) + mesh.n_elements)]
+    number = 0
+    for _, _, va, vb, tag in rows.tolist():
+        number += 1
+        group = tag_to_physical(int(tag))
+        text.append(f"{number} {T_LINE} 2 {group} {group} {min(va, vb) + 1} {max(va, vb) + 1}")
+    for quad in (mesh.elements + 1).tolist():
+        number += 1
+        text.append(f"{number} {T_QUAD} 2 0 0 " + " ".join(map(str, quad)))
+    text.append("$EndElements")
+    Path(path).write_text("\n".join(text) + "\n")
 
 
-def binary_msh41(mesh_nodes, quads, lines, curve_groups, names=(), big_endian=False,
+def binary_msh41(nodes, quads, lines, curve_groups, names=(), big_endian=False,
                  size_bytes=8) -> bytes:
-    """A binary MSH 4.1 file (for tests and converters): nodes [(tag, x, y)],
-    quads [(tag, n0..n3)] on surface 1, lines [(tag, curve, na, nb)] on
-    their curves, curve_groups {curve: [physical groups]}, names
-    [(dim, tag, name)]."""
-    e = ">" if big_endian else "<"
-    st = "I" if size_bytes == 4 else "Q"
+    """A binary MSH 4.1 file of ``nodes`` [(tag, x, y)] on surface 1,
+    ``quads`` [(tag, n0, n1, n2, n3)] on surface 1, ``lines`` [(tag, curve,
+    na, nb)] on their curves, ``curve_groups`` {curve: [physical group]}
+    and ``names`` [(dim, group, name)] (for tests and converters)."""
+    end = ">" if big_endian else "<"
+    size = "I" if size_bytes == 4 else "Q"
+    out = bytearray()
 
-    def pack(fmt, *v):
-        return struct.pack(e + fmt, *v)
+    def put(fmt: str, *values):
+        out.extend(struct.pack(end + fmt, *values))
 
-    b = bytearray(f"$MeshFormat\n4.1 1 {size_bytes}\n".encode())
-    b += pack("i", 1) + b"\n$EndMeshFormat\n"
+    def text(s: str):
+        out.extend(s.encode())
+
+    text(f"$MeshFormat\n4.1 1 {size_bytes}\n")
+    put("i", 1)
+    text("\n$EndMeshFormat\n")
     if names:
-        b += f"$PhysicalNames\n{len(names)}\n".encode()
-        for dim, tag, name in names:
-            b += f'{dim} {tag} "{name}"\n'.encode()
-        b += b"$EndPhysicalNames\n"
+        text(f"$PhysicalNames\n{len(names)}\n")
+        for dim, group, label in names:
+            text(f'{dim} {group} "{label}"\n')
+        text("$EndPhysicalNames\n")
     curves = sorted(curve_groups)
-    b += b"$Entities\n" + pack(st * 4, 0, len(curves), 1, 0)
+    text("$Entities\n")
+    put(size * 4, 0, len(curves), 1, 0)
     for c in curves:
-        g = curve_groups[c]
-        b += pack("i", c) + pack("6d", *([0.0] * 6)) + pack(st, len(g))
-        b += pack(f"{len(g)}i", *g) + pack(st, 0)
-    b += pack("i", 1) + pack("6d", *([0.0] * 6)) + pack(st, 0) + pack(st, 0)
-    b += b"\n$EndEntities\n$Nodes\n"
-    tags = [t for t, _, _ in mesh_nodes]
-    b += pack(st * 4, 1, len(mesh_nodes), min(tags), max(tags))
-    b += pack("iii", 2, 1, 0) + pack(st, len(mesh_nodes))
-    b += pack(st * len(tags), *tags)
-    for _, x, y in mesh_nodes:
-        b += pack("3d", x, y, 0.0)
-    b += b"\n$EndNodes\n$Elements\n"
-    blocks = [(2, 1, QUAD, [(q[0], *q[1:]) for q in quads])]
+        groups = list(curve_groups[c])
+        put("i6d", c, *([0.0] * 6))
+        put(size, len(groups))
+        put("i" * len(groups), *groups)
+        put(size, 0)
+    put("i6d", 1, *([0.0] * 6))
+    put(size * 2, 0, 0)
+    text("\n$EndEntities\n$Nodes\n")
+    tags = [n[0] for n in nodes]
+    put(size * 4, 1, len(nodes), min(tags), max(tags))
+    put("iii", 2, 1, 0)
+    put(size, len(nodes))
+    put(size * len(tags), *tags)
+    for _, x, y in nodes:
+        put("3d", x, y, 0.0)
+    text("\n$EndNodes\n$Elements\n")
+    blocks = [(2, 1, T_QUAD, [tuple(q) for q in quads])] if quads else []
     for c in curves:
-        blocks.append((1, c, LINE, [(t, na, nb) for t, cc, na, nb in lines if cc == c]))
-    blocks = [blk for blk in blocks if blk[3]]
-    n = sum(len(blk[3]) for blk in blocks)
-    all_tags = [row[0] for blk in blocks for row in blk[3]]
-    b += pack(st * 4, len(blocks), n, min(all_tags), max(all_tags))
-    for dim, ent, etype, rows in blocks:
-        b += pack("iii", dim, ent, etype) + pack(st, len(rows))
+        rows = [(tag, a, b) for tag, cc, a, b in lines if cc == c]
+        if rows:
+            blocks.append((1, c, T_LINE, rows))
+    every = [row[0] for _, _, _, rows in blocks for row in rows]
+    put(size * 4, len(blocks), len(every), min(every, default=0), max(every, default=0))
+    for dim, entity, etype, rows in blocks:
+        put("iii", dim, entity, etype)
+        put(size, len(rows))
         for row in rows:
-            b += pack(st * len(row), *row)
-    b += b"\n$EndElements\n"
-    return bytes(b)
+            put(size * len(row), *row)
+    text("\n$EndElements\n")
+    return bytes(out)
