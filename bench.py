@@ -157,17 +157,43 @@ def build_workload(n_elements: int, order: int):
     return cases.coastal_box(n_elements=n_elements, order=order)
 
 
-def oracle_baseline(case, steps: int, threads: int) -> dict:
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo), or the machine."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+
+    return platform.machine()
+
+
+def oracle_steps(case, steps: int, threads: int, warmup: int = 0, contract: bool = False,
+                 state=None, t_start: float = 0.0) -> dict:
     """The oracle (C++ restatement of the reference CPU path, OpenMP) timed
-    on the host cores over ``steps`` SSP-RK3 steps of ``case``."""
+    on the host cores over ``steps`` SSP-RK3 steps of ``case`` after
+    ``warmup`` untimed ones; ``contract``: the FMA-contracted build."""
     sys.path.insert(0, str(ROOT / "tests"))
     from oracle_lib import oracle
 
-    ref = oracle(case.form, threads=threads)
+    ref = oracle(case.form, threads=threads, contract=contract)
     try:
-        ref.upload(*case.state)
+        ref.upload(*(state if state is not None else case.state))
+        t = t_start
+        for _ in range(warmup):
+            dt = ref.compute_dt_ssp(case.cfl)
+            ref.step(t, dt)
+            t += dt
         t0 = time.perf_counter()
-        t = 0.0
         for _ in range(steps):
             dt = ref.compute_dt_ssp(case.cfl)
             ref.step(t, dt)
@@ -179,56 +205,71 @@ def oracle_baseline(case, steps: int, threads: int) -> dict:
     return {"value": 3.0 * nodes * steps / seconds, "seconds": seconds, "steps": steps}
 
 
+def cpu_baseline_figures(case, threads: int, budget_s: float = 10.0) -> dict:
+    """Both oracle builds on the whole workload from its start: the build
+    that rounds every multiply and add (the reference's arithmetic, and its
+    target-cpu=native tuning) as the baseline, the FMA-contracted build
+    beside it; each over as many steps (1 to 10) as fit ``budget_s``."""
+    probe = oracle_steps(case, 1, threads)
+    steps = int(max(1, min(10, budget_s / max(probe["seconds"], 1e-3))))
+    plain = oracle_steps(case, steps, threads)
+    fma = oracle_steps(case, steps, threads, contract=True)
+    model = cpu_model()
+    return {
+        "value": plain["value"], "unit": UNIT, "cores": threads, "kind": "port",
+        "sample": (f"{steps} SSP-RK3 steps of the whole {case.form.mesh.n_elements}-element mesh "
+                   f"from rest, {plain['seconds']:.1f} s on {threads} host threads of {model}; "
+                   "oracle build -O3 -ffp-contract=off with the host CPU's tuning"),
+        "cpu_model": model,
+        "contraction_on": {"value": fma["value"], "unit": UNIT, "seconds": fma["seconds"],
+                           "steps": steps, "build": "-O3 -ffp-contract=fast with the host "
+                                                    "CPU's tuning (FMA-contracted)"},
+    }
+
+
 def run_reference(args, rank: int, world: int):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    # each bench step is one oracle SSP-RK3 step; the mesh shrinks when many
-    # steps are asked for, so the whole run stays within a few minutes
-    total = args.steps + args.warmup
-    n_el = args.elements if total <= 12 else max(50_000, int(args.elements * 12 / total))
-    # the line names the workload of the GPU arm; the sample is the same
-    # generator at n_el elements (DOF-updates/s of the CPU path do not depend
-    # on the mesh size beyond cache effects)
-    full_case = build_workload(args.elements, args.order)
-    full = full_case.form
-    case = full_case if n_el == args.elements else build_workload(n_el, args.order)
-    sys.path.insert(0, str(ROOT / "tests"))
-    from oracle_lib import oracle
-
-    ref = oracle(case.form, threads=threads)
-    ref.upload(*case.state)
-    t = 0.0
-    for _ in range(args.warmup):
-        dt = ref.compute_dt_ssp(case.cfl)
-        ref.step(t, dt)
-        t += dt
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        dt = ref.compute_dt_ssp(case.cfl)
-        ref.step(t, dt)
-        t += dt
-    seconds = time.perf_counter() - t0
-    ref.close()
-    nodes = case.form.n_values
+    # each bench step is one oracle SSP-RK3 step of the whole workload the
+    # GPU arm times (≈ 0.15 s a step on 16 host threads)
+    case = build_workload(args.elements, args.order)
+    full = case.form
+    run = oracle_steps(case, args.steps, threads, warmup=args.warmup)
+    fma = oracle_steps(case, args.steps, threads, warmup=args.warmup, contract=True)
+    seconds = run["seconds"]
+    nodes = full.n_values
     value = 3.0 * nodes * args.steps / seconds
-    sample = (f"{args.steps} SSP-RK3 steps of the coastal box at {case.form.mesh.n_elements} "
-              f"elements, N={args.order}, oracle port on {threads} host threads")
+    model = cpu_model()
+    sample = (f"{args.steps} SSP-RK3 steps (after {args.warmup}) of the whole coastal box, "
+              f"{full.mesh.n_elements} elements, N={args.order}, from rest; oracle port "
+              f"(-O3 -ffp-contract=off, host CPU tuning) on {threads} host threads of {model}")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * seconds / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": f"coastal box {full.mesh.n_elements} quads N={args.order} "
-                               "SSP-RK3 (wet/dry, Manning, Coriolis, 4-constituent tide)",
-                   "elements": full.mesh.n_elements, "order": args.order,
-                   "nodes": full.n_values, "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2 (state and tables ≫ 129 MB)"},
+        "config": workload_config(full, args.order, world),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": sample},
+                         "sample": sample, "cpu_model": model,
+                         "contraction_on": {"value": fma["value"], "unit": UNIT,
+                                            "seconds": fma["seconds"], "steps": args.steps,
+                                            "build": "-O3 -ffp-contract=fast with the host "
+                                                     "CPU's tuning (FMA-contracted)"}},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def workload_config(form, order: int, world: int, weather: bool = False) -> dict:
+    return {"workload": f"coastal box {form.mesh.n_elements} quads N={order} "
+                        "SSP-RK3 (wet/dry, Manning, Coriolis, 4-constituent tide"
+                        + (", synthetic storm: wind, pressure, raised open boundary)"
+                           if weather else ")"),
+            "elements": form.mesh.n_elements, "order": order,
+            "nodes": form.n_values, "parallelism": f"replicas x{world}",
+            "start": "from rest at t = 0 under the 1-hour tide ramp",
+            "l2": "inputs larger than L2 (state and tables ≫ 129 MB)"}
 
 
 def run_ours(args, rank: int, world: int, local: int):
@@ -282,21 +323,42 @@ def run_ours(args, rank: int, world: int, local: int):
     total_nodes = dist.sum(float(nodes))
     value = 3.0 * total_nodes * args.steps / seconds
 
+    # the same box flowing, after the ramp: the step time on a state whose
+    # wet nodes all move (η = 0.5 cos(2πx/Lx) m, (u, v) = (0.3, −0.1) m/s)
+    # from t = 2 h, so the friction, wave-speed and subcell branches of a
+    # running tide are the ones taken
+    flowing = None
+    if not args.no_flowing:
+        from dgcom_gb300 import cases
+
+        dev.upload(*cases.with_flow(case))
+        profile(args.warmup, 7200.0)
+        flow = profile(args.steps, 7200.0)
+        flowing = {"ms_per_step": flow.total_ms / args.steps,
+                   "value": 3.0 * nodes * args.steps / (flow.total_ms * 1e-3), "unit": UNIT,
+                   "kernel_ms": {"stage": flow.stage_ms / args.steps,
+                                 "face": flow.face_ms / args.steps,
+                                 "dt": flow.dt_ms / args.steps},
+                   "state": "eta = 0.5 cos(2 pi x/Lx) m, (u, v) = (0.3, -0.1) m/s at the wet "
+                            "nodes, from t = 2 h (after the ramp)"}
+
     # e2e: through the C ABI with pinned host buffers, every step: upload
     # the state, the positivity-bounded dt, one step, download the state
-    e2e_steps = max(1, min(args.steps, 5))
+    e2e_steps = max(1, args.steps)
     try:
         import torch
 
         pinned = [torch.empty(nodes, dtype=torch.float64, pin_memory=True).numpy() for _ in range(3)]
     except Exception:  # noqa: BLE001 - pinned memory is an optimisation of the copy
         pinned = [np.empty(nodes) for _ in range(3)]
+    dev.upload(*case.state)
+    profile(args.warmup, 0.0)
     h, hu, hv = dev.download()
     for dst, src in zip(pinned, (h, hu, hv)):
         dst[:] = src
     dist.barrier()
     t0 = time.perf_counter()
-    t = timed.t_final
+    t = warm.t_final
     for _ in range(e2e_steps):
         dev.upload(*pinned)
         dt = dev.compute_dt_ssp(case.cfl)
@@ -315,15 +377,7 @@ def run_ours(args, rank: int, world: int, local: int):
     achieved = bytes_per_launch / (stage_avg_ms * 1e-3) / 1e9
     baseline = None
     if rank == 0 and not args.no_cpu_baseline:
-        threads = os.cpu_count() or 1
-        dev_state = dev.download()
-        probe = oracle_baseline(case, 1, threads)
-        steps = int(max(1, min(10, 15.0 / max(probe["seconds"], 1e-3))))
-        b = oracle_baseline(case, steps, threads)
-        baseline = {"value": b["value"], "unit": UNIT, "cores": threads, "kind": "port",
-                    "sample": f"{steps} SSP-RK3 steps of the same {form.mesh.n_elements}-element "
-                              f"mesh from rest ({b['seconds']:.1f} s on {threads} host threads)"}
-        del dev_state
+        baseline = cpu_baseline_figures(case, os.cpu_count() or 1)
     dev.close()
     if rank == 0:
         line = {
@@ -331,13 +385,7 @@ def run_ours(args, rank: int, world: int, local: int):
             "warmup": args.warmup, "ms_per_step": 1e3 * seconds / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": f"coastal box {form.mesh.n_elements} quads N={args.order} "
-                                   "SSP-RK3 (wet/dry, Manning, Coriolis, 4-constituent tide"
-                                   + (", synthetic storm: wind, pressure, raised open boundary)"
-                                      if args.weather else ")"),
-                       "elements": form.mesh.n_elements, "order": args.order,
-                       "nodes": nodes, "parallelism": f"replicas x{world}",
-                       "l2": "inputs larger than L2 (state and tables ≫ 129 MB)"},
+            "config": workload_config(form, args.order, world, args.weather),
             "launch": {"face_threads": tuning["face_threads"],
                        "stage_threads": tuning["stage_threads"],
                        "face_ms": tuning["face_ms"], "stage_ms": tuning["stage_ms"]},
@@ -356,6 +404,7 @@ def run_ours(args, rank: int, world: int, local: int):
                                 + timed.control_launches),
             "clocks": clocks,
             "cpu_baseline": baseline,
+            "flowing": flowing,
         }
         print(json.dumps(line), flush=True)
     dist.close()
@@ -818,6 +867,8 @@ def main():
     ap.add_argument("--elements", type=int, default=1_000_000)
     ap.add_argument("--order", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-flowing", action="store_true",
+                    help="skip the step time on the flowing state of the same box")
     ap.add_argument("--weather", action="store_true",
                     help="coastal: add a synthetic storm (GriddedAtmosphere2D's device form)")
     ap.add_argument("--workload", default="coastal",

@@ -31,13 +31,14 @@ def cuda_lib():
 @pytest.fixture(scope="session")
 def reference_data():
     """A data file of the reference repository (read-only, CPU tests only),
-    or a skip where the repository is not present."""
-    import os
-
-    root = Path(os.environ.get("DGCOM_REFERENCE", "/root/reference"))
+    found under the directory the DGCOM_REFERENCE environment variable
+    names, or a skip where it is unset or the file is absent."""
+    root = os.environ.get("DGCOM_REFERENCE")
 
     def get(relative: str) -> Path:
-        path = root / relative
+        if not root:
+            pytest.skip("DGCOM_REFERENCE (the reference repository's root) is not set")
+        path = Path(root) / relative
         if not path.is_file():
             pytest.skip(f"reference data {relative} not present")
         return path

@@ -46,24 +46,25 @@ POINTWISE = {
     "time_stencil": (C.c_int, [_dp, C.c_int64, C.c_double, C.c_int, C.POINTER(C.c_int64), _dp]),
 }
 
-_lib = None
+_libs: dict = {}
 
 
-def oracle_library() -> abi.Library:
-    global _lib
-    if _lib is None:
+def oracle_library(contract: bool = False) -> abi.Library:
+    """The oracle's library: the parity build, or with ``contract`` the
+    FMA-contracted build (timed as a second CPU figure, never a checker)."""
+    if contract not in _libs:
         sys.path.insert(0, str(ROOT / "oracle"))
         import build as oracle_build  # oracle/build.py
 
-        path = oracle_build.build()
-        _lib = abi.Library(C.CDLL(str(path)), "oracle", POINTWISE)
-    return _lib
+        path = oracle_build.build(contract=contract)
+        _libs[contract] = abi.Library(C.CDLL(str(path)), "oracle", POINTWISE)
+    return _libs[contract]
 
 
-def oracle(form, threads: int | None = None) -> SWEPhysics2D:
+def oracle(form, threads: int | None = None, contract: bool = False) -> SWEPhysics2D:
     """The oracle's physics on ``form`` (the CUDA library's wrapper, bound
     to the oracle)."""
-    lib = oracle_library()
+    lib = oracle_library(contract)
     if threads:
         lib.set_threads(threads)
     return SWEPhysics2D(form, 0, library=lib)
