@@ -444,6 +444,16 @@ def plain_run_seconds(form, state, steps: int, warmup: int, cfl: float, device: 
     return seconds
 
 
+def member_share(members: list, rank: int, world: int) -> list:
+    """The ensemble members rank ``rank`` of ``world`` advances: every
+    world-th member from its rank, so each member runs on exactly one rank
+    and the ranks' element counts stay close (members are independent: no
+    exchange between ranks)."""
+    if not 0 <= rank < world:
+        raise ValueError(f"rank {rank} of {world}")
+    return members[rank::world]
+
+
 def run_ensemble(args, rank: int, world: int, local: int):
     """The batched ensemble against the same members run one after another
     with the plain method, on the same GPU: members are independent, so
@@ -454,7 +464,7 @@ def run_ensemble(args, rank: int, world: int, local: int):
     dist = Dist(world, "nccl")
     t_gen = time.perf_counter()
     members = cases.ensemble_members(args.members, k_range=(args.k_min, args.k_max))
-    mine = members[rank::world]
+    mine = member_share(members, rank, world)
     t_gen = time.perf_counter() - t_gen
     nodes = sum(c.form.n_values for c in mine)
     cfl = mine[0].cfl
