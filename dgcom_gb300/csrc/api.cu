@@ -1082,13 +1082,12 @@ int dgswe_profile_steps(dgswe_handle* h, const dgswe_run_config* run, int64_t n_
 namespace {
 
 // The working memory of dgswe_compute_rhs_noalloc: 64 MiB, 256-byte aligned.
-// In host code this name stands for the array; its device address comes
-// from cudaGetSymbolAddress, once per device.
+// In host code this name stands for the array, not for its device address;
+// that comes from cudaGetSymbolAddress with the device current, looked up
+// by a handle's first call and kept on the handle (a handle lives in one
+// context, so the address it keeps cannot outlive the module it names).
 constexpr size_t kNoAllocBytes = size_t(64) << 20;
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocBytes / sizeof(double)];
-
-constexpr int kMaxNoAllocDevices = 64;
-double* g_noalloc_ptr[kMaxNoAllocDevices] = {};
 
 }  // namespace
 
@@ -1099,8 +1098,9 @@ int dgswe_compute_rhs_noalloc(dgswe_handle* h, const double* hh, const double* h
     if (n != h->n_values || !hh || !hu || !hv || !out_h || !out_hu || !out_hv)
         return fail(h, DGSWE_ERR_INVALID, "compute_rhs_noalloc: %lld values (expected %lld), or a NULL pointer",
                     (long long)n, (long long)h->n_values);
-    if (h->device < 0 || h->device >= kMaxNoAllocDevices)
-        return fail(h, DGSWE_ERR_INVALID, "compute_rhs_noalloc: device %d", h->device);
+    if (!(time >= h->parent_range.first && time <= h->parent_range.second))
+        return fail(h, DGSWE_ERR_INVALID, "compute_rhs_noalloc: t = %g leaves the forcing's snapshots",
+                    time);
     // face fluxes (3 × n_elements·4·(N+1)) and node velocities (2 × n)
     const size_t nf = (size_t)h->K * 4 * h->n1;
     const size_t need = (3 * nf + 2 * (size_t)n) * sizeof(double);
@@ -1110,13 +1110,12 @@ int dgswe_compute_rhs_noalloc(dgswe_handle* h, const double* hh, const double* h
                     "the %zu-byte array holds (use dgswe_compute_rhs)",
                     need, kNoAllocBytes);
     CK(cudaSetDevice(h->device));
-    double*& base = g_noalloc_ptr[h->device];
-    if (!base) {
+    if (!h->noalloc_scratch) {
         void* p = nullptr;
         CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-        base = (double*)p;
+        h->noalloc_scratch = (double*)p;
     }
-    double* fb_h = base;
+    double* fb_h = h->noalloc_scratch;
     double* fb_hu = fb_h + nf;
     double* fb_hv = fb_hu + nf;
     DevBuf in{const_cast<double*>(hh), const_cast<double*>(hu), const_cast<double*>(hv),

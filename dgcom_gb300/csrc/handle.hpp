@@ -88,6 +88,9 @@ struct dgswe_handle {
     } dplan;
     // the times every parent series covers (a run must stay within them)
     std::pair<double, double> parent_range{-INFINITY, INFINITY};
+    // device address of dgswe_compute_rhs_noalloc's working array, looked up
+    // by the handle's first call to it (not memory the handle owns)
+    double* noalloc_scratch = nullptr;
 
     ~dgswe_handle() {
         delete planner;

@@ -18,7 +18,9 @@
  *    n_elements·(order+1)² doubles, node i = j·(order+1) + a with r fastest
  *    (src/operators/operators_2d.rs:388-412).
  *  - Arrays passed in a `dgswe_form` are copied by `dgswe_create`; the caller
- *    keeps ownership. The handle owns all device memory.
+ *    keeps ownership. The handle owns all device memory it uses, except the
+ *    one fixed working array of dgswe_compute_rhs_noalloc, which belongs to
+ *    the library (64 MiB on every device where its device code is loaded).
  *  - A handle is used by one host thread at a time; each handle has its own
  *    CUDA stream.
  *  - Every function returns DGSWE_OK (0) or a status; the handle keeps a
@@ -610,17 +612,22 @@ int dgswe_profile_steps(dgswe_handle* handle, const dgswe_run_config* run,
  * its own pool up front, or a hot loop where an allocation would synchronise
  * the device or fail halfway through a run. h/hu/hv and out_* are device
  * pointers of n = dgswe_n_values() doubles each, owned by the caller; the
- * result is dgswe_compute_rhs's. Its working memory (the face fluxes and the
- * node velocities, n_elements·(12(N+1) + 2(N+1)²) doubles) lives in one
- * 64 MiB array inside the library, so meshes up to ≈ 104,000 elements at
- * N = 3 (≈ 155,000 at N = 2) fit; larger ones are refused with
- * DGSWE_ERR_INVALID. Every GPU on which the library's device code is loaded
- * holds that array until the process exits. Every call shares it: calls that
- * overlap on the GPU (other streams, other handles, other host threads)
- * race. Each call writes every value it reads, so nothing needs clearing
- * between calls. The first call on a device looks up the array's address
- * with that device current (cudaGetSymbolAddress): make that first call
- * before any stream capture. Returns when the RHS is complete. */
+ * result is dgswe_compute_rhs's, bit for bit, and `time` must lie within the
+ * snapshots of any forcing series the form holds, as there. Its working
+ * memory (the face fluxes and the node velocities, n_elements·(12(N+1) +
+ * 2(N+1)²) doubles) lives in one 64 MiB array inside the library, so meshes
+ * up to ≈ 104,000 elements at N = 3 (≈ 155,000 at N = 2) fit; larger ones
+ * are refused with DGSWE_ERR_INVALID. Every GPU on which the library's
+ * device code is loaded holds that array until the process exits. Every
+ * call shares it: calls that overlap on the GPU (other streams, other
+ * handles, other host threads) race. Each call writes every value it reads,
+ * so nothing needs clearing between calls.
+ * The call runs on the handle's own stream and does not wait for other
+ * streams: finish (or order by an event) the work that writes h/hu/hv
+ * before calling. It returns when the RHS is complete. A handle's first
+ * call looks up the array's device address (cudaGetSymbolAddress, with the
+ * handle's device current) and keeps it on the handle: make that first call
+ * before any stream capture. */
 int dgswe_compute_rhs_noalloc(dgswe_handle* handle, const double* h, const double* hu,
                               const double* hv, double time, double* out_h, double* out_hu,
                               double* out_hv, int64_t n);
