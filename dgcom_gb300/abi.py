@@ -387,6 +387,15 @@ CUDA_ONLY = {
     "autotune": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.POINTER(Tuning)]),
     "compute_rhs_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]),
+    # the Standard-kernel helpers of the reference's RHS bench, batched over
+    # elements on device arrays
+    "apply_diff_matrix": (C.c_int, [C.c_int] + [C.c_void_p] * 7 + [C.c_int64, C.c_int64]),
+    "apply_lift": (C.c_int, [C.c_int] + [C.c_void_p] * 7 + [C.c_int64, C.c_int64, C.c_void_p,
+                                                            C.c_int64]),
+    "coriolis_source": (C.c_int, [C.c_int] + [C.c_void_p] * 4 + [C.c_double, C.c_int64]),
+    "combine_derivatives": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)] + [C.c_void_p] * 4
+                            + [C.c_int64, C.c_int64]),
+    "helpers_last_error": (C.c_char_p, []),
     # ensembles of independent members
     "ensemble_create": (C.c_int, [C.POINTER(Form), C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
     "ensemble_destroy": (None, [C.c_void_p]),

@@ -633,6 +633,55 @@ int dgswe_compute_rhs_noalloc(dgswe_handle* handle, const double* h, const doubl
                               double* out_hv, int64_t n);
 
 /* ---------------------------------------------------------------------------
+ * The Standard-kernel helpers of the reference's RHS bench
+ * (benches/rhs_swe_2d_bench.rs), on the device.
+ *
+ * Each applies one helper of src/solver/simd/kernels.rs to n_elements
+ * elements at once: element e's vectors start at e·n_nodes (e·n_face_nodes
+ * for face data) in device arrays of the caller's; a matrix (D, LIFT) is one
+ * row-major device array shared by all elements. Every product and sum is
+ * rounded on its own, in the helper's order, so each element's result is
+ * the reference's helper's bit for bit (its scalar and SIMD forms agree).
+ * `device` is the GPU the pointers live on. Each call runs on the default
+ * stream and returns when it is complete. Errors: DGSWE_ERR_INVALID (NULL
+ * pointers, sizes), DGSWE_ERR_NO_DEVICE, DGSWE_ERR_CUDA; the text of the
+ * calling thread's last failure is dgswe_helpers_last_error(). */
+
+/* out = D·flux per element for h, hu, hv (n_nodes ≤ 64). Replaces
+ * apply_diff_matrix / apply_diff_matrix_scalar
+ * (src/solver/simd/kernels.rs:31-61, 315-359). */
+int dgswe_apply_diff_matrix(int device, const double* d, const double* flux_h,
+                            const double* flux_hu, const double* flux_hv, double* out_h,
+                            double* out_hu, double* out_hv, int64_t n_nodes, int64_t n_elements);
+
+/* out += scale[e]·LIFT·flux_diff per element (LIFT n_nodes × n_face_nodes).
+ * Replaces apply_lift / apply_lift_scalar (src/solver/simd/kernels.rs:74-104,
+ * 361-389), whose one `scale` becomes one per element. */
+int dgswe_apply_lift(int device, const double* lift, const double* flux_diff_h,
+                     const double* flux_diff_hu, const double* flux_diff_hv, double* out_h,
+                     double* out_hu, double* out_hv, int64_t n_nodes, int64_t n_face_nodes,
+                     const double* scale, int64_t n_elements);
+
+/* out_hu += f·hv, out_hv += −f·hu over n_values nodes. Replaces
+ * coriolis_source / coriolis_source_scalar (src/solver/simd/kernels.rs:
+ * 117-131, 391-403). */
+int dgswe_coriolis_source(int device, const double* hu, const double* hv, double* out_hu,
+                          double* out_hv, double f, int64_t n_values);
+
+/* out = −(dfx_dr·rx + dfx_ds·sx + dfy_dr·ry + dfy_ds·sy) per element, with
+ * `derivatives` the reference's twelve inputs in its argument order
+ * (dfx_dr_h, dfx_dr_hu, dfx_dr_hv, dfx_ds_h, …, dfy_ds_hv) and `metric`
+ * the element's (rx, sx, ry, sy), four per element. Replaces
+ * combine_derivatives / combine_derivatives_scalar
+ * (src/solver/simd/kernels.rs:184-224, 405-440). */
+int dgswe_combine_derivatives(int device, const double* const derivatives[12], double* out_h,
+                              double* out_hu, double* out_hv, const double* metric,
+                              int64_t n_nodes, int64_t n_elements);
+
+/* The text of the calling thread's last helper failure ("" if none). */
+const char* dgswe_helpers_last_error(void);
+
+/* ---------------------------------------------------------------------------
  * Ensembles: independent runs advanced together.
  *
  * No counterpart in the reference, which runs one case per

@@ -2454,4 +2454,62 @@ double oracle_tide_elevation(const dgswe_boundary* b, double t) {
     return bc.elevation(t);
 }
 
+
+// The Standard-kernel helpers (src/solver/simd/kernels.rs), one element
+// each, as the reference's scalar forms compute them
+
+// apply_diff_matrix_scalar (src/solver/simd/kernels.rs:31-61)
+void oracle_apply_diff_matrix(const double* d, const double* fh, const double* fhu,
+                              const double* fhv, double* oh, double* ohu, double* ohv, int64_t n) {
+    for (int64_t i = 0; i < n; ++i) {
+        double sh = 0.0, shu = 0.0, shv = 0.0;
+        for (int64_t j = 0; j < n; ++j) {
+            const double dij = d[i * n + j];
+            sh += dij * fh[j];
+            shu += dij * fhu[j];
+            shv += dij * fhv[j];
+        }
+        oh[i] = sh;
+        ohu[i] = shu;
+        ohv[i] = shv;
+    }
+}
+
+// apply_lift_scalar (src/solver/simd/kernels.rs:74-104)
+void oracle_apply_lift(const double* lift, const double* dh, const double* dhu, const double* dhv,
+                       double* oh, double* ohu, double* ohv, int64_t n, int64_t nf, double scale) {
+    for (int64_t i = 0; i < n; ++i) {
+        double sh = 0.0, shu = 0.0, shv = 0.0;
+        for (int64_t fi = 0; fi < nf; ++fi) {
+            const double l = lift[i * nf + fi];
+            sh += l * dh[fi];
+            shu += l * dhu[fi];
+            shv += l * dhv[fi];
+        }
+        oh[i] += scale * sh;
+        ohu[i] += scale * shu;
+        ohv[i] += scale * shv;
+    }
+}
+
+// coriolis_source_scalar (src/solver/simd/kernels.rs:117-131)
+void oracle_coriolis_source(const double* hu, const double* hv, double* ohu, double* ohv, double f,
+                            int64_t n) {
+    for (int64_t i = 0; i < n; ++i) {
+        ohu[i] += f * hv[i];
+        ohv[i] += -f * hu[i];
+    }
+}
+
+// combine_derivatives_scalar (src/solver/simd/kernels.rs:184-224)
+void oracle_combine_derivatives(const double* const in[12], double* oh, double* ohu, double* ohv,
+                                double rx, double sx, double ry, double sy, int64_t n) {
+    double* out[3] = {oh, ohu, ohv};
+    for (int64_t i = 0; i < n; ++i)
+        for (int v = 0; v < 3; ++v) {
+            const double div = in[v][i] * rx + in[3 + v][i] * sx + in[6 + v][i] * ry + in[9 + v][i] * sy;
+            out[v][i] = -div;
+        }
+}
+
 }  // extern "C"

@@ -72,6 +72,16 @@ void oracle_damp_nodes(int64_t n, const double* h, double* hu, double* hv, const
                        double h_dry, double relaxation_time);
 double oracle_tide_elevation(const dgswe_boundary* b, double t);
 
+/* the Standard-kernel helpers of the reference's RHS bench, one element */
+void oracle_apply_diff_matrix(const double* d, const double* fh, const double* fhu,
+                              const double* fhv, double* oh, double* ohu, double* ohv, int64_t n);
+void oracle_apply_lift(const double* lift, const double* dh, const double* dhu, const double* dhv,
+                       double* oh, double* ohu, double* ohv, int64_t n, int64_t nf, double scale);
+void oracle_coriolis_source(const double* hu, const double* hv, double* ohu, double* ohv, double f,
+                            int64_t n);
+void oracle_combine_derivatives(const double* const in[12], double* oh, double* ohu, double* ohv,
+                                double rx, double sx, double ry, double sy, int64_t n);
+
 #ifdef __cplusplus
 }
 #endif
