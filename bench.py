@@ -410,9 +410,11 @@ def run_ours(args, rank: int, world: int, local: int):
     dist.close()
 
 
-def plain_run_seconds(form, state, steps: int, warmup: int, cfl: float, device: int) -> float:
+def plain_run_seconds(form, state, steps: int, warmup: int, cfl: float, device: int,
+                      t_start: float = 0.0) -> float:
     """Host wall time of one plain-method run (dgswe_run, the CaseDevice
-    path) of ``steps`` SSP-RK3 steps of one member, after ``warmup`` steps."""
+    path) of ``steps`` SSP-RK3 steps of one member from ``t_start``, after
+    ``warmup`` steps."""
     import ctypes as C
 
     from dgcom_gb300 import abi
@@ -436,12 +438,39 @@ def plain_run_seconds(form, state, steps: int, warmup: int, cfl: float, device: 
             raise RuntimeError(lib.error_text(dev.handle, st))
         return report.final_time
 
-    t = run(warmup, 0.0) if warmup else 0.0
+    t = run(warmup, t_start) if warmup else t_start
     t0 = time.perf_counter()
     run(steps, t)
     seconds = time.perf_counter() - t0
     dev.close()
     return seconds
+
+
+def sequential_breakdown(per_member: list, steps: int, batched_seconds: float) -> dict:
+    """The sequential arm member by member: a least-squares fit of each
+    run's seconds per step to overhead + nodes / throughput, the share the
+    overhead takes, and the batching bound — the sequential time over the
+    time the members' work takes at the largest throughput any run reached
+    (a batched run that wasted nothing would take that long)."""
+    nodes = np.array([m[2] for m in per_member], dtype=np.float64)
+    per_step = np.array([m[3] for m in per_member]) / steps
+    a = np.stack([np.ones_like(nodes), nodes], axis=1)
+    (overhead, per_node), *_ = np.linalg.lstsq(a, per_step, rcond=None)
+    total = float(per_step.sum())
+    best = float((3.0 * nodes / per_step).max())          # DOF-updates/s of the fastest run
+    ideal = float(3.0 * nodes.sum() / best)                 # s per step of all members at it
+    sizes = np.quantile(nodes, [0.0, 0.5, 1.0]).tolist()
+    return {"members": len(per_member), "overhead_ms_per_run_step": 1e3 * float(overhead),
+            "ns_per_node_step": 1e9 * float(per_node),
+            "overhead_share": float(overhead) * len(per_member) / total,
+            "fastest_run_dof_per_s": best,
+            "sequential_ms_per_step": 1e3 * total,
+            "batched_ms_per_step": 1e3 * batched_seconds / steps,
+            "ideal_ms_per_step": 1e3 * ideal,
+            "bound_speedup": total / ideal,
+            "member_nodes_min_median_max": sizes,
+            "runs": [{"elements": m[0], "order": m[1], "ms_per_step": 1e3 * m[3] / steps}
+                     for m in per_member]}
 
 
 def member_share(members: list, rank: int, world: int) -> list:
@@ -468,18 +497,22 @@ def run_ensemble(args, rank: int, world: int, local: int):
     t_gen = time.perf_counter() - t_gen
     nodes = sum(c.form.n_values for c in mine)
     cfl = mine[0].cfl
+    # from rest at t = 0 (in the tide's ramp), or flowing after the ramp:
+    # η = 0.5 cos(2πx/Lx) m and (u, v) = (0.3, −0.1) m/s at the wet nodes
+    starts = [cases.with_flow(c) if args.ens_flowing else c.state for c in mine]
+    t_first = 7200.0 if args.ens_flowing else 0.0
     t_setup = time.perf_counter()
     ens = Ensemble([c.form for c in mine], local)
-    for i, c in enumerate(mine):
-        ens.upload(i, *c.state)
+    for i, q in enumerate(starts):
+        ens.upload(i, *q)
     t_setup = time.perf_counter() - t_setup
     if args.warmup:
-        ens.run(args.warmup, cfl)
+        ens.run(args.warmup, cfl, t_start=t_first)
     sampler = ClockSampler(local)
     dist.barrier()
     sampler.start()
     t0 = time.perf_counter()
-    reports, prof = ens.run(args.steps, cfl, t_start=float("nan"))
+    reports, prof = ens.run(args.steps, cfl, t_start=t_first if not args.warmup else float("nan"))
     wall = time.perf_counter() - t0
     clocks = sampler.stop()
     dist.barrier()
@@ -487,10 +520,15 @@ def run_ensemble(args, rank: int, world: int, local: int):
     total_nodes = dist.sum(float(nodes))
     value = 3.0 * total_nodes * args.steps / seconds
     ens.close()
-    # the same members, one plain-method run after another
+    # the same members, one plain-method run after another, each timed: its
+    # seconds per step against its nodes give the per-run overhead and the
+    # throughput a member reaches alone
     seq = 0.0
-    for c in mine:
-        seq += plain_run_seconds(c.form, c.state, args.steps, args.warmup, cfl, local)
+    per_member = []
+    for c, q in zip(mine, starts):
+        sec = plain_run_seconds(c.form, q, args.steps, args.warmup, cfl, local, t_first)
+        seq += sec
+        per_member.append((c.form.mesh.n_elements, c.form.order, c.form.n_values, sec))
     seq_seconds = dist.max(seq)
     seq_value = 3.0 * total_nodes * args.steps / seq_seconds
     orders = sorted({c.form.order for c in members})
@@ -503,7 +541,8 @@ def run_ensemble(args, rank: int, world: int, local: int):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": f"ensemble of {len(members)} coastal-box members, "
                                    f"{args.k_min}-{args.k_max} quads log-uniform, N in {orders}, "
-                                   "Manning n and M2 amplitude per member, SSP-RK3 from rest",
+                                   "Manning n and M2 amplitude per member, SSP-RK3 "
+                                   + ("flowing after the ramp" if args.ens_flowing else "from rest"),
                        "members": len(members), "elements": elements,
                        "nodes": int(total_nodes), "parallelism": f"members split over {world}",
                        "l2": "inputs larger than L2"},
@@ -514,6 +553,9 @@ def run_ensemble(args, rank: int, world: int, local: int):
             "gpu_launches": int(prof.face_launches + prof.stage_launches + prof.dt_launches
                                 + prof.control_launches),
             "setup_s": {"generate": t_gen, "create_and_upload": t_setup},
+            "sequential_breakdown": sequential_breakdown(per_member, args.steps, seconds),
+            "start": ("flowing after the ramp, from t = 2 h" if args.ens_flowing
+                      else "from rest at t = 0 in the tide's ramp"),
             "clocks": clocks,
             "members_failed": sum(0 if r.success else 1 for r in reports),
         }
@@ -891,6 +933,8 @@ def main():
     ap.add_argument("--members", type=int, default=256)
     ap.add_argument("--k-min", type=int, default=5_000)
     ap.add_argument("--k-max", type=int, default=200_000)
+    ap.add_argument("--ens-flowing", action="store_true",
+                    help="start the ensemble's members flowing, after the ramp")
     ap.add_argument("--adj-nx", type=int, default=1000)
     ap.add_argument("--adj-ny", type=int, default=100)
     ap.add_argument("--fd-directions", type=int, default=20)

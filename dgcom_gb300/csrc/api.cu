@@ -526,6 +526,8 @@ int create_impl(dgswe_handle* h, const dgswe_form* f, int device) {
     UP(weight_ratio, t.weight_ratio);
     UP(dtm_own, t.dtm_own);
     UP(dtm_face, t.dtm_face);
+    UP(dtm32_own, t.dtm32_own);
+    UP(dtm32_face, t.dtm32_face);
     UP(edge_geo, t.edge_geo);
     UP(bface_geo, t.bface_geo);
     UP(outer_idx, t.outer_idx);

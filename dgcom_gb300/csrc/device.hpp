@@ -25,6 +25,7 @@ struct DevTables {
     int64_t n_edges = 0, n_bfaces = 0;
     const double *bed, *jinv, *pair_hm, *gdb, *contra, *lift_scale, *outer_dist;
     const double *fcor, *g_n2, *mass, *inv_area, *weight_ratio, *dtm_own, *dtm_face;
+    const float *dtm32_own, *dtm32_face;  // dtm_own, dtm_face truncated to floats
     const double *edge_geo, *bface_geo;
     const int64_t *outer_idx, *nb_face_node, *edge_left, *edge_right, *bface;
     const int32_t* bface_cond;

@@ -135,6 +135,8 @@ int build_group(dgswe_ensemble* h, Group& G, std::vector<Tables>& tabs,
         append(all.weight_ratio, t.weight_ratio);
         append(all.dtm_own, t.dtm_own);
         append(all.dtm_face, t.dtm_face);
+        append(all.dtm32_own, t.dtm32_own);
+        append(all.dtm32_face, t.dtm32_face);
         append(all.nb_face_node, t.nb_face_node);
         append(all.edge_left, t.edge_left);
         append(all.edge_right, t.edge_right);
@@ -181,6 +183,8 @@ int build_group(dgswe_ensemble* h, Group& G, std::vector<Tables>& tabs,
     UP(weight_ratio, all.weight_ratio);
     UP(dtm_own, all.dtm_own);
     UP(dtm_face, all.dtm_face);
+    UP(dtm32_own, all.dtm32_own);
+    UP(dtm32_face, all.dtm32_face);
     UP(edge_geo, all.edge_geo);
     UP(bface_geo, all.bface_geo);
     UP(outer_idx, all.outer_idx);

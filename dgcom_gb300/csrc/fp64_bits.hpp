@@ -82,5 +82,25 @@ DG_HD bool gt_nn(double a, double b) { return bits(a) > bits(b); }
 DG_HD double max_nn(double a, double b) { return bits(a) > bits(b) ? a : b; }
 DG_HD double min_nn(double a, double b) { return bits(a) < bits(b) ? a : b; }
 
+// The float at or toward zero from a double: sign, rebiased exponent and
+// the top 23 bits of the mantissa, by integer operations (on the device a
+// conversion instruction would run on the FP64 pipe); ±0 below 2^-126, ±∞
+// from 2^128. The same bits on the host (tables built there) and on the
+// device.
+DG_HD float f32_trunc(double x) {
+    const uint64_t b = (uint64_t)bits(x);
+    const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+    const uint32_t e = (uint32_t)(b >> 52) & 0x7FFu;
+    const uint32_t mag = (uint32_t)(b >> 29) - (896u << 23);
+    const uint32_t out = sign | (e <= 896u ? 0u : (e >= 1151u ? 0x7F800000u : mag));
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(out);
+#else
+    float f;
+    memcpy(&f, &out, sizeof f);
+    return f;
+#endif
+}
+
 }  // namespace fp
 }  // namespace dgswe

@@ -970,30 +970,34 @@ __global__ void velocity_kernel(DevBuf b, int64_t n, double h_min) {
 // ---------------------------------------------------------------------------
 // the time step (src/solver/rhs/swe_2d.rs:2072-2115, 1346-1367, 2165-2258)
 
-// The dt pass stages each node's rate, depth and mass weight per element,
-// then one lane per element takes the maximum and the positivity sums in
-// node order, the reference's order: a sum spread over an element's lanes
-// would serialise on one lane per element and hold the FP64 pipe for the
-// whole warp each step.
+// The dt pass. An element's step needs only the largest of its nodes' rates
+// (its own nodes and the neighbours' face nodes, each with its own metric),
+// so the rates are first taken in single precision — on the FP32 and
+// integer pipes, which run 64 times faster than the FP64 pipe — with a bound
+// on their error; only the rates that can still be the largest are then
+// computed in FP64, by dense lanes from a list in shared memory, and their
+// maximum is the exact one. One lane per element then takes the positivity
+// sums in node order, the reference's order.
+//
+// node_rate_f32 (point.cuh) is within 2⁻²⁰·B of the FP64 rate, B its error
+// scale; a node whose r₃₂ + δ·B is below the largest r₃₂ − δ·B of its
+// element (δ = 2⁻¹⁶, sixteen times the bound) cannot hold the maximum.
 template <int N1>
 struct DtCfg {
     static constexpr int NN = N1 * N1;
     static constexpr int EPB = 32;  // elements per block: one lane of warp 0 each
     static constexpr int THREADS = EPB * NN;
     static constexpr int PITCH = NN + 1;  // odd row pitch: lanes spread over the banks
+    static constexpr int SLOTS = NN + 4 * N1;  // own nodes, then neighbours' face nodes
 };
 
-// The element's dt from its nodes' rates, depths and mass weights
-// (element_dt, swe_2d.rs:2072-2115, with PositivityBound::element_cfl and
-// positivity_relaxation, swe_2d.rs:2220-2258)
+// The element's dt from its largest rate and its nodes' depths and mass
+// weights (element_dt, swe_2d.rs:2072-2115, with PositivityBound::element_cfl
+// and positivity_relaxation, swe_2d.rs:2220-2258)
 template <int N1>
 __device__ __forceinline__ double element_dt(const DtParams& D, int order, double weight_ratio,
-                                             const double* rate, const double* h,
-                                             const double* mass) {
+                                             double rmax, const double* h, const double* mass) {
     constexpr int NN = N1 * N1;
-    double rmax = 0.0;
-#pragma unroll
-    for (int p = 0; p < NN; ++p) rmax = fp::max_nn(rate[p], rmax);  // rates are ≥ +0
     double cfl = D.cfl;
     if (D.positivity) {
         double water = 0.0, water_b = 0.0;
@@ -1022,8 +1026,13 @@ __global__ void __launch_bounds__(DtCfg<N1>::THREADS)
     dt_kernel(DevTables T, Physics P, DevBuf q, DtParams D, double* dt_el, StepCtl* ctl,
               const int* active) {
     using C = DtCfg<N1>;
-    constexpr int NN = C::NN, EPB = C::EPB, PITCH = C::PITCH;
-    __shared__ double s_rate[EPB * PITCH];
+    constexpr int NN = C::NN, EPB = C::EPB, PITCH = C::PITCH, SLOTS = C::SLOTS;
+    __shared__ float s_r[EPB][SLOTS];                 // r₃₂, −1 for a dry node
+    __shared__ float s_b[EPB][SLOTS];                 // δ·B
+    __shared__ unsigned int s_lo[EPB];                // the element's largest r₃₂ − δ·B (bits)
+    __shared__ unsigned long long s_rmax[EPB];        // its largest exact rate (bits)
+    __shared__ short s_list[EPB * SLOTS];             // candidates: e·SLOTS + slot
+    __shared__ int s_count;
     __shared__ double s_h[EPB * PITCH];
     __shared__ double s_mass[EPB * PITCH];
     if (!*active) return;
@@ -1033,31 +1042,89 @@ __global__ void __launch_bounds__(DtCfg<N1>::THREADS)
     const int64_t k = k0 + e;
     const int64_t gi = k * NN + i;
     const double g = P.g, h_min = P.h_min;
-    double rate = 0.0, h = 0.0, mass = 0.0;
+    const float g32 = f32_trunc(g);
+    constexpr float kDelta = 1.0f / 65536.0f;      // δ = 2⁻¹⁶
+    constexpr float kFloor = 1e-30f;               // the sub-float-range terms
+    if (tid < EPB) {
+        s_lo[tid] = 0u;
+        s_rmax[tid] = 0ull;  // +0: a dry node's rate
+    }
+    if (tid == 0) s_count = 0;
+    double h = 0.0, mass = 0.0;
+    // single-precision rates of the node and of the neighbour face nodes it takes
+    auto slot_rate = [&](int slot, double hs, double us, double vs, const float* m) {
+        float r = -1.0f, b = 0.0f;
+        if (fp::gt(hs, h_min)) {
+            node_rate_f32(hs, us, vs, m, g32, r, b);
+            b = kDelta * b + kFloor;
+        }
+        s_r[e][slot] = r;
+        s_b[e][slot] = b;
+    };
     if (k < T.K) {
         h = q.h[gi];
         mass = T.mass[gi];
-        if (fp::gt(h, h_min)) rate = node_rate(h, q.u[gi], q.v[gi], &T.dtm_own[gi * 6], g);
+        slot_rate(i, h, q.u[gi], q.v[gi], &T.dtm32_own[gi * 6]);
         for (int it = i; it < 4 * N1; it += NN) {
             const int64_t o = k * 4 * N1 + it;
             const int64_t nb = T.nb_face_node[o];
-            if (nb < 0) continue;
-            const double hn = q.h[nb];
-            if (!fp::gt(hn, h_min)) continue;
-            rate = fp::max_nn(node_rate(hn, q.u[nb], q.v[nb], &T.dtm_face[o * 6], g), rate);
+            if (nb < 0) {
+                s_r[e][NN + it] = -1.0f;
+                s_b[e][NN + it] = 0.0f;
+                continue;
+            }
+            slot_rate(NN + it, q.h[nb], q.u[nb], q.v[nb], &T.dtm32_face[o * 6]);
         }
     }
-    s_rate[e * PITCH + i] = rate;
     s_h[e * PITCH + i] = h;
     s_mass[e * PITCH + i] = mass;
+    __syncthreads();
+    // the element's threshold: its largest r₃₂ − δ·B (non-negative floats
+    // order as their bits)
+    if (k < T.K) {
+        for (int sl = i; sl < SLOTS; sl += NN) {
+            const float r = s_r[e][sl];
+            if (r >= 0.0f) atomicMax(&s_lo[e], __float_as_uint(fmaxf(r - s_b[e][sl], 0.0f)));
+        }
+    }
+    __syncthreads();
+    if (k < T.K) {
+        const float lo = __uint_as_float(s_lo[e]);
+        for (int sl = i; sl < SLOTS; sl += NN) {
+            const float r = s_r[e][sl];
+            if (r >= 0.0f && r + s_b[e][sl] >= lo)
+                s_list[atomicAdd(&s_count, 1)] = (short)(e * SLOTS + sl);
+        }
+    }
+    __syncthreads();
+    // exact rates of the candidates, one per lane
+    const int n_cand = s_count;
+    for (int c = tid; c < n_cand; c += C::THREADS) {
+        const int es = s_list[c];
+        const int ce = es / SLOTS, sl = es % SLOTS;
+        const int64_t kc = k0 + ce;
+        int64_t node;
+        const double* m;
+        if (sl < NN) {
+            node = kc * NN + sl;
+            m = &T.dtm_own[node * 6];
+        } else {
+            const int64_t o = kc * 4 * N1 + (sl - NN);
+            node = T.nb_face_node[o];
+            m = &T.dtm_face[o * 6];
+        }
+        const double r = node_rate(q.h[node], q.u[node], q.v[node], m, g);
+        atomicMax(&s_rmax[ce], (unsigned long long)fp::bits(r));  // r ≥ +0
+    }
     __syncthreads();
     if (tid >= 32) return;  // warp 0: lane l finishes element k0 + l
     const int64_t kl = k0 + tid;
     unsigned long long dt_bits = 0x7FF0000000000000ull;  // +∞
     int member = -1;
     if (kl < T.K) {
-        const double dt = element_dt<N1>(D, P.order, T.weight_ratio[kl], &s_rate[tid * PITCH],
-                                         &s_h[tid * PITCH], &s_mass[tid * PITCH]);
+        const double rmax = fp::from_bits((int64_t)s_rmax[tid]);
+        const double dt = element_dt<N1>(D, P.order, T.weight_ratio[kl], rmax, &s_h[tid * PITCH],
+                                         &s_mass[tid * PITCH]);
         if (dt_el) dt_el[kl] = dt;
         dt_bits = (unsigned long long)fp::bits(dt);
         member = T.elem_member ? T.elem_member[kl] : 0;

@@ -405,6 +405,24 @@ DG_PT double node_rate(double h, double u, double v, const double* m,
     return lr + ls;
 }
 
+using fp::f32_trunc;
+
+// node_rate in single precision from truncated inputs (the metric m already
+// truncated: f32_trunc of the double table), and its error scale
+// B = (|u| + |v| + c)·(m4 + m5): each term of the rate (|u·m0 + v·m1|,
+// c·m4, …) is within 2^-20 of its magnitude (truncation < 2^-23 per input,
+// rounding 2^-24 per operation), and the magnitudes sum to at most B since
+// |m0|, |m1| ≤ m4 and |m2|, |m3| ≤ m5; so |node_rate − r| ≤ 2^-20·B, less
+// terms of the size of 2^-126 from values below the float range
+DG_PT void node_rate_f32(double h, double u, double v, const float* m, float g32, float& r,
+                         float& bound) {
+    const float h32 = f32_trunc(h), u32 = f32_trunc(u), v32 = f32_trunc(v);
+    const float m0 = m[0], m1 = m[1], m2 = m[2], m3 = m[3], m4 = m[4], m5 = m[5];
+    const float c = sqrtf(g32 * h32);
+    r = (fabsf(u32 * m0 + v32 * m1) + c * m4) + (fabsf(u32 * m2 + v32 * m3) + c * m5);
+    bound = (fabsf(u32) + fabsf(v32) + c) * (m4 + m5);
+}
+
 // The interior velocity of BCContext2D (velocity_simple): (hu, hv)/h where
 // h > h_min, else 0
 DG_PT void interior_velocity(const Q& qi, double h_min, double& u, double& v) {

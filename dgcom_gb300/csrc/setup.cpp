@@ -2,6 +2,8 @@
 
 #include "setup.hpp"
 
+#include "fp64_bits.hpp"
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -557,6 +559,10 @@ std::string build_tables(const dgswe_form& f, const Operators& ops, const Topolo
                 t.bface_geo.insert(t.bface_geo.end(), g5, g5 + 5);
             }
         }
+    t.dtm32_own.resize(t.dtm_own.size());
+    t.dtm32_face.resize(t.dtm_face.size());
+    for (size_t i = 0; i < t.dtm_own.size(); ++i) t.dtm32_own[i] = fp::f32_trunc(t.dtm_own[i]);
+    for (size_t i = 0; i < t.dtm_face.size(); ++i) t.dtm32_face[i] = fp::f32_trunc(t.dtm_face[i]);
     return "";
 }
 

@@ -106,6 +106,9 @@ struct Tables {
     std::vector<double> weight_ratio; // [K] W/W∂
     std::vector<double> dtm_own;    // [K·nn·6] ¼ of ∇r, ∇s, |∇r|, |∇s| of own nodes
     std::vector<double> dtm_face;   // [K·4·n1·6] the same at face nodes (own node's stored)
+    // the same two tables as floats truncated toward zero (f32_trunc), read
+    // by the dt pass's single-precision filter
+    std::vector<float> dtm32_own, dtm32_face;
     std::vector<int64_t> nb_face_node; // [K·4·n1] neighbour's coincident node (global) or −1
     // faces
     std::vector<int64_t> edge_left, edge_right; // [E] k·4 + face

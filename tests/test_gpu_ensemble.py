@@ -88,3 +88,38 @@ def test_two_runs_continue_like_one():
             want, t_want = alone(c.form, states[i], 4)
             assert reports[i].final_time == t_want
             assert all(np.array_equal(g, w) for g, w in zip(ens.download(i), want))
+
+
+def test_mixed_order_members_match_the_oracle():
+    """Each member of a batched run of mixed orders (two coastal boxes of
+    order 2 and 3, and a drying channel of order 3) against the oracle
+    stepping that member alone: every step from the same state, the
+    member's own time step to 1e-13 and its state to 1e-12 of each field's
+    largest value."""
+    from oracle_lib import oracle
+
+    ms = members(abi.NUMERICS_FAST)
+    assert {c.form.order for c in ms} == {2, 3}
+    states = [cases.with_flow(c) for c in ms]
+    refs = [oracle(c.form) for c in ms]
+    t = [0.0] * len(ms)
+    try:
+        with Ensemble([c.form for c in ms]) as ens:
+            for i, s in enumerate(states):
+                ens.upload(i, *s)
+                refs[i].upload(*s)
+            for step in range(5):
+                reports, _ = ens.run(1, CFL, t_start=0.0 if step == 0 else float("nan"))
+                for i, ref in enumerate(refs):
+                    dt = ref.compute_dt_ssp(CFL)
+                    ref.step(t[i], dt)
+                    t[i] += dt
+                    assert abs(reports[i].final_time - t[i]) <= 1e-13 * t[i], (i, step)
+                    got, want = ens.download(i), ref.download()
+                    for g, w in zip(got, want):
+                        err = np.abs(g - w).max() / max(np.abs(w).max(), 1e-300)
+                        assert err <= 1e-12, f"member {i} (order {ms[i].form.order}), step {step}: {err:.3e}"
+                    ens.upload(i, *want)
+    finally:
+        for r in refs:
+            r.close()

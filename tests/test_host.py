@@ -161,3 +161,26 @@ def test_coastal_paving_is_an_unstructured_conforming_quad_mesh():
     assert 70.0 < lo < 130.0 and 330.0 < hi < 470.0, (lo, hi)
     valence = np.bincount(a, minlength=v.shape[0])
     assert (valence == 3).any() and (valence > 4).any()
+
+
+def test_dt_single_precision_filter_bound(tmp_path):
+    """The dt pass's float rates (point.cuh node_rate_f32) stay within their
+    stated error bound of the double rates, and the filter keeps every
+    element's largest rate, on random nodes (host build)."""
+    import shutil
+    import subprocess
+    from pathlib import Path
+
+    gxx = shutil.which("g++")
+    if gxx is None:
+        import pytest
+
+        pytest.skip("g++ not available")
+    here = Path(__file__).resolve().parent
+    exe = tmp_path / "dt_filter_check"
+    subprocess.run([gxx, "-O2", "-std=c++17", "-ffp-contract=off",
+                    "-I", str(here.parent / "dgcom_gb300" / "csrc"),
+                    str(here / "dt_filter_check.cpp"), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert out.stdout.startswith("ok ")
