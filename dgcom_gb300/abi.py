@@ -383,6 +383,9 @@ CUDA_ONLY = {
                                  C.POINTER(C.c_uint8), C.POINTER(C.c_int32)]),
     "planner_spread": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint8), C.c_int32,
                                  C.POINTER(C.c_uint8), C.POINTER(C.c_uint8)]),
+    # a step of a host state: upload, dt, step, download overlapped
+    "step_host": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_double, _dp, _dp,
+                            _dp, C.c_int64, _dp]),
     # device pointers in and out; working memory in the library's own array
     "autotune": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.POINTER(Tuning)]),
     "compute_rhs_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,

@@ -888,6 +888,112 @@ int dgswe_step(dgswe_handle* h, int32_t scheme, double t, double dt) {
     return sync(h);
 }
 
+int dgswe_step_host(dgswe_handle* h, int32_t scheme, double t, double cfl, double dt_max,
+                    double* hh, double* hu, double* hv, int64_t n, double* dt_out) {
+    if (!h) return DGSWE_ERR_INVALID;
+    if (scheme != DGSWE_SSP_RK3 && scheme != DGSWE_SSP_RK43)
+        return fail(h, DGSWE_ERR_INVALID, "step_host: scheme %d", scheme);
+    if (n != h->n_values || !hh || !hu || !hv || !(cfl > 0.0) || !(dt_max >= 0.0))
+        return fail(h, DGSWE_ERR_INVALID,
+                    "step_host: %lld values (expected %lld), NULL arrays, cfl %g or dt_max %g",
+                    (long long)n, (long long)h->n_values, cfl, dt_max);
+    if (!(t >= h->parent_range.first && t < h->parent_range.second))
+        return fail(h, DGSWE_ERR_INVALID, "step_host: t = %g leaves the forcing's snapshots", t);
+    CK(cudaSetDevice(h->device));
+    double st[4][4];
+    const int n_st = scheme_table(scheme, st);
+    for (int b = 1; b < n_st; ++b)
+        if (int s = ensure_buffer(h, b)) return s;
+    if (!h->copy_stream) {
+        CK(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+        for (cudaEvent_t& e : h->chunk_done)
+            CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    // one step of the device clock from t; it lands on the end of any
+    // forcing series' snapshots rather than leave them
+    {
+        long long clips0 = 0;
+        CK(cudaMemcpy(&clips0, &h->ctl->clips, sizeof clips0, cudaMemcpyDeviceToHost));
+        StepCtl& c = *h->h_ctl;
+        std::memset(&c, 0, sizeof c);
+        c.t = t;
+        c.t_end = h->parent_range.second;
+        c.target = h->parent_range.second;
+        c.dt_max = dt_max;
+        c.cfl = cfl;
+        c.dt_min_used = INFINITY;
+        c.dt_bits = 0x7FF0000000000000ull;
+        c.clips = clips0;
+        c.always = 1;
+        c.scheme_stages = n_st;
+        for (int s = 0; s < n_st; ++s) {
+            c.st_start[s] = st[s][0];
+            c.st_input[s] = st[s][1];
+            c.st_beta[s] = st[s][2];
+            c.st_c[s] = st[s][3];
+        }
+        CK(cudaMemcpyAsync(h->ctl, &c, sizeof c, cudaMemcpyHostToDevice, h->stream));
+    }
+    // the state in element chunks on the copy stream, each chunk's node
+    // velocities computed while the next one arrives
+    const DevBuf& q = h->buf[DGSWE_STATE].view;
+    const int64_t per = (h->K + kHostChunks - 1) / kHostChunks;
+    CK(cudaEventRecord(h->chunk_done[0], h->stream));  // after the work queued before
+    CK(cudaStreamWaitEvent(h->copy_stream, h->chunk_done[0], 0));
+    for (int c = 0; c < kHostChunks; ++c) {
+        const int64_t k0 = c * per, k1 = std::min<int64_t>(h->K, k0 + per);
+        if (k1 <= k0) break;
+        const size_t off = (size_t)k0 * h->nn, cnt = (size_t)(k1 - k0) * h->nn;
+        const size_t len = cnt * sizeof(double);
+        CK(cudaMemcpyAsync(q.h + off, hh + off, len, cudaMemcpyHostToDevice, h->copy_stream));
+        CK(cudaMemcpyAsync(q.hu + off, hu + off, len, cudaMemcpyHostToDevice, h->copy_stream));
+        CK(cudaMemcpyAsync(q.hv + off, hv + off, len, cudaMemcpyHostToDevice, h->copy_stream));
+        CK(cudaEventRecord(h->chunk_done[c], h->copy_stream));
+        CK(cudaStreamWaitEvent(h->stream, h->chunk_done[c], 0));
+        const DevBuf part{q.h + off, q.hu + off, q.hv + off, q.u + off, q.v + off};
+        h->ks->velocity(part, (int64_t)cnt, h->P.h_min, h->stream);
+    }
+    const int* active = &h->ctl->active;
+    const DtParams D = dt_params(h->form, cfl, scheme);
+    h->ks->step_begin(h->ctl, 1, h->stream);
+    h->ks->dt(h->n1, h->T, h->P, q, D, nullptr, h->ctl, active, h->stream);
+    h->ks->step_dt(h->ctl, 1, h->stream);
+    for (int s = 0; s + 1 < n_st; ++s)
+        launch_stage(h, s == 0 ? DGSWE_STATE : s, DGSWE_STATE, s + 1, DGSWE_STATE, s, kModePost, 0,
+                     active);
+    // the last stage in element chunks, each copied back while the next runs
+    const int last = n_st - 1;
+    const DevBuf& in = h->buf[last].view;
+    h->ks->face(h->n1, h->T, h->P, in, h->fb_h, h->fb_hu, h->fb_hv, h->ctl, last, active,
+                h->stream);
+    for (int c = 0; c < kHostChunks; ++c) {
+        const int64_t k0 = c * per, k1 = std::min<int64_t>(h->K, k0 + per);
+        if (k1 <= k0) break;
+        StageExtra X = h->X;
+        X.k_first = k0;
+        X.k_last = k1;
+        h->ks->stage(h->n1, h->T, h->P, X, in, q, q, q, h->fb_h, h->fb_hu, h->fb_hv, h->ctl, last,
+                     kModePost, 1, active, h->stream);
+        CK(cudaEventRecord(h->chunk_done[c], h->stream));
+        CK(cudaStreamWaitEvent(h->copy_stream, h->chunk_done[c], 0));
+        const size_t off = (size_t)k0 * h->nn, len = (size_t)(k1 - k0) * h->nn * sizeof(double);
+        CK(cudaMemcpyAsync(hh + off, q.h + off, len, cudaMemcpyDeviceToHost, h->copy_stream));
+        CK(cudaMemcpyAsync(hu + off, q.hu + off, len, cudaMemcpyDeviceToHost, h->copy_stream));
+        CK(cudaMemcpyAsync(hv + off, q.hv + off, len, cudaMemcpyDeviceToHost, h->copy_stream));
+    }
+    h->ks->step_end(h->ctl, 1, h->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(h->h_ctl, h->ctl, sizeof(StepCtl), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->copy_stream));
+    if (int s = sync(h)) return s;
+    const StepCtl& c = *h->h_ctl;
+    if (dt_out) *dt_out = c.dt;
+    if (c.failure || c.nonfinite || !c.active)
+        return fail(h, DGSWE_ERR_NONFINITE, "step_host: the step did not complete (%d%s)",
+                    c.failure, c.nonfinite ? ", a non-finite state" : "");
+    return DGSWE_OK;
+}
+
 int dgswe_run(dgswe_handle* h, const dgswe_run_config* run, dgswe_callback callback, void* user,
               dgswe_report* report) {
     if (!h) return DGSWE_ERR_INVALID;

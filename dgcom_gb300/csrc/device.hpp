@@ -139,6 +139,9 @@ struct StageExtra {
     // a RHS that keeps its subcell mass fluxes: [K][2·n1·(n1 − 1)], NaN in
     // the elements without subcells (null: not kept)
     double* subcell_mass = nullptr;
+    // the elements [k_first, k_last) a whole-mesh stage pass covers (a pass
+    // in chunks, each chunk's result copied out while the next runs)
+    int64_t k_first = 0, k_last = INT64_MAX;
 };
 
 // The element step's parameters: the CFL and the positivity bound of a

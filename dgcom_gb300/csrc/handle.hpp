@@ -21,6 +21,13 @@ namespace host {
 
 constexpr int kRhsBuffer = DGSWE_N_BUFFERS;  // scratch buffer of dgswe_compute_rhs
 
+}  // namespace host
+
+// dgswe_step_host's upload and last stage run in this many element chunks
+constexpr int kHostChunks = 8;
+
+namespace host {
+
 struct DeviceBuffer {
     double* base = nullptr;  // one allocation of 5 fields
     DevBuf view{};
@@ -91,8 +98,15 @@ struct dgswe_handle {
     // device address of dgswe_compute_rhs_noalloc's working array, looked up
     // by the handle's first call to it (not memory the handle owns)
     double* noalloc_scratch = nullptr;
+    // dgswe_step_host: the stream that copies the state in and out beside
+    // the compute, and one event per chunk (created on first use)
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t chunk_done[dgswe::kHostChunks] = {};
 
     ~dgswe_handle() {
+        for (cudaEvent_t e : chunk_done)
+            if (e) cudaEventDestroy(e);
+        if (copy_stream) cudaStreamDestroy(copy_stream);
         delete planner;
         if (dplan.host) cudaFreeHost(dplan.host);
         for (cudaEvent_t e : ev_lts)

@@ -437,10 +437,12 @@ __global__ void __launch_bounds__(Cfg<N1, SHAPE>::THREADS, Cfg<N1, SHAPE>::MIN_B
     const int e = tid / NN, i = tid % NN;
     int64_t k = (int64_t)blockIdx.x * EPB + e;
     if (LISTED) k = k < lp.n ? (int64_t)lp.list[k] : T.K;
+    else k += X.k_first;
+    const int64_t k_end = (LISTED || X.k_last > T.K) ? T.K : X.k_last;
     // the element's member (its StepCtl); an ensemble member that has
     // stopped keeps its state: its elements take no part
-    StepCtl* const cm = ctl + ((T.elem_member && k < T.K) ? T.elem_member[k] : 0);
-    const bool valid = k < T.K && (!T.elem_member || cm->active);
+    StepCtl* const cm = ctl + ((T.elem_member && k < k_end) ? T.elem_member[k] : 0);
+    const bool valid = k < k_end && (!T.elem_member || cm->active);
     const int64_t gi = k * NN + i;
     const int a = i % N1, j = i / N1;
     const double g = P.g, h_min = P.h_min, sqrt_g = P.sqrt_g, half_g = P.half_g;

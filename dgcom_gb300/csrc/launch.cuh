@@ -53,16 +53,20 @@ static void stage_n(const DevTables& T, const Physics& P, const StageExtra& X, c
                     const DevBuf& base, const DevBuf& out, const DevBuf& acc, const double* fh,
                     const double* fhu, const double* fhv, StepCtl* ctl, int slot, int mode,
                     int check_finite, const int* active, const DevBuf& keep, cudaStream_t s) {
+    // the pass's elements: all, or the chunk [k_first, k_last) of X
+    const int64_t k1 = X.k_last < T.K ? X.k_last : T.K;
+    const int64_t count = k1 - X.k_first;
+    if (count <= 0) return;
     if (P.stage_shape == 1) {
         using C1 = Cfg<N1, 1>;
-        const unsigned blocks = (unsigned)((T.K + C1::EPB - 1) / C1::EPB);
+        const unsigned blocks = (unsigned)((count + C1::EPB - 1) / C1::EPB);
         stage_kernel<N1, false, 1><<<blocks, C1::THREADS, 0, s>>>(
             T, P, X, in, base, out, acc, fh, fhu, fhv, ctl, slot, mode, check_finite, active, keep,
             LtsPass{});
         return;
     }
     using C = Cfg<N1>;
-    const unsigned blocks = (unsigned)((T.K + C::EPB - 1) / C::EPB);
+    const unsigned blocks = (unsigned)((count + C::EPB - 1) / C::EPB);
     stage_kernel<N1, false><<<blocks, C::THREADS, 0, s>>>(T, P, X, in, base, out, acc, fh, fhu, fhv,
                                                           ctl, slot, mode, check_finite, active,
                                                           keep, LtsPass{});

@@ -211,6 +211,19 @@ class SWEPhysics2D:
         """One fused one-level SSP step of the state."""
         self._check(self.lib.step(self.handle, scheme, t, dt), "step")
 
+    def step_host(self, t: float, cfl: float, h, hu, hv, scheme: int = abi.SSP_RK3,
+                  dt_max: float = 0.0) -> float:
+        """One step of a host state (contiguous float64 arrays of n_values,
+        updated in place): upload, the CFL step on the device, the step, the
+        result copied back while the last stage runs. Returns the step."""
+        for a in (h, hu, hv):
+            if a.dtype != np.float64 or not a.flags.c_contiguous or a.size != self.n_values:
+                raise ValueError("step_host takes contiguous float64 arrays of n_values")
+        dt = C.c_double()
+        self._check(self.lib.step_host(self.handle, scheme, t, cfl, dt_max, _ptr(h), _ptr(hu),
+                                       _ptr(hv), self.n_values, C.byref(dt)), "step_host")
+        return dt.value
+
     def negative_depth_clips(self) -> int:
         return int(self.lib.negative_depth_clips(self.handle))
 

@@ -472,6 +472,22 @@ int dgswe_element_dt(dgswe_handle* handle, double cfl, int32_t scheme,
  * src/time/multirate.rs:1285-1315). */
 int dgswe_step(dgswe_handle* handle, int32_t scheme, double t, double dt);
 
+/* One global SSP step of a state the caller holds on the host, as the
+ * reference's CPU solver steps its SWESolution2D in place
+ * (SSPRK3::step_with_relaxation, src/time/integrator.rs:472-500, with the
+ * step of compute_dt_ssp): uploads h, hu, hv (n = dgswe_n_values each),
+ * takes the positivity-bounded CFL step at `cfl` on the device (capped at
+ * dt_max when it is > 0; it lands on the end of any forcing series'
+ * snapshots rather than leave them), advances the state from t and writes
+ * it back into the same arrays, and the step taken into dt_out (may be
+ * NULL). The upload and the last stage run in element chunks, each chunk
+ * copied while the next one computes; page-locked host arrays give the full
+ * overlap. The result is that of dgswe_upload, dgswe_element_dt,
+ * dgswe_step and dgswe_download, bit for bit; the state buffer holds it
+ * too. DGSWE_ERR_NONFINITE if the new state is not finite. */
+int dgswe_step_host(dgswe_handle* handle, int32_t scheme, double t, double cfl, double dt_max,
+                    double* h, double* hu, double* hv, int64_t n, double* dt_out);
+
 /* Simulation::run_with_callback (src/simulation/runner.rs:264-500) on the
  * state: dt from the positivity-bounded element steps, capped by dt_max,
  * landing on every callback time and the end; the callback gets the state
