@@ -153,13 +153,17 @@ class Adjoint:
             dts_out.ctypes.data_as(_dp), C.byref(J)))
         return J.value, eta, dts_out
 
-    def reverse(self) -> Gradient:
+    def reverse(self, bed: bool = True) -> Gradient:
+        """The gradients of the last forward sweep; ``bed=False`` skips the
+        bed's (its field is then zero), which the sweep then does not form."""
         n = self.n_values
         out = [np.zeros(n) for _ in range(5)]
         nb = max(1, sum(self.n_conditions))
         tide = np.zeros((nb, abi.MAX_CONSTITUENTS, 2))
-        self._check(self.lib.adjoint_reverse(self.handle, *(_ptr(x) for x in out),
-                                             tide.ctypes.data_as(_dp)))
+        ptrs = [_ptr(x) for x in out]
+        if not bed:
+            ptrs[3] = None
+        self._check(self.lib.adjoint_reverse(self.handle, *ptrs, tide.ctypes.data_as(_dp)))
         return Gradient(*out, tide)
 
     def set_parameters(self, manning=None, tide=None):

@@ -108,6 +108,8 @@ struct dgswe_adjoint {
     DevBuf S[4]{};  // the step's stage inputs and last output
     DevBuf Kp[3]{}; // kept combination and damped momentum of each stage
     double *lam[3] = {}, *lam_t[3] = {}, *lam_b[3] = {};
+    // the current reverse sweep sums λ of the bed (its caller asked for it)
+    bool want_bed = true;
     AdjStage A{};
     bool forward_done = false;
     dgswe_adjoint_stats stats{};
@@ -282,6 +284,7 @@ int reverse_stages(dgswe_adjoint* a, const DevBuf* in, const DevBuf* keep) {
         As.lo_h = lo[0];
         As.lo_hu = lo[1];
         As.lo_hv = lo[2];
+        if (!a->want_bed) As.lbed = nullptr;  // λ of the bed neither summed nor written
         t.ks->stage_adjoint(t.n1, *t.T, *t.P, *t.X, in[s], keep[s], As, t.ctl, s, st);
         t.ks->face_adjoint(t.n1, *t.T, *t.P, in[s], As, t.ctl, s, st);
         t.ks->adjoint_combine(in[s], As, a->lam_t[0], a->lam_t[1], a->lam_t[2], nv, t.P->h_min,
@@ -740,6 +743,7 @@ int dgswe_adjoint_reverse(dgswe_adjoint* a, double* grad_h0, double* grad_hu0, d
         ACK(cudaMemsetAsync(a->lam_b[c], 0, bv, st));
     }
     AdjStage& A = a->A;
+    a->want_bed = grad_bed != nullptr;
     ACK(cudaMemsetAsync(A.lx_h, 0, 5 * bv, st));
     ACK(cudaMemsetAsync(A.lbed, 0, bv, st));
     ACK(cudaMemsetAsync(A.lgn2, 0, bv, st));
@@ -789,7 +793,8 @@ int dgswe_adjoint_reverse(dgswe_adjoint* a, double* grad_h0, double* grad_hu0, d
             }
             for (int64_t n = c1 - 1; n >= c0; --n) {
                 t.ks->station_seed(a->d_eta + n * n_st, a->d_obs + n * n_st, a->d_node0, a->d_w,
-                                   n_st, nn, a->lam[0], t.P->has_bed ? A.lbed : nullptr, st);
+                                   n_st, nn, a->lam[0],
+                                   t.P->has_bed && a->want_bed ? A.lbed : nullptr, st);
                 const DevBuf in[3] = {view(n, c0, 0), view(n, c0, 1), view(n, c0, 2)};
                 const DevBuf keep[3] = {keep_view(n, c0, 0), keep_view(n, c0, 1),
                                         keep_view(n, c0, 2)};
@@ -814,7 +819,8 @@ int dgswe_adjoint_reverse(dgswe_adjoint* a, double* grad_h0, double* grad_hu0, d
         for (int64_t n = c1 - 1; n >= c0; --n) {
             // J's dependence on q_{n+1}
             t.ks->station_seed(a->d_eta + n * n_st, a->d_obs + n * n_st, a->d_node0, a->d_w, n_st,
-                               nn, a->lam[0], t.P->has_bed ? A.lbed : nullptr, st);
+                               nn, a->lam[0],
+                               t.P->has_bed && a->want_bed ? A.lbed : nullptr, st);
             // the step's start state and its stages, recomputed with what the reverse keeps
             const double* q0 = a->stride > 1 ? a->d_seg + (n - c0) * 3 * nv : ck;
             if (int s = unpack(a, q, q0, nv, st)) return s;

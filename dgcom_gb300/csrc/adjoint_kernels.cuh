@@ -27,21 +27,34 @@
 namespace dgswe {
 namespace DGSWE_NS {
 
-template <int N1>
+// The stage adjoint runs as two passes over the mesh: kAdjWet over the
+// elements without subcells (the split-form pairs reversed), kAdjSub over
+// those with subcells. Every element belongs to exactly one pass; a block
+// whose elements all belong to the other pass leaves after the subcell
+// test. Apart, the wet pass needs neither the subcells' scratch nor the
+// array where λ lands from an element's other nodes, and its registers are
+// the pair path's alone, so more of its blocks fit on an SM.
+enum { kAdjWet = 0, kAdjSub = 1 };
+
+template <int N1, int PATH>
 struct AdjCfg {
     static constexpr int NN = N1 * N1;
     static constexpr int NP = N1 - 1;
     static constexpr int NA = 2 * (N1 - 1);
     static constexpr int EPB = (64 / NN) > 0 ? (64 / NN) : 1;
     static constexpr int THREADS = EPB * NN;
-    static constexpr int PAIR = NN * NP * 12 + 2 * NN;          // λ per slot side (3), out (6), bed (2)
+    // λ of each pair slot's two sides (3 each), then in the same place the
+    // slot's six outputs; the bed-slope weights (2 per node)
+    static constexpr int PAIR = NN * NP * 6 + 2 * NN;
     static constexpr int FACES = 2 * NN * 8;                    // subcell faces
     static constexpr int IFL = 2 * N1 * (N1 - 1) * 6;           // subcell interface fluxes
     static constexpr int SUB = 2 * FACES + IFL;                 // faces, their λ, interfaces' λ
-    static constexpr int X = PAIR > SUB ? PAIR : SUB;
-    static_assert(X >= 6 * NN, "the limiter's scratch shares s_x");
-    // 8 blocks per SM: ≤ 128 registers; shared memory ≈ 27 KB per block
-    static constexpr int MIN_BLOCKS = 8;
+    static constexpr int VOL = PATH == kAdjWet ? PAIR : (PAIR > SUB ? PAIR : SUB);
+    static constexpr int X = VOL > 6 * NN ? VOL : 6 * NN;       // the limiter's scratch too
+    static constexpr int LAND = PATH == kAdjSub ? NN : 1;
+    // the wet pass: 10 blocks per SM (≤ 102 registers); the subcell pass:
+    // 8 (≤ 128 registers; shared memory ≈ 27 KB a block)
+    static constexpr int MIN_BLOCKS = PATH == kAdjWet ? 10 : 8;
 };
 
 // The node's face slots in the reference's face order (as the forward's lift)
@@ -63,15 +76,15 @@ __device__ __forceinline__ void node_face_slots(int a, int j, int64_t k, int64_t
     s_b = slot(f_b);
 }
 
-template <int N1>
-__global__ void __launch_bounds__(AdjCfg<N1>::THREADS, AdjCfg<N1>::MIN_BLOCKS)
+template <int N1, int PATH>
+__global__ void __launch_bounds__(AdjCfg<N1, PATH>::THREADS, AdjCfg<N1, PATH>::MIN_BLOCKS)
     stage_adjoint_kernel(DevTables T, Physics P, StageExtra X, DevBuf in, DevBuf keep, AdjStage A,
                          const StepCtl* ctl, int slot) {
-    using C = AdjCfg<N1>;
+    using C = AdjCfg<N1, PATH>;
     constexpr int NN = C::NN, NP = C::NP, NA = C::NA, EPB = C::EPB;
-    __shared__ double s_q[EPB][6][NN];   // stage input: h, hu, hv, u, v, b
-    __shared__ double s_l[EPB][6][NN];   // λ landing from the element's other nodes
-    __shared__ double s_x[EPB][C::X];    // limiter, then the pair or subcell scratch
+    __shared__ double s_q[EPB][6][NN];        // stage input: h, hu, hv, u, v, b
+    __shared__ double s_l[EPB][6][C::LAND];   // λ landing from the element's other nodes
+    __shared__ double s_x[EPB][C::X];         // limiter, then the pair or subcell scratch
     __shared__ int s_flag[EPB][2];
     __shared__ double s_red[EPB][12];
     __shared__ int s_arg[EPB];
@@ -80,7 +93,7 @@ __global__ void __launch_bounds__(AdjCfg<N1>::THREADS, AdjCfg<N1>::MIN_BLOCKS)
     const int tid = threadIdx.x;
     const int e = tid / NN, i = tid % NN;
     const int64_t k = (int64_t)blockIdx.x * EPB + e;
-    const bool valid = k < T.K;
+    bool valid = k < T.K;
     const int64_t gi = k * NN + i;
     const int a = i % N1, j = i / N1;
     const double g = P.g, h_min = P.h_min, sqrt_g = P.sqrt_g, half_g = P.half_g;
@@ -105,12 +118,17 @@ __global__ void __launch_bounds__(AdjCfg<N1>::THREADS, AdjCfg<N1>::MIN_BLOCKS)
     s_q[e][3][i] = u;
     s_q[e][4][i] = v;
     s_q[e][5][i] = b;
+    if (PATH == kAdjSub) {
 #pragma unroll
-    for (int c = 0; c < 6; ++c) s_l[e][c][i] = 0.0;
+        for (int c = 0; c < 6; ++c) s_l[e][c][i] = 0.0;
+    }
     __syncthreads();
     if (valid && P.formulation == kWetDry && fp::lt(h, P.subcell_depth)) atomicOr(&s_flag[e][0], 1);
     __syncthreads();
-    const bool sub = s_flag[e][0] != 0;
+    // this pass's elements; a block with none of them leaves together
+    if ((PATH == kAdjSub) != (s_flag[e][0] != 0)) valid = false;
+    if (!__syncthreads_or(valid ? 1 : 0)) return;
+    constexpr bool sub = PATH == kAdjSub;
     const bool affine = valid ? T.affine[k] != 0 : true;
     // the element's member's stage weights (an ensemble: one StepCtl each)
     const StageArgs sa = ctl[(T.elem_member && valid) ? T.elem_member[k] : 0].stage[slot];
@@ -308,8 +326,10 @@ __global__ void __launch_bounds__(AdjCfg<N1>::THREADS, AdjCfg<N1>::MIN_BLOCKS)
     double* faces_b = &s_x[e][C::FACES];           // their λ
     double* ifl_b = &s_x[e][2 * C::FACES];         // λ of the interface fluxes [..][6]
     double* lf = &s_x[e][0];                       // pair path: [slot][side][3]
-    double* lp = &s_x[e][NN * NP * 6];             // pair path: [slot][λh_a, λh_c, λhu, λhv, λu, λv]
-    double* s_ab = &s_x[e][NN * NP * 12];          // pair path: bed-slope weights −h·λr [2][NN]
+    // pair path: [slot][λh_a, λh_c, λhu, λhv, λu, λv], written over the
+    // slot's own λ once its owner has read them (no other thread reads them)
+    double* lp = lf;
+    double* s_ab = &s_x[e][NN * NP * 6];           // pair path: bed-slope weights −h·λr [2][NN]
     auto node_side = [&](int n) {
         return Sd{s_q[e][0][n], s_q[e][3][n], s_q[e][4][n], s_q[e][5][n]};
     };
@@ -496,7 +516,7 @@ __global__ void __launch_bounds__(AdjCfg<N1>::THREADS, AdjCfg<N1>::MIN_BLOCKS)
             Lu += o[4];
             Lv += o[5];
         }
-        if (P.has_bed) {
+        if (P.has_bed && A.lbed) {
             // gdb_i = g Σ_dir Σ_c D[pos_i][pos_c] B_c w(i, c), transposed: this
             // node as c, the coefficients from the gdb_t table
             const double* t = &T.gdb_t[gi * 4 * N1];
@@ -604,7 +624,7 @@ __global__ void __launch_bounds__(AdjCfg<N1>::THREADS, AdjCfg<N1>::MIN_BLOCKS)
                     atomicAdd(&A.lx_h[og_l], mb.h);
                     atomicAdd(&A.lx_u[og_l], mb.u);
                     atomicAdd(&A.lx_v[og_l], mb.v);
-                    if (P.has_bed) atomicAdd(&A.lbed[og_l], mb.b);
+                    if (P.has_bed && A.lbed) atomicAdd(&A.lbed[og_l], mb.b);
                 }
                 if (n_r >= 0) {
                     atomicAdd(&s_l[e][0][n_r], pb.h);
@@ -615,7 +635,7 @@ __global__ void __launch_bounds__(AdjCfg<N1>::THREADS, AdjCfg<N1>::MIN_BLOCKS)
                     atomicAdd(&A.lx_h[og_r], pb.h);
                     atomicAdd(&A.lx_u[og_r], pb.u);
                     atomicAdd(&A.lx_v[og_r], pb.v);
-                    if (P.has_bed) atomicAdd(&A.lbed[og_r], pb.b);
+                    if (P.has_bed && A.lbed) atomicAdd(&A.lbed[og_r], pb.b);
                 }
             } else {  // no reconstruction: both faces are the node's state
                 Lh += lb.h + rb.h;
@@ -627,13 +647,15 @@ __global__ void __launch_bounds__(AdjCfg<N1>::THREADS, AdjCfg<N1>::MIN_BLOCKS)
     }
     __syncthreads();
     if (valid) {
-        A.li_h[gi] = Lh + s_l[e][0][i];
-        A.li_hu[gi] = Lhu + s_l[e][1][i];
-        A.li_hv[gi] = Lhv + s_l[e][2][i];
-        A.li_u[gi] = Lu + s_l[e][3][i];
-        A.li_v[gi] = Lv + s_l[e][4][i];
-        const double lb_all = Lb + s_l[e][5][i];
-        if (P.has_bed && lb_all != 0.0) atomicAdd(&A.lbed[gi], lb_all);
+        // λ landed from the element's other nodes (the subcell pass only)
+        auto land = [&](int c) { return PATH == kAdjSub ? s_l[e][c][i] : 0.0; };
+        A.li_h[gi] = Lh + land(0);
+        A.li_hu[gi] = Lhu + land(1);
+        A.li_hv[gi] = Lhv + land(2);
+        A.li_u[gi] = Lu + land(3);
+        A.li_v[gi] = Lv + land(4);
+        const double lb_all = Lb + land(5);
+        if (P.has_bed && A.lbed && lb_all != 0.0) atomicAdd(&A.lbed[gi], lb_all);
     }
 }
 
@@ -655,7 +677,7 @@ __global__ void __launch_bounds__(256)
         if (lhv != 0.0) atomicAdd(&A.lx_hv[gn], lhv);
         if (lu != 0.0) atomicAdd(&A.lx_u[gn], lu);
         if (lv != 0.0) atomicAdd(&A.lx_v[gn], lv);
-        if (P.has_bed && lb != 0.0) atomicAdd(&A.lbed[gn], lb);
+        if (P.has_bed && A.lbed && lb != 0.0) atomicAdd(&A.lbed[gn], lb);
     };
     if (item < n_int) {
         const int64_t e = item / N1;

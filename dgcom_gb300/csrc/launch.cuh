@@ -173,9 +173,13 @@ template <int N1>
 static void stage_adjoint_n(const DevTables& T, const Physics& P, const StageExtra& X,
                             const DevBuf& in, const DevBuf& keep, const AdjStage& A,
                             const StepCtl* ctl, int slot, cudaStream_t s) {
-    using C = AdjCfg<N1>;
-    const unsigned blocks = (unsigned)((T.K + C::EPB - 1) / C::EPB);
-    stage_adjoint_kernel<N1><<<blocks, C::THREADS, 0, s>>>(T, P, X, in, keep, A, ctl, slot);
+    // the wet elements' pass, then the subcell elements'
+    using CW = AdjCfg<N1, kAdjWet>;
+    stage_adjoint_kernel<N1, kAdjWet><<<(unsigned)((T.K + CW::EPB - 1) / CW::EPB), CW::THREADS, 0,
+                                        s>>>(T, P, X, in, keep, A, ctl, slot);
+    using CS = AdjCfg<N1, kAdjSub>;
+    stage_adjoint_kernel<N1, kAdjSub><<<(unsigned)((T.K + CS::EPB - 1) / CS::EPB), CS::THREADS, 0,
+                                        s>>>(T, P, X, in, keep, A, ctl, slot);
 }
 
 template <int N1>

@@ -824,7 +824,9 @@ int dgswe_adjoint_forward(dgswe_adjoint* adjoint, const double* h0, const double
                           double* eta_out, double* dts_out, double* J);
 /* The reverse sweep of the last forward sweep: ∂J/∂h0, ∂J/∂hu0, ∂J/∂hv0,
  * ∂J/∂B and ∂J/∂n per node (n_values each), and ∂J/∂(amplitude, phase)
- * as [n_boundaries][DGSWE_MAX_CONSTITUENTS][2]. Any output may be NULL. */
+ * as [n_boundaries][DGSWE_MAX_CONSTITUENTS][2]. Any output may be NULL;
+ * with grad_bed NULL the sweep does not form the bed's λ at all, which
+ * saves its arithmetic and atomics. */
 int dgswe_adjoint_reverse(dgswe_adjoint* adjoint, double* grad_h0, double* grad_hu0,
                           double* grad_hv0, double* grad_bed, double* grad_manning,
                           double* grad_tide);

@@ -260,3 +260,18 @@ def test_replayed_steps_give_the_recorded_functional():
         J2, eta2, dts2 = adj.forward(state, dts=dts)
     assert np.array_equal(dts, dts2)
     assert abs(J - J2) <= 1e-14 * abs(J)
+
+
+def test_a_sweep_without_the_bed_gradient_gives_the_others():
+    """dgswe_adjoint_reverse with no bed output skips the bed's λ; the state,
+    Manning and tide gradients stay those of a full sweep (to the atomic
+    sums' ordering, 1e-12), on a drying flat (subcell and limiter paths)."""
+    case, form, state = setup(2, False)
+    with Adjoint(form, STEPS, STATIONS, t_start=T_START) as adj:
+        adj.forward(state)
+        full = adj.reverse()
+        part = adj.reverse(bed=False)
+    assert np.abs(full.bed).max() > 0.0 and not part.bed.any()
+    for a, b in [(full.h0, part.h0), (full.hu0, part.hu0), (full.hv0, part.hv0),
+                 (full.manning, part.manning), (full.tide, part.tide)]:
+        assert np.abs(a - b).max() <= 1e-12 * max(np.abs(a).max(), 1e-300)

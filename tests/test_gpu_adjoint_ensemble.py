@@ -153,3 +153,61 @@ def test_ensemble_gradient_matches_finite_differences():
         fd = (J_at(tide=tide0 + eps * dt) - J_at(tide=tide0 - eps * dt)) / (2 * eps)
         adj = float(np.sum(g.tide * dt))
         assert abs(adj - fd) <= 1e-6 * max(abs(fd), abs(adj)), (adj, fd)
+
+
+def test_ensemble_gradient_matches_the_oracle_forward():
+    """The batched gradient for one member against central differences of
+    the oracle (the CPU restatement of the reference forward) running that
+    member alone over the member's own time steps: Manning's n per element
+    of member 1 in a random direction, at 1e-6."""
+    from oracle_lib import oracle
+
+    ms, forms, stations, member, state = members()
+    nn = (forms[0].order + 1) ** 2
+    rng = np.random.default_rng(11)
+    with Adjoint.ensemble(forms, STEPS, stations, member, t_start=T_START) as ens:
+        tide0 = ens.tide_parameters()
+        n0 = np.concatenate([np.asarray(f.manning_n) for f in forms])
+        tide_obs = tide0.copy()
+        c0 = 0
+        for m, f in enumerate(forms):
+            tide_obs[c0 + open_row(f)] = ms[m].tide_obs
+            c0 += len(f.boundaries)
+        n_obs = np.concatenate([m.manning_obs for m in ms])
+        _, _, dts = ens.forward(state)
+        ens.set_parameters(manning=n_obs, tide=tide_obs)
+        _, eta_obs, _ = ens.forward(state, dts=dts)
+        ens.set_parameters(manning=n0, tide=tide0)
+        ens.forward(state, dts=dts, eta_obs=eta_obs)
+        g = ens.reverse()
+        sl = ens.member_slice(1)
+        st_elem, st_w = ens.station_weights()
+    mine = np.nonzero(member == 1)[0]
+    k0 = sl.start // nn
+    form1 = forms[1]
+    q1 = tuple(np.ascontiguousarray(x[sl]) for x in state)
+    b1 = form1.bathymetry.reshape(-1)
+
+    def J_oracle(manning):
+        ref = oracle(dataclasses.replace(form1, manning_n=manning))
+        try:
+            ref.upload(*q1)
+            t, J = T_START, 0.0
+            for n in range(STEPS):
+                ref.step(t, float(dts[n, 1]))
+                t += float(dts[n, 1])
+                h = ref.download()[0]
+                for s in mine:
+                    k = int(st_elem[s]) - k0
+                    eta = float(np.dot(st_w[s], h[k * nn:(k + 1) * nn] + b1[k * nn:(k + 1) * nn]))
+                    J += (eta - float(eta_obs[n, s])) ** 2
+        finally:
+            ref.close()
+        return J
+
+    n1 = np.asarray(form1.manning_n, dtype=np.float64).reshape(-1)
+    d1 = np.repeat(rng.standard_normal(n1.size // nn), nn)
+    eps = 3e-3 * float(n0.max())
+    fd = (J_oracle(n1 + eps * d1) - J_oracle(n1 - eps * d1)) / (2 * eps)
+    adj = float(np.dot(g.manning[sl], d1))
+    assert abs(adj - fd) <= 1e-6 * max(abs(fd), abs(adj)), (adj, fd)
