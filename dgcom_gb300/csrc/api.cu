@@ -122,6 +122,32 @@ int begin_run(dgswe_handle* h, const dgswe_run_config* run, double target) {
     return sync(h);
 }
 
+int ensure_dt_stream(dgswe_handle* h) {
+    if (h->dt_stream) return DGSWE_OK;
+    CK(cudaStreamCreateWithFlags(&h->dt_stream, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&h->dt_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&h->dt_join, cudaEventDisableTiming));
+    return DGSWE_OK;
+}
+
+// A step's dt pass and fit on the dt stream beside its first stage's face
+// pass on the handle's stream: both read the step's start state; the face
+// pass is held by the FP64 pipe and the dt pass by memory, so the one hides
+// the other. The first stage's time comes from step_begin, so the face pass
+// needs nothing from the fit. The stage pass that follows waits for both.
+int dt_beside_first_face(dgswe_handle* h, const DtParams& D, const int* active) {
+    CK(cudaEventRecord(h->dt_fork, h->stream));
+    CK(cudaStreamWaitEvent(h->dt_stream, h->dt_fork, 0));
+    h->ks->dt(h->n1, h->T, h->P, h->buf[DGSWE_STATE].view, D, nullptr, h->ctl, active,
+              h->dt_stream);
+    h->ks->step_dt(h->ctl, 1, h->dt_stream);
+    CK(cudaEventRecord(h->dt_join, h->dt_stream));
+    h->ks->face(h->n1, h->T, h->P, h->buf[DGSWE_STATE].view, h->fb_h, h->fb_hu, h->fb_hv, h->ctl,
+                0, active, h->stream);
+    CK(cudaStreamWaitEvent(h->stream, h->dt_join, 0));
+    return DGSWE_OK;
+}
+
 int run_device_step_graph(dgswe_handle* h, int scheme, double cfl) {
     if (h->step_graph && h->graph_scheme == scheme && h->graph_cfl == cfl) return DGSWE_OK;
     if (h->step_graph) {
@@ -133,16 +159,25 @@ int run_device_step_graph(dgswe_handle* h, int scheme, double cfl) {
     for (int b = 1; b < n; ++b)
         if (int s = ensure_buffer(h, b)) return s;
     const DtParams D = dt_params(h->form, cfl, scheme);
+    if (int s = ensure_dt_stream(h)) return s;
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     const int* active = &h->ctl->active;
     h->ks->step_begin(h->ctl, 1, h->stream);
-    h->ks->dt(h->n1, h->T, h->P, h->buf[DGSWE_STATE].view, D, nullptr, h->ctl, active, h->stream);
-    h->ks->step_dt(h->ctl, 1, h->stream);
+    if (int s = dt_beside_first_face(h, D, active)) {
+        cudaStreamEndCapture(h->stream, &graph);
+        if (graph) cudaGraphDestroy(graph);
+        return s;
+    }
     for (int s = 0; s < n; ++s) {
         const int in = s == 0 ? DGSWE_STATE : s;
         const int out = s + 1 < n ? s + 1 : DGSWE_STATE;
-        launch_stage(h, in, DGSWE_STATE, out, DGSWE_STATE, s, kModePost, s + 1 == n, active);
+        if (s == 0)  // its face pass ran beside the dt pass
+            h->ks->stage(h->n1, h->T, h->P, h->X, h->buf[in].view, h->buf[DGSWE_STATE].view,
+                         h->buf[out].view, h->buf[DGSWE_STATE].view, h->fb_h, h->fb_hu, h->fb_hv,
+                         h->ctl, s, kModePost, s + 1 == n, active, h->stream);
+        else
+            launch_stage(h, in, DGSWE_STATE, out, DGSWE_STATE, s, kModePost, s + 1 == n, active);
     }
     h->ks->step_end(h->ctl, 1, h->stream);
     cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
@@ -955,12 +990,17 @@ int dgswe_step_host(dgswe_handle* h, int32_t scheme, double t, double cfl, doubl
     }
     const int* active = &h->ctl->active;
     const DtParams D = dt_params(h->form, cfl, scheme);
+    if (int s = ensure_dt_stream(h)) return s;
     h->ks->step_begin(h->ctl, 1, h->stream);
-    h->ks->dt(h->n1, h->T, h->P, q, D, nullptr, h->ctl, active, h->stream);
-    h->ks->step_dt(h->ctl, 1, h->stream);
-    for (int s = 0; s + 1 < n_st; ++s)
-        launch_stage(h, s == 0 ? DGSWE_STATE : s, DGSWE_STATE, s + 1, DGSWE_STATE, s, kModePost, 0,
-                     active);
+    if (int s = dt_beside_first_face(h, D, active)) return s;
+    for (int s = 0; s + 1 < n_st; ++s) {
+        const int in = s == 0 ? DGSWE_STATE : s;
+        if (s == 0)  // its face pass ran beside the dt pass
+            h->ks->stage(h->n1, h->T, h->P, h->X, h->buf[in].view, q, h->buf[s + 1].view, q,
+                         h->fb_h, h->fb_hu, h->fb_hv, h->ctl, s, kModePost, 0, active, h->stream);
+        else
+            launch_stage(h, in, DGSWE_STATE, s + 1, DGSWE_STATE, s, kModePost, 0, active);
+    }
     // the last stage in element chunks, each copied back while the next runs
     const int last = n_st - 1;
     const DevBuf& in = h->buf[last].view;
@@ -1109,11 +1149,16 @@ int dgswe_profile_steps(dgswe_handle* h, const dgswe_run_config* run, int64_t n_
     for (int b = 1; b < n; ++b)
         if (int s = ensure_buffer(h, b)) return s;
     if (int s = begin_run(h, run, INFINITY)) return s;
+    if (int s = ensure_dt_stream(h)) return s;
     const DtParams D = dt_params(h->form, run->cfl, run->scheme);
     const int* active = &h->ctl->active;
-    // per step: begin, dt, fit, n × (face, stage), end → 4 + 2n kernels
-    const int per_step = 4 + 2 * n;
-    std::vector<cudaEvent_t> ev((size_t)n_steps * (per_step + 1));
+    // per step, as the step graph runs it: begin; the dt pass and the fit on
+    // the dt stream beside the first face pass; then the first stage pass and
+    // n − 1 × (face, stage); end. Events: before begin, after begin (the
+    // fork), after dt and after the fit (dt stream), after the first face
+    // pass, after the join, after each later pass → 5 + 2n per step
+    const int per_step = 5 + 2 * n;
+    std::vector<cudaEvent_t> ev((size_t)n_steps * per_step + 1);
     for (auto& e : ev) CK(cudaEventCreate(&e));
     auto cleanup = [&]() {
         for (auto& e : ev)
@@ -1123,18 +1168,27 @@ int dgswe_profile_steps(dgswe_handle* h, const dgswe_run_config* run, int64_t n_
     for (int64_t step = 0; step < n_steps; ++step) {
         CK(cudaEventRecord(ev[q++], h->stream));
         h->ks->step_begin(h->ctl, 1, h->stream);
-        CK(cudaEventRecord(ev[q++], h->stream));
+        cudaEvent_t fork = ev[q++], dt_done = ev[q++], fit_done = ev[q++];
+        CK(cudaEventRecord(fork, h->stream));
+        CK(cudaStreamWaitEvent(h->dt_stream, fork, 0));
         h->ks->dt(h->n1, h->T, h->P, h->buf[DGSWE_STATE].view, D, nullptr, h->ctl, active,
-                  h->stream);
+                  h->dt_stream);
+        CK(cudaEventRecord(dt_done, h->dt_stream));
+        h->ks->step_dt(h->ctl, 1, h->dt_stream);
+        CK(cudaEventRecord(fit_done, h->dt_stream));
+        h->ks->face(h->n1, h->T, h->P, h->buf[DGSWE_STATE].view, h->fb_h, h->fb_hu, h->fb_hv,
+                    h->ctl, 0, active, h->stream);
         CK(cudaEventRecord(ev[q++], h->stream));
-        h->ks->step_dt(h->ctl, 1, h->stream);
+        CK(cudaStreamWaitEvent(h->stream, fit_done, 0));
         CK(cudaEventRecord(ev[q++], h->stream));
         for (int s = 0; s < n; ++s) {
             const int in = s == 0 ? DGSWE_STATE : s;
             const int o = s + 1 < n ? s + 1 : DGSWE_STATE;
-            h->ks->face(h->n1, h->T, h->P, h->buf[in].view, h->fb_h, h->fb_hu, h->fb_hv, h->ctl, s,
-                        active, h->stream);
-            CK(cudaEventRecord(ev[q++], h->stream));
+            if (s > 0) {
+                h->ks->face(h->n1, h->T, h->P, h->buf[in].view, h->fb_h, h->fb_hu, h->fb_hv,
+                            h->ctl, s, active, h->stream);
+                CK(cudaEventRecord(ev[q++], h->stream));
+            }
             h->ks->stage(h->n1, h->T, h->P, h->X, h->buf[in].view, h->buf[DGSWE_STATE].view,
                          h->buf[o].view, h->buf[DGSWE_STATE].view, h->fb_h, h->fb_hu, h->fb_hv,
                          h->ctl, s, kModePost, s + 1 == n, active, h->stream);
@@ -1154,20 +1208,25 @@ int dgswe_profile_steps(dgswe_handle* h, const dgswe_run_config* run, int64_t n_
         cudaEventElapsedTime(&v, ev[a], ev[b]);
         return (double)v;
     };
+    // the parts: the first face pass and the dt pass overlap, so the parts
+    // sum to more than the step; total_ms is the step's own time
     q = 0;
     for (int64_t step = 0; step < n_steps; ++step) {
         const size_t s0 = q;
-        out->control_ms += ms(s0, s0 + 1);  // begin
-        out->dt_ms += ms(s0 + 1, s0 + 2);
+        out->control_ms += ms(s0, s0 + 1);      // begin
+        out->dt_ms += ms(s0 + 1, s0 + 2);       // from the fork
         out->control_ms += ms(s0 + 2, s0 + 3);  // fit
-        size_t e = s0 + 3;
-        for (int s = 0; s < n; ++s) {
+        out->face_ms += ms(s0 + 1, s0 + 4);     // the first face pass, from the fork
+        size_t e = s0 + 5;                      // after the join
+        out->stage_ms += ms(e, e + 1);
+        e += 1;
+        for (int s = 1; s < n; ++s) {
             out->face_ms += ms(e, e + 1);
             out->stage_ms += ms(e + 1, e + 2);
             e += 2;
         }
-        out->control_ms += ms(e, e + 1);  // end (to the next step's first event)
-        q = e + 1;
+        q = e + 1;  // the next step's first event (or the last)
+        out->control_ms += ms(e, q);  // end
     }
     out->total_ms = ms(0, last);
     out->steps = n_steps;

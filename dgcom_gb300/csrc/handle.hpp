@@ -102,11 +102,18 @@ struct dgswe_handle {
     // the compute, and one event per chunk (created on first use)
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t chunk_done[dgswe::kHostChunks] = {};
+    // the dt pass's own stream, beside the first stage's face pass, and the
+    // fork and join between them (created on first use)
+    cudaStream_t dt_stream = nullptr;
+    cudaEvent_t dt_fork = nullptr, dt_join = nullptr;
 
     ~dgswe_handle() {
         for (cudaEvent_t e : chunk_done)
             if (e) cudaEventDestroy(e);
         if (copy_stream) cudaStreamDestroy(copy_stream);
+        for (cudaEvent_t e : {dt_fork, dt_join})
+            if (e) cudaEventDestroy(e);
+        if (dt_stream) cudaStreamDestroy(dt_stream);
         delete planner;
         if (dplan.host) cudaFreeHost(dplan.host);
         for (cudaEvent_t e : ev_lts)

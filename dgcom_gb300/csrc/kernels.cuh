@@ -987,7 +987,10 @@ __global__ void velocity_kernel(DevBuf b, int64_t n, double h_min) {
 template <int N1>
 struct DtCfg {
     static constexpr int NN = N1 * N1;
-    static constexpr int EPB = 32;  // elements per block: one lane of warp 0 each
+    // elements per block, one lane of warp 0 each: 16, so that a dt block
+    // (256 threads at N = 3, 40 registers) fits on an SM beside two blocks
+    // of the face pass it runs with
+    static constexpr int EPB = 16;
     static constexpr int THREADS = EPB * NN;
     static constexpr int PITCH = NN + 1;  // odd row pitch: lanes spread over the banks
     static constexpr int SLOTS = NN + 4 * N1;  // own nodes, then neighbours' face nodes
@@ -1119,11 +1122,11 @@ __global__ void __launch_bounds__(DtCfg<N1>::THREADS)
         atomicMax(&s_rmax[ce], (unsigned long long)fp::bits(r));  // r ≥ +0
     }
     __syncthreads();
-    if (tid >= 32) return;  // warp 0: lane l finishes element k0 + l
+    if (tid >= 32) return;  // warp 0: lane l < EPB finishes element k0 + l
     const int64_t kl = k0 + tid;
     unsigned long long dt_bits = 0x7FF0000000000000ull;  // +∞
     int member = -1;
-    if (kl < T.K) {
+    if (tid < EPB && kl < T.K) {
         const double rmax = fp::from_bits((int64_t)s_rmax[tid]);
         const double dt = element_dt<N1>(D, P.order, T.weight_ratio[kl], rmax, &s_h[tid * PITCH],
                                          &s_mass[tid * PITCH]);
@@ -1163,6 +1166,9 @@ __global__ void step_begin(StepCtl* ctl, int n) {
         run = false;
     }
     c->active = run ? 1 : 0;
+    // the first stage's time needs no dt (its offset is 0 in every scheme):
+    // set here, a pass of the first stage can start beside the dt pass
+    if (run && c->st_c[0] == 0.0) c->stage[0].time = c->t;
 }
 
 // dt from the element steps, capped, checked, fitted to land on the target;
@@ -1188,7 +1194,8 @@ __global__ void step_dt(StepCtl* ctl, int n) {
     c->dt = dt;
     for (int s = 0; s < c->scheme_stages; ++s) {
         StageArgs& a = c->stage[s];
-        a.time = __dadd_rn(c->t, __dmul_rn(c->st_c[s], dt));  // rounded apart, as the reference
+        if (s > 0 || c->st_c[0] != 0.0)  // the first stage's time from step_begin
+            a.time = __dadd_rn(c->t, __dmul_rn(c->st_c[s], dt));  // rounded apart, as the reference
         a.a = c->st_start[s];
         a.b = c->st_input[s];
         a.c = c->st_beta[s] * dt;
