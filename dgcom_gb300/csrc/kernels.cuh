@@ -427,7 +427,7 @@ __global__ void __launch_bounds__(Cfg<N1, SHAPE>::THREADS, Cfg<N1, SHAPE>::MIN_B
                  int check_finite, const int* active, DevBuf keep, LtsPass lp) {
     using C = Cfg<N1, SHAPE>;
     constexpr int NN = C::NN, NP = C::NP, NA = C::NA, EPB = C::EPB;
-    __shared__ double s_q[EPB][6][NN];
+    __shared__ double s_q[EPB][7][NN];  // h, hu, hv, u, v, b, 2g·h
     __shared__ double s_x[EPB][C::X];
     __shared__ int s_flag[EPB][3];
     __shared__ double s_red[EPB][5];
@@ -467,6 +467,7 @@ __global__ void __launch_bounds__(Cfg<N1, SHAPE>::THREADS, Cfg<N1, SHAPE>::MIN_B
     s_q[e][3][i] = u;
     s_q[e][4][i] = v;
     s_q[e][5][i] = b;
+    s_q[e][6][i] = P.two_g * h;  // the pairs' pressure 2g·h_a·h_c takes one multiply
     __syncthreads();
     if (valid && P.formulation == kWetDry && fp::lt(h, P.subcell_depth)) {
         atomicOr(&s_flag[e][0], 1);
@@ -490,18 +491,17 @@ __global__ void __launch_bounds__(Cfg<N1, SHAPE>::THREADS, Cfg<N1, SHAPE>::MIN_B
 
     // ---- phase A: pair fluxes, or the subcells' reconstructed faces ----
     if (valid && !sub) {
-        const double two_g = P.two_g;
 #pragma unroll
         for (int q = 0; q < NP; ++q) {
             const int8_t* own = &T.sched_owned[(i * NP + q) * 5];
             const int na = own[0], nc = own[1];
             const double hm0 = T.pair_hm[(gi * NP + q) * 2];
             const double hm1 = T.pair_hm[(gi * NP + q) * 2 + 1];
-            const double ha = s_q[e][0][na], hc = s_q[e][0][nc];
+            const double hc = s_q[e][0][nc];
             // ½·F#(q_a, q_c)·{{Ja}} scaled: mass, 2·F_hu, 2·F_hv
             const double mass = (s_q[e][1][na] + s_q[e][1][nc]) * hm0 +
                                 (s_q[e][2][na] + s_q[e][2][nc]) * hm1;
-            const double gp2 = two_g * (ha * hc);
+            const double gp2 = s_q[e][6][na] * hc;
             const double g_hu = mass * (s_q[e][3][na] + s_q[e][3][nc]) + gp2 * hm0;
             const double g_hv = mass * (s_q[e][4][na] + s_q[e][4][nc]) + gp2 * hm1;
             double* slot_f = &s_x[e][(i * NP + q) * 3];
