@@ -9,7 +9,9 @@ open western side, Manning n = 0.02, Coriolis at 63° N.
 Metric: DOF-updates/s = 3 · K · (N+1)² · steps / s (one DOF advanced by one
 full step). ``value`` is device time (CUDA events on the library's stream)
 with the state resident in HBM; ``e2e`` is the same metric through the C
-ABI with host buffers (pinned upload, dt, step, download every step).
+ABI with host buffers: every step one ``dgswe_step_host`` call on a pinned
+host state (upload, dt, step, download, the copies overlapped with the
+compute in element chunks).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
