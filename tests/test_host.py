@@ -184,3 +184,27 @@ def test_dt_single_precision_filter_bound(tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True)
     assert out.returncode == 0, out.stdout + out.stderr
     assert out.stdout.startswith("ok ")
+
+
+def test_sequential_breakdown_recovers_overhead_and_bound():
+    """The ensemble bench's breakdown of the sequential arm: runs whose step
+    costs overhead + nodes × cost give back both, the overhead's share, and
+    the batching bound (sequential time over the members' work at the
+    fastest run's throughput)."""
+    import sys
+    from pathlib import Path
+
+    sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
+    import bench
+
+    steps, overhead, cost = 10, 2e-4, 1e-9
+    nodes = [16 * k for k in (5_000, 20_000, 80_000, 200_000)]
+    runs = [(n // 16, 3, n, steps * (overhead + cost * n)) for n in nodes]
+    b = bench.sequential_breakdown(runs, steps, batched_seconds=steps * cost * sum(nodes))
+    assert abs(b["overhead_ms_per_run_step"] - 0.2) < 1e-9
+    assert abs(b["ns_per_node_step"] - 1.0) < 1e-9
+    seq = sum(overhead + cost * n for n in nodes)
+    assert abs(b["overhead_share"] - 4 * overhead / seq) < 1e-12
+    fastest = max(3 * n / (overhead + cost * n) for n in nodes)
+    assert abs(b["bound_speedup"] - seq / (3 * sum(nodes) / fastest)) < 1e-9
+    assert len(b["runs"]) == 4
