@@ -13,7 +13,7 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 LIBRARY_PATH = HERE / "libdgswe.so"
 
-ABI_VERSION = 3
+ABI_VERSION = 4
 
 # dgswe_status
 OK, ERR_INVALID, ERR_CUDA, ERR_NONFINITE, ERR_DT_MIN, ERR_MAX_STEPS, ERR_STOPPED, \
@@ -122,7 +122,7 @@ class Tuning(C.Structure):
         ("face_threads", C.c_int32),
         ("stage_threads", C.c_int32),
         ("face_ms", C.c_double * 3),
-        ("stage_ms", C.c_double * 2),
+        ("stage_ms", C.c_double * 3),
     ]
 
 

@@ -764,7 +764,7 @@ int dgswe_compute_rhs_mass_fluxes(dgswe_handle* h, int32_t input, double time, d
 int dgswe_autotune(dgswe_handle* h, int32_t repeats, int32_t force_face, int32_t force_stage,
                    dgswe_tuning* out) {
     if (!h) return DGSWE_ERR_INVALID;
-    if (!out || repeats < 1 || force_stage > 1 ||
+    if (!out || repeats < 1 || force_stage > 2 ||
         (force_face >= 0 && force_face != 64 && force_face != 128 && force_face != 256))
         return fail(h, DGSWE_ERR_INVALID, "autotune: repeats %d, face %d, stage %d", repeats,
                     force_face, force_stage);
@@ -814,18 +814,20 @@ int dgswe_autotune(dgswe_handle* h, int32_t repeats, int32_t force_face, int32_t
     if (force_stage >= 0) {
         h->P.stage_shape = force_stage;
     } else {
-        for (int c = 0; c < 2 && status == DGSWE_OK; ++c) {
+        int best = 0;
+        for (int c = 0; c < 3 && status == DGSWE_OK; ++c) {
             h->P.stage_shape = c;
             status = timed(stage, out->stage_ms[c]);
+            if (out->stage_ms[c] < out->stage_ms[best]) best = c;
         }
-        h->P.stage_shape = out->stage_ms[1] < out->stage_ms[0] ? 1 : 0;
+        h->P.stage_shape = best;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (status != DGSWE_OK) return status;
     CK(cudaGetLastError());
     out->face_threads = h->P.face_threads;
-    const int per = h->P.stage_shape == 0 ? 128 : 64;
+    const int per = h->P.stage_shape == 1 ? 64 : 128;
     out->stage_threads = std::max(1, per / h->nn) * h->nn;
     // the step graph holds the old shapes in its launches
     if (h->step_graph) {

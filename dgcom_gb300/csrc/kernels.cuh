@@ -348,21 +348,22 @@ __global__ void __launch_bounds__(256) face_kernel(DevTables T, Physics P, DevBu
 // the stage kernel
 
 // SHAPE 0: ⌊128/NN⌋ elements a block; SHAPE 1: ⌊64/NN⌋ elements a block
-// at twice the blocks per SM (the same registers and warps per SM), one of
-// the launch shapes dgswe_autotune chooses between
+// at twice the blocks per SM (the same registers and warps per SM); SHAPE 2:
+// ⌊128/NN⌋ elements a block at 6 blocks per SM (80 registers at N1 = 4,
+// with a few spilled). The launch shapes dgswe_autotune chooses between.
 template <int N1, int SHAPE = 0>
 struct Cfg {
     static constexpr int NN = N1 * N1;
     static constexpr int NP = N1 - 1;      // pairs a node owns
     static constexpr int NA = 2 * (N1 - 1);  // pairs a node is in
-    static constexpr int PER = SHAPE == 0 ? 128 : 64;
+    static constexpr int PER = SHAPE == 1 ? 64 : 128;
     static constexpr int EPB = (PER / NN) > 0 ? (PER / NN) : 1;
     static constexpr int THREADS = EPB * NN;
     // stage_kernel blocks per SM: 5 caps it at ≤ 102 registers (96 at
     // N1 = 4, no spills) for 20 warps per SM; it is bound by the FP64 pipe
     // and waits on it, so more warps keep it busier (measured 5 % faster
     // on the 1 M-quad N = 3 case than 4 blocks)
-    static constexpr int MIN_BLOCKS = SHAPE == 0 ? 5 : 10;
+    static constexpr int MIN_BLOCKS = SHAPE == 0 ? 5 : (SHAPE == 1 ? 10 : 6);
     static constexpr int PAIR_DOUBLES = NN * NP * 3;
     static constexpr int FACE_DOUBLES = 2 * NN * 8;           // reconstructed faces
     static constexpr int NSUB = 2 * N1 * (N1 - 1);            // subcell interfaces

@@ -65,6 +65,14 @@ static void stage_n(const DevTables& T, const Physics& P, const StageExtra& X, c
             LtsPass{});
         return;
     }
+    if (P.stage_shape == 2) {
+        using C2 = Cfg<N1, 2>;
+        const unsigned blocks = (unsigned)((count + C2::EPB - 1) / C2::EPB);
+        stage_kernel<N1, false, 2><<<blocks, C2::THREADS, 0, s>>>(
+            T, P, X, in, base, out, acc, fh, fhu, fhv, ctl, slot, mode, check_finite, active, keep,
+            LtsPass{});
+        return;
+    }
     using C = Cfg<N1>;
     const unsigned blocks = (unsigned)((count + C::EPB - 1) / C::EPB);
     stage_kernel<N1, false><<<blocks, C::THREADS, 0, s>>>(T, P, X, in, base, out, acc, fh, fhu, fhv,

@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define DGSWE_ABI_VERSION 3u
+#define DGSWE_ABI_VERSION 4u
 
 /* ---- status codes ------------------------------------------------------ */
 enum dgswe_status {
@@ -598,19 +598,20 @@ int dgswe_planner_spread(dgswe_planner* planner, uint8_t* levels, int32_t limit,
 /* Launch shapes of a handle's kernels, chosen by timing them on its own
  * mesh and state (an autotuner): the face kernel's threads per
  * block (64, 128 or 256) and the stage kernel's elements per block
- * (⌊128/(N+1)²⌋ at 5 blocks per SM, or ⌊64/(N+1)²⌋ at 10). The shapes change
- * no result (tests compare them bit for bit). No reference counterpart. */
+ * (shape 0: ⌊128/(N+1)²⌋ at 5 blocks per SM; 1: ⌊64/(N+1)²⌋ at 10; 2:
+ * ⌊128/(N+1)²⌋ at 6). The shapes change no result (tests compare them bit
+ * for bit). No reference counterpart. */
 typedef struct dgswe_tuning {
     int32_t face_threads;      /* chosen */
     int32_t stage_threads;     /* chosen: elements per block × (N+1)² */
     double face_ms[3];         /* one face pass at 64, 128, 256 threads */
-    double stage_ms[2];        /* one RHS stage at the two shapes */
+    double stage_ms[3];        /* one RHS stage at the three shapes */
 } dgswe_tuning;
 
 /* Times `repeats` face passes and RHS stages of buffer 0 at each shape
  * (CUDA events on the handle's stream; the state is not changed), keeps the
  * fastest shapes for every later launch and returns them. force_face /
- * force_stage ≥ 0 set a shape without timing (threads; shape 0 or 1). */
+ * force_stage ≥ 0 set a shape without timing (threads; shape 0, 1 or 2). */
 int dgswe_autotune(dgswe_handle* handle, int32_t repeats, int32_t force_face,
                    int32_t force_stage, dgswe_tuning* out);
 
