@@ -41,8 +41,10 @@ def test_diff_matrix_batched_equals_the_reference_helper(cuda_lib, n):
     f = [batch(n, s) for s in (1, 2, 3)]
     out = [torch.full((n * ELEMENTS,), float("nan"), dtype=torch.float64, device="cuda:0")
            for _ in range(3)]
-    st = cuda_lib.apply_diff_matrix(0, vp(dev(d)), *[vp(dev(x)) for x in f], *map(vp, out), n,
-                                    ELEMENTS)
+    # the device copies must outlive the call: a dropped tensor's memory goes
+    # back to torch's cache and the next copy would take it
+    d_d, d_f = dev(d), [dev(x) for x in f]
+    st = cuda_lib.apply_diff_matrix(0, vp(d_d), *map(vp, d_f), *map(vp, out), n, ELEMENTS)
     assert st == abi.OK, cuda_lib.helpers_last_error()
     got = [o.cpu().numpy() for o in out]
     want = [np.empty(n * ELEMENTS) for _ in range(3)]
@@ -66,8 +68,9 @@ def test_lift_batched_equals_the_reference_helper(cuda_lib, n):
     base = [batch(n, s) for s in (7, 8, 9)]
     scale = np.random.default_rng(3).uniform(0.1, 10.0, ELEMENTS)
     out = [dev(b) for b in base]
-    st = cuda_lib.apply_lift(0, vp(dev(lift)), *[vp(dev(x)) for x in diff], *map(vp, out), n, nf,
-                             vp(dev(scale)), ELEMENTS)
+    d_lift, d_diff, d_scale = dev(lift), [dev(x) for x in diff], dev(scale)
+    st = cuda_lib.apply_lift(0, vp(d_lift), *map(vp, d_diff), *map(vp, out), n, nf, vp(d_scale),
+                             ELEMENTS)
     assert st == abi.OK, cuda_lib.helpers_last_error()
     got = [o.cpu().numpy() for o in out]
     want = [b.copy() for b in base]
@@ -88,7 +91,8 @@ def test_coriolis_and_combine_equal_the_reference_helpers(cuda_lib):
     hu, hv = batch(n, 11), batch(n, 12)
     ohu, ohv = batch(n, 13), batch(n, 14)
     d_ohu, d_ohv = dev(ohu), dev(ohv)
-    st = cuda_lib.coriolis_source(0, vp(dev(hu)), vp(dev(hv)), vp(d_ohu), vp(d_ohv), 1.2e-4,
+    d_hu, d_hv = dev(hu), dev(hv)
+    st = cuda_lib.coriolis_source(0, vp(d_hu), vp(d_hv), vp(d_ohu), vp(d_ohv), 1.2e-4,
                                   n * ELEMENTS)
     assert st == abi.OK, cuda_lib.helpers_last_error()
     ora.oracle_coriolis_source(ptr(hu), ptr(hv), ptr(ohu), ptr(ohv), 1.2e-4, n * ELEMENTS)
@@ -100,7 +104,8 @@ def test_coriolis_and_combine_equal_the_reference_helpers(cuda_lib):
     d_ins = [dev(x) for x in ins]
     arr = (C.c_void_p * 12)(*[t.data_ptr() for t in d_ins])
     out = [torch.empty(n * ELEMENTS, dtype=torch.float64, device="cuda:0") for _ in range(3)]
-    st = cuda_lib.combine_derivatives(0, arr, *map(vp, out), vp(dev(metric)), n, ELEMENTS)
+    d_metric = dev(metric)
+    st = cuda_lib.combine_derivatives(0, arr, *map(vp, out), vp(d_metric), n, ELEMENTS)
     assert st == abi.OK, cuda_lib.helpers_last_error()
     got = [o.cpu().numpy() for o in out]
     for e in range(0, ELEMENTS, 7):
