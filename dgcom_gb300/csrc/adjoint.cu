@@ -216,13 +216,6 @@ int64_t find_element(const dgswe_form& f, double x, double y, double& r, double&
     return -1;
 }
 
-__global__ void sum_clear_kernel(double* out, const double* a, double* b, int64_t n) {
-    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= n) return;
-    out[g] = a[g] + b[g];
-    b[g] = 0.0;
-}
-
 // copy (h, hu, hv) between a DevBuf and 3n packed doubles
 int pack(dgswe_adjoint* a, double* dst, const DevBuf& src, int64_t n, cudaStream_t st) {
     const size_t bytes = (size_t)n * sizeof(double);
@@ -287,12 +280,12 @@ int reverse_stages(dgswe_adjoint* a, const DevBuf* in, const DevBuf* keep) {
         if (!a->want_bed) As.lbed = nullptr;  // λ of the bed neither summed nor written
         t.ks->stage_adjoint(t.n1, *t.T, *t.P, *t.X, in[s], keep[s], As, t.ctl, s, st);
         t.ks->face_adjoint(t.n1, *t.T, *t.P, in[s], As, t.ctl, s, st);
-        t.ks->adjoint_combine(in[s], As, a->lam_t[0], a->lam_t[1], a->lam_t[2], nv, t.P->h_min,
-                              st);
+        // the first stage's input is the step's start: its λ, with the base
+        // terms, into lam
+        double** out = s == 0 ? a->lam : a->lam_t;
+        t.ks->adjoint_combine(in[s], As, out[0], out[1], out[2], s == 0 ? a->lam_b : nullptr, nv,
+                              t.P->h_min, st);
     }
-    for (int c = 0; c < 3; ++c)
-        sum_clear_kernel<<<(unsigned)((nv + 255) / 256), 256, 0, st>>>(a->lam[c], a->lam_t[c],
-                                                                       a->lam_b[c], nv);
     return DGSWE_OK;
 }
 
@@ -404,6 +397,8 @@ int setup(dgswe_adjoint* a, const dgswe_form* forms, const dgswe_adjoint_config*
     if ((s = dalloc(a, (size_t)nv, &A.lbed))) return s;
     if ((s = dalloc(a, (size_t)nv, &A.lgn2))) return s;
     if ((s = dalloc(a, (size_t)std::max(1, t.n_cond) * 2 * kMaxConstituents, &A.ltide))) return s;
+    if ((s = dalloc(a, (size_t)std::max<int64_t>(1, t.T->K), &A.sub_list))) return s;
+    if ((s = dalloc(a, 1, &A.sub_count))) return s;
     A.lb_h = a->lam_b[0];
     A.lb_hu = a->lam_b[1];
     A.lb_hv = a->lam_b[2];
@@ -747,6 +742,7 @@ int dgswe_adjoint_reverse(dgswe_adjoint* a, double* grad_h0, double* grad_hu0, d
     ACK(cudaMemsetAsync(A.lx_h, 0, 5 * bv, st));
     ACK(cudaMemsetAsync(A.lbed, 0, bv, st));
     ACK(cudaMemsetAsync(A.lgn2, 0, bv, st));
+    ACK(cudaMemsetAsync(A.sub_count, 0, sizeof(unsigned long long), st));
     ACK(cudaMemsetAsync(A.ltide, 0,
                         (size_t)std::max(1, t.n_cond) * 2 * kMaxConstituents * sizeof(double), st));
     const int* on = &t.ctl[0].always;

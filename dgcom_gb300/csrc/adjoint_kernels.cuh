@@ -27,13 +27,13 @@
 namespace dgswe {
 namespace DGSWE_NS {
 
-// The stage adjoint runs as two passes over the mesh: kAdjWet over the
-// elements without subcells (the split-form pairs reversed), kAdjSub over
-// those with subcells. Every element belongs to exactly one pass; a block
-// whose elements all belong to the other pass leaves after the subcell
-// test. Apart, the wet pass needs neither the subcells' scratch nor the
-// array where λ lands from an element's other nodes, and its registers are
-// the pair path's alone, so more of its blocks fit on an SM.
+// The stage adjoint runs as two passes: kAdjWet over the mesh, reversing
+// the elements without subcells (the split-form pairs) and listing those
+// with subcells, and kAdjSub over that list. Every element belongs to
+// exactly one pass. Apart, the wet pass needs neither the subcells' scratch
+// nor the array where λ lands from an element's other nodes, and its
+// registers are the pair path's alone, so more of its blocks fit on an SM;
+// the subcell pass's work is the list's, its other blocks leave at once.
 enum { kAdjWet = 0, kAdjSub = 1 };
 
 template <int N1, int PATH>
@@ -92,7 +92,17 @@ __global__ void __launch_bounds__(AdjCfg<N1, PATH>::THREADS, AdjCfg<N1, PATH>::M
 
     const int tid = threadIdx.x;
     const int e = tid / NN, i = tid % NN;
-    const int64_t k = (int64_t)blockIdx.x * EPB + e;
+    // the subcell pass takes its elements from the wet pass's list; its
+    // blocks past the list's end leave at once
+    int64_t k;
+    if (PATH == kAdjSub) {
+        const unsigned long long n_sub = *A.sub_count;
+        const unsigned long long at = (unsigned long long)blockIdx.x * EPB;
+        if (at >= n_sub) return;
+        k = at + e < n_sub ? A.sub_list[at + e] : T.K;
+    } else {
+        k = (int64_t)blockIdx.x * EPB + e;
+    }
     bool valid = k < T.K;
     const int64_t gi = k * NN + i;
     const int a = i % N1, j = i / N1;
@@ -125,6 +135,9 @@ __global__ void __launch_bounds__(AdjCfg<N1, PATH>::THREADS, AdjCfg<N1, PATH>::M
     __syncthreads();
     if (valid && P.formulation == kWetDry && fp::lt(h, P.subcell_depth)) atomicOr(&s_flag[e][0], 1);
     __syncthreads();
+    // the wet pass lists the subcell elements for the subcell pass
+    if (PATH == kAdjWet && i == 0 && valid && s_flag[e][0] != 0)
+        A.sub_list[atomicAdd(A.sub_count, 1ull)] = k;
     // this pass's elements; a block with none of them leaves together
     if ((PATH == kAdjSub) != (s_flag[e][0] != 0)) valid = false;
     if (!__syncthreads_or(valid ? 1 : 0)) return;
@@ -746,14 +759,25 @@ __global__ void __launch_bounds__(256)
 }
 
 // λ of the stage input: own element + faces and neighbours, the node
-// velocity folded into h, hu, hv; clears the atomic accumulators
+// velocity folded into h, hu, hv; clears the atomic accumulators. For the
+// step's first stage (`base_h` set) λ of the step's start state: that plus
+// the three stages' base terms, whose sums are cleared
 __global__ void adjoint_combine_kernel(DevBuf in, AdjStage A, double* out_h, double* out_hu,
-                                       double* out_hv, int64_t n, double h_min) {
+                                       double* out_hv, double* base_h, double* base_hu,
+                                       double* base_hv, int64_t n, double h_min) {
     const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n) return;
     double lh = A.li_h[g] + A.lx_h[g], lhu = A.li_hu[g] + A.lx_hu[g], lhv = A.li_hv[g] + A.lx_hv[g];
     const double lu = A.li_u[g] + A.lx_u[g], lv = A.li_v[g] + A.lx_v[g];
     node_velocity_rev(in.h[g], in.hu[g], in.hv[g], h_min, lu, lv, lh, lhu, lhv);
+    if (base_h) {
+        lh = lh + base_h[g];
+        lhu = lhu + base_hu[g];
+        lhv = lhv + base_hv[g];
+        base_h[g] = 0.0;
+        base_hu[g] = 0.0;
+        base_hv[g] = 0.0;
+    }
     out_h[g] = lh;
     out_hu[g] = lhu;
     out_hv[g] = lhv;
@@ -762,6 +786,7 @@ __global__ void adjoint_combine_kernel(DevBuf in, AdjStage A, double* out_h, dou
     A.lx_hv[g] = 0.0;
     A.lx_u[g] = 0.0;
     A.lx_v[g] = 0.0;
+    if (g == 0) *A.sub_count = 0;  // the stage's subcell list is spent
 }
 
 // η = Σ w_i (h_i + B_i) at each station (its element's nodes, Lagrange

@@ -206,6 +206,8 @@ struct AdjStage {
     double* lbed;                                // of the bed elevation (atomic)
     double* lgn2;                                // of g·n² per node (added)
     double* ltide;                               // [condition][constituent][amplitude, phase]
+    int64_t* sub_list;                           // the stage's subcell elements (wet pass)
+    unsigned long long* sub_count;               // their number (reset by the combine)
 };
 
 }  // namespace dgswe

@@ -33,8 +33,11 @@ struct KernelSet {
                           const StepCtl* ctl, int slot, cudaStream_t);
     void (*face_adjoint)(int n1, const DevTables&, const Physics&, const DevBuf& in,
                          const AdjStage&, const StepCtl* ctl, int slot, cudaStream_t);
+    // out = λ of the stage input; with `base` (the first stage), + base,
+    // which is cleared
     void (*adjoint_combine)(const DevBuf& in, const AdjStage&, double* out_h, double* out_hu,
-                            double* out_hv, int64_t n, double h_min, cudaStream_t);
+                            double* out_hv, double* const* base, int64_t n, double h_min,
+                            cudaStream_t);
     void (*station_eval)(const double* h, const double* bed, const int64_t* node0,
                          const double* w, int n_stations, int nn, double* eta, cudaStream_t);
     void (*station_seed)(const double* eta, const double* obs, const int64_t* node0,

@@ -212,10 +212,12 @@ static void face_adjoint(int n1, const DevTables& T, const Physics& P, const Dev
 #undef DGSWE_BY_ORDER
 
 static void adjoint_combine(const DevBuf& in, const AdjStage& A, double* out_h, double* out_hu,
-                            double* out_hv, int64_t n, double h_min, cudaStream_t s) {
+                            double* out_hv, double* const* base, int64_t n, double h_min,
+                            cudaStream_t s) {
     if (n == 0) return;
-    adjoint_combine_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(in, A, out_h, out_hu,
-                                                                        out_hv, n, h_min);
+    adjoint_combine_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
+        in, A, out_h, out_hu, out_hv, base ? base[0] : nullptr, base ? base[1] : nullptr,
+        base ? base[2] : nullptr, n, h_min);
 }
 
 static void station_eval(const double* h, const double* bed, const int64_t* node0, const double* w,

@@ -81,6 +81,6 @@ def test_bad_shapes_are_refused():
         t = abi.Tuning()
         assert dev.lib.autotune(dev.handle, 1, 100, -1, t) == abi.ERR_INVALID
         assert dev.lib.autotune(dev.handle, 0, -1, -1, t) == abi.ERR_INVALID
-        assert dev.lib.autotune(dev.handle, 1, -1, 2, t) == abi.ERR_INVALID
+        assert dev.lib.autotune(dev.handle, 1, -1, 3, t) == abi.ERR_INVALID
     finally:
         dev.close()
