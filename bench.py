@@ -46,7 +46,7 @@ UNIT = "DOF-updates/s"
 BYTES_PER_NODE_STAGE = {2: 81.8, 3: 77.5}  # algorithmic bytes (state, bed, mesh), N=2 / N=3
 # stage_kernel<4>'s DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per
 # node-stage in one ncu capture of the 200k-quad coastal box, for scaling by nodes
-STAGE_TRAFFIC_PER_NODE_STAGE = {3: 190.4}
+STAGE_TRAFFIC_PER_NODE_STAGE = {3: 187.3}
 
 
 def peaks():
@@ -390,7 +390,7 @@ def run_ours(args, rank: int, world: int, local: int):
                          "traffic": (STAGE_TRAFFIC_PER_NODE_STAGE[args.order] * nodes
                                      if args.order in STAGE_TRAFFIC_PER_NODE_STAGE else None),
                          "peak_kind": peak_kind, "kernel": f"stage_kernel<{args.order + 1}>",
-                         "note": "bound by the FP64 pipe (86.4 % of it in ncu), not HBM; traffic "
+                         "note": "bound by the FP64 pipe (86.9 % of it in ncu), not HBM; traffic "
                                  "from an ncu capture at 200k quads scaled by nodes"},
             "kernel_ms": {"stage": timed.stage_ms / args.steps, "face": timed.face_ms / args.steps,
                           "dt": timed.dt_ms / args.steps, "control": timed.control_ms / args.steps},
@@ -801,9 +801,9 @@ def run_adjoint_ensemble(args, rank: int, world: int, local: int):
             ens.set_parameters(manning=manning, tide=tide)
             return ens.forward(state, dts=dts, eta_obs=eta_obs)[0]
 
-        # each direction at two steps: the difference's rounding noise
-        # falls and its truncation error grows with the step, so their
-        # agreement shows which dominates; the closer one is reported
+        # each direction at two or three steps: the difference's rounding
+        # noise falls and its truncation error grows with the step, so their
+        # agreement shows which dominates; the closest one is reported
         rng = np.random.default_rng(17)
         checks = []
         for i in range(args.fd_directions):
@@ -813,7 +813,9 @@ def run_adjoint_ensemble(args, rank: int, world: int, local: int):
                 d = np.zeros_like(n0)
                 d[sl] = np.repeat(rng.standard_normal((sl.stop - sl.start) // nn), nn)
                 adj = float(np.dot(g.manning, d))
-                steps_rel = (1e-3, 1e-4)
+                # J is piecewise smooth in n at the scale of 1e-4 of it (wet/dry
+                # and limiter switches move with n), so the steps are smaller
+                steps_rel = (1e-4, 1e-5, 3e-6)
                 scale = float(n0[sl].max())
                 J_dir = lambda e, d=d: J_at(manning=n0 + e * d)
                 kind = "manning"
@@ -867,9 +869,10 @@ def run_adjoint_ensemble(args, rank: int, world: int, local: int):
             "setup_s": {"generate": t_gen, "create": t_create},
             "fd_check": {"directions": len(checks), "what": "central differences of the batched "
                          "GPU forward with the adjoint's time steps replayed and the parameters "
-                         "moved in place: Manning n per element of one member (steps 1e-3 and "
-                         "1e-4 relative), all eight constituents' (amplitude, phase) of one "
-                         "member (steps 1e-4 and 1e-5); each check reports the closer step",
+                         "moved in place: Manning n per element of one member (steps 1e-4, "
+                         "1e-5 and 3e-6 relative), all eight constituents' (amplitude, phase) "
+                         "of one member (steps 1e-4 and 1e-5); each check reports the closest "
+                         "step",
                          "max_rel": max(rels) if rels else None,
                          "median_rel": float(np.median(rels)) if rels else None,
                          "checks": checks},

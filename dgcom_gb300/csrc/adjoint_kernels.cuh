@@ -140,6 +140,31 @@ __global__ void __launch_bounds__(AdjCfg<N1, PATH>::THREADS, AdjCfg<N1, PATH>::M
         A.sub_list[atomicAdd(A.sub_count, 1ull)] = k;
     // this pass's elements; a block with none of them leaves together
     if ((PATH == kAdjSub) != (s_flag[e][0] != 0)) valid = false;
+    // λ of the stage output. An element whose output λ is zero at every node
+    // sends zero back through its whole reverse (linear in λ, with finite
+    // partials): its nodes' and face slots' λ are written as zeros, its
+    // sums (base, g·n², bed, neighbours) are left, and it takes no further
+    // part; a block without a live element leaves
+    double lo_h = 0, lo_hu = 0, lo_hv = 0;
+    if (valid) {
+        lo_h = A.lo_h[gi];
+        lo_hu = A.lo_hu[gi];
+        lo_hv = A.lo_hv[gi];
+        if (fp::nz(lo_h) || fp::nz(lo_hu) || fp::nz(lo_hv)) s_live[e] = 1;
+    }
+    __syncthreads();
+    if (valid && s_live[e] == 0) {
+        A.li_h[gi] = 0.0;
+        A.li_hu[gi] = 0.0;
+        A.li_hv[gi] = 0.0;
+        A.li_u[gi] = 0.0;
+        A.li_v[gi] = 0.0;
+        int64_t s_a, s_b;
+        node_face_slots<N1>(a, j, k, s_a, s_b);
+        if (s_a >= 0) A.lf_h[s_a] = A.lf_hu[s_a] = A.lf_hv[s_a] = 0.0;
+        if (s_b >= 0) A.lf_h[s_b] = A.lf_hu[s_b] = A.lf_hv[s_b] = 0.0;
+        valid = false;
+    }
     if (!__syncthreads_or(valid ? 1 : 0)) return;
     constexpr bool sub = PATH == kAdjSub;
     const bool affine = valid ? T.affine[k] != 0 : true;
@@ -151,17 +176,12 @@ __global__ void __launch_bounds__(AdjCfg<N1, PATH>::THREADS, AdjCfg<N1, PATH>::M
 
     // ---- the wet/dry correction, reversed ----
     double vh = 0, vhu = 0, vhv = 0, dhu = 0, dhv = 0;
-    double lo_h = 0, lo_hu = 0, lo_hv = 0;
     if (valid) {
         vh = keep.h[gi];
         vhu = keep.hu[gi];
         vhv = keep.hv[gi];
         dhu = keep.u[gi];
         dhv = keep.v[gi];
-        lo_h = A.lo_h[gi];
-        lo_hu = A.lo_hu[gi];
-        lo_hv = A.lo_hv[gi];
-        if (fp::nz(lo_h) || fp::nz(lo_hu) || fp::nz(lo_hv)) s_live[e] = 1;
     }
     double ldh = lo_h, ldhu = lo_hu, ldhv = lo_hv;  // λ of (vh, dhu, dhv)
     if (P.has_wet_dry) {
@@ -346,12 +366,8 @@ __global__ void __launch_bounds__(AdjCfg<N1, PATH>::THREADS, AdjCfg<N1, PATH>::M
     auto node_side = [&](int n) {
         return Sd{s_q[e][0][n], s_q[e][3][n], s_q[e][4][n], s_q[e][5][n]};
     };
-    // An element whose output λ is zero at every node sends zero back
-    // through its volume term (the reverse is linear in λ, its partials
-    // finite): it skips the volume phases, whose outputs are sums into
-    // shared λ and atomics
     __syncthreads();
-    const bool work = valid && s_live[e] != 0;
+    const bool work = valid;  // live elements only (above)
     // step 1: pair slots' λ, or the subcell faces (forward)
     if (work && !sub) {
         if (P.has_bed) {
@@ -699,13 +715,17 @@ __global__ void __launch_bounds__(256)
         const int64_t kl = L >> 2, kr = R >> 2;
         const int fl = (int)(L & 3), fr = (int)(R & 3);
         const int rfi = N1 - 1 - fi;
-        const int64_t gl = kl * NN + P.face_node[fl][fi], gr = kr * NN + P.face_node[fr][rfi];
-        const Q ql = load_q(in, T, P, gl), qr = load_q(in, T, P, gr);
-        const double* geo = &T.edge_geo[e * 5];
         const int64_t sl = (L * N1) + fi, sr = (R * N1) + rfi;
         // the right slot stored −fb
         const F3 la{A.lf_h[sl], A.lf_hu[sl], A.lf_hv[sl]};
         const F3 lb{-A.lf_h[sr], -A.lf_hu[sr], -A.lf_hv[sr]};
+        // zero λ on both sides sends zero back (linear in λ)
+        if (!(fp::nz(la.h) || fp::nz(la.hu) || fp::nz(la.hv) || fp::nz(lb.h) || fp::nz(lb.hu) ||
+              fp::nz(lb.hv)))
+            return;
+        const int64_t gl = kl * NN + P.face_node[fl][fi], gr = kr * NN + P.face_node[fr][rfi];
+        const Q ql = load_q(in, T, P, gl), qr = load_q(in, T, P, gr);
+        const double* geo = &T.edge_geo[e * 5];
         Sd ab{}, bb{};
         hydro_hll_rev(side(ql), side(qr), geo[0], geo[1], geo[2], geo[3], geo[4], g, sqrt_g, half_g,
                       h_min, la, lb, ab, bb);
@@ -718,14 +738,15 @@ __global__ void __launch_bounds__(256)
     const int64_t B = T.bface[bfi];
     const int64_t k = B >> 2;
     const int face = (int)(B & 3);
+    const int64_t sl = B * N1 + fi;
+    const F3 lfs{A.lf_h[sl], A.lf_hu[sl], A.lf_hv[sl]};
+    if (!(fp::nz(lfs.h) || fp::nz(lfs.hu) || fp::nz(lfs.hv))) return;  // zero λ: zero back
     const int64_t gn = k * NN + P.face_node[face][fi];
     const Q qi = load_q(in, T, P, gn);
     const double* geo = &T.bface_geo[bfi * 5];
     const double nx = geo[0], ny = geo[1];
     const int ci = T.bface_cond[bfi];
     const Condition& c = T.cond ? T.cond[ci] : P.cond[ci];
-    const int64_t sl = B * N1 + fi;
-    const F3 lfs{A.lf_h[sl], A.lf_hu[sl], A.lf_hv[sl]};
     double u, v;
     interior_velocity(qi, h_min, u, v);
     if (c.kind == kBcWall) {
