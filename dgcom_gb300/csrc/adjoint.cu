@@ -114,6 +114,10 @@ struct dgswe_adjoint {
     bool forward_done = false;
     dgswe_adjoint_stats stats{};
     cudaEvent_t e0 = nullptr, e1 = nullptr;
+    // the stage adjoint's subcell pass runs on its own stream beside the
+    // wet pass, forked from and joined to the target's stream
+    cudaStream_t sub_stream = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
 
     ~dgswe_adjoint() {
         if (h || ens) {
@@ -121,6 +125,9 @@ struct dgswe_adjoint {
             for (void* p : allocations) cudaFree(p);
             if (e0) cudaEventDestroy(e0);
             if (e1) cudaEventDestroy(e1);
+            if (fork) cudaEventDestroy(fork);
+            if (join) cudaEventDestroy(join);
+            if (sub_stream) cudaStreamDestroy(sub_stream);
         }
         if (h) dgswe_destroy(h);
         if (ens) dgswe_ensemble_destroy(ens);
@@ -271,6 +278,9 @@ int reverse_stages(dgswe_adjoint* a, const DevBuf* in, const DevBuf* keep) {
     const Target& t = a->tg;
     const int64_t nv = t.nv;
     cudaStream_t st = t.stream;
+    // the three stage inputs' subcell elements
+    ACK(cudaMemsetAsync(a->A.sub_count, 0, 3 * sizeof(unsigned long long), st));
+    t.ks->subcell_list(*t.T, *t.P, in[0].h, in[1].h, in[2].h, a->A, t.nn, st);
     for (int s = 2; s >= 0; --s) {
         AdjStage As = a->A;
         double** lo = s == 2 ? a->lam : a->lam_t;
@@ -278,7 +288,14 @@ int reverse_stages(dgswe_adjoint* a, const DevBuf* in, const DevBuf* keep) {
         As.lo_hu = lo[1];
         As.lo_hv = lo[2];
         if (!a->want_bed) As.lbed = nullptr;  // λ of the bed neither summed nor written
-        t.ks->stage_adjoint(t.n1, *t.T, *t.P, *t.X, in[s], keep[s], As, t.ctl, s, st);
+        // the subcell pass beside the wet pass; the face adjoint after both
+        ACK(cudaEventRecord(a->fork, st));
+        ACK(cudaStreamWaitEvent(a->sub_stream, a->fork, 0));
+        t.ks->stage_adjoint(t.n1, *t.T, *t.P, *t.X, in[s], keep[s], As, t.ctl, s, 1,
+                            a->sub_stream);
+        ACK(cudaEventRecord(a->join, a->sub_stream));
+        t.ks->stage_adjoint(t.n1, *t.T, *t.P, *t.X, in[s], keep[s], As, t.ctl, s, 0, st);
+        ACK(cudaStreamWaitEvent(st, a->join, 0));
         t.ks->face_adjoint(t.n1, *t.T, *t.P, in[s], As, t.ctl, s, st);
         // the first stage's input is the step's start: its λ, with the base
         // terms, into lam
@@ -320,6 +337,9 @@ int setup(dgswe_adjoint* a, const dgswe_form* forms, const dgswe_adjoint_config*
     ACK(cudaSetDevice(t.device));
     ACK(cudaEventCreate(&a->e0));
     ACK(cudaEventCreate(&a->e1));
+    ACK(cudaEventCreateWithFlags(&a->fork, cudaEventDisableTiming));
+    ACK(cudaEventCreateWithFlags(&a->join, cudaEventDisableTiming));
+    ACK(cudaStreamCreateWithFlags(&a->sub_stream, cudaStreamNonBlocking));
     const int64_t nf = t.K * 4 * n1;
     // the bed slope's transpose: for node c, each line partner i's
     // ∂(g∇B)_i/∂B_c = g·D[pos_i][pos_c]·w(i, c), with w the forward's metric
@@ -397,8 +417,8 @@ int setup(dgswe_adjoint* a, const dgswe_form* forms, const dgswe_adjoint_config*
     if ((s = dalloc(a, (size_t)nv, &A.lbed))) return s;
     if ((s = dalloc(a, (size_t)nv, &A.lgn2))) return s;
     if ((s = dalloc(a, (size_t)std::max(1, t.n_cond) * 2 * kMaxConstituents, &A.ltide))) return s;
-    if ((s = dalloc(a, (size_t)std::max<int64_t>(1, t.T->K), &A.sub_list))) return s;
-    if ((s = dalloc(a, 1, &A.sub_count))) return s;
+    if ((s = dalloc(a, 3 * (size_t)std::max<int64_t>(1, t.T->K), &A.sub_list))) return s;
+    if ((s = dalloc(a, 3, &A.sub_count))) return s;
     A.lb_h = a->lam_b[0];
     A.lb_hu = a->lam_b[1];
     A.lb_hv = a->lam_b[2];
@@ -742,7 +762,6 @@ int dgswe_adjoint_reverse(dgswe_adjoint* a, double* grad_h0, double* grad_hu0, d
     ACK(cudaMemsetAsync(A.lx_h, 0, 5 * bv, st));
     ACK(cudaMemsetAsync(A.lbed, 0, bv, st));
     ACK(cudaMemsetAsync(A.lgn2, 0, bv, st));
-    ACK(cudaMemsetAsync(A.sub_count, 0, sizeof(unsigned long long), st));
     ACK(cudaMemsetAsync(A.ltide, 0,
                         (size_t)std::max(1, t.n_cond) * 2 * kMaxConstituents * sizeof(double), st));
     const int* on = &t.ctl[0].always;

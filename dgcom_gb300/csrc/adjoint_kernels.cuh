@@ -28,12 +28,17 @@ namespace dgswe {
 namespace DGSWE_NS {
 
 // The stage adjoint runs as two passes: kAdjWet over the mesh, reversing
-// the elements without subcells (the split-form pairs) and listing those
-// with subcells, and kAdjSub over that list. Every element belongs to
-// exactly one pass. Apart, the wet pass needs neither the subcells' scratch
-// nor the array where λ lands from an element's other nodes, and its
-// registers are the pair path's alone, so more of its blocks fit on an SM;
-// the subcell pass's work is the list's, its other blocks leave at once.
+// the elements without subcells (the split-form pairs), and kAdjSub over
+// the list of those with subcells (subcell_list_kernel, the same test).
+// Every element belongs to exactly one pass, and the two write disjoint
+// nodes and face slots (their sums into neighbours are atomic), so they
+// run side by side. Apart, the wet pass needs neither the subcells'
+// scratch nor the array where λ lands from an element's other nodes, and
+// its registers are the pair path's alone, so more of its blocks fit on an
+// SM; the subcell pass's work is the list's, its other blocks leave at
+// once. The few subcell elements' reverse is long (each warp's FP64
+// instructions in sequence), so beside the wet pass it costs no time of
+// its own.
 enum { kAdjWet = 0, kAdjSub = 1 };
 
 template <int N1, int PATH>
@@ -96,10 +101,10 @@ __global__ void __launch_bounds__(AdjCfg<N1, PATH>::THREADS, AdjCfg<N1, PATH>::M
     // blocks past the list's end leave at once
     int64_t k;
     if (PATH == kAdjSub) {
-        const unsigned long long n_sub = *A.sub_count;
+        const unsigned long long n_sub = A.sub_count[slot];
         const unsigned long long at = (unsigned long long)blockIdx.x * EPB;
         if (at >= n_sub) return;
-        k = at + e < n_sub ? A.sub_list[at + e] : T.K;
+        k = at + e < n_sub ? A.sub_list[slot * T.K + (int64_t)(at + e)] : T.K;
     } else {
         k = (int64_t)blockIdx.x * EPB + e;
     }
@@ -135,9 +140,6 @@ __global__ void __launch_bounds__(AdjCfg<N1, PATH>::THREADS, AdjCfg<N1, PATH>::M
     __syncthreads();
     if (valid && P.formulation == kWetDry && fp::lt(h, P.subcell_depth)) atomicOr(&s_flag[e][0], 1);
     __syncthreads();
-    // the wet pass lists the subcell elements for the subcell pass
-    if (PATH == kAdjWet && i == 0 && valid && s_flag[e][0] != 0)
-        A.sub_list[atomicAdd(A.sub_count, 1ull)] = k;
     // this pass's elements; a block with none of them leaves together
     if ((PATH == kAdjSub) != (s_flag[e][0] != 0)) valid = false;
     // λ of the stage output. An element whose output λ is zero at every node
@@ -779,6 +781,23 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// The subcell elements of a step's three stage inputs h0, h1, h2 (a node
+// shallower than the subcell depth, in the WetDry formulation): stage s's
+// list at A.sub_list + s·K, its length in A.sub_count[s] (zeroed before).
+// One thread per element; the lists' order does not matter.
+__global__ void subcell_list_kernel(DevTables T, Physics P, const double* h0, const double* h1,
+                                    const double* h2, AdjStage A, int nn) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= T.K || P.formulation != kWetDry) return;
+    const double* hs[3] = {h0, h1, h2};
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+        bool sub = false;
+        for (int i = 0; i < nn; ++i) sub |= fp::lt(hs[s][k * nn + i], P.subcell_depth);
+        if (sub) A.sub_list[s * T.K + (int64_t)atomicAdd(&A.sub_count[s], 1ull)] = k;
+    }
+}
+
 // λ of the stage input: own element + faces and neighbours, the node
 // velocity folded into h, hu, hv; clears the atomic accumulators. For the
 // step's first stage (`base_h` set) λ of the step's start state: that plus
@@ -807,7 +826,6 @@ __global__ void adjoint_combine_kernel(DevBuf in, AdjStage A, double* out_h, dou
     A.lx_hv[g] = 0.0;
     A.lx_u[g] = 0.0;
     A.lx_v[g] = 0.0;
-    if (g == 0) *A.sub_count = 0;  // the stage's subcell list is spent
 }
 
 // η = Σ w_i (h_i + B_i) at each station (its element's nodes, Lagrange

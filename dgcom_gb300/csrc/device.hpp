@@ -206,8 +206,8 @@ struct AdjStage {
     double* lbed;                                // of the bed elevation (atomic)
     double* lgn2;                                // of g·n² per node (added)
     double* ltide;                               // [condition][constituent][amplitude, phase]
-    int64_t* sub_list;                           // the stage's subcell elements (wet pass)
-    unsigned long long* sub_count;               // their number (reset by the combine)
+    int64_t* sub_list;                           // [3][K] each stage's subcell elements
+    unsigned long long* sub_count;               // [3] their numbers
 };
 
 }  // namespace dgswe

@@ -27,10 +27,11 @@ struct KernelSet {
                        const DevBuf& in, const DevBuf& base, const DevBuf& out, const double* fh,
                        const double* fhu, const double* fhv, StepCtl* ctl, int slot,
                        int check_finite, const DevBuf& keep, cudaStream_t);
-    // the adjoint of one stage (adjoint_kernels.cuh)
+    // the adjoint of one stage (adjoint_kernels.cuh): the wet elements'
+    // pass (`subcells` 0) or the listed subcell elements' (1)
     void (*stage_adjoint)(int n1, const DevTables&, const Physics&, const StageExtra&,
                           const DevBuf& in, const DevBuf& keep, const AdjStage&,
-                          const StepCtl* ctl, int slot, cudaStream_t);
+                          const StepCtl* ctl, int slot, int subcells, cudaStream_t);
     void (*face_adjoint)(int n1, const DevTables&, const Physics&, const DevBuf& in,
                          const AdjStage&, const StepCtl* ctl, int slot, cudaStream_t);
     // out = λ of the stage input; with `base` (the first stage), + base,
@@ -61,6 +62,10 @@ struct KernelSet {
     // per element: every node deeper than d0, d1, d2 (bits 0, 1, 2)
     void (*depth_flags)(const double* h, int64_t K, int nn, double d0, double d1, double d2,
                         uint8_t* flags, cudaStream_t);
+    // the subcell elements of a step's three stage inputs, one list each,
+    // for the stage adjoint's subcell pass
+    void (*subcell_list)(const DevTables&, const Physics&, const double* h0, const double* h1,
+                         const double* h2, const AdjStage&, int nn, cudaStream_t);
 };
 
 // kernels_fast.cu: FMA contraction, division-free Manning rate

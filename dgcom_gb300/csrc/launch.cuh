@@ -180,14 +180,18 @@ static void finish_listed(int n1, const DevTables& T, const Physics& P, const De
 template <int N1>
 static void stage_adjoint_n(const DevTables& T, const Physics& P, const StageExtra& X,
                             const DevBuf& in, const DevBuf& keep, const AdjStage& A,
-                            const StepCtl* ctl, int slot, cudaStream_t s) {
-    // the wet elements' pass, then the subcell elements'
-    using CW = AdjCfg<N1, kAdjWet>;
-    stage_adjoint_kernel<N1, kAdjWet><<<(unsigned)((T.K + CW::EPB - 1) / CW::EPB), CW::THREADS, 0,
-                                        s>>>(T, P, X, in, keep, A, ctl, slot);
-    using CS = AdjCfg<N1, kAdjSub>;
-    stage_adjoint_kernel<N1, kAdjSub><<<(unsigned)((T.K + CS::EPB - 1) / CS::EPB), CS::THREADS, 0,
-                                        s>>>(T, P, X, in, keep, A, ctl, slot);
+                            const StepCtl* ctl, int slot, int subcells, cudaStream_t s) {
+    if (T.K == 0) return;
+    if (!subcells) {
+        using CW = AdjCfg<N1, kAdjWet>;
+        stage_adjoint_kernel<N1, kAdjWet><<<(unsigned)((T.K + CW::EPB - 1) / CW::EPB),
+                                            CW::THREADS, 0, s>>>(T, P, X, in, keep, A, ctl, slot);
+    } else {
+        // sized for every element; the blocks past the list's end leave at once
+        using CS = AdjCfg<N1, kAdjSub>;
+        stage_adjoint_kernel<N1, kAdjSub><<<(unsigned)((T.K + CS::EPB - 1) / CS::EPB),
+                                            CS::THREADS, 0, s>>>(T, P, X, in, keep, A, ctl, slot);
+    }
 }
 
 template <int N1>
@@ -200,8 +204,8 @@ static void face_adjoint_n(const DevTables& T, const Physics& P, const DevBuf& i
 
 static void stage_adjoint(int n1, const DevTables& T, const Physics& P, const StageExtra& X,
                           const DevBuf& in, const DevBuf& keep, const AdjStage& A,
-                          const StepCtl* ctl, int slot, cudaStream_t s) {
-    DGSWE_BY_ORDER(stage_adjoint_n, T, P, X, in, keep, A, ctl, slot, s);
+                          const StepCtl* ctl, int slot, int subcells, cudaStream_t s) {
+    DGSWE_BY_ORDER(stage_adjoint_n, T, P, X, in, keep, A, ctl, slot, subcells, s);
 }
 
 static void face_adjoint(int n1, const DevTables& T, const Physics& P, const DevBuf& in,
@@ -218,6 +222,12 @@ static void adjoint_combine(const DevBuf& in, const AdjStage& A, double* out_h, 
     adjoint_combine_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
         in, A, out_h, out_hu, out_hv, base ? base[0] : nullptr, base ? base[1] : nullptr,
         base ? base[2] : nullptr, n, h_min);
+}
+
+static void subcell_list(const DevTables& T, const Physics& P, const double* h0, const double* h1,
+                         const double* h2, const AdjStage& A, int nn, cudaStream_t s) {
+    if (T.K == 0) return;
+    subcell_list_kernel<<<(unsigned)((T.K + 255) / 256), 256, 0, s>>>(T, P, h0, h1, h2, A, nn);
 }
 
 static void station_eval(const double* h, const double* bed, const int64_t* node0, const double* w,
@@ -263,7 +273,7 @@ static const KernelSet kSet = {face,          stage,         finish,          dt
                                 velocity,      stage_keep,    stage_adjoint,   face_adjoint,
                                 adjoint_combine, station_eval, station_seed,   begin,
                                 dt_fit,        end,           face_listed,     stage_listed,
-                                finish_listed, depth_flags};
+                                finish_listed, depth_flags,    subcell_list};
 
 }  // namespace DGSWE_NS
 }  // namespace dgswe
