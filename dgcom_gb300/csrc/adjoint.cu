@@ -339,7 +339,10 @@ int setup(dgswe_adjoint* a, const dgswe_form* forms, const dgswe_adjoint_config*
     ACK(cudaEventCreate(&a->e1));
     ACK(cudaEventCreateWithFlags(&a->fork, cudaEventDisableTiming));
     ACK(cudaEventCreateWithFlags(&a->join, cudaEventDisableTiming));
-    ACK(cudaStreamCreateWithFlags(&a->sub_stream, cudaStreamNonBlocking));
+    // the highest priority: the few subcell blocks, each long, start first
+    int least = 0, greatest = 0;
+    ACK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    ACK(cudaStreamCreateWithPriority(&a->sub_stream, cudaStreamNonBlocking, greatest));
     const int64_t nf = t.K * 4 * n1;
     // the bed slope's transpose: for node c, each line partner i's
     // ∂(g∇B)_i/∂B_c = g·D[pos_i][pos_c]·w(i, c), with w the forward's metric

@@ -48,9 +48,11 @@ struct AdjCfg {
     static constexpr int NA = 2 * (N1 - 1);
     static constexpr int EPB = (64 / NN) > 0 ? (64 / NN) : 1;
     static constexpr int THREADS = EPB * NN;
-    // λ of each pair slot's two sides (3 each), then in the same place the
-    // slot's six outputs; the bed-slope weights (2 per node)
-    static constexpr int PAIR = NN * NP * 6 + 2 * NN;
+    // per pair slot a row of 7: λ of its two sides (3 each), then in the
+    // same place the pair's factors for its two nodes; the bed-slope
+    // weights (2 per node)
+    static constexpr int ROW = 7;
+    static constexpr int PAIR = NN * NP * ROW + 2 * NN;
     static constexpr int FACES = 2 * NN * 8;                    // subcell faces
     static constexpr int IFL = 2 * N1 * (N1 - 1) * 6;           // subcell interface fluxes
     static constexpr int SUB = 2 * FACES + IFL;                 // faces, their λ, interfaces' λ
@@ -97,8 +99,8 @@ __global__ void __launch_bounds__(AdjCfg<N1, PATH>::THREADS, AdjCfg<N1, PATH>::M
 
     const int tid = threadIdx.x;
     const int e = tid / NN, i = tid % NN;
-    // the subcell pass takes its elements from the wet pass's list; its
-    // blocks past the list's end leave at once
+    // the subcell pass takes its elements from the stage's subcell list;
+    // its blocks past the list's end leave at once
     int64_t k;
     if (PATH == kAdjSub) {
         const unsigned long long n_sub = A.sub_count[slot];
@@ -118,7 +120,11 @@ __global__ void __launch_bounds__(AdjCfg<N1, PATH>::THREADS, AdjCfg<N1, PATH>::M
         s_flag[e][1] = 0;
         s_live[e] = 0;
     }
+    // the node's input, λ of its output and the kept values, loaded together
+    // (one memory latency), though an element of the other pass uses none
     double h = 0, hu = 0, hv = 0, u = 0, v = 0, b = 0;
+    double lo_h = 0, lo_hu = 0, lo_hv = 0;
+    double vh = 0, vhu = 0, vhv = 0, dhu = 0, dhv = 0;
     if (valid) {
         h = in.h[gi];
         hu = in.hu[gi];
@@ -126,6 +132,14 @@ __global__ void __launch_bounds__(AdjCfg<N1, PATH>::THREADS, AdjCfg<N1, PATH>::M
         u = in.u[gi];
         v = in.v[gi];
         b = P.has_bed ? T.bed[gi] : 0.0;
+        lo_h = A.lo_h[gi];
+        lo_hu = A.lo_hu[gi];
+        lo_hv = A.lo_hv[gi];
+        vh = keep.h[gi];
+        vhu = keep.hu[gi];
+        vhv = keep.hv[gi];
+        dhu = keep.u[gi];
+        dhv = keep.v[gi];
     }
     s_q[e][0][i] = h;
     s_q[e][1][i] = hu;
@@ -147,13 +161,7 @@ __global__ void __launch_bounds__(AdjCfg<N1, PATH>::THREADS, AdjCfg<N1, PATH>::M
     // partials): its nodes' and face slots' λ are written as zeros, its
     // sums (base, g·n², bed, neighbours) are left, and it takes no further
     // part; a block without a live element leaves
-    double lo_h = 0, lo_hu = 0, lo_hv = 0;
-    if (valid) {
-        lo_h = A.lo_h[gi];
-        lo_hu = A.lo_hu[gi];
-        lo_hv = A.lo_hv[gi];
-        if (fp::nz(lo_h) || fp::nz(lo_hu) || fp::nz(lo_hv)) s_live[e] = 1;
-    }
+    if (valid && (fp::nz(lo_h) || fp::nz(lo_hu) || fp::nz(lo_hv))) s_live[e] = 1;
     __syncthreads();
     if (valid && s_live[e] == 0) {
         A.li_h[gi] = 0.0;
@@ -177,14 +185,7 @@ __global__ void __launch_bounds__(AdjCfg<N1, PATH>::THREADS, AdjCfg<N1, PATH>::M
     double Lh = 0, Lhu = 0, Lhv = 0, Lu = 0, Lv = 0, Lb = 0;
 
     // ---- the wet/dry correction, reversed ----
-    double vh = 0, vhu = 0, vhv = 0, dhu = 0, dhv = 0;
-    if (valid) {
-        vh = keep.h[gi];
-        vhu = keep.hu[gi];
-        vhv = keep.hv[gi];
-        dhu = keep.u[gi];
-        dhv = keep.v[gi];
-    }
+
     double ldh = lo_h, ldhu = lo_hu, ldhv = lo_hv;  // λ of (vh, dhu, dhv)
     if (P.has_wet_dry) {
         if (valid && fp::lt(vh, P.h_dry)) atomicOr(&s_flag[e][1], 1);
@@ -360,11 +361,15 @@ __global__ void __launch_bounds__(AdjCfg<N1, PATH>::THREADS, AdjCfg<N1, PATH>::M
     double* faces = &s_x[e][0];                    // subcell [dir][line][pos][8]
     double* faces_b = &s_x[e][C::FACES];           // their λ
     double* ifl_b = &s_x[e][2 * C::FACES];         // λ of the interface fluxes [..][6]
-    double* lf = &s_x[e][0];                       // pair path: [slot][side][3]
-    // pair path: [slot][λh_a, λh_c, λhu, λhv, λu, λv], written over the
-    // slot's own λ once its owner has read them (no other thread reads them)
+    constexpr int ROW = C::ROW;
+    double* lf = &s_x[e][0];                       // pair path: [slot][side·3 + c] in rows of 7
+    // pair path: [slot][λp, λm, m0, m1, λu, λv, m] — λ of the pair's
+    // pressure and mass flux, its metric, λ of its velocity sums and its mass
+    // flux — written over the slot's own λ once its owner has read them (no
+    // other thread reads them); each node takes λp·h(other node),
+    // λm·(m0, m1) and (λu, λv)·m
     double* lp = lf;
-    double* s_ab = &s_x[e][NN * NP * 6];           // pair path: bed-slope weights −h·λr [2][NN]
+    double* s_ab = &s_x[e][NN * NP * ROW];         // pair path: bed-slope weights −h·λr [2][NN]
     auto node_side = [&](int n) {
         return Sd{s_q[e][0][n], s_q[e][3][n], s_q[e][4][n], s_q[e][5][n]};
     };
@@ -381,7 +386,7 @@ __global__ void __launch_bounds__(AdjCfg<N1, PATH>::THREADS, AdjCfg<N1, PATH>::M
         for (int q = 0; q < NA; ++q) {
             const int sl = T.sched_slot[i * NA + q];
             const int side = T.sched_owned[sl * 5] == i ? 0 : 1;
-            double* o = &lf[(sl * 2 + side) * 3];
+            double* o = &lf[sl * ROW + side * 3];
             o[0] = -T.sched_coef[i * NA + q] * lrh;
             o[1] = -T.sched_hcoef[i * NA + q] * lrhu;
             o[2] = -T.sched_hcoef[i * NA + q] * lrhv;
@@ -449,22 +454,22 @@ __global__ void __launch_bounds__(AdjCfg<N1, PATH>::THREADS, AdjCfg<N1, PATH>::M
             const int na = own[0], nc = own[1];
             const double hm0 = T.pair_hm[(gi * NP + q) * 2];
             const double hm1 = T.pair_hm[(gi * NP + q) * 2 + 1];
-            const double* l0 = &lf[(sl * 2) * 3];
-            const double* l1 = &lf[(sl * 2 + 1) * 3];
+            const double* l0 = &lf[sl * ROW];
+            const double* l1 = &lf[sl * ROW + 3];
             const double f0 = l0[0] + l1[0], f1 = l0[1] + l1[1], f2 = l0[2] + l1[2];
-            const double ha = s_q[e][0][na], hc = s_q[e][0][nc];
             const double mass = (s_q[e][1][na] + s_q[e][1][nc]) * hm0 +
                                 (s_q[e][2][na] + s_q[e][2][nc]) * hm1;
             const double lmass =
                 f0 + f1 * (s_q[e][3][na] + s_q[e][3][nc]) + f2 * (s_q[e][4][na] + s_q[e][4][nc]);
             const double lgp2 = (f1 * hm0 + f2 * hm1) * two_g;
-            double* o = &lp[sl * 6];  // both nodes share all but λh
-            o[0] = lgp2 * hc;
-            o[1] = lgp2 * ha;
-            o[2] = lmass * hm0;
-            o[3] = lmass * hm1;
-            o[4] = f1 * mass;
-            o[5] = f2 * mass;
+            double* o = &lp[sl * ROW];
+            o[0] = lgp2;
+            o[1] = lmass;
+            o[2] = hm0;
+            o[3] = hm1;
+            o[4] = f1;
+            o[5] = f2;
+            o[6] = mass;
         }
     } else if (work && sub) {
 #pragma unroll
@@ -539,13 +544,14 @@ __global__ void __launch_bounds__(AdjCfg<N1, PATH>::THREADS, AdjCfg<N1, PATH>::M
 #pragma unroll
         for (int q = 0; q < NA; ++q) {
             const int sl = T.sched_slot[i * NA + q];
-            const int side = T.sched_owned[sl * 5] == i ? 0 : 1;
-            const double* o = &lp[sl * 6];
-            Lh += o[side];
-            Lhu += o[2];
-            Lhv += o[3];
-            Lu += o[4];
-            Lv += o[5];
+            const int8_t* own = &T.sched_owned[sl * 5];
+            const int other = own[0] == i ? own[1] : own[0];
+            const double* o = &lp[sl * ROW];
+            Lh += o[0] * s_q[e][0][other];
+            Lhu += o[1] * o[2];
+            Lhv += o[1] * o[3];
+            Lu += o[4] * o[6];
+            Lv += o[5] * o[6];
         }
         if (P.has_bed && A.lbed) {
             // gdb_i = g Σ_dir Σ_c D[pos_i][pos_c] B_c w(i, c), transposed: this
@@ -721,12 +727,14 @@ __global__ void __launch_bounds__(256)
         // the right slot stored −fb
         const F3 la{A.lf_h[sl], A.lf_hu[sl], A.lf_hv[sl]};
         const F3 lb{-A.lf_h[sr], -A.lf_hu[sr], -A.lf_hv[sr]};
+        // (the states are loaded before the test below, so that one memory
+        // latency covers both)
+        const int64_t gl = kl * NN + P.face_node[fl][fi], gr = kr * NN + P.face_node[fr][rfi];
+        const Q ql = load_q(in, T, P, gl), qr = load_q(in, T, P, gr);
         // zero λ on both sides sends zero back (linear in λ)
         if (!(fp::nz(la.h) || fp::nz(la.hu) || fp::nz(la.hv) || fp::nz(lb.h) || fp::nz(lb.hu) ||
               fp::nz(lb.hv)))
             return;
-        const int64_t gl = kl * NN + P.face_node[fl][fi], gr = kr * NN + P.face_node[fr][rfi];
-        const Q ql = load_q(in, T, P, gl), qr = load_q(in, T, P, gr);
         const double* geo = &T.edge_geo[e * 5];
         Sd ab{}, bb{};
         hydro_hll_rev(side(ql), side(qr), geo[0], geo[1], geo[2], geo[3], geo[4], g, sqrt_g, half_g,
@@ -807,13 +815,20 @@ __global__ void adjoint_combine_kernel(DevBuf in, AdjStage A, double* out_h, dou
                                        double* base_hv, int64_t n, double h_min) {
     const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n) return;
+    // every load first, so that one memory latency covers them all
+    double bh = 0.0, bhu = 0.0, bhv = 0.0;
+    if (base_h) {
+        bh = base_h[g];
+        bhu = base_hu[g];
+        bhv = base_hv[g];
+    }
     double lh = A.li_h[g] + A.lx_h[g], lhu = A.li_hu[g] + A.lx_hu[g], lhv = A.li_hv[g] + A.lx_hv[g];
     const double lu = A.li_u[g] + A.lx_u[g], lv = A.li_v[g] + A.lx_v[g];
     node_velocity_rev(in.h[g], in.hu[g], in.hv[g], h_min, lu, lv, lh, lhu, lhv);
     if (base_h) {
-        lh = lh + base_h[g];
-        lhu = lhu + base_hu[g];
-        lhv = lhv + base_hv[g];
+        lh = lh + bh;
+        lhu = lhu + bhu;
+        lhv = lhv + bhv;
         base_h[g] = 0.0;
         base_hu[g] = 0.0;
         base_hv[g] = 0.0;

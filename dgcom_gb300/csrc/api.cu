@@ -124,7 +124,12 @@ int begin_run(dgswe_handle* h, const dgswe_run_config* run, double target) {
 
 int ensure_dt_stream(dgswe_handle* h) {
     if (h->dt_stream) return DGSWE_OK;
-    CK(cudaStreamCreateWithFlags(&h->dt_stream, cudaStreamNonBlocking));
+    // the highest priority: the block scheduler starts the dt pass's blocks
+    // before the face pass's, so the stage pass waiting for both is not
+    // left waiting for the dt pass's tail
+    int least = 0, greatest = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    CK(cudaStreamCreateWithPriority(&h->dt_stream, cudaStreamNonBlocking, greatest));
     CK(cudaEventCreateWithFlags(&h->dt_fork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&h->dt_join, cudaEventDisableTiming));
     return DGSWE_OK;
@@ -182,7 +187,8 @@ int run_device_step_graph(dgswe_handle* h, int scheme, double cfl) {
     h->ks->step_end(h->ctl, 1, h->stream);
     cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
     if (e != cudaSuccess) return fail(h, DGSWE_ERR_CUDA, "stream capture: %s", cudaGetErrorString(e));
-    e = cudaGraphInstantiate(&h->step_graph, graph, 0);
+    // the kernel nodes keep the priority of the stream they were captured on
+    e = cudaGraphInstantiate(&h->step_graph, graph, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return fail(h, DGSWE_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
     h->graph_scheme = scheme;
