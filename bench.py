@@ -47,6 +47,36 @@ BYTES_PER_NODE_STAGE = {2: 81.8, 3: 77.5}  # algorithmic bytes (state, bed, mesh
 # stage_kernel<4>'s DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per
 # node-stage in one ncu capture of the 200k-quad coastal box, for scaling by nodes
 STAGE_TRAFFIC_PER_NODE_STAGE = {3: 187.3}
+# FP64 floating-point operations the step's kernels execute per node (an FMA
+# as 2): ncu's dadd + dmul + 2·dfma instruction counts of one capture of the
+# 200k-quad coastal box at N = 3 — the stage and face kernels per stage (three
+# a step) and the dt kernel once a step
+FP64_FLOPS_PER_NODE = {3: {"stage": 157.4, "face": 77.1, "dt": 11.4}}
+
+
+def fp64_gemm_tflops(device: int, n: int = 6144, reps: int = 5) -> float | None:
+    """cuBLAS FP64 GEMM throughput on this GPU (torch.mm of n × n doubles,
+    CUDA events, after one warm-up): the FP64 roof the kernels are held to."""
+    try:
+        import torch
+
+        a = torch.randn(n, n, dtype=torch.float64, device=f"cuda:{device}")
+        b = torch.randn(n, n, dtype=torch.float64, device=f"cuda:{device}")
+        torch.mm(a, b)
+        torch.cuda.synchronize(device)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            torch.mm(a, b)
+        e1.record()
+        torch.cuda.synchronize(device)
+        seconds = e0.elapsed_time(e1) * 1e-3
+        del a, b
+        torch.cuda.empty_cache()
+        return 2.0 * n ** 3 * reps / seconds / 1e12
+    except Exception:  # noqa: BLE001 - a missing roof leaves the figure without a fraction
+        return None
 
 
 def peaks():
@@ -375,6 +405,20 @@ def run_ours(args, rank: int, world: int, local: int):
     if rank == 0 and not args.no_cpu_baseline:
         baseline = cpu_baseline_figures(case, os.cpu_count() or 1)
     dev.close()
+    fp64 = None
+    if args.order in FP64_FLOPS_PER_NODE:
+        f = FP64_FLOPS_PER_NODE[args.order]
+        per_node_step = 3.0 * (f["stage"] + f["face"]) + f["dt"]
+        achieved_tf = per_node_step * nodes * args.steps / (timed.total_ms * 1e-3) / 1e12
+        gemm = fp64_gemm_tflops(local)
+        sm_ghz = (clocks or {}).get("sm_mhz", 2070.0) / 1e3
+        fp64 = {"achieved": achieved_tf, "unit": "TFLOP/s", "flops_per_node_step": per_node_step,
+                "peak_dgemm": gemm, "frac_of_dgemm": achieved_tf / gemm if gemm else None,
+                "peak_pipe": 152 * 2 * 2 * sm_ghz / 1e3,
+                "note": "FP64 operations the step's kernels execute (ncu instruction counts at "
+                        "200k quads, an FMA as 2) over the step's device time; peak_dgemm is "
+                        "cuBLAS FP64 GEMM measured in this run, peak_pipe 2 FP64 FMA per SM "
+                        "per clock at the sampled SM clock"}
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -392,6 +436,7 @@ def run_ours(args, rank: int, world: int, local: int):
                          "peak_kind": peak_kind, "kernel": f"stage_kernel<{args.order + 1}>",
                          "note": "bound by the FP64 pipe (86.9 % of it in ncu), not HBM; traffic "
                                  "from an ncu capture at 200k quads scaled by nodes"},
+            "fp64": fp64,
             "kernel_ms": {"stage": timed.stage_ms / args.steps, "face": timed.face_ms / args.steps,
                           "dt": timed.dt_ms / args.steps, "control": timed.control_ms / args.steps},
             # the state each way, and the step's 496-byte control record each
