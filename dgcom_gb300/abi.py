@@ -355,6 +355,8 @@ ENTRY_POINTS = {
                                           C.c_int64, _dp, C.c_int64, _dp, C.c_int64]),
     "stage": (C.c_int, [C.c_void_p, C.POINTER(StagePlan)]),
     "finish": (C.c_int, [C.c_void_p, C.c_int32]),
+    "implicit_damping": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_double]),
+    "post_process": (C.c_int, [C.c_void_p, C.c_int32]),
     "element_dt": (C.c_int, [C.c_void_p, C.c_double, C.c_int32, _dp, _dp]),
     "step": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double]),
     "run": (C.c_int, [C.c_void_p, C.POINTER(RunConfig), CALLBACK, C.c_void_p, C.POINTER(Report)]),

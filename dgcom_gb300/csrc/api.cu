@@ -883,6 +883,37 @@ int dgswe_finish(dgswe_handle* h, int32_t acc) {
     return sync(h);
 }
 
+int dgswe_implicit_damping(dgswe_handle* h, int32_t stage, int32_t from, double dt) {
+    if (!h) return DGSWE_ERR_INVALID;
+    if (!valid_buffer(stage) || !valid_buffer(from) || !(dt >= 0.0) || !std::isfinite(dt))
+        return fail(h, DGSWE_ERR_INVALID, "implicit_damping: buffers %d, %d, dt %g", stage, from,
+                    dt);
+    // ImplicitDamping2D::is_active: neither friction nor the thin layer, no change
+    if (!h->P.friction && !h->P.has_wet_dry) return DGSWE_OK;
+    CK(cudaSetDevice(h->device));
+    if (int s = ensure_buffer(h, stage)) return s;
+    if (int s = ensure_buffer(h, from)) return s;
+    h->ks->implicit_damping(h->T, h->P, h->buf[stage].view, h->buf[from].view, dt, h->n_values,
+                            h->stream);
+    CK(cudaGetLastError());
+    return sync(h);
+}
+
+int dgswe_post_process(dgswe_handle* h, int32_t buffer) {
+    if (!h) return DGSWE_ERR_INVALID;
+    if (!valid_buffer(buffer))
+        return fail(h, DGSWE_ERR_INVALID, "post_process: invalid buffer %d", buffer);
+    CK(cudaSetDevice(h->device));
+    if (int s = ensure_buffer(h, buffer)) return s;
+    // the end of a substep with the buffer as both its sum and its state:
+    // each node read before it is written, the limiter's element sums from
+    // shared memory
+    h->ks->finish(h->n1, h->T, h->P, h->buf[buffer].view, h->buf[buffer].view, h->ctl,
+                  h->stream);
+    CK(cudaGetLastError());
+    return sync(h);
+}
+
 int dgswe_element_dt(dgswe_handle* h, double cfl, int32_t scheme, double* dt_elements,
                      double* dt_min) {
     if (!h) return DGSWE_ERR_INVALID;

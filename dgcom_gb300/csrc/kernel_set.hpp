@@ -66,6 +66,10 @@ struct KernelSet {
     // for the stage adjoint's subcell pass
     void (*subcell_list)(const DevTables&, const Physics&, const double* h0, const double* h1,
                          const double* h2, const AdjStage&, int nn, cudaStream_t);
+    // the point-implicit damping of `stage` over dt, rates frozen at `from`
+    // (n values), and the stage's node velocities
+    void (*implicit_damping)(const DevTables&, const Physics&, const DevBuf& stage,
+                             const DevBuf& from, double dt, int64_t n, cudaStream_t);
 };
 
 // kernels_fast.cu: FMA contraction, division-free Manning rate

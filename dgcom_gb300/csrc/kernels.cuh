@@ -960,6 +960,27 @@ __global__ void depth_flags_kernel(const double* h, int64_t K, int nn, double d0
     flags[k] = (uint8_t)((a ? 1 : 0) | (b ? 2 : 0) | (c ? 4 : 0));
 }
 
+// The point-implicit damping of a stage value over dt with the rates frozen
+// at `from` (apply_implicit_damping_2d, src/solver/algorithms/
+// wetting_drying.rs:376-389: damp_node at every node), then the stage's
+// node velocities
+__global__ void damping_kernel(DevTables T, Physics P, DevBuf stage, DevBuf from, double dt,
+                               int64_t n) {
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    const double h = stage.h[g];
+    double hu = stage.hu[g], hv = stage.hv[g];
+    const double g_n2 = P.friction == 2 ? T.g_n2[g] : P.g_n2;
+    damp(P, g_n2, h, hu, hv, DampIn{from.h[g], from.hu[g], from.hv[g], from.u[g], from.v[g]},
+         dt);
+    stage.hu[g] = hu;
+    stage.hv[g] = hv;
+    double u, v;
+    node_velocity(h, hu, hv, P.h_min, u, v);
+    stage.u[g] = u;
+    stage.v[g] = v;
+}
+
 // node velocities of a buffer (after an upload)
 __global__ void velocity_kernel(DevBuf b, int64_t n, double h_min) {
     const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;

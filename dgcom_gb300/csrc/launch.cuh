@@ -252,6 +252,12 @@ static void depth_flags(const double* h, int64_t K, int nn, double d0, double d1
     depth_flags_kernel<<<(unsigned)((K + 255) / 256), 256, 0, s>>>(h, K, nn, d0, d1, d2, flags);
 }
 
+static void implicit_damping(const DevTables& T, const Physics& P, const DevBuf& stage,
+                             const DevBuf& from, double dt, int64_t n, cudaStream_t s) {
+    if (n == 0) return;
+    damping_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(T, P, stage, from, dt, n);
+}
+
 static void velocity(const DevBuf& b, int64_t n, double h_min, cudaStream_t s) {
     if (n == 0) return;
     velocity_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b, n, h_min);
@@ -273,7 +279,8 @@ static const KernelSet kSet = {face,          stage,         finish,          dt
                                 velocity,      stage_keep,    stage_adjoint,   face_adjoint,
                                 adjoint_combine, station_eval, station_seed,   begin,
                                 dt_fit,        end,           face_listed,     stage_listed,
-                                finish_listed, depth_flags,    subcell_list};
+                                finish_listed, depth_flags,    subcell_list,
+                                implicit_damping};
 
 }  // namespace DGSWE_NS
 }  // namespace dgswe

@@ -177,6 +177,17 @@ class SWEPhysics2D:
         """state ← acc, post-processed."""
         self._check(self.lib.finish(self.handle, acc), "finish")
 
+    def implicit_damping(self, stage: int, from_: int, dt: float):
+        """PhysicsModule::implicit_damping: buffer ``stage`` damped over ``dt``
+        (bottom friction, thin-layer relaxation), the rates frozen at buffer
+        ``from_``."""
+        self._check(self.lib.implicit_damping(self.handle, stage, from_, dt), "implicit_damping")
+
+    def post_process(self, buffer: int = abi.STATE):
+        """PhysicsModule::post_process: the wet/dry correction of ``buffer``
+        in place."""
+        self._check(self.lib.post_process(self.handle, buffer), "post_process")
+
     # -- LocalTimeStepping passes (a host-planned multirate coarse step) ----------
     def begin_coarse_step(self, levels, rates):
         """LocalTimeStepping::begin_coarse_step: the coarse step's levels

@@ -459,6 +459,21 @@ int dgswe_stage(dgswe_handle* handle, const dgswe_stage_plan* plan);
  * (LocalTimeStepping::finish_where, src/physics/builder.rs:739-782). */
 int dgswe_finish(dgswe_handle* handle, int32_t acc);
 
+/* Point-implicit damping of a stage value (PhysicsModule::implicit_damping,
+ * src/physics/builder.rs:501-504; apply_implicit_damping_2d,
+ * src/solver/algorithms/wetting_drying.rs:376-389): buffer `stage`, formed
+ * from an RHS at buffer `from` with weight dt on it, damped over dt by the
+ * bottom friction and the wet/dry thin-layer relaxation with the rates
+ * frozen at `from` (damp_node at every node); the stage's node velocities
+ * follow. Without friction or a wet/dry correction nothing changes. */
+int dgswe_implicit_damping(dgswe_handle* handle, int32_t stage, int32_t from, double dt);
+
+/* The wet/dry correction of a buffer in place (PhysicsModule::post_process,
+ * src/physics/builder.rs:488-499): per element, the positivity limiter where
+ * a node is below h_dry, then correct_node at every node; clipped elements
+ * add to dgswe_negative_depth_clips. */
+int dgswe_post_process(dgswe_handle* handle, int32_t buffer);
+
 /* Every element's stable step at `cfl` for `scheme` (element_dt_swe_2d,
  * src/solver/rhs/swe_2d.rs:2018-2043, with the positivity bound of a
  * wet/dry run) into dt_elements (n_elements values; may be NULL), and their

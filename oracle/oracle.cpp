@@ -2185,6 +2185,38 @@ int oracle_finish(oracle_handle* h, int32_t acc) {
     return DGSWE_OK;
 }
 
+// PhysicsModule::implicit_damping (src/physics/builder.rs:501-504;
+// apply_implicit_damping_2d, src/solver/algorithms/wetting_drying.rs:376-389):
+// damp_node at every node of buffer `stage`, the rates frozen at `from`
+int oracle_implicit_damping(oracle_handle* h, int32_t stage, int32_t from, double dt) {
+    Model& m = *h->m;
+    if (!check_buffer(m, stage).empty() || !check_buffer(m, from).empty()) return DGSWE_ERR_INVALID;
+    if (m.form.friction == DGSWE_FRICTION_NONE && !m.form.has_wet_dry) return DGSWE_OK;
+    Buffer& s = m.buf[stage];
+    const Buffer& f = m.buf[from];
+    const int64_t n = (int64_t)m.n_values();
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) damp_node(m, (size_t)i, s.h[i], s.hu[i], s.hv[i], f.get(i), dt);
+    return DGSWE_OK;
+}
+
+// PhysicsModule::post_process (src/physics/builder.rs:488-499) of a buffer in
+// place, element by element, the clipped elements counted
+int oracle_post_process(oracle_handle* h, int32_t buffer) {
+    Model& m = *h->m;
+    if (!check_buffer(m, buffer).empty()) return DGSWE_ERR_INVALID;
+    Buffer& b = m.buf[buffer];
+    const int nn = m.ops.nn;
+    int64_t clips = 0;
+#pragma omp parallel for schedule(static) reduction(+ : clips)
+    for (int64_t k = 0; k < m.mesh.n_elements; ++k) {
+        const size_t o = (size_t)k * nn;
+        clips += post_process_element(m, k, &b.h[o], &b.hu[o], &b.hv[o]) ? 1 : 0;
+    }
+    m.clips += clips;
+    return DGSWE_OK;
+}
+
 int oracle_element_dt(oracle_handle* h, double cfl, int32_t scheme, double* dt_el, double* dt_min) {
     double d = min_element_dt(*h->m, cfl, scheme, dt_el);
     if (dt_min) *dt_min = d;

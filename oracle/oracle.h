@@ -32,6 +32,8 @@ int oracle_subcell_divergence(oracle_handle* h, int64_t k, const double* hu, con
                               const double* interfaces, const double* face, double* div);
 int oracle_stage(oracle_handle* h, const dgswe_stage_plan* plan);
 int oracle_finish(oracle_handle* h, int32_t acc);
+int oracle_implicit_damping(oracle_handle* h, int32_t stage, int32_t from, double dt);
+int oracle_post_process(oracle_handle* h, int32_t buffer);
 int oracle_element_dt(oracle_handle* h, double cfl, int32_t scheme, double* dt_elements,
                       double* dt_min);
 int oracle_step(oracle_handle* h, int32_t scheme, double t, double dt);
