@@ -48,11 +48,10 @@ struct AdjCfg {
     static constexpr int NA = 2 * (N1 - 1);
     static constexpr int EPB = (64 / NN) > 0 ? (64 / NN) : 1;
     static constexpr int THREADS = EPB * NN;
-    // per pair slot a row of 7: λ of its two sides (3 each), then in the
-    // same place the pair's factors for its two nodes; the bed-slope
-    // weights (2 per node)
+    // per pair slot a row of 7, the pair's factors for its two nodes; the
+    // bed-slope weights (2 per node); each node's λ of the RHS (3 per node)
     static constexpr int ROW = 7;
-    static constexpr int PAIR = NN * NP * ROW + 2 * NN;
+    static constexpr int PAIR = NN * NP * ROW + 5 * NN;
     static constexpr int FACES = 2 * NN * 8;                    // subcell faces
     static constexpr int IFL = 2 * N1 * (N1 - 1) * 6;           // subcell interface fluxes
     static constexpr int SUB = 2 * FACES + IFL;                 // faces, their λ, interfaces' λ
@@ -362,14 +361,12 @@ __global__ void __launch_bounds__(AdjCfg<N1, PATH>::THREADS, AdjCfg<N1, PATH>::M
     double* faces_b = &s_x[e][C::FACES];           // their λ
     double* ifl_b = &s_x[e][2 * C::FACES];         // λ of the interface fluxes [..][6]
     constexpr int ROW = C::ROW;
-    double* lf = &s_x[e][0];                       // pair path: [slot][side·3 + c] in rows of 7
     // pair path: [slot][λp, λm, m0, m1, λu, λv, m] — λ of the pair's
     // pressure and mass flux, its metric, λ of its velocity sums and its mass
-    // flux — written over the slot's own λ once its owner has read them (no
-    // other thread reads them); each node takes λp·h(other node),
-    // λm·(m0, m1) and (λu, λv)·m
-    double* lp = lf;
+    // flux; each node takes λp·h(other node), λm·(m0, m1) and (λu, λv)·m
+    double* lp = &s_x[e][0];
     double* s_ab = &s_x[e][NN * NP * ROW];         // pair path: bed-slope weights −h·λr [2][NN]
+    double* s_lr = &s_x[e][NN * NP * ROW + 2 * NN];  // pair path: λ of the RHS [3][NN]
     auto node_side = [&](int n) {
         return Sd{s_q[e][0][n], s_q[e][3][n], s_q[e][4][n], s_q[e][5][n]};
     };
@@ -382,15 +379,9 @@ __global__ void __launch_bounds__(AdjCfg<N1, PATH>::THREADS, AdjCfg<N1, PATH>::M
         }
         s_ab[i] = -h * lrhu;
         s_ab[NN + i] = -h * lrhv;
-#pragma unroll
-        for (int q = 0; q < NA; ++q) {
-            const int sl = T.sched_slot[i * NA + q];
-            const int side = T.sched_owned[sl * 5] == i ? 0 : 1;
-            double* o = &lf[sl * ROW + side * 3];
-            o[0] = -T.sched_coef[i * NA + q] * lrh;
-            o[1] = -T.sched_hcoef[i * NA + q] * lrhu;
-            o[2] = -T.sched_hcoef[i * NA + q] * lrhv;
-        }
+        s_lr[i] = lrh;
+        s_lr[NN + i] = lrhu;
+        s_lr[2 * NN + i] = lrhv;
     } else if (work && sub) {
 #pragma unroll
         for (int dir = 0; dir < 2; ++dir) {
@@ -454,9 +445,12 @@ __global__ void __launch_bounds__(AdjCfg<N1, PATH>::THREADS, AdjCfg<N1, PATH>::M
             const int na = own[0], nc = own[1];
             const double hm0 = T.pair_hm[(gi * NP + q) * 2];
             const double hm1 = T.pair_hm[(gi * NP + q) * 2 + 1];
-            const double* l0 = &lf[sl * ROW];
-            const double* l1 = &lf[sl * ROW + 3];
-            const double f0 = l0[0] + l1[0], f1 = l0[1] + l1[1], f2 = l0[2] + l1[2];
+            // λ of the pair's flux: its two nodes' λ of the RHS, each times
+            // its accumulation coefficient (−coef into h, −coef/2 into hu, hv)
+            const double* pc = &T.pair_coef[sl * 4];
+            const double f0 = -(pc[0] * s_lr[na] + pc[1] * s_lr[nc]);
+            const double f1 = -(pc[2] * s_lr[NN + na] + pc[3] * s_lr[NN + nc]);
+            const double f2 = -(pc[2] * s_lr[2 * NN + na] + pc[3] * s_lr[2 * NN + nc]);
             const double mass = (s_q[e][1][na] + s_q[e][1][nc]) * hm0 +
                                 (s_q[e][2][na] + s_q[e][2][nc]) * hm1;
             const double lmass =

@@ -584,6 +584,7 @@ int create_impl(dgswe_handle* h, const dgswe_form* f, int device) {
     std::vector<double> hcoef(sched.accum_coef.size());
     for (size_t q = 0; q < hcoef.size(); ++q) hcoef[q] = 0.5 * sched.accum_coef[q];
     UP(sched_hcoef, hcoef);
+    UP(pair_coef, pair_coef_table(sched));
 #undef UP
 
     fill_physics(*f, ops, !t.fcor.empty(), h->P, h->X);

@@ -36,6 +36,7 @@ struct DevTables {
     const int32_t* sched_slot;  // [nn][2(n1-1)]
     const double* sched_coef;   // [nn][2(n1-1)]
     const double* sched_hcoef;  // [nn][2(n1-1)] sched_coef / 2
+    const double* pair_coef;    // [nn·(n1-1)][4] per owned slot: both nodes' coefficients, halves
     // An ensemble's concatenated members: each element's member (its
     // StepCtl is ctl[member]) and the members' boundary conditions, which
     // bface_cond indexes. Both null for one mesh (ctl[0], Physics::cond).

@@ -203,6 +203,7 @@ int build_group(dgswe_ensemble* h, Group& G, std::vector<Tables>& tabs,
     std::vector<double> hcoef(sched.accum_coef.size());
     for (size_t q = 0; q < hcoef.size(); ++q) hcoef[q] = 0.5 * sched.accum_coef[q];
     UP(sched_hcoef, hcoef);
+    UP(pair_coef, pair_coef_table(sched));
 #undef UP
     fill_physics(h->form0, ops, fcor, G.P, G.X);
     G.P.has_bed = h->form0.bathymetry ? 1 : 0;

@@ -245,4 +245,21 @@ inline std::vector<int8_t> owned_table(const PairSchedule& sched) {
     return owned;
 }
 
+// Per owned pair slot, its two nodes' accumulation coefficients and their
+// halves: [slot][coef of a, coef of c, coef of a / 2, coef of c / 2] (the
+// adjoint's pair path, which forms both products at the owner)
+inline std::vector<double> pair_coef_table(const PairSchedule& sched) {
+    const int na = 2 * (sched.n1 - 1);
+    std::vector<double> pc(sched.owned.size() * 4, 0.0);
+    for (int i = 0; i < sched.nn; ++i)
+        for (int q = 0; q < na; ++q) {
+            const int sl = sched.accum_slot[(size_t)i * na + q];
+            const int side = sched.owned[sl].a == i ? 0 : 1;
+            const double c = sched.accum_coef[(size_t)i * na + q];
+            pc[(size_t)sl * 4 + side] = c;
+            pc[(size_t)sl * 4 + 2 + side] = 0.5 * c;
+        }
+    return pc;
+}
+
 }  // namespace dgswe
