@@ -963,6 +963,47 @@ int dgswe_step(dgswe_handle* h, int32_t scheme, double t, double dt) {
     return sync(h);
 }
 
+namespace {
+
+// The ready lists of dgswe_step_host's upload chunks (element chunks of
+// ⌈K/kHostChunks⌉): an element's dt pass reads its nodes and its face
+// neighbours' face nodes, so it is ready with the last of their chunks; an
+// interior edge with the later of its two elements' chunks; a boundary face
+// with its element's. Each list in index order.
+int build_ready_lists(dgswe_handle* h) {
+    if (h->ready_built) return DGSWE_OK;
+    const int64_t K = h->K, per = (K + kHostChunks - 1) / kHostChunks;
+    auto chunk = [&](int64_t k) { return (int)(k / per); };
+    std::vector<int32_t> elems[kHostChunks], edges[kHostChunks], bfaces[kHostChunks];
+    for (int64_t k = 0; k < K; ++k) {
+        int c = chunk(k);
+        for (int f = 0; f < 4; ++f)
+            if (h->nb[k][f] >= 0) c = std::max(c, chunk(h->nb[k][f]));
+        elems[c].push_back((int32_t)k);
+    }
+    for (size_t e = 0; e < h->h_edge_left.size(); ++e)
+        edges[std::max(chunk(h->h_edge_left[e] >> 2), chunk(h->h_edge_right[e] >> 2))].push_back(
+            (int32_t)e);
+    for (size_t b = 0; b < h->h_bface.size(); ++b)
+        bfaces[chunk(h->h_bface[b] >> 2)].push_back((int32_t)b);
+    auto flatten = [&](std::vector<int32_t>* parts, int64_t* off, const int32_t** out) {
+        std::vector<int32_t> all;
+        for (int c = 0; c < kHostChunks; ++c) {
+            off[c] = (int64_t)all.size();
+            all.insert(all.end(), parts[c].begin(), parts[c].end());
+        }
+        off[kHostChunks] = (int64_t)all.size();
+        return upload_vec(h, all, out);
+    };
+    if (int s = flatten(elems, h->ready_elem_off, &h->ready_elems)) return s;
+    if (int s = flatten(edges, h->ready_edge_off, &h->ready_edges)) return s;
+    if (int s = flatten(bfaces, h->ready_bface_off, &h->ready_bfaces)) return s;
+    h->ready_built = true;
+    return DGSWE_OK;
+}
+
+}  // namespace
+
 int dgswe_step_host(dgswe_handle* h, int32_t scheme, double t, double cfl, double dt_max,
                     double* hh, double* hu, double* hv, int64_t n, double* dt_out) {
     if (!h) return DGSWE_ERR_INVALID;
@@ -1009,33 +1050,45 @@ int dgswe_step_host(dgswe_handle* h, int32_t scheme, double t, double cfl, doubl
         }
         CK(cudaMemcpyAsync(h->ctl, &c, sizeof c, cudaMemcpyHostToDevice, h->stream));
     }
-    // the state in element chunks on the copy stream, each chunk's node
-    // velocities computed while the next one arrives
+    // the state in element chunks on the copy stream; as each chunk
+    // arrives, its node velocities, and the dt pass and the first stage's
+    // face fluxes of whatever reads nothing later
+    if (int s = build_ready_lists(h)) return s;
     const DevBuf& q = h->buf[DGSWE_STATE].view;
+    const int* active = &h->ctl->active;
+    const DtParams D = dt_params(h->form, cfl, scheme);
     const int64_t per = (h->K + kHostChunks - 1) / kHostChunks;
+    h->ks->step_begin(h->ctl, 1, h->stream);  // the dt reset, the first stage's time
     CK(cudaEventRecord(h->chunk_done[0], h->stream));  // after the work queued before
     CK(cudaStreamWaitEvent(h->copy_stream, h->chunk_done[0], 0));
     for (int c = 0; c < kHostChunks; ++c) {
-        const int64_t k0 = c * per, k1 = std::min<int64_t>(h->K, k0 + per);
-        if (k1 <= k0) break;
-        const size_t off = (size_t)k0 * h->nn, cnt = (size_t)(k1 - k0) * h->nn;
-        const size_t len = cnt * sizeof(double);
-        CK(cudaMemcpyAsync(q.h + off, hh + off, len, cudaMemcpyHostToDevice, h->copy_stream));
-        CK(cudaMemcpyAsync(q.hu + off, hu + off, len, cudaMemcpyHostToDevice, h->copy_stream));
-        CK(cudaMemcpyAsync(q.hv + off, hv + off, len, cudaMemcpyHostToDevice, h->copy_stream));
-        CK(cudaEventRecord(h->chunk_done[c], h->copy_stream));
-        CK(cudaStreamWaitEvent(h->stream, h->chunk_done[c], 0));
-        const DevBuf part{q.h + off, q.hu + off, q.hv + off, q.u + off, q.v + off};
-        h->ks->velocity(part, (int64_t)cnt, h->P.h_min, h->stream);
+        const int64_t k0 = std::min<int64_t>(h->K, c * per), k1 = std::min<int64_t>(h->K, k0 + per);
+        if (k1 > k0) {
+            const size_t off = (size_t)k0 * h->nn, cnt = (size_t)(k1 - k0) * h->nn;
+            const size_t len = cnt * sizeof(double);
+            CK(cudaMemcpyAsync(q.h + off, hh + off, len, cudaMemcpyHostToDevice, h->copy_stream));
+            CK(cudaMemcpyAsync(q.hu + off, hu + off, len, cudaMemcpyHostToDevice,
+                               h->copy_stream));
+            CK(cudaMemcpyAsync(q.hv + off, hv + off, len, cudaMemcpyHostToDevice,
+                               h->copy_stream));
+            CK(cudaEventRecord(h->chunk_done[c], h->copy_stream));
+            CK(cudaStreamWaitEvent(h->stream, h->chunk_done[c], 0));
+            const DevBuf part{q.h + off, q.hu + off, q.hv + off, q.u + off, q.v + off};
+            h->ks->velocity(part, (int64_t)cnt, h->P.h_min, h->stream);
+        }
+        const int64_t e0 = h->ready_elem_off[c], e1 = h->ready_elem_off[c + 1];
+        h->ks->dt_listed(h->n1, h->T, h->P, q, D, nullptr, h->ctl, active, h->ready_elems + e0,
+                         e1 - e0, h->stream);
+        const int64_t f0 = h->ready_edge_off[c], f1 = h->ready_edge_off[c + 1];
+        const int64_t b0 = h->ready_bface_off[c], b1 = h->ready_bface_off[c + 1];
+        h->ks->face_ready(h->n1, h->T, h->P, q, h->fb_h, h->fb_hu, h->fb_hv, h->ctl, 0, active,
+                          h->ready_edges + f0, f1 - f0, h->ready_bfaces + b0, b1 - b0, h->stream);
     }
-    const int* active = &h->ctl->active;
-    const DtParams D = dt_params(h->form, cfl, scheme);
-    if (int s = ensure_dt_stream(h)) return s;
-    h->ks->step_begin(h->ctl, 1, h->stream);
-    if (int s = dt_beside_first_face(h, D, active)) return s;
+    h->ks->node_sources(h->T, h->P, q, h->ctl, 0, h->stream);
+    h->ks->step_dt(h->ctl, 1, h->stream);
     for (int s = 0; s + 1 < n_st; ++s) {
         const int in = s == 0 ? DGSWE_STATE : s;
-        if (s == 0)  // its face pass ran beside the dt pass
+        if (s == 0)  // its face fluxes came with the upload
             h->ks->stage(h->n1, h->T, h->P, h->X, h->buf[in].view, q, h->buf[s + 1].view, q,
                          h->fb_h, h->fb_hu, h->fb_hv, h->ctl, s, kModePost, 0, active, h->stream);
         else

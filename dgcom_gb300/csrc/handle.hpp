@@ -102,6 +102,15 @@ struct dgswe_handle {
     // the compute, and one event per chunk (created on first use)
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t chunk_done[dgswe::kHostChunks] = {};
+    // per upload chunk, what the first stage can take once that chunk has
+    // arrived (everything it reads in it or before it): the elements' dt
+    // pass, the interior edges' and boundary faces' fluxes (ready_*[off[c]
+    // .. off[c+1]), built on first use)
+    const int32_t *ready_elems = nullptr, *ready_edges = nullptr, *ready_bfaces = nullptr;
+    int64_t ready_elem_off[dgswe::kHostChunks + 1] = {};
+    int64_t ready_edge_off[dgswe::kHostChunks + 1] = {};
+    int64_t ready_bface_off[dgswe::kHostChunks + 1] = {};
+    bool ready_built = false;
     // the dt pass's own stream, beside the first stage's face pass, and the
     // fork and join between them (created on first use)
     cudaStream_t dt_stream = nullptr;

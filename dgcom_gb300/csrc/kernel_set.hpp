@@ -70,6 +70,19 @@ struct KernelSet {
     // (n values), and the stage's node velocities
     void (*implicit_damping)(const DevTables&, const Physics&, const DevBuf& stage,
                              const DevBuf& from, double dt, int64_t n, cudaStream_t);
+    // a global stage's face fluxes of the listed interior edges and boundary
+    // faces, without the node sources (a stage taken in parts as its input
+    // arrives); the node sources alone (weather, relaxation band)
+    void (*face_ready)(int n1, const DevTables&, const Physics&, const DevBuf& in, double* fh,
+                       double* fhu, double* fhv, const StepCtl* ctl, int slot, const int* active,
+                       const int32_t* edges, int64_t n_edges, const int32_t* bfaces,
+                       int64_t n_bfaces, cudaStream_t);
+    void (*node_sources)(const DevTables&, const Physics&, const DevBuf& in, const StepCtl* ctl,
+                         int slot, cudaStream_t);
+    // the dt pass over the listed elements
+    void (*dt_listed)(int n1, const DevTables&, const Physics&, const DevBuf& q, const DtParams&,
+                      double* dt_el, StepCtl* ctl, const int* active, const int32_t* list,
+                      int64_t n, cudaStream_t);
 };
 
 // kernels_fast.cu: FMA contraction, division-free Manning rate

@@ -303,7 +303,10 @@ __global__ void __launch_bounds__(256) face_kernel(DevTables T, Physics P, DevBu
         // tide per boundary node (characteristic_boundary_state,
         // src/boundary/characteristic.rs:411-437)
         const int member = T.elem_member ? T.elem_member[k] : 0;
-        const double t = LISTED ? lts_stage(lp, k).time : ctl[member].stage[slot].time;
+        // a multirate pass: the element's own stage time; a listed global
+        // pass (no levels): the stage's
+        const double t =
+            (LISTED && lp.level) ? lts_stage(lp, k).time : ctl[member].stage[slot].time;
         Q qb;
         if (c.kind == kBcNodeTides || c.kind == kBcParent) {
             const int64_t s = T.bface_slot[bfi * N1 + fi];
@@ -1048,12 +1051,14 @@ __device__ __forceinline__ double element_dt(const DtParams& D, int order, doubl
     return fp::lt(rmax, 1e-14) ? INFINITY : cfl / ((2.0 * (double)order + 1.0) * rmax);
 }
 
-template <int N1>
+// LISTED: the elements list[0..n_list) (any order, any subset), else all
+template <int N1, bool LISTED>
 __global__ void __launch_bounds__(DtCfg<N1>::THREADS)
     dt_kernel(DevTables T, Physics P, DevBuf q, DtParams D, double* dt_el, StepCtl* ctl,
-              const int* active) {
+              const int* active, const int32_t* list, int64_t n_list) {
     using C = DtCfg<N1>;
     constexpr int NN = C::NN, EPB = C::EPB, PITCH = C::PITCH, SLOTS = C::SLOTS;
+    __shared__ int64_t s_k[EPB];                      // the block's elements
     __shared__ float s_r[EPB][SLOTS];                 // r₃₂, −1 for a dry node
     __shared__ float s_b[EPB][SLOTS];                 // δ·B
     __shared__ unsigned int s_lo[EPB];                // the element's largest r₃₂ − δ·B (bits)
@@ -1065,8 +1070,9 @@ __global__ void __launch_bounds__(DtCfg<N1>::THREADS)
     if (!*active) return;
     const int tid = threadIdx.x;
     const int e = tid / NN, i = tid % NN;
-    const int64_t k0 = (int64_t)blockIdx.x * EPB;
-    const int64_t k = k0 + e;
+    const int64_t at = (int64_t)blockIdx.x * EPB + e;
+    const int64_t k = LISTED ? (at < n_list ? (int64_t)list[at] : T.K) : at;
+    if (i == 0) s_k[e] = k;
     const int64_t gi = k * NN + i;
     const double g = P.g, h_min = P.h_min;
     const float g32 = f32_trunc(g);
@@ -1129,7 +1135,7 @@ __global__ void __launch_bounds__(DtCfg<N1>::THREADS)
     for (int c = tid; c < n_cand; c += C::THREADS) {
         const int es = s_list[c];
         const int ce = es / SLOTS, sl = es % SLOTS;
-        const int64_t kc = k0 + ce;
+        const int64_t kc = s_k[ce];
         int64_t node;
         const double* m;
         if (sl < NN) {
@@ -1144,11 +1150,11 @@ __global__ void __launch_bounds__(DtCfg<N1>::THREADS)
         atomicMax(&s_rmax[ce], (unsigned long long)fp::bits(r));  // r ≥ +0
     }
     __syncthreads();
-    if (tid >= 32) return;  // warp 0: lane l < EPB finishes element k0 + l
-    const int64_t kl = k0 + tid;
+    if (tid >= 32) return;  // warp 0: lane l < EPB finishes the block's element l
+    const int64_t kl = tid < EPB ? s_k[tid] : T.K;
     unsigned long long dt_bits = 0x7FF0000000000000ull;  // +∞
     int member = -1;
-    if (tid < EPB && kl < T.K) {
+    if (kl < T.K) {
         const double rmax = fp::from_bits((int64_t)s_rmax[tid]);
         const double dt = element_dt<N1>(D, P.order, T.weight_ratio[kl], rmax, &s_h[tid * PITCH],
                                          &s_mass[tid * PITCH]);

@@ -116,7 +116,37 @@ static void dt_n(const DevTables& T, const Physics& P, const DevBuf& q, const Dt
                  double* dt_el, StepCtl* ctl, const int* active, cudaStream_t s) {
     using C = DtCfg<N1>;
     const unsigned blocks = (unsigned)((T.K + C::EPB - 1) / C::EPB);
-    dt_kernel<N1><<<blocks, C::THREADS, 0, s>>>(T, P, q, D, dt_el, ctl, active);
+    dt_kernel<N1, false><<<blocks, C::THREADS, 0, s>>>(T, P, q, D, dt_el, ctl, active, nullptr, 0);
+}
+
+template <int N1>
+static void dt_listed_n(const DevTables& T, const Physics& P, const DevBuf& q, const DtParams& D,
+                        double* dt_el, StepCtl* ctl, const int* active, const int32_t* list,
+                        int64_t n, cudaStream_t s) {
+    using C = DtCfg<N1>;
+    if (n <= 0) return;
+    const unsigned blocks = (unsigned)((n + C::EPB - 1) / C::EPB);
+    dt_kernel<N1, true><<<blocks, C::THREADS, 0, s>>>(T, P, q, D, dt_el, ctl, active, list, n);
+}
+
+// The face fluxes of the listed interior edges and boundary faces of a
+// global stage (no node sources: node_sources launches those)
+template <int N1>
+static void face_ready_n(const DevTables& T, const Physics& P, const DevBuf& in, double* fh,
+                         double* fhu, double* fhv, const StepCtl* ctl, int slot,
+                         const int* active, const int32_t* edges, int64_t n_edges,
+                         const int32_t* bfaces, int64_t n_bfaces, cudaStream_t s) {
+    const int64_t items = (n_edges + n_bfaces) * N1;
+    if (items <= 0) return;
+    LtsPass lp{};  // no levels: the boundary faces at the stage's time
+    lp.edges = edges;
+    lp.n_edges = n_edges;
+    lp.bfaces = bfaces;
+    lp.n_bfaces = n_bfaces;
+    const int threads = P.face_threads > 0 && P.face_threads <= 256 ? P.face_threads : 256;
+    const unsigned blocks = (unsigned)((items + threads - 1) / threads);
+    face_kernel<N1, true><<<blocks, threads, 0, s>>>(T, P, in, fh, fhu, fhv, ctl, slot, active,
+                                                     lp);
 }
 
 #define DGSWE_BY_ORDER(fn, ...)            \
@@ -131,6 +161,25 @@ static void face(int n1, const DevTables& T, const Physics& P, const DevBuf& in,
                  double* fhu, double* fhv, const StepCtl* ctl, int slot, const int* active,
                  cudaStream_t s) {
     DGSWE_BY_ORDER(face_n, T, P, in, fh, fhu, fhv, ctl, slot, active, s);
+}
+
+static void face_ready(int n1, const DevTables& T, const Physics& P, const DevBuf& in, double* fh,
+                       double* fhu, double* fhv, const StepCtl* ctl, int slot, const int* active,
+                       const int32_t* edges, int64_t n_edges, const int32_t* bfaces,
+                       int64_t n_bfaces, cudaStream_t s) {
+    DGSWE_BY_ORDER(face_ready_n, T, P, in, fh, fhu, fhv, ctl, slot, active, edges, n_edges, bfaces,
+                   n_bfaces, s);
+}
+
+static void node_sources(const DevTables& T, const Physics& P, const DevBuf& in,
+                         const StepCtl* ctl, int slot, cudaStream_t s) {
+    relax<false>(T, P, in, ctl, slot, LtsPass{}, s);
+}
+
+static void dt_listed(int n1, const DevTables& T, const Physics& P, const DevBuf& q,
+                      const DtParams& D, double* dt_el, StepCtl* ctl, const int* active,
+                      const int32_t* list, int64_t n, cudaStream_t s) {
+    DGSWE_BY_ORDER(dt_listed_n, T, P, q, D, dt_el, ctl, active, list, n, s);
 }
 
 static void stage(int n1, const DevTables& T, const Physics& P, const StageExtra& X,
@@ -280,7 +329,8 @@ static const KernelSet kSet = {face,          stage,         finish,          dt
                                 adjoint_combine, station_eval, station_seed,   begin,
                                 dt_fit,        end,           face_listed,     stage_listed,
                                 finish_listed, depth_flags,    subcell_list,
-                                implicit_damping};
+                                implicit_damping, face_ready,  node_sources,
+                                dt_listed};
 
 }  // namespace DGSWE_NS
 }  // namespace dgswe

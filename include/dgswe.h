@@ -495,9 +495,11 @@ int dgswe_step(dgswe_handle* handle, int32_t scheme, double t, double dt);
  * dt_max when it is > 0; it lands on the end of any forcing series'
  * snapshots rather than leave them), advances the state from t and writes
  * it back into the same arrays, and the step taken into dt_out (may be
- * NULL). The upload and the last stage run in element chunks, each chunk
- * copied while the next one computes; page-locked host arrays give the full
- * overlap. The result is that of dgswe_upload, dgswe_element_dt,
+ * NULL). The upload runs in element chunks, and as each chunk arrives the
+ * dt pass and the first stage's face fluxes run for what reads nothing
+ * later; the last stage runs in element chunks, each copied back while the
+ * next one computes. Page-locked host arrays give the full overlap. The
+ * result is that of dgswe_upload, dgswe_element_dt,
  * dgswe_step and dgswe_download, bit for bit; the state buffer holds it
  * too. DGSWE_ERR_NONFINITE if the new state is not finite. */
 int dgswe_step_host(dgswe_handle* handle, int32_t scheme, double t, double cfl, double dt_max,

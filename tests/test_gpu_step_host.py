@@ -63,3 +63,28 @@ def test_step_host_caps_the_step_and_refuses_bad_arrays():
             dev.step_host(0.0, -1.0, *q)
     finally:
         dev.close()
+
+
+@pytest.mark.parametrize("nx,ny", [(3, 2), (9, 1), (40, 4)])
+def test_step_host_on_meshes_of_fewer_elements_than_chunks_and_more(nx, ny):
+    """Meshes of 6, 9 and 160 elements: chunks left empty, chunks of one
+    element, and every element's dt and every face's flux taken as its
+    chunk arrives; the same bits as the call-by-call step."""
+    case = cases.tidal_channel(nx=nx, ny=ny)
+    q0 = cases.with_flow(case)
+    a, b = SWEPhysics2D(case.form, 0), SWEPhysics2D(case.form, 0)
+    try:
+        host = [np.ascontiguousarray(x) for x in q0]
+        b.upload(*q0)
+        t = 0.0
+        for _ in range(3):
+            dt = a.step_host(t, case.cfl, *host)
+            want_dt = b.compute_dt_ssp(case.cfl)
+            assert dt == want_dt
+            b.step(t, want_dt)
+            for g, w in zip(host, b.download()):
+                assert np.array_equal(g, w)
+            t += dt
+    finally:
+        a.close()
+        b.close()
