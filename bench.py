@@ -389,9 +389,13 @@ def run_ours(args, rank: int, world: int, local: int):
     h, hu, hv = dev.download()
     for dst, src in zip(pinned, (h, hu, hv)):
         dst[:] = src
+    # warm-up calls (the first builds the upload chunks' ready lists and the
+    # copy stream), then the timed ones, each from the state the last left
+    t = warm.t_final
+    for _ in range(max(1, min(args.warmup, 3))):
+        t += dev.step_host(t, case.cfl, *pinned)
     dist.barrier()
     t0 = time.perf_counter()
-    t = warm.t_final
     for _ in range(e2e_steps):
         t += dev.step_host(t, case.cfl, *pinned)
     e2e_seconds = dist.max(time.perf_counter() - t0)

@@ -499,6 +499,8 @@ int dgswe_step(dgswe_handle* handle, int32_t scheme, double t, double dt);
  * dt pass and the first stage's face fluxes run for what reads nothing
  * later; the last stage runs in element chunks, each copied back while the
  * next one computes. Page-locked host arrays give the full overlap. The
+ * handle's first call builds the chunks' ready lists (host work and device
+ * memory in proportion to the mesh) and its copy stream. The
  * result is that of dgswe_upload, dgswe_element_dt,
  * dgswe_step and dgswe_download, bit for bit; the state buffer holds it
  * too. DGSWE_ERR_NONFINITE if the new state is not finite. */
