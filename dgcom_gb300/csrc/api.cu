@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstddef>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -1024,12 +1025,14 @@ int dgswe_step_host(dgswe_handle* h, int32_t scheme, double t, double cfl, doubl
         CK(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
         for (cudaEvent_t& e : h->chunk_done)
             CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        for (cudaEvent_t& e : h->vel_done)
+            CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     }
+    if (int s = ensure_dt_stream(h)) return s;
     // one step of the device clock from t; it lands on the end of any
-    // forcing series' snapshots rather than leave them
+    // forcing series' snapshots rather than leave them. The running clip
+    // count stays on the device: the record is written around it
     {
-        long long clips0 = 0;
-        CK(cudaMemcpy(&clips0, &h->ctl->clips, sizeof clips0, cudaMemcpyDeviceToHost));
         StepCtl& c = *h->h_ctl;
         std::memset(&c, 0, sizeof c);
         c.t = t;
@@ -1039,7 +1042,6 @@ int dgswe_step_host(dgswe_handle* h, int32_t scheme, double t, double cfl, doubl
         c.cfl = cfl;
         c.dt_min_used = INFINITY;
         c.dt_bits = 0x7FF0000000000000ull;
-        c.clips = clips0;
         c.always = 1;
         c.scheme_stages = n_st;
         for (int s = 0; s < n_st; ++s) {
@@ -1048,7 +1050,10 @@ int dgswe_step_host(dgswe_handle* h, int32_t scheme, double t, double cfl, doubl
             c.st_beta[s] = st[s][2];
             c.st_c[s] = st[s][3];
         }
-        CK(cudaMemcpyAsync(h->ctl, &c, sizeof c, cudaMemcpyHostToDevice, h->stream));
+        const size_t at = offsetof(StepCtl, clips), past = at + sizeof c.clips;
+        CK(cudaMemcpyAsync(h->ctl, &c, at, cudaMemcpyHostToDevice, h->stream));
+        CK(cudaMemcpyAsync((char*)h->ctl + past, (const char*)&c + past, sizeof c - past,
+                           cudaMemcpyHostToDevice, h->stream));
     }
     // the state in element chunks on the copy stream; as each chunk
     // arrives, its node velocities, and the dt pass and the first stage's
@@ -1076,16 +1081,22 @@ int dgswe_step_host(dgswe_handle* h, int32_t scheme, double t, double cfl, doubl
             const DevBuf part{q.h + off, q.hu + off, q.hv + off, q.u + off, q.v + off};
             h->ks->velocity(part, (int64_t)cnt, h->P.h_min, h->stream);
         }
+        // the dt pass on its own stream beside the face fluxes, once the
+        // chunk's velocities (and so every earlier chunk's) are in
+        CK(cudaEventRecord(h->vel_done[c], h->stream));
+        CK(cudaStreamWaitEvent(h->dt_stream, h->vel_done[c], 0));
         const int64_t e0 = h->ready_elem_off[c], e1 = h->ready_elem_off[c + 1];
         h->ks->dt_listed(h->n1, h->T, h->P, q, D, nullptr, h->ctl, active, h->ready_elems + e0,
-                         e1 - e0, h->stream);
+                         e1 - e0, h->dt_stream);
         const int64_t f0 = h->ready_edge_off[c], f1 = h->ready_edge_off[c + 1];
         const int64_t b0 = h->ready_bface_off[c], b1 = h->ready_bface_off[c + 1];
         h->ks->face_ready(h->n1, h->T, h->P, q, h->fb_h, h->fb_hu, h->fb_hv, h->ctl, 0, active,
                           h->ready_edges + f0, f1 - f0, h->ready_bfaces + b0, b1 - b0, h->stream);
     }
+    h->ks->step_dt(h->ctl, 1, h->dt_stream);
+    CK(cudaEventRecord(h->dt_join, h->dt_stream));
     h->ks->node_sources(h->T, h->P, q, h->ctl, 0, h->stream);
-    h->ks->step_dt(h->ctl, 1, h->stream);
+    CK(cudaStreamWaitEvent(h->stream, h->dt_join, 0));
     for (int s = 0; s + 1 < n_st; ++s) {
         const int in = s == 0 ? DGSWE_STATE : s;
         if (s == 0)  // its face fluxes came with the upload
