@@ -1025,10 +1025,7 @@ int dgswe_step_host(dgswe_handle* h, int32_t scheme, double t, double cfl, doubl
         CK(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
         for (cudaEvent_t& e : h->chunk_done)
             CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-        for (cudaEvent_t& e : h->vel_done)
-            CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     }
-    if (int s = ensure_dt_stream(h)) return s;
     // one step of the device clock from t; it lands on the end of any
     // forcing series' snapshots rather than leave them. The running clip
     // count stays on the device: the record is written around it
@@ -1081,22 +1078,16 @@ int dgswe_step_host(dgswe_handle* h, int32_t scheme, double t, double cfl, doubl
             const DevBuf part{q.h + off, q.hu + off, q.hv + off, q.u + off, q.v + off};
             h->ks->velocity(part, (int64_t)cnt, h->P.h_min, h->stream);
         }
-        // the dt pass on its own stream beside the face fluxes, once the
-        // chunk's velocities (and so every earlier chunk's) are in
-        CK(cudaEventRecord(h->vel_done[c], h->stream));
-        CK(cudaStreamWaitEvent(h->dt_stream, h->vel_done[c], 0));
         const int64_t e0 = h->ready_elem_off[c], e1 = h->ready_elem_off[c + 1];
         h->ks->dt_listed(h->n1, h->T, h->P, q, D, nullptr, h->ctl, active, h->ready_elems + e0,
-                         e1 - e0, h->dt_stream);
+                         e1 - e0, h->stream);
         const int64_t f0 = h->ready_edge_off[c], f1 = h->ready_edge_off[c + 1];
         const int64_t b0 = h->ready_bface_off[c], b1 = h->ready_bface_off[c + 1];
         h->ks->face_ready(h->n1, h->T, h->P, q, h->fb_h, h->fb_hu, h->fb_hv, h->ctl, 0, active,
                           h->ready_edges + f0, f1 - f0, h->ready_bfaces + b0, b1 - b0, h->stream);
     }
-    h->ks->step_dt(h->ctl, 1, h->dt_stream);
-    CK(cudaEventRecord(h->dt_join, h->dt_stream));
     h->ks->node_sources(h->T, h->P, q, h->ctl, 0, h->stream);
-    CK(cudaStreamWaitEvent(h->stream, h->dt_join, 0));
+    h->ks->step_dt(h->ctl, 1, h->stream);
     for (int s = 0; s + 1 < n_st; ++s) {
         const int in = s == 0 ? DGSWE_STATE : s;
         if (s == 0)  // its face fluxes came with the upload

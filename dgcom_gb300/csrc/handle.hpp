@@ -24,7 +24,7 @@ constexpr int kRhsBuffer = DGSWE_N_BUFFERS;  // scratch buffer of dgswe_compute_
 }  // namespace host
 
 // dgswe_step_host's upload and last stage run in this many element chunks
-constexpr int kHostChunks = 16;
+constexpr int kHostChunks = 8;
 
 namespace host {
 
@@ -102,7 +102,6 @@ struct dgswe_handle {
     // the compute, and one event per chunk (created on first use)
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t chunk_done[dgswe::kHostChunks] = {};
-    cudaEvent_t vel_done[dgswe::kHostChunks] = {};  // a chunk's velocities, for the dt stream
     // per upload chunk, what the first stage can take once that chunk has
     // arrived (everything it reads in it or before it): the elements' dt
     // pass, the interior edges' and boundary faces' fluxes (ready_*[off[c]
@@ -119,8 +118,6 @@ struct dgswe_handle {
 
     ~dgswe_handle() {
         for (cudaEvent_t e : chunk_done)
-            if (e) cudaEventDestroy(e);
-        for (cudaEvent_t e : vel_done)
             if (e) cudaEventDestroy(e);
         if (copy_stream) cudaStreamDestroy(copy_stream);
         for (cudaEvent_t e : {dt_fork, dt_join})
