@@ -966,39 +966,18 @@ int dgswe_step(dgswe_handle* h, int32_t scheme, double t, double dt) {
 
 namespace {
 
-// The ready lists of dgswe_step_host's upload chunks (element chunks of
-// ⌈K/kHostChunks⌉): an element's dt pass reads its nodes and its face
-// neighbours' face nodes, so it is ready with the last of their chunks; an
-// interior edge with the later of its two elements' chunks; a boundary face
-// with its element's. Each list in index order.
+// The ready lists of dgswe_step_host's upload chunks (ready_lists,
+// host_common.hpp), on the device
 int build_ready_lists(dgswe_handle* h) {
     if (h->ready_built) return DGSWE_OK;
-    const int64_t K = h->K, per = (K + kHostChunks - 1) / kHostChunks;
-    auto chunk = [&](int64_t k) { return (int)(k / per); };
-    std::vector<int32_t> elems[kHostChunks], edges[kHostChunks], bfaces[kHostChunks];
-    for (int64_t k = 0; k < K; ++k) {
-        int c = chunk(k);
-        for (int f = 0; f < 4; ++f)
-            if (h->nb[k][f] >= 0) c = std::max(c, chunk(h->nb[k][f]));
-        elems[c].push_back((int32_t)k);
-    }
-    for (size_t e = 0; e < h->h_edge_left.size(); ++e)
-        edges[std::max(chunk(h->h_edge_left[e] >> 2), chunk(h->h_edge_right[e] >> 2))].push_back(
-            (int32_t)e);
-    for (size_t b = 0; b < h->h_bface.size(); ++b)
-        bfaces[chunk(h->h_bface[b] >> 2)].push_back((int32_t)b);
-    auto flatten = [&](std::vector<int32_t>* parts, int64_t* off, const int32_t** out) {
-        std::vector<int32_t> all;
-        for (int c = 0; c < kHostChunks; ++c) {
-            off[c] = (int64_t)all.size();
-            all.insert(all.end(), parts[c].begin(), parts[c].end());
-        }
-        off[kHostChunks] = (int64_t)all.size();
-        return upload_vec(h, all, out);
-    };
-    if (int s = flatten(elems, h->ready_elem_off, &h->ready_elems)) return s;
-    if (int s = flatten(edges, h->ready_edge_off, &h->ready_edges)) return s;
-    if (int s = flatten(bfaces, h->ready_bface_off, &h->ready_bfaces)) return s;
+    const ReadyLists r = ready_lists(h->K, kHostChunks, h->nb, h->h_edge_left, h->h_edge_right,
+                                     h->h_bface);
+    std::copy(r.elem_off.begin(), r.elem_off.end(), h->ready_elem_off);
+    std::copy(r.edge_off.begin(), r.edge_off.end(), h->ready_edge_off);
+    std::copy(r.bface_off.begin(), r.bface_off.end(), h->ready_bface_off);
+    if (int s = upload_vec(h, r.elems, &h->ready_elems)) return s;
+    if (int s = upload_vec(h, r.edges, &h->ready_edges)) return s;
+    if (int s = upload_vec(h, r.bfaces, &h->ready_bfaces)) return s;
     h->ready_built = true;
     return DGSWE_OK;
 }

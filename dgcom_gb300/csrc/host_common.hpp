@@ -3,6 +3,8 @@
 // the device physics constants of a form.
 #pragma once
 
+#include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -260,6 +262,50 @@ inline std::vector<double> pair_coef_table(const PairSchedule& sched) {
             pc[(size_t)sl * 4 + 2 + side] = 0.5 * c;
         }
     return pc;
+}
+
+// The ready lists of a state uploaded in `chunks` element chunks of
+// ⌈K/chunks⌉ (dgswe_step_host): an element's dt pass reads its nodes and its
+// face neighbours' face nodes, so it is ready with the last of their chunks;
+// an interior edge with the later of its two elements' chunks; a boundary
+// face with its element's. Each list in index order; off[c]..off[c+1] is
+// chunk c's part. nb[k][f]: the neighbour across face f, −1 on the boundary;
+// edge_left/right and bface: element·4 + face.
+struct ReadyLists {
+    std::vector<int32_t> elems, edges, bfaces;
+    std::vector<int64_t> elem_off, edge_off, bface_off;  // chunks + 1 each
+};
+
+inline ReadyLists ready_lists(int64_t K, int chunks, const std::vector<std::array<int64_t, 4>>& nb,
+                              const std::vector<int64_t>& edge_left,
+                              const std::vector<int64_t>& edge_right,
+                              const std::vector<int64_t>& bface) {
+    const int64_t per = std::max<int64_t>(1, (K + chunks - 1) / chunks);
+    auto chunk = [&](int64_t k) { return (int)(k / per); };
+    std::vector<std::vector<int32_t>> el(chunks), ed(chunks), bf(chunks);
+    for (int64_t k = 0; k < K; ++k) {
+        int c = chunk(k);
+        for (int f = 0; f < 4; ++f)
+            if (nb[k][f] >= 0) c = std::max(c, chunk(nb[k][f]));
+        el[c].push_back((int32_t)k);
+    }
+    for (size_t e = 0; e < edge_left.size(); ++e)
+        ed[std::max(chunk(edge_left[e] >> 2), chunk(edge_right[e] >> 2))].push_back((int32_t)e);
+    for (size_t b = 0; b < bface.size(); ++b) bf[chunk(bface[b] >> 2)].push_back((int32_t)b);
+    ReadyLists r;
+    auto flatten = [&](std::vector<std::vector<int32_t>>& parts, std::vector<int32_t>& all,
+                       std::vector<int64_t>& off) {
+        off.assign(chunks + 1, 0);
+        for (int c = 0; c < chunks; ++c) {
+            off[c] = (int64_t)all.size();
+            all.insert(all.end(), parts[c].begin(), parts[c].end());
+        }
+        off[chunks] = (int64_t)all.size();
+    };
+    flatten(el, r.elems, r.elem_off);
+    flatten(ed, r.edges, r.edge_off);
+    flatten(bf, r.bfaces, r.bface_off);
+    return r;
 }
 
 }  // namespace dgswe

@@ -208,3 +208,26 @@ def test_sequential_breakdown_recovers_overhead_and_bound():
     fastest = max(3 * n / (overhead + cost * n) for n in nodes)
     assert abs(b["bound_speedup"] - seq / (3 * sum(nodes) / fastest)) < 1e-9
     assert len(b["runs"]) == 4
+
+
+def test_host_step_ready_lists(tmp_path):
+    """The host-state step's ready lists (ready_lists in host_common.hpp)
+    on scrambled grids with boundary gaps: every element, edge and boundary
+    face listed once, in the chunk of the latest data it reads, in index
+    order (tests/ready_lists_check.cpp, host build)."""
+    import shutil
+    import subprocess
+    from pathlib import Path
+
+    gxx = shutil.which("g++")
+    if gxx is None:
+        import pytest
+
+        pytest.skip("g++ not available")
+    here = Path(__file__).resolve().parent
+    exe = tmp_path / "ready_lists_check"
+    subprocess.run([gxx, "-O2", "-std=c++17", "-I", str(here.parent / "dgcom_gb300" / "csrc"),
+                    str(here / "ready_lists_check.cpp"), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert out.stdout.startswith("ok ")
