@@ -843,7 +843,8 @@ def run_adjoint_ensemble(args, rank: int, world: int, local: int):
         ens.set_parameters(manning=n0, tide=tide0)
         J, _, _ = ens.forward(state, dts=dts, eta_obs=eta_obs)
         Jm = ens.member_J()
-        g = ens.reverse(bed=False)  # the gradients asked of the batched adjoint: Manning and the tides, no bed
+        # the gradients asked of the batched adjoint: Manning and the tides, no bed
+        g = ens.reverse(bed=False)
         st = ens.stats()
 
         def J_at(manning=None, tide=None):
