@@ -640,10 +640,10 @@ def run_adjoint(args, rank: int, world: int, local: int):
     results = {}
     g = None
     dts = None
-    # checkpoints every 45 steps: with the segment's full reverse data (8
+    # checkpoints every 45 steps: with the segment's full reverse data (10
     # states a step), or with its step-start states only; every state stored
     every = 45
-    full_budget = (math.ceil(steps / every) + 8 * every + 1) * state_bytes
+    full_budget = (math.ceil(steps / every) + 10 * every + 1) * state_bytes
     start_budget = (math.ceil(steps / every) + every + 1) * state_bytes
     for label, budget, ck in [("every 45, full segments", full_budget, every),
                               ("every 45, step-start segments", start_budget, every),

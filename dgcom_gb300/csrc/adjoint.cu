@@ -20,8 +20,9 @@
 // and the reverse replays each segment of s steps from its checkpoint
 // before reversing it:
 //  - full segments, when the budget holds them: the replay keeps every
-//    step's stage inputs and kept values (8 states a step), so each step is
-//    computed once in the reverse sweep;
+//    step's stage inputs with their node velocities and the kept values
+//    (10 states a step), so each step is computed once in the reverse
+//    sweep;
 //  - else step-start segments: the replay keeps the s step-start states and
 //    each step's stages are computed again as it is reversed (twice in all).
 // s is the caller's checkpoint interval, or the one the budget allows with
@@ -434,9 +435,9 @@ int setup(dgswe_adjoint* a, const dgswe_form* forms, const dgswe_adjoint_config*
         ACK(cudaMemGetInfo(&free_b, &total));
         budget = std::max(0.0, (double)free_b - 2.0 * (1ull << 30));
     }
-    // states held: checkpoints, and the segment (8 states a step when full)
+    // states held: checkpoints, and the segment (10 states a step when full)
     auto held = [&](int64_t st, bool full) {
-        return (double)((N + st - 1) / st + (st > 1 ? (full ? 8 : 1) * st : 0)) * sb;
+        return (double)((N + st - 1) / st + (st > 1 ? (full ? 10 : 1) * st : 0)) * sb;
     };
     int64_t stride = 0;
     bool full = false;
@@ -468,10 +469,10 @@ int setup(dgswe_adjoint* a, const dgswe_form* forms, const dgswe_adjoint_config*
     a->full = full;
     a->n_ckpt = (N + stride - 1) / stride;
     if ((s = dalloc(a, 3 * (size_t)nv * a->n_ckpt, &a->d_ckpt))) return s;
-    if (stride > 1 && (s = dalloc(a, (full ? 24 : 3) * (size_t)nv * stride, &a->d_seg))) return s;
+    if (stride > 1 && (s = dalloc(a, (full ? 30 : 3) * (size_t)nv * stride, &a->d_seg))) return s;
     a->stats.stride = stride;
     a->stats.full_segments = full ? 1 : 0;
-    a->stats.stored_states = a->n_ckpt + (stride > 1 ? (full ? 8 : 1) * stride : 0);
+    a->stats.stored_states = a->n_ckpt + (stride > 1 ? (full ? 10 : 1) * stride : 0);
     a->stats.stored_bytes = (double)a->stats.stored_states * sb;
     return DGSWE_OK;
 }
@@ -772,16 +773,16 @@ int dgswe_adjoint_reverse(dgswe_adjoint* a, double* grad_h0, double* grad_hu0, d
     ACK(cudaEventRecord(a->e0, st));
     int64_t recomputed = 0;
     DevBuf& q = a->S[0];
-    // a full segment's step n: its start state, the inputs of stages 1 and 2
-    // (h, hu, hv each; their velocities in S[b]'s, recomputed) and what the
+    // a full segment's step n: its start state and the inputs of stages 1
+    // and 2 (h, hu, hv and their node velocities, 5 fields each) and what the
     // three stages keep (5 fields each), written there by the replay itself
-    const size_t slot = 24 * (size_t)nv;
+    const size_t slot = 30 * (size_t)nv;
     auto view = [&](int64_t n, int64_t c0, int b) {
-        double* p = a->d_seg + (n - c0) * slot + 3 * (size_t)b * nv;
-        return DevBuf{p, p + nv, p + 2 * nv, a->S[b].u, a->S[b].v};
+        double* p = a->d_seg + (n - c0) * slot + 5 * (size_t)b * nv;
+        return DevBuf{p, p + nv, p + 2 * nv, p + 3 * nv, p + 4 * nv};
     };
     auto keep_view = [&](int64_t n, int64_t c0, int s) {
-        double* p = a->d_seg + (n - c0) * slot + (9 + 5 * (size_t)s) * nv;
+        double* p = a->d_seg + (n - c0) * slot + (15 + 5 * (size_t)s) * nv;
         return DevBuf{p, p + nv, p + 2 * nv, p + 3 * nv, p + 4 * nv};
     };
     for (int64_t c0 = (a->n_ckpt - 1) * a->stride; c0 >= 0; c0 -= a->stride) {
@@ -798,8 +799,8 @@ int dgswe_adjoint_reverse(dgswe_adjoint* a, double* grad_h0, double* grad_hu0, d
             for (int64_t n = c0; n < c1; ++n) {
                 if (int s = args_to_ctl(a, n)) return s;
                 const DevBuf in[3] = {view(n, c0, 0), view(n, c0, 1), view(n, c0, 2)};
-                // stage 2 writes the next step's start (its velocities where
-                // this step's start had its own: stage 0 has read them)
+                // stage 2 writes the next step's start; each stage writes its
+                // output's node velocities beside it
                 const DevBuf out[3] = {in[1], in[2], n + 1 < c1 ? view(n + 1, c0, 0) : a->S[3]};
                 for (int s = 0; s < 3; ++s) {
                     t.ks->face(t.n1, *t.T, *t.P, in[s], t.fb_h, t.fb_hu, t.fb_hv, t.ctl, s, on,
@@ -816,7 +817,6 @@ int dgswe_adjoint_reverse(dgswe_adjoint* a, double* grad_h0, double* grad_hu0, d
                 const DevBuf in[3] = {view(n, c0, 0), view(n, c0, 1), view(n, c0, 2)};
                 const DevBuf keep[3] = {keep_view(n, c0, 0), keep_view(n, c0, 1),
                                         keep_view(n, c0, 2)};
-                for (int b = 0; b < 3; ++b) t.ks->velocity(in[b], nv, t.P->h_min, st);
                 if (int s = args_to_ctl(a, n)) return s;
                 if (int s = reverse_stages(a, in, keep)) return s;
             }

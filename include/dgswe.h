@@ -775,8 +775,9 @@ int dgswe_ensemble_run(dgswe_ensemble* ensemble, const dgswe_run_config* run, in
  * equal (a continuous bed). Step-start states are stored in HBM within
  * memory_budget; when all N do not fit, a two-level checkpointing stores
  * every s-th one and replays each segment from it: keeping each step's
- * stage inputs and kept values when the budget holds 8 states a step of the
- * segment (full segments), else its step-start states only. */
+ * stage inputs with their node velocities and the kept values when the
+ * budget holds 10 states a step of the segment (full segments), else its
+ * step-start states only. */
 #define DGSWE_MAX_CONSTITUENTS 8
 
 typedef struct dgswe_adjoint dgswe_adjoint;

@@ -242,7 +242,7 @@ def test_checkpoint_segments_give_the_same_gradient():
         st = seg.stats()
         assert st.stride > 1 and not st.full_segments and st.recomputed_steps > STEPS
     # full segments every 4 steps: each step computed once
-    with Adjoint(form, STEPS, STATIONS, t_start=T_START, memory_budget=40 * state_bytes,
+    with Adjoint(form, STEPS, STATIONS, t_start=T_START, memory_budget=44 * state_bytes,
                  checkpoint_every=4) as seg:
         seg.forward(state)
         g3 = seg.reverse()
